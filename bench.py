@@ -1,0 +1,376 @@
+"""Benchmark: RGB-D panoramas per second at 1024 x 1024 matching, 32 candidates (the synthetic
+stand-in for the reference's prototype configuration: 4 double-sphere fisheye cameras, inputs
+1216 x 1216, references 2 and 3, rgb_to_stitch 1216 x 1216, panorama 2048 x 1024, sigma_i 10,
+sigma_s 25, min/max distance 0.55 / 100 m).
+
+One step = one RGB-D panorama (distance estimation on both reference cameras + stitching).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--mode fp32]
+
+--impl reference times the reference algorithm on the host cores: the C restatement of the
+reference (oracle/, OpenMP over all cores), one full frame per step.  Under torchrun only rank 0
+runs it.  --gpus N > 1 runs N independent replicas (frames are independent; no collective on
+the data path), timed between barriers, max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PACKAGE = "sphere-stereo_gb300"
+
+WORKLOAD = dict(width_in=1216, matching=(1024, 1024), stitch=(1216, 1216), panorama=(2048, 1024), candidates=32,
+                refs=[2, 3], sigma_i=10.0, sigma_s=25.0, min_dist=0.55, max_dist=100.0)
+WORKLOAD_NAME = ("4 double-sphere fisheye cameras (fx=0.28W, xi=-0.2, alpha=0.6) on a 0.2 m square, "
+                 "matching 1024x1024, 32 candidates, references 2,3, rgb_to_stitch 1216x1216, "
+                 "panorama 2048x1024, sigma_i 10, sigma_s 25")
+METRIC = "RGB-D panoramas/s @1024² match, 32 cand"
+UNIT = "panoramas/s"
+DATA = "synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast per frame (seed 2000+frame)"
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def frames_for_rank(total: int, rank: int, world: int) -> list[int]:
+    """Frame ids a replica renders for its input pool: disjoint across ranks."""
+    return [rank + world * i for i in range(total)]
+
+
+def render_pool(count: int, rank: int, world: int):
+    syn = importlib.import_module(PACKAGE + ".synthetic")
+    cams = syn.square_rig(WORKLOAD["width_in"])
+    frames = []
+    for f in frames_for_rank(count, rank, world):
+        rng = np.random.Generator(np.random.PCG64(syn.frame_seed(2, f)))
+        scene = syn.random_scene(rng)
+        frames.append(syn.render_frame(scene, cams, WORKLOAD["matching"], WORKLOAD["stitch"], WORKLOAD["refs"]))
+    return syn.basalt_calibration(cams), frames
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+class LaunchRecorder:
+    """Counts this library's kernel launches and brackets one entry point with CUDA events on
+    the stream it is launched on."""
+
+    def __init__(self, native, timed_entry: str):
+        self.native = native
+        self.timed_entry = timed_entry
+        self.launches = 0
+        self.events = []
+        self.active = False
+        self._orig = native.call
+
+    def __enter__(self):
+        import torch
+
+        native = self.native
+
+        def call(name, *args):
+            if not self.active:
+                return self._orig(name, *args)
+            self.launches += native.kernels_launched(name, args)
+            if name == self.timed_entry:
+                stream = torch.cuda.ExternalStream(args[-1]) if args[-1] else torch.cuda.current_stream()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                self._orig(name, *args)
+                b.record(stream)
+                self.events.append((a, b))
+                return None
+            return self._orig(name, *args)
+
+        native.call = call
+        return self
+
+    def __exit__(self, *exc):
+        self.native.call = self._orig
+
+    def mean_ms(self) -> float | None:
+        if not self.events:
+            return None
+        return sum(a.elapsed_time(b) for a, b in self.events) / len(self.events)
+
+
+def sweep_bytes_per_launch(cols: int, rows: int, cameras: int, candidates: int, cost_bytes: int) -> int:
+    """Algorithmic bytes of one sweep launch (one reference camera): the reference image and the
+    camera selection map read once, each source image read at most once (upper bound), the
+    cost volume written once."""
+    P = cols * rows
+    return 12 * P + 12 * P * (cameras - 1) + P + cost_bytes * candidates * P
+
+
+def run_ours(args, rank, world, device):
+    import torch
+
+    ss = importlib.import_module(PACKAGE)
+    native = ss._native
+    pool = max(2, args.pool)
+    calibration, frames = render_pool(pool, rank, world)
+    W = WORKLOAD
+    calibs = ss.parse_json_calib(calibration, W["matching"], device)
+    vp = torch.zeros(3, device=device)
+    for r in W["refs"]:
+        vp += calibs[r].rt[:3, 3] / len(W["refs"])
+    mw, mh = W["matching"]
+    masks = [torch.ones(1, mh, mw, device=device) for _ in calibs]
+    est = ss.RGBD_Estimator(calibs, W["min_dist"], W["max_dist"], W["candidates"], W["refs"], vp, masks, W["matching"],
+                            W["stitch"], W["panorama"], W["sigma_i"], W["sigma_s"], device)
+    dev_frames = [([torch.as_tensor(im, device=device).float() for im in f.images_to_match],
+                   [torch.as_tensor(im, device=device).float() for im in f.images_to_stitch]) for f in frames]
+    torch.cuda.synchronize()
+    for i in range(args.warmup):
+        est.estimate_RGBD_panorama(*dev_frames[i % pool])
+    torch.cuda.synchronize()
+    barrier(world)
+
+    # device-resident inputs: the pool's frames cycle, every step reads a different frame
+    # (pool x 83 MB of inputs, and a 128 MB cost volume per reference, exceed the 126 MB L2)
+    rec = LaunchRecorder(native, "ssg_sweep_cost")
+    with ClockSampler(device.index) as clocks, rec:
+        torch.cuda.synchronize()
+        barrier(world)
+        rec.active = True
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for i in range(args.steps):
+            est.estimate_RGBD_panorama(*dev_frames[i % pool])
+        end.record()
+        torch.cuda.synchronize()
+        rec.active = False
+        barrier(world)
+    ms = start.elapsed_time(end) / args.steps
+    ms = max_over_ranks(ms, world, device)
+
+    # end to end through the public API: pinned host inputs in, host outputs out, every step
+    host = [([torch.as_tensor(im).float().pin_memory() for im in f.images_to_match],
+             [torch.as_tensor(im).float().pin_memory() for im in f.images_to_stitch]) for f in frames]
+    staging = ([torch.empty_like(t, device=device) for t in host[0][0]],
+               [torch.empty_like(t, device=device) for t in host[0][1]])
+    out_rgb = torch.empty(est.fishey_stitcher.RGB_panorama.shape, dtype=torch.uint8).pin_memory()
+    out_d = torch.empty(est.fishey_stitcher.distance_panorama.shape).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host[0][0] + host[0][1])
+    d2h = out_rgb.numel() + out_d.numel() * 4
+
+    def e2e_step(i):
+        hm, hs = host[i % pool]
+        for d, h in zip(staging[0] + staging[1], hm + hs):
+            d.copy_(h, non_blocking=True)
+        rgb, dist = est.estimate_RGBD_panorama(*staging)
+        out_rgb.copy_(rgb, non_blocking=True)
+        out_d.copy_(dist, non_blocking=True)
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    torch.cuda.synchronize()
+    barrier(world)
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record()
+    for i in range(args.steps):
+        e2e_step(i)
+    e2.record()
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(s2.elapsed_time(e2) / args.steps, world, device)
+
+    peak, peak_kind = measured_peaks()
+    sweep_ms = rec.mean_ms()
+    sweep_bytes = sweep_bytes_per_launch(mw, mh, len(calibs), W["candidates"], 4)
+    achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9 if sweep_ms else None
+    return {
+        "value": world * 1000.0 / ms,
+        "ms_per_step": ms,
+        "e2e": {"value": world * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": rec.launches,
+        "clocks": clocks.summary(),
+        "roofline": {"bound": "hbm", "kernel": "sweep_cost_kernel", "achieved": achieved, "peak": peak,
+                     "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms},
+    }
+
+
+def cpu_baseline(frames_calib, sample_frames: int):
+    """The oracle (C restatement of the reference, OpenMP over all cores) on full frames."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import sphere_oracle
+
+    calibration, frames = frames_calib
+    W = WORKLOAD
+    masks = [np.ones(W["matching"][::-1], np.float32) for _ in range(4)]
+    rig = sphere_oracle.OracleRig(calibration, min_dist=W["min_dist"], max_dist=W["max_dist"],
+                                  candidate_count=W["candidates"], references_indices=W["refs"], masks=masks,
+                                  matching_resolution=W["matching"], rgb_to_stitch_resolution=W["stitch"],
+                                  panorama_resolution=W["panorama"], sigma_i=W["sigma_i"], sigma_s=W["sigma_s"])
+    inputs = [([im.astype(np.float32) for im in f.images_to_match], [im.astype(np.float32) for im in f.images_to_stitch])
+              for f in frames]
+    t0 = time.perf_counter()
+    for i in range(sample_frames):
+        rig.estimate(*inputs[i % len(inputs)])
+    dt = time.perf_counter() - t0
+    return {"value": sample_frames / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{sample_frames} full frame(s) of the workload, oracle/sphere_oracle.c (OpenMP, "
+                      f"{os.cpu_count()} threads), camera selection and stitcher tables excluded"}
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(value: float, world: int, device) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pool", type=int, default=2, help="distinct input frames cycled through")
+    ap.add_argument("--cpu-frames", type=int, default=2, help="frames timed for the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    local_rank = _env_int("LOCAL_RANK", 0)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        data = render_pool(1, 0, 1)
+        for _ in range(args.warmup):
+            cpu_baseline(data, 1)
+        base = cpu_baseline(data, max(1, args.steps))
+        line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / base["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
+                "config": {"workload": WORKLOAD_NAME, "mode": "reference algorithm on the host cores"},
+                "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local_rank)
+    torch.cuda.set_device(device)
+    ours = run_ours(args, rank, world, device)
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    base = None
+    if not args.no_cpu_baseline:
+        base = cpu_baseline(render_pool(1, 0, 1), args.cpu_frames)
+    line = {"metric": METRIC, "value": ours["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ours["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": {"workload": WORKLOAD_NAME, "mode": "fp32 cost volume, one frame per call",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": f"inputs cycle over {max(2, args.pool)} frames of 83 MB each; the 128 MB "
+                             "cost volume alone exceeds the 126 MB L2"},
+            "e2e": ours["e2e"], "gpu_launches": ours["gpu_launches"], "clocks": ours["clocks"],
+            "roofline": ours["roofline"], "cpu_baseline": base}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

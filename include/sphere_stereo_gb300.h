@@ -1,0 +1,197 @@
+/*
+ * sphere_stereo_gb300 -- C ABI of the GB300 (sm_103a) implementation of sphere-sweeping stereo's
+ * per-frame path: sphere sweep + matching cost, ISB multiscale cost filter, distance selection,
+ * distance post-filter, RGB-D panorama stitcher.
+ *
+ * Library: libsphere_stereo_gb300.so (built from sphere-stereo_gb300/csrc/*.cu).
+ *
+ * Conventions
+ *   - Every pointer named d_* (or documented as "device") is CUDA device memory of the current
+ *     device; other pointers are host memory read during the call only.
+ *   - Sizes follow the reference: images are row-major [rows][cols][3]; cost volumes are planar
+ *     [candidates][rows][cols] float32 (python/isb_filter.py:69-70) unless a function says
+ *     otherwise; resolutions are passed as (cols, rows) pairs where the reference does so.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Every call only enqueues work
+ *     on that stream; nothing synchronises the host.
+ *   - Every function returns SSG_OK or an error code; ssg_last_error() gives the message of the
+ *     calling thread's last failure.  Invalid arguments are rejected before any launch.
+ *
+ * Each declaration names the reference interface it stands in for (file:line within the
+ * reference project, KAIST-VCLAB/sphere-stereo).
+ */
+#ifndef SPHERE_STEREO_GB300_H
+#define SPHERE_STEREO_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SSG_API __attribute__((visibility("default")))
+#else
+#define SSG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    SSG_OK = 0,
+    SSG_ERR_INVALID_ARGUMENT = 1, /* rejected before launch */
+    SSG_ERR_CUDA = 2,             /* a CUDA runtime call or launch failed */
+    SSG_ERR_UNSUPPORTED = 3       /* a size beyond a documented compile-time limit */
+};
+
+/* Compile-time limits (also reported by ssg_limits). */
+#define SSG_MAX_CAMERAS 16
+#define SSG_MAX_CANDIDATES 256
+#define SSG_MAX_REFERENCES 16
+#define SSG_MAX_LEVELS 24
+
+/* Double-sphere camera in the form the reference's torch code uses it
+ * (python/utils.py:57-94 with python/utils.py:40-55): fx, fy, cx, cy are the float32 products
+ * `fl * matching_scale` and `principal * matching_scale`; xi and alpha are the calibration's
+ * double-precision values (the library rounds derived constants exactly as torch does). */
+typedef struct {
+    float fx, fy, cx, cy;
+    double xi, alpha;
+} ssg_camera;
+
+/* Double-sphere intrinsics as the stitcher kernels use them: the `Intrinsics` struct of
+ * python/stitcher.cu:31-35, filled by vectorize_calibration (python/stitcher.py:35-46). */
+typedef struct {
+    float fx, fy, cx, cy, xi, alpha;
+} ssg_intrinsics;
+
+/* Message of the calling thread's last failed call ("" if none). */
+SSG_API const char* ssg_last_error(void);
+/* Library version, major * 10000 + minor * 100 + patch. */
+SSG_API int ssg_version(void);
+/* Writes {max cameras, max candidates, max references, max levels}. */
+SSG_API void ssg_limits(int32_t* out4);
+
+/* ---------------------------------------------------------------------------------------------
+ * Guide image
+ * ------------------------------------------------------------------------------------------- */
+
+/* rgb2yCbCr followed by the uint8 cast: python/utils.py:144-155 and
+ * python/depth_estimation.py:227.  d_rgb: pixels x 3 float32 (channel order as stored);
+ * d_guide: pixels x 3 uint8. */
+SSG_API int ssg_rgb_to_guide(const float* d_rgb, int64_t pixels, uint8_t* d_guide, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Camera selection and sphere sweep
+ * ------------------------------------------------------------------------------------------- */
+
+/* RGBD_Estimator.select_camera for one reference camera: python/depth_estimation.py:83-135.
+ * cameras: camera_count entries (host); relative_poses: camera_count x 12 floats (host), rows
+ * 0..2 of inverse(camera.rt) @ reference.rt; d_masks: camera_count x rows x cols float32;
+ * d_selected: rows x cols int8, -1 where no camera qualifies. */
+SSG_API int ssg_select_camera(int cols, int rows, int camera_count, const ssg_camera* cameras, int reference,
+                      const float* relative_poses, const float* d_masks, double min_dist, double max_dist,
+                      int8_t* d_selected, void* stream);
+
+/* Sphere sweep and per-pixel matching cost for one reference camera:
+ * python/depth_estimation.py:141-175 (candidate volume, per-camera transform, projection,
+ * bilinear zero-padded grid_sample, L1 over the three channels, clamp at 500).
+ * d_images: camera_count device pointers (host array) to rows x cols x 3 float32 images;
+ * candidates: candidate_count distances (host), 1 / linspace(1/min_dist, 1/max_dist);
+ * d_cost: candidate_count x rows x cols float32. */
+SSG_API int ssg_sweep_cost(int cols, int rows, int camera_count, const ssg_camera* cameras, int reference,
+                   const float* relative_poses, const float* const* d_images, const int8_t* d_selected,
+                   const float* candidates, int candidate_count, float* d_cost, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * ISB filter
+ * ------------------------------------------------------------------------------------------- */
+
+/* One edge-aware 2x downsampling step: guideDownsample2xKernel, python/isb_filter.cu:44-119
+ * (launched by python/isb_filter.py:90-107).  Guides are rows x cols x 3 uint8, costs planar
+ * candidate_count x rows x cols float32; var_inv_i = 1 / (2 sigma_i^2). */
+SSG_API int ssg_isb_downsample(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in, int cols_in,
+                       uint8_t* d_guide_out, float* d_cost_out, int rows_out, int cols_out, int candidate_count,
+                       float var_inv_i, void* stream);
+
+/* One edge-aware 2x upsample-and-merge step, fine level updated in place:
+ * guideUpsample2xKernel, python/isb_filter.cu:132-329 (python/isb_filter.py:109-134). */
+SSG_API int ssg_isb_upsample(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in, int cols_in,
+                     uint8_t* d_guide_inout, float* d_cost_inout, int rows_inout, int cols_inout,
+                     int candidate_count, float weight_up, float weight_down, float var_inv_i, void* stream);
+
+/* Number of pyramid levels for a cols x rows image: python/isb_filter.py:60. */
+SSG_API int ssg_isb_level_count(int cols, int rows);
+
+/* ISB_Filter.apply as one call: python/isb_filter.py:72-136.  d_guides / d_costs: level_count
+ * device pointers (host arrays); level 0 is the caller's guide and cost, filtered in place;
+ * levels 1.. are scratch of ceil(rows / 2^l) x ceil(cols / 2^l) (python/isb_filter.py:62-70). */
+SSG_API int ssg_isb_apply(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
+                  int candidate_count, double sigma_i, double sigma_s, void* stream);
+
+/* Distance selection: python/depth_estimation.py:179-198 (argmin / max over candidates,
+ * parabolic sub-candidate step, flat-cost fallback, index -> distance).  d_cost: planar
+ * candidate_count x pixels; d_distance: pixels float32; d_index: pixels int32 (may be NULL). */
+SSG_API int ssg_select_distance(const float* d_cost, int candidate_count, int64_t pixels, const float* candidates,
+                        float* d_distance, int32_t* d_index, void* stream);
+
+/* The last upsampling step of ISB_Filter.apply (level 1 -> level 0) fused with distance
+ * selection: python/isb_filter.cu:132-329 followed by python/depth_estimation.py:179-198.
+ * Reads the fine cost but never writes it; writes the filtered level-0 guide and the distance. */
+SSG_API int ssg_isb_upsample_select(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in, int cols_in,
+                            uint8_t* d_guide_inout, const float* d_cost_fine, int rows_fine, int cols_fine,
+                            int candidate_count, float weight_up, float weight_down, float var_inv_i,
+                            const float* candidates, float* d_distance, int32_t* d_index, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Stitcher
+ * ------------------------------------------------------------------------------------------- */
+
+/* createInpaintingWeightsKernel, python/stitcher.cu:212-272.  translation: 3 floats (host),
+ * (inverse(rt) @ [viewpoint, 1])[:3] (python/stitcher.py:130); d_table: rows x cols x 2 uint8. */
+SSG_API int ssg_inpainting_table(int cols, int rows, const ssg_intrinsics* intrinsics, const float* translation,
+                         double min_dist, double max_dist, uint8_t* d_table, void* stream);
+
+/* Box mean over a (2 radius + 1)^2 window of each of `planes` rows x cols float32 planes, with
+ * pad_value outside the image: the torch conv2d smoothing of python/stitcher.py:144-148
+ * (pad_value 1) and :162-163 (pad_value 0). */
+SSG_API int ssg_box_filter(const float* d_in, int planes, int rows, int cols, int radius, float pad_value, float* d_out,
+                   void* stream);
+
+/* createBlendingLutKernel, python/stitcher.cu:338-401, for reference_count cameras.
+ * intrinsics / rotations (3x3 row-major, inverse of each camera rotation) / translations: host
+ * arrays; d_masks: box-filtered masks, reference_count x rows x cols; d_lut:
+ * reference_count x pano_rows x pano_cols x 2; d_weights: reference_count x pano_rows x pano_cols. */
+SSG_API int ssg_blending_lut(int cols, int rows, int pano_cols, int pano_rows, int reference_count,
+                     const ssg_intrinsics* intrinsics, const float* rotations, const float* translations,
+                     const float* d_masks, double min_dist, double max_dist, float* d_lut, float* d_weights,
+                     void* stream);
+
+/* Blending-weight normalisation over references (python/stitcher.py:164), in place. */
+SSG_API int ssg_normalize_weights(float* d_weights, int reference_count, int64_t pixels, void* stream);
+
+/* Distance reprojection to the panorama viewpoint (z-buffer): reprojectDistanceKernel,
+ * python/stitcher.cu:181-204, with the fill of python/stitcher.py:184 when fill != 0.
+ * Each target pixel receives the minimum distance; targets outside the map are dropped. */
+SSG_API int ssg_reproject_distance(const float* d_distance_in, float* d_distance_out, int cols, int rows,
+                           const ssg_intrinsics* intrinsics, const float* translation, int fill, void* stream);
+
+/* Hole filling: `iterations` launches of inpaintKernel, python/stitcher.cu:283-323
+ * (python/stitcher.py:195-200), each a Jacobi step (every pixel reads the map as it was before
+ * the step).  Runs as tiled passes of up to 16 steps each in shared memory, alternating between
+ * d_distance and d_scratch (rows x cols float32, caller-owned); the result ends in d_distance.
+ * Table entries whose offset field is 3 are ignored (the table kernel never writes one). */
+SSG_API int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scratch, int cols, int rows, double max_dist,
+                int iterations, void* stream);
+
+/* mergeRGBDPanoramaKernel, python/stitcher.cu:423-473.  d_reprojected, d_distances:
+ * reference_count x rows x cols; d_images: reference_count x image_rows x image_cols x 3 uint8;
+ * outputs pano_rows x pano_cols float32 distance and x 3 uint8 colour. */
+SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                       const float* d_distances, const uint8_t* d_images, int image_rows, int image_cols,
+                       const float* translations, const ssg_intrinsics* intrinsics, int reference_count, int cols,
+                       int rows, int pano_cols, int pano_rows, float* d_distance_panorama, uint8_t* d_rgb_panorama,
+                       void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHERE_STEREO_GB300_H */

@@ -1,0 +1,172 @@
+"""ctypes binding of libsphere_stereo_gb300.so (the C ABI declared in include/sphere_stereo_gb300.h).
+
+There is no fallback: if the library is missing or fails to load, every entry point raises
+NativeLibraryError.  Device pointers are passed as integers (``tensor.data_ptr()``), streams as
+``torch.cuda.current_stream().cuda_stream``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBRARY = os.path.join(HERE, "libsphere_stereo_gb300.so")
+
+SSG_OK = 0
+SSG_ERR_INVALID_ARGUMENT = 1
+SSG_ERR_CUDA = 2
+SSG_ERR_UNSUPPORTED = 3
+MAX_CAMERAS = 16
+MAX_CANDIDATES = 256
+MAX_REFERENCES = 16
+MAX_LEVELS = 24
+
+
+class NativeLibraryError(RuntimeError):
+    """The CUDA library is not built or cannot be loaded."""
+
+
+class SSGError(RuntimeError):
+    """A library call failed on the device side."""
+
+
+class ssg_camera(ctypes.Structure):
+    _fields_ = [("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float), ("cy", ctypes.c_float),
+                ("xi", ctypes.c_double), ("alpha", ctypes.c_double)]
+
+
+class ssg_intrinsics(ctypes.Structure):
+    _fields_ = [("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float), ("cy", ctypes.c_float),
+                ("xi", ctypes.c_float), ("alpha", ctypes.c_float)]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_F = ctypes.c_float
+_D = ctypes.c_double
+
+# name -> (restype, argtypes); must match include/sphere_stereo_gb300.h
+SIGNATURES = {
+    "ssg_last_error": (ctypes.c_char_p, []),
+    "ssg_version": (_I, []),
+    "ssg_limits": (None, [_P]),
+    "ssg_rgb_to_guide": (_I, [_P, _I64, _P, _P]),
+    "ssg_select_camera": (_I, [_I, _I, _I, _P, _I, _P, _P, _D, _D, _P, _P]),
+    "ssg_sweep_cost": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _I, _P, _P]),
+    "ssg_isb_downsample": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _P]),
+    "ssg_isb_upsample": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P]),
+    "ssg_isb_level_count": (_I, [_I, _I]),
+    "ssg_isb_apply": (_I, [_P, _P, _I, _I, _I, _I, _D, _D, _P]),
+    "ssg_select_distance": (_I, [_P, _I, _I64, _P, _P, _P, _P]),
+    "ssg_isb_upsample_select": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P]),
+    "ssg_inpainting_table": (_I, [_I, _I, _P, _P, _D, _D, _P, _P]),
+    "ssg_box_filter": (_I, [_P, _I, _I, _I, _I, _F, _P, _P]),
+    "ssg_blending_lut": (_I, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _D, _D, _P, _P, _P]),
+    "ssg_normalize_weights": (_I, [_P, _I, _I64, _P]),
+    "ssg_reproject_distance": (_I, [_P, _P, _I, _I, _P, _P, _I, _P]),
+    "ssg_inpaint": (_I, [_P, _P, _P, _I, _I, _D, _I, _P]),
+    "ssg_merge_panorama": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P]),
+}
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+
+def library() -> ctypes.CDLL:
+    """Load (once) and return the library; raises NativeLibraryError when it is unavailable."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIBRARY):
+            raise NativeLibraryError(
+                f"{LIBRARY} is not built; run `python -c \"import __graft_entry__ as g; g.build()\"` "
+                "(needs nvcc) -- there is no CPU fallback")
+        try:
+            lib = ctypes.CDLL(LIBRARY)
+        except OSError as e:
+            raise NativeLibraryError(f"cannot load {LIBRARY}: {e}") from e
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def last_error() -> str:
+    return library().ssg_last_error().decode(errors="replace")
+
+
+def check(code: int, what: str) -> None:
+    if code == SSG_OK:
+        return
+    msg = f"{what}: {last_error()}"
+    if code == SSG_ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    raise SSGError(msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(library(), name)(*args), name)
+
+
+def stream_of(t: torch.Tensor) -> int:
+    if t.device.type != "cuda":
+        raise ValueError(f"expected a CUDA tensor, got one on {t.device}")
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def require(t: torch.Tensor, name: str, dtype: torch.dtype, shape: tuple | None = None, device=None) -> None:
+    """Argument validation before any launch (the reference has none; see the module docstring
+    of depth_estimation.py)."""
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch.Tensor")
+    if t.device.type != "cuda":
+        raise ValueError(f"{name} must be a CUDA tensor (got {t.device}); there is no CPU path")
+    if device is not None and t.device != torch.device(device):
+        raise ValueError(f"{name} is on {t.device}, expected {device}")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype} (got {t.dtype})")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} must have shape {tuple(shape)} (got {tuple(t.shape)})")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+def cameras_array(cams: list[ssg_camera]):
+    return (ssg_camera * len(cams))(*cams)
+
+
+def intrinsics_array(ks: list[ssg_intrinsics]):
+    return (ssg_intrinsics * len(ks))(*ks)
+
+
+def floats(values) -> ctypes.Array:
+    values = [float(v) for v in values]
+    return (ctypes.c_float * len(values))(*values)
+
+
+def pointers(values) -> ctypes.Array:
+    return (ctypes.c_void_p * len(values))(*[int(v) for v in values])
+
+
+def kernels_launched(name: str, args) -> int:
+    """Number of kernels one call of entry point ``name`` with ``args`` launches."""
+    if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count"):
+        return 0
+    if name == "ssg_isb_apply":
+        return 2 * max(0, int(args[2]) - 1)
+    if name == "ssg_reproject_distance":
+        return 2 if args[6] else 1
+    if name == "ssg_inpaint":
+        return -(-int(args[6]) // 16)
+    return 1

@@ -1,0 +1,534 @@
+// RGB-D panorama stitcher (python/stitcher.cu, python/stitcher.py).
+//
+// Differences from the reference's GPU code, all towards one deterministic result:
+//  * reprojection is a z-buffer of atomicMin on the float bits (distances are non-negative), so
+//    each target pixel gets the minimum distance in one launch (the reference runs a racy
+//    compare-and-store twice, stitcher.py:185-192) and targets outside the map are dropped (the
+//    reference's index is unchecked, stitcher.cu:198);
+//  * inpainting is a sequence of Jacobi steps (every pixel reads the map as it was before the
+//    step; the reference updates in place and its result depends on thread timing).  Up to 16
+//    steps run per launch on a shared-memory tile with a 16-pixel halo, ping-ponging between
+//    the map and a scratch map in global memory;
+//  * a table entry whose two best weights stay 0 (outside the model's valid area) encodes the
+//    offsets (0, 0); the reference leaves them uninitialised (stitcher.cu:231).
+#include <atomic>
+#include <cmath>
+#include <cstring>
+
+#include "ssg_common.cuh"
+
+namespace ssg {
+
+constexpr int kStitchBlock = 256;
+
+// createInpaintingWeightsKernel, stitcher.cu:212-272
+__global__ void __launch_bounds__(kStitchBlock) inpainting_table_kernel(int cols, int rows, Intr k, float tx,
+                                                                        float ty, float tz, float dmin, float dmax,
+                                                                        uint8_t* __restrict__ table)
+{
+    const int64_t P = (int64_t)cols * rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    float unit[3];
+    unproject_cu((float)(i % cols), (float)(i / cols), k, unit);
+    const float pc[3] = {fsub(fmul(dmin, unit[0]), tx), fsub(fmul(dmin, unit[1]), ty), fsub(fmul(dmin, unit[2]), tz)};
+    const float pf[3] = {fsub(fmul(dmax, unit[0]), tx), fsub(fmul(dmax, unit[1]), ty), fsub(fmul(dmax, unit[2]), tz)};
+    float uc[2], uf[2];
+    project_cu(pc, k, uc, nullptr);
+    project_cu(pf, k, uf, nullptr);
+    float dx = fsub(uf[0], uc[0]), dy = fsub(uf[1], uc[1]);
+    const float den = fdiv(1.0f, hypotf(dx, dy));
+    dx = fmul(dx, den);
+    dy = fmul(dy, den);
+    int nx[2] = {0, 0}, ny[2] = {0, 0};
+    float w[2] = {0.0f, 0.0f};
+#pragma unroll
+    for (int n = -1; n <= 1; ++n)
+#pragma unroll
+        for (int m = -1; m <= 1; ++m) {
+            if (!(n || m)) continue;
+            const float pd = fdiv(1.0f, hypotf((float)n, (float)m));
+            const float wt = fadd(fmul(fmul((float)n, pd), dx), fmul(fmul((float)m, pd), dy));
+            if (wt > w[1]) {
+                w[0] = w[1];
+                nx[0] = nx[1];
+                ny[0] = ny[1];
+                w[1] = wt;
+                nx[1] = n;
+                ny[1] = m;
+            } else if (wt > w[0]) {
+                w[0] = wt;
+                nx[0] = n;
+                ny[0] = m;
+            }
+        }
+    const unsigned q0 = (__float2uint_rz(fmul(w[0], 255.0f)) & 0xFFu) & 240u;
+    const unsigned q1 = (__float2uint_rz(fmul(w[1], 255.0f)) & 0xFFu) & 240u;
+    table[2 * i] = (uint8_t)(q0 + 4u * (unsigned)(1 + ny[0]) + (unsigned)(1 + nx[0]));
+    table[2 * i + 1] = (uint8_t)(q1 + 4u * (unsigned)(1 + ny[1]) + (unsigned)(1 + nx[1]));
+}
+
+// Box mean with constant padding, summed in row-major window order (stitcher.py:144-148, :162-163)
+__global__ void __launch_bounds__(kStitchBlock) box_filter_kernel(const float* __restrict__ in, int rows, int cols,
+                                                                  int radius, float pad, float kw,
+                                                                  float* __restrict__ out)
+{
+    const int64_t P = (int64_t)cols * rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int plane = blockIdx.y;
+    if (i >= P) return;
+    const float* src = in + (int64_t)plane * P;
+    const int x = (int)(i % cols), y = (int)(i / cols);
+    float s = 0.0f;
+    for (int dy = -radius; dy <= radius; ++dy) {
+        const int yy = y + dy;
+        const bool row_in = yy >= 0 && yy < rows;
+        for (int dx = -radius; dx <= radius; ++dx) {
+            const int xx = x + dx;
+            const float v = (row_in && xx >= 0 && xx < cols) ? __ldg(src + (int64_t)yy * cols + xx) : pad;
+            s = fadd(s, fmul(v, kw));
+        }
+    }
+    out[(int64_t)plane * P + i] = s;
+}
+
+struct LutParams {
+    int cols, rows, pano_cols, pano_rows, nref;
+    float dmin, dmax;
+    Intr k[SSG_MAX_REFERENCES];
+    float rot[SSG_MAX_REFERENCES][9];
+    float t[SSG_MAX_REFERENCES][3];
+};
+
+// createBlendingLutKernel, stitcher.cu:338-401
+__global__ void __launch_bounds__(kStitchBlock) blending_lut_kernel(const __grid_constant__ LutParams p,
+                                                                    const float* __restrict__ masks,
+                                                                    float2* __restrict__ lut,
+                                                                    float* __restrict__ weights)
+{
+    const int64_t Q = (int64_t)p.pano_cols * p.pano_rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q) return;
+    const double PI = 3.14159265;  // stitcher.cu:325, a double literal
+    const float px = (float)(i % p.pano_cols), py = (float)(i / p.pano_cols);
+    const float phi = (float)(__dsub_rn(__ddiv_rn(__dmul_rn((double)fadd(py, 0.5f), PI), (double)p.pano_rows), PI / 2.0));
+    const float theta =
+        (float)(__dadd_rn(__ddiv_rn(__dmul_rn((double)fmul(fadd(px, 0.5f), 2.0f), PI), (double)p.pano_cols), PI));
+    const float cp = cosf(phi);
+    const float unit[3] = {fmul(cp, sinf(theta)), sinf(phi), fmul(cp, cosf(theta))};
+    const float colsm = fsub((float)p.cols, 1.1f), rowsm = fsub((float)p.rows, 1.1f);
+    float bw[SSG_MAX_REFERENCES];
+    float sum = 0.0f;
+    for (int r = 0; r < p.nref; ++r) {
+        const float* m = p.rot[r];
+        float uf[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            uf[a] = fadd(fadd(fmul(m[3 * a], unit[0]), fmul(m[3 * a + 1], unit[1])), fmul(m[3 * a + 2], unit[2]));
+        bool valid = true;
+        float uv[2];
+        project_cu(uf, p.k[r], uv, &valid);
+        uv[0] = fminf(fmaxf(uv[0], 0.1f), colsm);
+        uv[1] = fminf(fmaxf(uv[1], 0.1f), rowsm);
+        lut[(int64_t)r * Q + i] = make_float2(uv[0], uv[1]);
+        bw[r] = 1e-8f;
+        const float* t = p.t[r];
+        const float pn3[3] = {fsub(fmul(p.dmin, uf[0]), t[0]), fsub(fmul(p.dmin, uf[1]), t[1]),
+                              fsub(fmul(p.dmin, uf[2]), t[2])};
+        const float pf3[3] = {fsub(fmul(p.dmax, uf[0]), t[0]), fsub(fmul(p.dmax, uf[1]), t[1]),
+                              fsub(fmul(p.dmax, uf[2]), t[2])};
+        float pn[2], pf[2];
+        project_cu(pn3, p.k[r], pn, &valid);
+        pn[0] = fminf(fmaxf(pn[0], 0.1f), colsm);
+        pn[1] = fadd((float)(r * p.rows), fminf(fmaxf(pn[1], 0.1f), rowsm));
+        project_cu(pf3, p.k[r], pf, &valid);
+        pf[0] = fminf(fmaxf(pf[0], 0.1f), colsm);
+        pf[1] = fadd((float)(r * p.rows), fminf(fmaxf(pf[1], 0.1f), rowsm));
+        if (valid && (double)interp_f(masks, pn[0], pn[1], p.cols) > 0.99 &&
+            (double)interp_f(masks, pf[0], pf[1], p.cols) > 0.99) {
+            const float s = hypotf(fsub(pf[0], pn[0]), fsub(pf[1], pn[1]));
+            const double e = __ddiv_rn((double)fmul(-s, s), 1e-4 * p.rows * p.cols);
+            bw[r] = cw_expf((float)e);
+        }
+        sum = fadd(sum, bw[r]);
+    }
+    for (int r = 0; r < p.nref; ++r) weights[(int64_t)r * Q + i] = fdiv(bw[r], sum);
+}
+
+// python/stitcher.py:164: weights /= sum over references
+__global__ void __launch_bounds__(kStitchBlock) normalize_weights_kernel(float* __restrict__ w, int nref, int64_t Q)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q) return;
+    float s = w[i];
+    for (int r = 1; r < nref; ++r) s = fadd(s, w[(int64_t)r * Q + i]);
+    for (int r = 0; r < nref; ++r) w[(int64_t)r * Q + i] = fdiv(w[(int64_t)r * Q + i], s);
+}
+
+__global__ void __launch_bounds__(kStitchBlock) fill_kernel(float* __restrict__ out, int64_t n, float v)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = v;
+}
+
+// reprojectDistanceKernel, stitcher.cu:181-204, as a z-buffer on the float bits
+__global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const float* __restrict__ din,
+                                                                 float* __restrict__ dout, int cols, int rows, Intr k,
+                                                                 float tx, float ty, float tz)
+{
+    const int64_t P = (int64_t)cols * rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    float pt[3];
+    unproject_cu((float)(i % cols), (float)(i / cols), k, pt);
+    const float d = din[i];
+    pt[0] = fsub(fmul(d, pt[0]), tx);
+    pt[1] = fsub(fmul(d, pt[1]), ty);
+    pt[2] = fsub(fmul(d, pt[2]), tz);
+    float o[2];
+    project_cu(pt, k, o, nullptr);
+    const float dist = norm3df(pt[0], pt[1], pt[2]);
+    // __float2int_rn(y) * COLS + __float2int_rn(x) in 32-bit wrap-around arithmetic
+    const int idx = (int)((unsigned)__float2int_rn(o[1]) * (unsigned)cols + (unsigned)__float2int_rn(o[0]));
+    if (idx < 0 || (int64_t)idx >= P || !(dist >= 0.0f)) return;
+    atomicMin(reinterpret_cast<int*>(dout) + idx, __float_as_int(dist));
+}
+
+// Tiled Jacobi inpainting: kTileW x kTileH outputs, a halo of kHalo >= steps pixels.
+constexpr int kTileW = 64, kTileH = 32, kHalo = 16;
+constexpr int kRegW = kTileW + 2 * kHalo, kRegH = kTileH + 2 * kHalo;
+constexpr int kInpaintBlock = 512;
+constexpr size_t kInpaintSmem = sizeof(float) * 2 * kRegW * kRegH + sizeof(uchar2) * kRegW * kRegH;
+
+__global__ void __launch_bounds__(kInpaintBlock) inpaint_tile_kernel(const float* __restrict__ src,
+                                                                     float* __restrict__ dst,
+                                                                     const uchar2* __restrict__ table, int cols,
+                                                                     int rows, int steps, float hole_at_least,
+                                                                     float valid_at_most)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* buf0 = reinterpret_cast<float*>(smem);
+    float* buf1 = buf0 + kRegW * kRegH;
+    uchar2* tab = reinterpret_cast<uchar2*>(buf1 + kRegW * kRegH);
+    const int ox = blockIdx.x * kTileW - kHalo, oy = blockIdx.y * kTileH - kHalo;
+    for (int j = threadIdx.x; j < kRegW * kRegH; j += blockDim.x) {
+        const int x = ox + j % kRegW, y = oy + j / kRegW;
+        const bool in = x >= 0 && x < cols && y >= 0 && y < rows;
+        const int64_t g = (int64_t)y * cols + x;
+        buf0[j] = in ? src[g] : 0.0f;
+        tab[j] = in ? table[g] : make_uchar2(0, 0);
+    }
+    __syncthreads();
+    float* cur = buf0;
+    float* nxt = buf1;
+    for (int s = 0; s < steps; ++s) {
+        for (int j = threadIdx.x; j < kRegW * kRegH; j += blockDim.x) {
+            const float v = cur[j];
+            float out = v;
+            const int lx = j % kRegW, ly = j / kRegW;
+            const int x = ox + lx, y = oy + ly;
+            // hole test of stitcher.cu:287 and the interior test of :291; neighbours must lie
+            // inside the region (pixels whose neighbours do not are farther than `steps` from
+            // the tile's outputs and never reach them)
+            if (v >= hole_at_least && x >= 1 && y >= 1 && x < cols - 1 && y < rows - 1 && lx >= 1 && ly >= 1 &&
+                lx < kRegW - 1 && ly < kRegH - 1) {
+                const uchar2 t = tab[j];
+                const int n0 = j + ((t.x & 12) / 4 - 1) * kRegW + ((t.x & 3) - 1);
+                const int n1 = j + ((t.y & 12) / 4 - 1) * kRegW + ((t.y & 3) - 1);
+                // an offset field of 3 (a step of 2) never comes out of the table kernel; such a
+                // neighbour is ignored instead of read outside the 3x3 neighbourhood
+                const bool ok0 = (t.x & 3) != 3 && (t.x & 12) != 12, ok1 = (t.y & 3) != 3 && (t.y & 12) != 12;
+                const float w0 = ok0 ? (float)(t.x & 240) : 0.0f, w1 = ok1 ? (float)(t.y & 240) : 0.0f;
+                float val = 0.0f, ws = 0.0f;
+                if (w0 > 0.0f) {
+                    const float sd = cur[n0];
+                    if (sd <= valid_at_most) {
+                        val = fadd(val, fmul(w0, sd));
+                        ws = fadd(ws, w0);
+                    }
+                }
+                if (w1 > 0.0f) {
+                    const float sd = cur[n1];
+                    if (sd <= valid_at_most) {
+                        val = fadd(val, fmul(w1, sd));
+                        ws = fadd(ws, w1);
+                    }
+                }
+                if (ws > 0.0f) out = fdiv(val, ws);
+            }
+            nxt[j] = out;
+        }
+        __syncthreads();
+        float* tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    for (int j = threadIdx.x; j < kTileW * kTileH; j += blockDim.x) {
+        const int lx = kHalo + j % kTileW, ly = kHalo + j / kTileW;
+        const int x = ox + lx, y = oy + ly;
+        if (x < cols && y < rows) dst[(int64_t)y * cols + x] = cur[ly * kRegW + lx];
+    }
+}
+
+struct MergeParams {
+    int cols, rows, pano_cols, pano_rows, nref, image_rows, image_cols;
+    float ratio_x, ratio_y;
+    Intr k[SSG_MAX_REFERENCES];
+    float t[SSG_MAX_REFERENCES][3];
+};
+
+// interp (stitcher.cu:56-83) on uint8 RGB
+__device__ __forceinline__ void interp_rgb(const uint8_t* __restrict__ img, float u, float v, int cols, float out[3])
+{
+    const int u1 = __float2int_rd(u), v1 = __float2int_rd(v), u2 = u1 + 1, v2 = v1 + 1;
+    const float w1 = fmul(fsub((float)u2, u), fsub((float)v2, v)), w2 = fmul(fsub((float)u2, u), fsub(v, (float)v1));
+    const float w3 = fmul(fsub(u, (float)u1), fsub((float)v2, v)), w4 = fmul(fsub(u, (float)u1), fsub(v, (float)v1));
+    const uint8_t* p1 = img + 3 * ((int64_t)v1 * cols + u1);
+    const uint8_t* p2 = img + 3 * ((int64_t)v2 * cols + u1);
+    const uint8_t* p3 = img + 3 * ((int64_t)v1 * cols + u2);
+    const uint8_t* p4 = img + 3 * ((int64_t)v2 * cols + u2);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+        out[ch] = fadd(fadd(fadd(fmul((float)p1[ch], w1), fmul((float)p2[ch], w2)), fmul((float)p3[ch], w3)),
+                       fmul((float)p4[ch], w4));
+}
+
+// mergeRGBDPanoramaKernel, stitcher.cu:423-473
+__global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_constant__ MergeParams p,
+                                                             const float2* __restrict__ lut,
+                                                             const float* __restrict__ weights,
+                                                             const float* __restrict__ reproj,
+                                                             const float* __restrict__ dists,
+                                                             const uint8_t* __restrict__ images,
+                                                             float* __restrict__ dist_pano,
+                                                             uint8_t* __restrict__ rgb_pano)
+{
+    const int64_t Q = (int64_t)p.pano_cols * p.pano_rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q) return;
+    float inv = 0.0f, rgb[3] = {0.0f, 0.0f, 0.0f};
+    const float colsm = fsub((float)p.image_cols, 1.1f), rowsm = fsub((float)p.image_rows, 1.1f);
+    for (int r = 0; r < p.nref; ++r) {
+        const float w = weights[(int64_t)r * Q + i];
+        const float2 uv = lut[(int64_t)r * Q + i];
+        const float vo = fadd(uv.y, (float)(r * p.rows));
+        const float rd = interp_f(reproj, uv.x, vo, p.cols);
+        inv = fadd(inv, fdiv(fmul(w, 1.0f), rd));
+        float dc = interp_f(dists, uv.x, vo, p.cols);
+        dc = fminf(rd, dc);
+        float pt[3];
+        unproject_cu(uv.x, uv.y, p.k[r], pt);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pt[a] = fadd(fmul(dc, pt[a]), p.t[r][a]);
+        float o[2];
+        project_cu(pt, p.k[r], o, nullptr);
+        o[0] = fmul(o[0], p.ratio_x);
+        o[1] = fmul(o[1], p.ratio_y);
+        o[0] = fminf(fmaxf(o[0], 0.1f), colsm);
+        o[1] = fminf(fmaxf(o[1], 0.1f), rowsm);
+        o[1] = fadd(o[1], (float)(r * p.image_rows));
+        float c[3];
+        interp_rgb(images, o[0], o[1], p.image_cols, c);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) rgb[ch] = fadd(rgb[ch], fmul(c[ch], w));
+    }
+    dist_pano[i] = fdiv(1.0f, inv);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) rgb_pano[3 * i + ch] = (uint8_t)__float2uint_rz(fminf(rgb[ch], 255.0f));
+}
+
+// smallest float f with (double)f >= v, and largest float f with (double)f <= v
+static float float_at_least(double v)
+{
+    float f = (float)v;
+    while ((double)f < v) f = std::nextafter(f, INFINITY);
+    while ((double)std::nextafter(f, -INFINITY) >= v) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+static float float_at_most(double v)
+{
+    float f = (float)v;
+    while ((double)f > v) f = std::nextafter(f, -INFINITY);
+    while ((double)std::nextafter(f, INFINITY) <= v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
+// The tile kernel needs more than 48 KB of dynamic shared memory: opt in once per device.
+static int enable_inpaint_smem()
+{
+    static std::atomic<uint64_t> done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return launch_status("cudaGetDevice");
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done.load() & bit) return SSG_OK;
+    const cudaError_t e =
+        cudaFuncSetAttribute(inpaint_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInpaintSmem);
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaFuncSetAttribute(inpaint_tile_kernel): %s", cudaGetErrorString(e));
+    done.fetch_or(bit);
+    return SSG_OK;
+}
+
+static int check_intrinsics(const ssg_intrinsics* k, int n)
+{
+    SSG_REQUIRE(k, "intrinsics must not be NULL");
+    for (int r = 0; r < n; ++r) {
+        SSG_REQUIRE(std::isfinite(k[r].xi) && std::isfinite(k[r].alpha) && k[r].alpha > 0.0f && k[r].alpha <= 1.0f,
+                    "intrinsics %d: xi must be finite and alpha in (0, 1]", r);
+        SSG_REQUIRE(k[r].fx != 0.0f && k[r].fy != 0.0f, "intrinsics %d: zero focal length", r);
+    }
+    return SSG_OK;
+}
+
+}  // namespace ssg
+
+using namespace ssg;
+
+extern "C" int ssg_inpainting_table(int cols, int rows, const ssg_intrinsics* intrinsics, const float* translation,
+                                    double min_dist, double max_dist, uint8_t* d_table, void* stream)
+{
+    SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
+    SSG_REQUIRE(translation && d_table, "null pointer");
+    if (int e = check_intrinsics(intrinsics, 1)) return e;
+    const int64_t P = (int64_t)cols * rows;
+    inpainting_table_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+        cols, rows, to_intr(*intrinsics), translation[0], translation[1], translation[2], (float)min_dist,
+        (float)max_dist, d_table);
+    return launch_status("inpainting_table_kernel");
+}
+
+extern "C" int ssg_box_filter(const float* d_in, int planes, int rows, int cols, int radius, float pad_value,
+                              float* d_out, void* stream)
+{
+    SSG_REQUIRE(d_in && d_out && d_in != d_out, "null or aliased pointers");
+    SSG_REQUIRE(planes > 0 && planes <= 65535 && rows > 0 && cols > 0 && radius >= 0, "invalid sizes");
+    const int64_t P = (int64_t)cols * rows;
+    const int side = 2 * radius + 1;
+    const float kw = 1.0f / (float)(side * side);
+    dim3 grid(grid_1d(P, kStitchBlock), planes);
+    box_filter_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(d_in, rows, cols, radius, pad_value, kw, d_out);
+    return launch_status("box_filter_kernel");
+}
+
+extern "C" int ssg_blending_lut(int cols, int rows, int pano_cols, int pano_rows, int reference_count,
+                                const ssg_intrinsics* intrinsics, const float* rotations, const float* translations,
+                                const float* d_masks, double min_dist, double max_dist, float* d_lut, float* d_weights,
+                                void* stream)
+{
+    SSG_REQUIRE(cols > 0 && rows > 0 && pano_cols > 0 && pano_rows > 0, "resolutions must be positive");
+    SSG_REQUIRE(reference_count >= 1 && reference_count <= SSG_MAX_REFERENCES, "reference_count %d outside [1, %d]",
+                reference_count, SSG_MAX_REFERENCES);
+    SSG_REQUIRE(rotations && translations && d_masks && d_lut && d_weights, "null pointer");
+    if (int e = check_intrinsics(intrinsics, reference_count)) return e;
+    LutParams p{};
+    p.cols = cols;
+    p.rows = rows;
+    p.pano_cols = pano_cols;
+    p.pano_rows = pano_rows;
+    p.nref = reference_count;
+    p.dmin = (float)min_dist;
+    p.dmax = (float)max_dist;
+    for (int r = 0; r < reference_count; ++r) {
+        p.k[r] = to_intr(intrinsics[r]);
+        std::memcpy(p.rot[r], rotations + 9 * r, sizeof(float) * 9);
+        std::memcpy(p.t[r], translations + 3 * r, sizeof(float) * 3);
+    }
+    const int64_t Q = (int64_t)pano_cols * pano_rows;
+    blending_lut_kernel<<<grid_1d(Q, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+        p, d_masks, reinterpret_cast<float2*>(d_lut), d_weights);
+    return launch_status("blending_lut_kernel");
+}
+
+extern "C" int ssg_normalize_weights(float* d_weights, int reference_count, int64_t pixels, void* stream)
+{
+    SSG_REQUIRE(d_weights, "null pointer");
+    SSG_REQUIRE(reference_count >= 1 && pixels >= 0, "invalid sizes");
+    if (pixels == 0) return SSG_OK;
+    normalize_weights_kernel<<<grid_1d(pixels, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+        d_weights, reference_count, pixels);
+    return launch_status("normalize_weights_kernel");
+}
+
+extern "C" int ssg_reproject_distance(const float* d_distance_in, float* d_distance_out, int cols, int rows,
+                                      const ssg_intrinsics* intrinsics, const float* translation, int fill,
+                                      void* stream)
+{
+    SSG_REQUIRE(d_distance_in && d_distance_out && translation, "null pointer");
+    SSG_REQUIRE(d_distance_in != d_distance_out, "input and output maps must differ");
+    SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
+    if (int e = check_intrinsics(intrinsics, 1)) return e;
+    const int64_t P = (int64_t)cols * rows;
+    if (fill) {
+        fill_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(d_distance_out, P, 1e8f);
+        if (int e = launch_status("fill_kernel")) return e;
+    }
+    reproject_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+        d_distance_in, d_distance_out, cols, rows, to_intr(*intrinsics), translation[0], translation[1],
+        translation[2]);
+    return launch_status("reproject_kernel");
+}
+
+extern "C" int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scratch, int cols, int rows,
+                           double max_dist, int iterations, void* stream)
+{
+    SSG_REQUIRE(d_distance && d_table && d_scratch && d_distance != d_scratch, "null or aliased pointer");
+    SSG_REQUIRE(cols > 0 && rows > 0 && iterations >= 0, "invalid sizes");
+    if (int e = enable_inpaint_smem()) return e;
+    // hole: distance >= MAX_DIST + 0.1 (double, stitcher.cu:287); usable neighbour:
+    // distance <= MAX_DIST + 0.1f (stitcher.cu:311)
+    const float hole = float_at_least(max_dist + 0.1);
+    const float ok = float_at_most(max_dist + (double)0.1f);
+    dim3 grid((cols + kTileW - 1) / kTileW, (rows + kTileH - 1) / kTileH);
+    float* a = d_distance;
+    float* b = d_scratch;
+    for (int done = 0; done < iterations;) {
+        const int steps = iterations - done < kHalo ? iterations - done : kHalo;
+        inpaint_tile_kernel<<<grid, kInpaintBlock, kInpaintSmem, as_stream(stream)>>>(
+            a, b, reinterpret_cast<const uchar2*>(d_table), cols, rows, steps, hole, ok);
+        if (int e = launch_status("inpaint_tile_kernel")) return e;
+        float* t = a;
+        a = b;
+        b = t;
+        done += steps;
+    }
+    if (a != d_distance) {
+        cudaError_t e = cudaMemcpyAsync(d_distance, a, sizeof(float) * (size_t)cols * rows, cudaMemcpyDeviceToDevice,
+                                        as_stream(stream));
+        if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemcpyAsync: %s", cudaGetErrorString(e));
+    }
+    return SSG_OK;
+}
+
+extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                                  const float* d_distances, const uint8_t* d_images, int image_rows, int image_cols,
+                                  const float* translations, const ssg_intrinsics* intrinsics, int reference_count,
+                                  int cols, int rows, int pano_cols, int pano_rows, float* d_distance_panorama,
+                                  uint8_t* d_rgb_panorama, void* stream)
+{
+    SSG_REQUIRE(d_lut && d_weights && d_reprojected && d_distances && d_images && translations &&
+                    d_distance_panorama && d_rgb_panorama,
+                "null pointer");
+    SSG_REQUIRE(cols > 1 && rows > 1 && pano_cols > 0 && pano_rows > 0 && image_rows > 1 && image_cols > 1,
+                "invalid sizes");
+    SSG_REQUIRE(reference_count >= 1 && reference_count <= SSG_MAX_REFERENCES, "reference_count %d outside [1, %d]",
+                reference_count, SSG_MAX_REFERENCES);
+    if (int e = check_intrinsics(intrinsics, reference_count)) return e;
+    MergeParams p{};
+    p.cols = cols;
+    p.rows = rows;
+    p.pano_cols = pano_cols;
+    p.pano_rows = pano_rows;
+    p.nref = reference_count;
+    p.image_rows = image_rows;
+    p.image_cols = image_cols;
+    p.ratio_x = (float)image_cols / (float)cols;
+    p.ratio_y = (float)image_rows / (float)rows;
+    for (int r = 0; r < reference_count; ++r) {
+        p.k[r] = to_intr(intrinsics[r]);
+        std::memcpy(p.t[r], translations + 3 * r, sizeof(float) * 3);
+    }
+    const int64_t Q = (int64_t)pano_cols * pano_rows;
+    merge_kernel<<<grid_1d(Q, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+        p, reinterpret_cast<const float2*>(d_lut), d_weights, d_reprojected, d_distances, d_images,
+        d_distance_panorama, d_rgb_panorama);
+    return launch_status("merge_kernel");
+}

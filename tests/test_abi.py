@@ -1,0 +1,76 @@
+"""The C ABI surface, without a GPU: the library loads, exports every function that
+include/sphere_stereo_gb300.h declares, the ctypes binding agrees with the header, and invalid
+arguments are rejected with an error code and a message before anything touches a device."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "sphere_stereo_gb300.h")
+
+
+def declared():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"SSG_API\s+([\w\s\*]+?)\b(ssg_\w+)\s*\(([^)]*)\)\s*;", text):
+        args = [a.strip() for a in m.group(3).split(",") if a.strip() and a.strip() != "void"]
+        out[m.group(2)] = args
+    return out
+
+
+def test_header_declares_the_abi():
+    decl = declared()
+    assert len(decl) >= 19
+    for name in ("ssg_sweep_cost", "ssg_isb_apply", "ssg_isb_upsample_select", "ssg_inpaint", "ssg_merge_panorama"):
+        assert name in decl
+
+
+def test_library_exports_every_declared_symbol(native):
+    for name in declared():
+        assert hasattr(native, name), name
+
+
+def test_binding_matches_header(ss):
+    decl = declared()
+    sigs = ss._native.SIGNATURES
+    assert set(sigs) == set(decl)
+    for name, args in decl.items():
+        assert len(sigs[name][1]) == len(args), name
+
+
+def test_version_and_limits(native, ss):
+    assert native.ssg_version() >= 100
+    out = (ctypes.c_int32 * 4)()
+    native.ssg_limits(out)
+    assert list(out) == [ss._native.MAX_CAMERAS, ss._native.MAX_CANDIDATES, ss._native.MAX_REFERENCES,
+                         ss._native.MAX_LEVELS]
+
+
+def test_invalid_arguments_rejected_without_a_device(native, ss):
+    N = ss._native
+    assert native.ssg_rgb_to_guide(None, 10, None, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "null" in N.last_error()
+    assert native.ssg_select_distance(None, 4, 10, None, None, None, None) == N.SSG_ERR_INVALID_ARGUMENT
+    # a 2x downsampling must halve the size
+    assert native.ssg_isb_downsample(1, 1, 10, 10, 1, 1, 8, 5, 3, 0.1, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "downsampling" in N.last_error()
+    # pyramid depth must match the image
+    ptrs = N.pointers([1] * 3)
+    assert native.ssg_isb_apply(ptrs, ptrs, 3, 64, 64, 4, 10.0, 25.0, None) == N.SSG_ERR_INVALID_ARGUMENT
+    cams = N.cameras_array([N.ssg_camera(100, 100, 32, 32, -0.2, 0.6)] * 2)
+    poses = N.floats([0.0] * 24)
+    assert native.ssg_sweep_cost(64, 64, 2, cams, 0, poses, N.pointers([1, 1]), 1, N.floats([1.0] * 3), 300, 1,
+                                 None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "candidate_count" in N.last_error()
+    bad = N.cameras_array([N.ssg_camera(100, 100, 32, 32, -0.2, 1.5)] * 2)
+    assert native.ssg_sweep_cost(64, 64, 2, bad, 0, poses, N.pointers([1, 1]), 1, N.floats([1.0] * 3), 3, 1,
+                                 None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "alpha" in N.last_error()
+    with pytest.raises(ValueError):
+        N.call("ssg_rgb_to_guide", None, 10, None, None)

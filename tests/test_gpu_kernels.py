@@ -1,0 +1,236 @@
+"""Per-kernel parity of the CUDA library against the C oracle, through the C ABI.
+
+The oracle runs with the library's exponential (exp_mode="device"), so every kernel whose only
+transcendental is that exponential must match bit for bit: guide, camera selection, sweep cost,
+ISB filter, distance selection, inpainting tables, box filter, inpainting.  The blending table
+calls sinf / cosf and the reprojection / merge norm3df / hypotf, whose last bit may differ
+between CUDA and libm; those are compared with tolerances stated per test.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda:0"
+
+
+def _t(a, dtype=None):
+    t = torch.as_tensor(np.ascontiguousarray(a), device=DEV)
+    return t if dtype is None else t.to(dtype)
+
+
+@pytest.fixture(scope="module")
+def dev_oracle(oracle_mod):
+    return oracle_mod.Oracle("f32", exp_mode="device")
+
+
+@pytest.fixture(scope="module")
+def small_rig(oracle_mod, golden_small):
+    g = golden_small
+    return oracle_mod.OracleRig(g["calibration"], masks=list(g["masks"]), exp_mode="device", **g["config"])
+
+
+def _estimator(ss, g):
+    cfg = g["config"]
+    calibs = ss.parse_json_calib(g["calibration"], cfg["matching_resolution"], DEV)
+    refs = cfg["references_indices"]
+    vp = torch.zeros(3, device=DEV)
+    for r in refs:
+        vp += calibs[r].rt[:3, 3] / len(refs)
+    masks = [_t(m)[None] for m in g["masks"]]
+    return ss.RGBD_Estimator(calibs, cfg["min_dist"], cfg["max_dist"], cfg["candidate_count"], refs, vp, masks,
+                             cfg["matching_resolution"], cfg["rgb_to_stitch_resolution"],
+                             cfg["panorama_resolution"], cfg["sigma_i"], cfg["sigma_s"], DEV)
+
+
+def test_rgb_to_guide_bit_exact(ss, native, dev_oracle):
+    rng = np.random.default_rng(1)
+    img = np.concatenate([rng.integers(0, 256, (64, 80, 3)).astype(np.float32),
+                          (rng.random((64, 80, 3)) * 255).astype(np.float32)])
+    out = ss.rgb_to_guide(_t(img)).cpu().numpy()
+    np.testing.assert_array_equal(out, dev_oracle.rgb2ycbcr(img))
+
+
+def test_select_camera_bit_exact(ss, native, small_rig, golden_small):
+    est = _estimator(ss, golden_small)
+    got = np.stack([s[0].cpu().numpy() for s in est.selected_cameras])
+    assert est.selected_cameras[0].dtype == torch.int64
+    np.testing.assert_array_equal(got, np.stack([small_rig.selected[r] for r in small_rig.refs]))
+    np.testing.assert_array_equal(got, golden_small["ref/selected_cameras"])
+
+
+def test_sweep_cost_bit_exact(ss, native, small_rig, golden_small):
+    est = _estimator(ss, golden_small)
+    g = golden_small
+    cols, rows = g["config"]["matching_resolution"]
+    images = [_t(im, torch.float32) for im in g["images_to_match"]]
+    N = ss._native
+    for slot, r in enumerate(small_rig.refs):
+        cost = torch.empty([g["config"]["candidate_count"], rows, cols], device=DEV)
+        N.call("ssg_sweep_cost", cols, rows, len(images), est._cams, r, est._poses[r],
+               N.pointers([im.data_ptr() for im in images]), est._selected[slot].data_ptr(), est._candidates,
+               cost.shape[0], cost.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        want = small_rig.o.sweep_cost(cols, rows, small_rig.cam6, r, small_rig.rts[r],
+                                      g["images_to_match"].astype(np.float32), small_rig.selected[r],
+                                      small_rig.candidates)
+        np.testing.assert_array_equal(cost.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("case", ["odd_37x29_n3", "even_64x48_n1", "odd_33x21_n32", "tall_40x71_n3"])
+def test_isb_filter(ss, native, dev_oracle, golden_isb, case):
+    guide, cost = golden_isb[f"{case}/guide"], golden_isb[f"{case}/cost"]
+    si, sg = (float(v) for v in golden_isb[f"{case}/sigma"])
+    n, rows, cols = cost.shape
+    filt = ss.ISB_Filter(n, (cols, rows), DEV)
+    c, gd = filt.apply(_t(guide), _t(cost), si, sg)
+    want_c, want_g = dev_oracle.isb_apply(guide, cost, si, sg)
+    np.testing.assert_array_equal(gd.cpu().numpy(), want_g)
+    np.testing.assert_array_equal(c.cpu().numpy(), want_c)
+    # against the reference itself (libm exponential): within float32 rounding
+    np.testing.assert_allclose(c.cpu().numpy(), golden_isb[f"{case}/filtered_cost"], rtol=1e-5, atol=1e-4)
+    assert (gd.cpu().numpy() == golden_isb[f"{case}/filtered_guide"]).mean() >= 0.999
+
+
+def _select(ss, cost, candidates, index=True):
+    n = cost.shape[0]
+    p = cost[0].numel()
+    dist = torch.empty(cost.shape[1:], device=DEV)
+    idx = torch.empty(cost.shape[1:], dtype=torch.int32, device=DEV)
+    N = ss._native
+    N.call("ssg_select_distance", cost.data_ptr(), n, p, N.floats(candidates), dist.data_ptr(),
+           idx.data_ptr() if index else None, torch.cuda.current_stream().cuda_stream)
+    return dist.cpu().numpy(), idx.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 32, 256])
+def test_select_distance_bit_exact(ss, native, dev_oracle, n):
+    rng = np.random.default_rng(n)
+    cost = (rng.random((n, 37, 53)) * 100).astype(np.float32)
+    cost[:, 0, :] = 7.0                        # flat costs: max == min
+    cost[:, 1, :] = np.round(cost[:, 1, :])    # frequent ties: the first minimum wins
+    cost[0, 2, :] = -1.0                       # argmin at the first candidate
+    cost[-1, 3, :] = -1.0                      # argmin at the last candidate
+    cand = ss.distance_candidates(0.55, 100.0, n).numpy()
+    d, i = _select(ss, _t(cost), cand)
+    wd, wi = dev_oracle.select_distance(cost, cand)
+    np.testing.assert_array_equal(i, wi)
+    np.testing.assert_array_equal(d, wd)
+    assert np.all(d[0] == cand[-1])
+
+
+def test_upsample_select_matches_two_steps(ss, native, golden_isb):
+    """The fused last level equals upsample-then-select, bit for bit."""
+    guide, cost = golden_isb["odd_33x21_n32/guide"], golden_isb["odd_33x21_n32/cost"]
+    n, rows, cols = cost.shape
+    shapes = [(rows, cols), ((rows + 1) // 2, (cols + 1) // 2)]
+    N = ss._native
+    st = torch.cuda.current_stream().cuda_stream
+    g0, c0 = _t(guide), _t(cost)
+    g1 = torch.empty([*shapes[1], 3], dtype=torch.uint8, device=DEV)
+    c1 = torch.empty([n, *shapes[1]], device=DEV)
+    N.call("ssg_isb_downsample", g0.data_ptr(), c0.data_ptr(), rows, cols, g1.data_ptr(), c1.data_ptr(), *shapes[1],
+           n, 0.005, st)
+    cand = ss.distance_candidates(0.55, 100.0, n).numpy()
+    dist = torch.empty([rows, cols], device=DEV)
+    idx = torch.empty([rows, cols], dtype=torch.int32, device=DEV)
+    g0b = g0.clone()
+    N.call("ssg_isb_upsample_select", g1.data_ptr(), c1.data_ptr(), *shapes[1], g0b.data_ptr(), c0.data_ptr(), rows,
+           cols, n, 0.6, 0.4, 0.005, N.floats(cand), dist.data_ptr(), idx.data_ptr(), st)
+    c0b = c0.clone()
+    N.call("ssg_isb_upsample", g1.data_ptr(), c1.data_ptr(), *shapes[1], g0.data_ptr(), c0b.data_ptr(), rows, cols, n,
+           0.6, 0.4, 0.005, st)
+    d2, i2 = _select(ss, c0b, cand)
+    np.testing.assert_array_equal(g0b.cpu().numpy(), g0.cpu().numpy())
+    np.testing.assert_array_equal(idx.cpu().numpy(), i2)
+    np.testing.assert_array_equal(dist.cpu().numpy(), d2)
+    np.testing.assert_array_equal(c0.cpu().numpy(), cost)  # the fine cost is read, never written
+
+
+def test_stitcher_tables(ss, native, small_rig, golden_small):
+    est = _estimator(ss, golden_small)
+    st = est.fishey_stitcher
+    tables = np.stack([t.cpu().numpy() for t in st.inpainting_weights_list])
+    np.testing.assert_array_equal(tables, small_rig.tables)
+    np.testing.assert_array_equal(st.translations.cpu().numpy(), small_rig.ts.reshape(-1))
+    # blending table: sinf / cosf may differ in the last bit from libm
+    np.testing.assert_allclose(st.blending_sampling.cpu().numpy(), small_rig.blending_lut, rtol=0, atol=1e-3)
+    np.testing.assert_allclose(st.blending_weights.cpu().numpy(), small_rig.blending_weights, rtol=0, atol=1e-5)
+
+
+@pytest.mark.parametrize("radius,pad", [(15, 1.0), (3, 0.0)])
+def test_box_filter_bit_exact(ss, native, dev_oracle, radius, pad):
+    rng = np.random.default_rng(radius)
+    img = rng.random((2, 45, 70)).astype(np.float32)
+    out = torch.empty(img.shape, device=DEV)
+    src = _t(img)
+    ss._native.call("ssg_box_filter", src.data_ptr(), 2, 45, 70, radius, pad, out.data_ptr(),
+                    torch.cuda.current_stream().cuda_stream)
+    want = np.stack([dev_oracle.box_filter(p, radius, pad) for p in img])
+    np.testing.assert_array_equal(out.cpu().numpy(), want)
+
+
+def test_reproject_and_inpaint(ss, native, small_rig, golden_small):
+    est = _estimator(ss, golden_small)
+    st = est.fishey_stitcher
+    dists = golden_small["ref/distance_filtered"]
+    N = ss._native
+    stream = torch.cuda.current_stream().cuda_stream
+    for r in range(len(small_rig.refs)):
+        d = _t(dists[r])
+        out = torch.empty_like(d)
+        N.call("ssg_reproject_distance", d.data_ptr(), out.data_ptr(), st.cols, st.rows,
+               N.intrinsics_array([st.intrinsics[r]]), N.floats(st.translations_host[3 * r:3 * r + 3].tolist()), 1,
+               stream)
+        want = small_rig.o.reproject(dists[r], small_rig.ks[r], small_rig.ts[r])
+        got = out.cpu().numpy()
+        # norm3df may differ from the correctly rounded norm in the last bit
+        assert (got == want).mean() >= 0.999
+        np.testing.assert_allclose(got, want, rtol=1e-6)
+        # inpainting from identical input: bit-exact (Jacobi steps, tiled)
+        src = _t(want)
+        N.call("ssg_inpaint", src.data_ptr(), st.inpainting_weights_list[r].data_ptr(),
+               st.inpainting_scratch.data_ptr(), st.cols, st.rows, st.max_dist, 32, stream)
+        np.testing.assert_array_equal(src.cpu().numpy(),
+                                      small_rig.o.inpaint(want, small_rig.tables[r], st.max_dist, 32))
+
+
+@pytest.mark.parametrize("iterations", [0, 1, 5, 16, 17, 40])
+def test_inpaint_iteration_counts(ss, native, dev_oracle, iterations):
+    """Tiled passes of up to 16 Jacobi steps equal one step per launch, at any count, on a map
+    larger than one tile with wide holes."""
+    rng = np.random.default_rng(iterations)
+    H, W = 83, 150
+    d = (1 + rng.random((H, W)) * 5).astype(np.float32)
+    d[10:70, 30:90] = 1e8
+    d[rng.random((H, W)) < 0.2] = 1e8
+    table = rng.integers(0, 256, (H, W, 2)).astype(np.uint8)
+    src = _t(d)
+    scratch = torch.empty_like(src)
+    tab = _t(table)
+    ss._native.call("ssg_inpaint", src.data_ptr(), tab.data_ptr(), scratch.data_ptr(), W, H, 100.0, iterations,
+                    torch.cuda.current_stream().cuda_stream)
+    np.testing.assert_array_equal(src.cpu().numpy(), dev_oracle.inpaint(d, table, 100.0, iterations))
+
+
+def test_merge_from_identical_inputs(ss, native, small_rig, golden_small):
+    est = _estimator(ss, golden_small)
+    st = est.fishey_stitcher
+    g = golden_small
+    reproj = g["ref/reprojected_distances"]
+    dists = g["ref/distance_filtered"]
+    images = g["images_to_stitch"]
+    st.blending_sampling.copy_(_t(small_rig.blending_lut))
+    st.blending_weights.copy_(_t(small_rig.blending_weights))
+    st.reprojected_distances.copy_(_t(reproj))
+    st.distances_stacked.copy_(_t(dists))
+    st.images_to_stitch.copy_(_t(images))
+    st.merge()
+    want_d, want_rgb = small_rig.o.merge(small_rig.blending_lut, small_rig.blending_weights, reproj, dists, images,
+                                         small_rig.ts, small_rig.ks)
+    from conftest import psnr
+
+    assert psnr(st.RGB_panorama.cpu().numpy(), want_rgb) >= 60
+    np.testing.assert_allclose(st.distance_panorama.cpu().numpy(), want_d, rtol=1e-5)

@@ -1,0 +1,136 @@
+"""RGBD_Estimator end to end on the GPU, against the oracle and against the reference's own
+outputs (golden vectors), with the acceptance bars of the task:
+  * >= 99.9 % of pixels select the same candidate index as the reference;
+  * inverse-distance MAE <= 1e-4 of the inverse-distance range (distance maps and panorama);
+  * panorama RGB PSNR >= 50 dB.
+Against the oracle in device-exponential mode the distance maps are bit-identical.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import inverse_distance_mae, psnr
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def _build(ss, g, **override):
+    cfg = {**g["config"], **override}
+    calibs = ss.parse_json_calib(g["calibration"], cfg["matching_resolution"], DEV)
+    refs = cfg["references_indices"]
+    vp = torch.zeros(3, device=DEV)
+    for r in refs:
+        vp += calibs[r].rt[:3, 3] / len(refs)
+    masks = [torch.as_tensor(m, device=DEV)[None] for m in g["masks"]]
+    est = ss.RGBD_Estimator(calibs, cfg["min_dist"], cfg["max_dist"], cfg["candidate_count"], refs, vp, masks,
+                            cfg["matching_resolution"], cfg["rgb_to_stitch_resolution"], cfg["panorama_resolution"],
+                            cfg["sigma_i"], cfg["sigma_s"], DEV)
+    return est, cfg
+
+
+def _run(est, g):
+    match = [torch.as_tensor(im, device=DEV).float() for im in g["images_to_match"]]
+    stitch = [torch.as_tensor(im, device=DEV).float() for im in g["images_to_stitch"]]
+    rgb, dist = est.estimate_RGBD_panorama(match, stitch)
+    torch.cuda.synchronize()
+    return rgb.cpu().numpy(), dist.cpu().numpy()
+
+
+def _index(d, candidates):
+    """Nearest candidate index of a distance before the post-filter: the inverse of
+    python/depth_estimation.py:196-197 (idx + step with |step| <= 0.5)."""
+    d0, dl, n = float(candidates[0]), float(candidates[-1]), len(candidates)
+    sel = (d0 / np.asarray(d, np.float64) - 1) * (n - 1) / (d0 / dl - 1)
+    return np.rint(sel).astype(np.int64)
+
+
+@pytest.mark.parametrize("name", ["small", "c1"])
+def test_pipeline_against_oracle_and_reference(ss, native, oracle_mod, golden_small, golden_c1, name):
+    g = golden_small if name == "small" else golden_c1
+    est, cfg = _build(ss, g)
+    rgb, dist = _run(est, g)
+    rig = oracle_mod.OracleRig(g["calibration"], masks=list(g["masks"]), exp_mode="device", **g["config"])
+    ref = rig.estimate([im.astype(np.float32) for im in g["images_to_match"]],
+                       [im.astype(np.float32) for im in g["images_to_stitch"]], keep_intermediates=True)
+    raw = est.distance_raw_maps.cpu().numpy()
+    filtered = est.fishey_stitcher.distances_stacked.cpu().numpy()
+    # oracle with the device exponential: identical arithmetic
+    np.testing.assert_array_equal(raw, ref["distance_raw"])
+    np.testing.assert_array_equal(filtered, ref["distance_filtered"])
+    inv_range = 1 / cfg["min_dist"] - 1 / cfg["max_dist"]
+    assert psnr(rgb, ref["rgb_panorama"]) >= 50
+    assert inverse_distance_mae(dist, ref["distance_panorama"]) <= 1e-4 * inv_range
+    # the reference's own outputs
+    cand = g["ref/candidates"]
+    ref_raw = g["ref/distance_raw"][:, 0]
+    same_index = (_index(raw, cand) == _index(ref_raw, cand)).mean()
+    assert same_index >= 0.999, same_index
+    assert inverse_distance_mae(raw, ref_raw) <= 1e-4 * inv_range
+    assert inverse_distance_mae(filtered, g["ref/distance_filtered"]) <= 1e-4 * inv_range
+    assert psnr(rgb, g["ref/rgb_panorama"]) >= 50
+    assert inverse_distance_mae(dist, g["ref/distance_panorama"]) <= 1e-4 * inv_range
+
+
+def test_deterministic_and_reusable(ss, native, golden_small):
+    est, _ = _build(ss, golden_small)
+    rgb1, d1 = _run(est, golden_small)
+    rgb2, d2 = _run(est, golden_small)
+    np.testing.assert_array_equal(rgb1, rgb2)
+    np.testing.assert_array_equal(d1, d2)
+
+
+@pytest.mark.parametrize("n", [1, 2, 256])
+def test_candidate_count_extremes(ss, native, oracle_mod, golden_small, n):
+    g = golden_small
+    est, cfg = _build(ss, g, candidate_count=n)
+    _run(est, g)
+    rig = oracle_mod.OracleRig(g["calibration"], masks=list(g["masks"]), exp_mode="device",
+                               **{**g["config"], "candidate_count": n})
+    ref = rig.estimate([im.astype(np.float32) for im in g["images_to_match"]],
+                       [im.astype(np.float32) for im in g["images_to_stitch"]], keep_intermediates=True)
+    np.testing.assert_array_equal(est.distance_raw_maps.cpu().numpy(), ref["distance_raw"])
+    np.testing.assert_array_equal(est.fishey_stitcher.distances_stacked.cpu().numpy(), ref["distance_filtered"])
+
+
+def test_single_reference_and_all_references(ss, native, oracle_mod, golden_small):
+    g = golden_small
+    for refs in ([1], [0, 1, 2, 3]):
+        gg = dict(g)
+        gg["images_to_stitch"] = np.stack([np.full((100, 120, 3), 40 * (r + 1), np.uint8) for r in refs])
+        est, cfg = _build(ss, gg, references_indices=refs)
+        rgb, dist = _run(est, gg)
+        assert np.isfinite(dist).all() and dist.min() > 0
+        rig = oracle_mod.OracleRig(g["calibration"], masks=list(g["masks"]), exp_mode="device",
+                                   **{**g["config"], "references_indices": refs})
+        ref = rig.estimate([im.astype(np.float32) for im in g["images_to_match"]],
+                           [im.astype(np.float32) for im in gg["images_to_stitch"]])
+        np.testing.assert_array_equal(est.fishey_stitcher.distances_stacked.cpu().numpy(), ref["distance_filtered"])
+        assert psnr(rgb, ref["rgb_panorama"]) >= 50
+
+
+def test_invalid_inputs_rejected_before_launch(ss, native, golden_small):
+    g = golden_small
+    est, cfg = _build(ss, g)
+    cols, rows = cfg["matching_resolution"]
+    good = [torch.as_tensor(im, device=DEV).float() for im in g["images_to_match"]]
+    stitch = [torch.as_tensor(im, device=DEV).float() for im in g["images_to_stitch"]]
+    with pytest.raises(TypeError):
+        est.estimate_RGBD_panorama([im.double() for im in good], stitch)
+    with pytest.raises(ValueError):
+        est.estimate_RGBD_panorama(good[:3], stitch)
+    with pytest.raises(ValueError):
+        est.estimate_RGBD_panorama([im[:, :-1].contiguous() for im in good], stitch)
+    with pytest.raises(ValueError):
+        est.estimate_RGBD_panorama([im.cpu() for im in good], stitch)
+    with pytest.raises(ValueError):
+        est.estimate_RGBD_panorama([im.transpose(0, 1) for im in good], stitch)
+    with pytest.raises(ValueError):
+        _build(ss, g, candidate_count=257)
+    filt = ss.ISB_Filter(3, (cols, rows), DEV)
+    with pytest.raises(ValueError):
+        filt.apply(torch.zeros([rows, cols, 3], dtype=torch.uint8, device=DEV), torch.zeros([2, rows, cols], device=DEV),
+                   10.0, 25.0)
+    torch.cuda.synchronize()
