@@ -310,7 +310,11 @@ __global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_consta
     const float colsm = fsub((float)p.image_cols, 1.1f), rowsm = fsub((float)p.image_rows, 1.1f);
     for (int r = 0; r < p.nref; ++r) {
         const float w = weights[(int64_t)r * Q + i];
-        const float2 uv = lut[(int64_t)r * Q + i];
+        float2 uv = lut[(int64_t)r * Q + i];
+        // the table kernel already clamps to [0.1, size - 1.1]; clamping again is exact for its
+        // output and keeps any other table inside the maps
+        uv.x = fminf(fmaxf(uv.x, 0.1f), fsub((float)p.cols, 1.1f));
+        uv.y = fminf(fmaxf(uv.y, 0.1f), fsub((float)p.rows, 1.1f));
         const float vo = fadd(uv.y, (float)(r * p.rows));
         const float rd = interp_f(reproj, uv.x, vo, p.cols);
         inv = fadd(inv, fdiv(fmul(w, 1.0f), rd));

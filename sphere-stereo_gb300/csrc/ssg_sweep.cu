@@ -68,8 +68,9 @@ __global__ void __launch_bounds__(kBlock) sweep_cost_kernel(const __grid_constan
     const float* refimg = p.images[p.reference] + 3 * i;
     const float r0 = __ldg(refimg), r1 = __ldg(refimg + 1), r2 = __ldg(refimg + 2);
     const int sel = selected[i];
-    if (sel < 0) {
-        // no camera: the sweeping volume stays zero (depth_estimation.py:150-152)
+    if (sel < 0 || sel >= p.ncam) {
+        // no camera: the sweeping volume stays zero (depth_estimation.py:150-152); a selection
+        // outside [0, cameras) is treated the same way instead of indexing past the camera arrays
         float c = fadd(fadd(fabsf(r0), fabsf(r1)), fabsf(r2));
         c = c > 500.0f ? 500.0f : c;
         for (int k = 0; k < p.ncand; ++k) cost[(int64_t)k * P + i] = c;
