@@ -93,7 +93,7 @@ def run_pipeline(ref, calibration: dict, images_to_match, images_to_stitch, mask
                                 list(panorama_resolution), sigma_i, sigma_s, device)
 
     rec = {"guide": [], "cost_raw": [], "cost_filtered": [], "distance_raw": [], "distance_filtered": [],
-           "guide_filtered_cost": [], "guide_filtered_distance": []}
+           "guide_filtered_cost": [], "guide_filtered_distance": [], "index": []}
     cost_apply, dist_apply = est.cost_filter.apply, est.distance_filter.apply
 
     def cost_wrap(guide, cost, si, ss):
@@ -101,6 +101,8 @@ def run_pipeline(ref, calibration: dict, images_to_match, images_to_stitch, mask
         rec["cost_raw"].append(cost.numpy().copy())
         c, g = cost_apply(guide, cost, si, ss)
         rec["cost_filtered"].append(c.numpy().copy())
+        # the selected candidate index, by the reference's own reduction (depth_estimation.py:180)
+        rec["index"].append(torch.min(c, dim=0, keepdim=True)[1][0].numpy().astype(np.int16))
         rec["guide_filtered_cost"].append(g.numpy().copy())
         return c, g
 

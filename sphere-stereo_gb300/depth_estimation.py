@@ -98,6 +98,8 @@ class RGBD_Estimator:
         self._guide0 = self.cost_filter.guides[0]
         # per reference: the distance map before the post-filter (depth_estimation.py:196-198)
         self.distance_raw_maps = torch.empty([len(self.references_indices), rows, cols], device=device)
+        # per reference: the selected candidate index (torch.min's index, depth_estimation.py:180)
+        self.index_maps = torch.empty([len(self.references_indices), rows, cols], dtype=torch.int32, device=device)
         self.select_camera(masks)
 
     # --------------------------------------------------------------------------------------
@@ -156,10 +158,10 @@ class RGBD_Estimator:
             wu, wd = weights[0]
             N.call("ssg_isb_upsample_select", guides[1].data_ptr(), costs[1].data_ptr(), rc, cc,
                    guides[0].data_ptr(), cost.data_ptr(), rows, cols, n, wu, wd, var_inv_i, self._candidates,
-                   raw.data_ptr(), None, stream)
+                   raw.data_ptr(), self.index_maps[slot].data_ptr(), stream)
         else:
-            N.call("ssg_select_distance", cost.data_ptr(), n, rows * cols, self._candidates, raw.data_ptr(), None,
-                   stream)
+            N.call("ssg_select_distance", cost.data_ptr(), n, rows * cols, self._candidates, raw.data_ptr(),
+                   self.index_maps[slot].data_ptr(), stream)
         # distance post-filter with higher edge preservation (python/depth_estimation.py:200-203)
         df = self.distance_filter
         df.guides[0].copy_(guide)

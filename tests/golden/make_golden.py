@@ -87,7 +87,7 @@ def make_pipeline(ref, cfg, filename, keep_volumes):
         "images_to_stitch": np.stack(frame.images_to_stitch),
         "masks": np.stack(masks),
     }
-    keep = ["rgb_panorama", "distance_panorama", "selected_cameras", "candidates", "distance_raw",
+    keep = ["rgb_panorama", "distance_panorama", "selected_cameras", "candidates", "index", "distance_raw",
             "distance_filtered", "guide", "translations", "calibration_vectors", "viewpoint"]
     if keep_volumes:
         keep += ["cost_raw", "cost_filtered", "blending_sampling", "guide_filtered_cost", "guide_filtered_distance",

@@ -39,14 +39,6 @@ def _run(est, g):
     return rgb.cpu().numpy(), dist.cpu().numpy()
 
 
-def _index(d, candidates):
-    """Nearest candidate index of a distance before the post-filter: the inverse of
-    python/depth_estimation.py:196-197 (idx + step with |step| <= 0.5)."""
-    d0, dl, n = float(candidates[0]), float(candidates[-1]), len(candidates)
-    sel = (d0 / np.asarray(d, np.float64) - 1) * (n - 1) / (d0 / dl - 1)
-    return np.rint(sel).astype(np.int64)
-
-
 @pytest.mark.parametrize("name", ["small", "c1"])
 def test_pipeline_against_oracle_and_reference(ss, native, oracle_mod, golden_small, golden_c1, name):
     g = golden_small if name == "small" else golden_c1
@@ -64,9 +56,9 @@ def test_pipeline_against_oracle_and_reference(ss, native, oracle_mod, golden_sm
     assert psnr(rgb, ref["rgb_panorama"]) >= 50
     assert inverse_distance_mae(dist, ref["distance_panorama"]) <= 1e-4 * inv_range
     # the reference's own outputs
-    cand = g["ref/candidates"]
+    np.testing.assert_array_equal(est.index_maps.cpu().numpy(), ref["index"])
     ref_raw = g["ref/distance_raw"][:, 0]
-    same_index = (_index(raw, cand) == _index(ref_raw, cand)).mean()
+    same_index = (est.index_maps.cpu().numpy() == g["ref/index"]).mean()
     assert same_index >= 0.999, same_index
     assert inverse_distance_mae(raw, ref_raw) <= 1e-4 * inv_range
     assert inverse_distance_mae(filtered, g["ref/distance_filtered"]) <= 1e-4 * inv_range
