@@ -41,6 +41,10 @@ enum {
     SSG_ERR_UNSUPPORTED = 3       /* a size beyond a documented compile-time limit */
 };
 
+/* 16-bit cost storage of the batched path (the fp32 path keeps float32). */
+#define SSG_STORAGE_F16 0     /* IEEE half */
+#define SSG_STORAGE_UNORM16 1 /* uint16 q = round(cost * 65535 / 500), costs being in [0, 500] */
+
 /* Compile-time limits (also reported by ssg_limits). */
 #define SSG_MAX_CAMERAS 16
 #define SSG_MAX_CANDIDATES 256
@@ -189,6 +193,81 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
                        const float* translations, const ssg_intrinsics* intrinsics, int reference_count, int cols,
                        int rows, int pano_cols, int pano_rows, float* d_distance_panorama, uint8_t* d_rgb_panorama,
                        void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched path.  A batch holds `frames` frames of one rig; an "instance" is a (frame, reference
+ * slot) pair, instance = frame * references + slot.  Buffers of a batch are contiguous arrays of
+ * equally sized per-frame / per-instance blocks.  The per-frame steps are those of
+ * RGBD_Estimator.estimate_RGBD_panorama (python/depth_estimation.py:205-242); these entry
+ * points have no single counterpart in the reference, which processes one frame and one
+ * reference camera per call.
+ *
+ * Cost volumes of the batched path are stored with 16 bits per candidate (SSG_STORAGE_*) in
+ * chunks of 8 candidates: per instance and level [ceil(N / 8)][pixels][8], all arithmetic fp32.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Image staging + guides: d_images frames x cameras x pixels x 3 float32 (the inputs of
+ * estimate_RGBD_panorama, python/depth_estimation.py:205-227) -> d_staged frames x cameras x
+ * pixels float4 (RGB, 0) and d_guides frames x references x pixels x 3 uint8 (rgb2yCbCr + uint8
+ * cast of each reference camera, python/utils.py:144-155). */
+SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int64_t pixels,
+                             const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
+                             void* stream);
+
+/* Sphere sweep + cost for every instance (python/depth_estimation.py:141-175), 16-bit output.
+ * relative_poses: references x cameras x 12 floats (host); d_selected: references x pixels
+ * int8; d_cost: instances x level-0 volume. */
+SSG_API int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_count, const ssg_camera* cameras,
+                                 int references, const int* reference_cameras, const float* relative_poses,
+                                 const float* d_staged, const int8_t* d_selected, const float* candidates,
+                                 int candidate_count, int storage, void* d_cost, void* stream);
+
+/* ISB down / up steps (python/isb_filter.cu:44-329) on `instances` contiguous levels. */
+SSG_API int ssg_isb_downsample_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
+                                     uint8_t* d_guide_out, void* d_cost_out, int rows_out, int cols_out,
+                                     int candidate_count, int instances, int storage, float var_inv_i, void* stream);
+SSG_API int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
+                                   uint8_t* d_guide_inout, void* d_cost_inout, int rows_inout, int cols_inout,
+                                   int candidate_count, int instances, int storage, float weight_up, float weight_down,
+                                   float var_inv_i, void* stream);
+
+/* Last ISB level fused with distance selection (python/isb_filter.cu:132-329 +
+ * python/depth_estimation.py:179-198): d_distance / d_index instances x fine pixels. */
+SSG_API int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
+                                          uint8_t* d_guide_inout, const void* d_cost_fine, int rows_fine,
+                                          int cols_fine, int candidate_count, int instances, int storage,
+                                          float weight_up, float weight_down, float var_inv_i,
+                                          const float* candidates, float* d_distance, int32_t* d_index, void* stream);
+
+/* Distance selection from a level-0 volume (pyramids of fewer than two levels). */
+SSG_API int ssg_select_distance_batch(const void* d_cost, int candidate_count, int64_t pixels, int instances,
+                                      int storage, const float* candidates, float* d_distance, int32_t* d_index,
+                                      void* stream);
+
+/* ISB_Filter.apply (python/isb_filter.py:72-136) on `instances` contiguous float32 pyramids:
+ * level l holds instances x (guide ceil(rows/2^l) x ceil(cols/2^l) x 3) and instances x
+ * (candidate_count x ... ) costs. */
+SSG_API int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
+                                int candidate_count, int instances, double sigma_i, double sigma_s, void* stream);
+
+/* Reprojection (python/stitcher.cu:181-204) of `instances` distance maps; instance i uses
+ * intrinsics / translation of slot i % references. */
+SSG_API int ssg_reproject_distance_batch(const float* d_distance_in, float* d_distance_out, int cols, int rows,
+                                         int instances, int references, const ssg_intrinsics* intrinsics,
+                                         const float* translations, int fill, void* stream);
+
+/* Inpainting (python/stitcher.cu:283-323) of `instances` maps; d_tables: references x rows x
+ * cols x 2 (instance i uses table i % references); d_scratch: instances x rows x cols. */
+SSG_API int ssg_inpaint_batch(float* d_distance, const uint8_t* d_tables, float* d_scratch, int cols, int rows,
+                              int instances, int references, double max_dist, int iterations, void* stream);
+
+/* Merge (python/stitcher.cu:423-473) of `frames` frames: maps frames x references x rows x
+ * cols, images frames x references x image_rows x image_cols x 3, panoramas per frame. */
+SSG_API int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                                     const float* d_distances, const uint8_t* d_images, int image_rows,
+                                     int image_cols, const float* translations, const ssg_intrinsics* intrinsics,
+                                     int reference_count, int cols, int rows, int pano_cols, int pano_rows, int frames,
+                                     float* d_distance_panorama, uint8_t* d_rgb_panorama, void* stream);
 
 #ifdef __cplusplus
 }

@@ -132,6 +132,10 @@ def run_pipeline(ref, calibration: dict, images_to_match, images_to_stitch, mask
         "translations": st.translations.numpy().copy(),
         "calibration_vectors": st.calibration_vectors.numpy().copy(),
         "viewpoint": viewpoint.numpy().copy(),
+        # rows 0..2 of inverse(camera.rt) @ reference.rt as the reference computes them
+        # (depth_estimation.py:156), per reference and camera
+        "relative_poses": np.stack([np.stack([torch.matmul(torch.inverse(c.rt), calibs[r].rt)[:3].reshape(12).numpy()
+                                              for c in calibs]) for r in references_indices]),
     }
     for k, v in rec.items():
         out[k] = np.stack(v)

@@ -330,6 +330,16 @@ class OracleRig:
         self.blending_lut = lut
         self.blending_weights = (weights / weights.sum(axis=0, keepdims=True)).astype(self.o.dtype)
 
+    def set_rig_tables(self, selected_cameras=None, relative_poses=None):
+        """Use another run's camera-selection maps ([references][rows, cols]) and relative poses
+        ([references][cameras, 12]) instead of this host's (see RGBD_Estimator.set_rig_tables)."""
+        if selected_cameras is not None:
+            for r, s in zip(self.refs, selected_cameras):
+                self.selected[r] = np.ascontiguousarray(s, np.int8).reshape(self.H, self.W)
+        if relative_poses is not None:
+            for r, p in zip(self.refs, relative_poses):
+                self.rts[r] = np.asarray(p, np.float64).reshape(-1, 12)
+
     def estimate(self, images_to_match, images_to_stitch, keep_intermediates=False):
         """estimate_RGBD_panorama (python/depth_estimation.py:205-242) on the oracle."""
         images = np.stack([np.asarray(im) for im in images_to_match]).astype(self.o.dtype)

@@ -70,6 +70,16 @@ SIGNATURES = {
     "ssg_reproject_distance": (_I, [_P, _P, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint": (_I, [_P, _P, _P, _I, _I, _D, _I, _P]),
     "ssg_merge_panorama": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "ssg_stage_images": (_I, [_P, _I, _I, _I64, _P, _I, _P, _P, _P]),
+    "ssg_sweep_cost_batch": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "ssg_isb_downsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _P]),
+    "ssg_isb_upsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P]),
+    "ssg_isb_upsample_select_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P]),
+    "ssg_select_distance_batch": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, _P]),
+    "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _P]),
+    "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
+    "ssg_inpaint_batch": (_I, [_P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
+    "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
 }
 
 _lock = threading.Lock()
@@ -155,6 +165,11 @@ def floats(values) -> ctypes.Array:
     return (ctypes.c_float * len(values))(*values)
 
 
+def ints(values) -> ctypes.Array:
+    values = [int(v) for v in values]
+    return (ctypes.c_int * len(values))(*values)
+
+
 def pointers(values) -> ctypes.Array:
     return (ctypes.c_void_p * len(values))(*[int(v) for v in values])
 
@@ -163,10 +178,14 @@ def kernels_launched(name: str, args) -> int:
     """Number of kernels one call of entry point ``name`` with ``args`` launches."""
     if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count"):
         return 0
-    if name == "ssg_isb_apply":
+    if name in ("ssg_isb_apply", "ssg_isb_apply_batch"):
         return 2 * max(0, int(args[2]) - 1)
     if name == "ssg_reproject_distance":
         return 2 if args[6] else 1
+    if name == "ssg_reproject_distance_batch":
+        return 2 if args[8] else 1
     if name == "ssg_inpaint":
         return -(-int(args[6]) // 16)
+    if name == "ssg_inpaint_batch":
+        return -(-int(args[8]) // 16)
     return 1

@@ -43,6 +43,11 @@ __global__ void __launch_bounds__(kIsbBlock) isb_down_kernel(const uint8_t* __re
     const int64_t pout = (int64_t)rows_out * cols_out, pin = (int64_t)rows_in * cols_in;
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pout) return;
+    // blockIdx.y: instance of a batch of equally sized, contiguous levels
+    guide_in += (int64_t)blockIdx.y * pin * 3;
+    guide_out += (int64_t)blockIdx.y * pout * 3;
+    cost_in += (int64_t)blockIdx.y * ncand * pin;
+    cost_out += (int64_t)blockIdx.y * ncand * pout;
     const int x = (int)(o % cols_out), y = (int)(o / cols_out);
     const int x2 = 2 * x, y2 = 2 * y;
     const int px = min(x2 + 1, cols_in - 1), py = min(y2 + 1, rows_in - 1);
@@ -217,6 +222,10 @@ __global__ void __launch_bounds__(kIsbBlock) isb_up_kernel(const uint8_t* __rest
     const int64_t pin = (int64_t)rows_in * cols_in, pio = (int64_t)rows_io * cols_io;
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pin) return;
+    guide_in += (int64_t)blockIdx.y * pin * 3;
+    guide_io += (int64_t)blockIdx.y * pio * 3;
+    cost_in += (int64_t)blockIdx.y * ncand * pin;
+    cost_io += (int64_t)blockIdx.y * ncand * pio;
     UpWeights u;
     up_weights(guide_in, rows_in, cols_in, guide_io, rows_io, cols_io, (int)(o % cols_in), (int)(o / cols_in),
                weight_up, weight_down, var_inv_i, u);
@@ -411,6 +420,40 @@ extern "C" int ssg_isb_apply(uint8_t* const* d_guides, float* const* d_costs, in
                                  d_guides[s], d_costs[s], level_rows(rows, s), level_rows(cols, s), candidate_count,
                                  c.weight_up[s], c.weight_down[s], c.var_inv_i, stream);
         if (e) return e;
+    }
+    return SSG_OK;
+}
+
+extern "C" int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows,
+                                   int cols, int candidate_count, int instances, double sigma_i, double sigma_s,
+                                   void* stream)
+{
+    SSG_REQUIRE(d_guides && d_costs, "null level arrays");
+    SSG_REQUIRE(level_count == ssg_isb_level_count(cols, rows),
+                "level_count %d differs from the pyramid of a %dx%d image (%d)", level_count, cols, rows,
+                ssg_isb_level_count(cols, rows));
+    SSG_REQUIRE(level_count <= SSG_MAX_LEVELS, "too many levels");
+    SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
+    SSG_REQUIRE(sigma_i > 0 && sigma_s > 0, "sigmas must be positive");
+    for (int s = 0; s < level_count; ++s) SSG_REQUIRE(d_guides[s] && d_costs[s], "level %d is NULL", s);
+    const Levels c = isb_constants(level_count, sigma_i, sigma_s);
+    cudaStream_t st = as_stream(stream);
+    for (int s = 1; s < level_count; ++s) {
+        const int ri = level_rows(rows, s - 1), ci = level_rows(cols, s - 1), ro = level_rows(rows, s),
+                  co = level_rows(cols, s);
+        dim3 grid(grid_1d((int64_t)ro * co, kIsbBlock), instances);
+        isb_down_kernel<<<grid, kIsbBlock, 0, st>>>(d_guides[s - 1], d_costs[s - 1], ri, ci, d_guides[s], d_costs[s], ro,
+                                                    co, candidate_count, c.var_inv_i);
+        if (int e = launch_status("isb_down_kernel")) return e;
+    }
+    for (int s = level_count - 2; s >= 0; --s) {
+        const int rc = level_rows(rows, s + 1), cc = level_rows(cols, s + 1), rf = level_rows(rows, s),
+                  cf = level_rows(cols, s);
+        dim3 grid(grid_1d((int64_t)rc * cc, kIsbBlock), instances);
+        isb_up_kernel<<<grid, kIsbBlock, 0, st>>>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s], rf,
+                                                  cf, candidate_count, c.weight_up[s], c.weight_down[s], c.var_inv_i);
+        if (int e = launch_status("isb_up_kernel")) return e;
     }
     return SSG_OK;
 }

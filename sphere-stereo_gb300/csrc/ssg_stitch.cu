@@ -171,20 +171,32 @@ __global__ void __launch_bounds__(kStitchBlock) fill_kernel(float* __restrict__ 
     if (i < n) out[i] = v;
 }
 
-// reprojectDistanceKernel, stitcher.cu:181-204, as a z-buffer on the float bits
-__global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const float* __restrict__ din,
-                                                                 float* __restrict__ dout, int cols, int rows, Intr k,
-                                                                 float tx, float ty, float tz)
+struct ReprojParams {
+    int cols, rows, references;
+    Intr k[SSG_MAX_REFERENCES];
+    float t[SSG_MAX_REFERENCES][3];
+};
+
+// reprojectDistanceKernel, stitcher.cu:181-204, as a z-buffer on the float bits.
+// blockIdx.y: instance (frame * references + reference slot) of contiguous maps.
+__global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_constant__ ReprojParams p,
+                                                                 const float* __restrict__ din,
+                                                                 float* __restrict__ dout)
 {
-    const int64_t P = (int64_t)cols * rows;
+    const int cols = p.cols;
+    const int64_t P = (int64_t)cols * p.rows;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
+    const int slot = blockIdx.y % p.references;
+    din += (int64_t)blockIdx.y * P;
+    dout += (int64_t)blockIdx.y * P;
+    const Intr& k = p.k[slot];
     float pt[3];
     unproject_cu((float)(i % cols), (float)(i / cols), k, pt);
     const float d = din[i];
-    pt[0] = fsub(fmul(d, pt[0]), tx);
-    pt[1] = fsub(fmul(d, pt[1]), ty);
-    pt[2] = fsub(fmul(d, pt[2]), tz);
+    pt[0] = fsub(fmul(d, pt[0]), p.t[slot][0]);
+    pt[1] = fsub(fmul(d, pt[1]), p.t[slot][1]);
+    pt[2] = fsub(fmul(d, pt[2]), p.t[slot][2]);
     float o[2];
     project_cu(pt, k, o, nullptr);
     const float dist = norm3df(pt[0], pt[1], pt[2]);
@@ -203,10 +215,15 @@ constexpr size_t kInpaintSmem = sizeof(float) * 2 * kRegW * kRegH + sizeof(uchar
 __global__ void __launch_bounds__(kInpaintBlock) inpaint_tile_kernel(const float* __restrict__ src,
                                                                      float* __restrict__ dst,
                                                                      const uchar2* __restrict__ table, int cols,
-                                                                     int rows, int steps, float hole_at_least,
-                                                                     float valid_at_most)
+                                                                     int rows, int references, int steps,
+                                                                     float hole_at_least, float valid_at_most)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    // blockIdx.z: instance (frame * references + reference slot); tables are per slot
+    const int64_t P = (int64_t)cols * rows;
+    src += (int64_t)blockIdx.z * P;
+    dst += (int64_t)blockIdx.z * P;
+    table += (int64_t)(blockIdx.z % references) * P;
     float* buf0 = reinterpret_cast<float*>(smem);
     float* buf1 = buf0 + kRegW * kRegH;
     uchar2* tab = reinterpret_cast<uchar2*>(buf1 + kRegW * kRegH);
@@ -306,6 +323,13 @@ __global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_consta
     const int64_t Q = (int64_t)p.pano_cols * p.pano_rows;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Q) return;
+    // blockIdx.y: frame of a batch of contiguous maps, images and panoramas
+    const int64_t frame = blockIdx.y;
+    reproj += frame * p.nref * (int64_t)p.cols * p.rows;
+    dists += frame * p.nref * (int64_t)p.cols * p.rows;
+    images += frame * p.nref * (int64_t)p.image_cols * p.image_rows * 3;
+    dist_pano += frame * Q;
+    rgb_pano += frame * Q * 3;
     float inv = 0.0f, rgb[3] = {0.0f, 0.0f, 0.0f};
     const float colsm = fsub((float)p.image_cols, 1.1f), rowsm = fsub((float)p.image_rows, 1.1f);
     for (int r = 0; r < p.nref; ++r) {
@@ -465,29 +489,73 @@ extern "C" int ssg_reproject_distance(const float* d_distance_in, float* d_dista
         fill_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(d_distance_out, P, 1e8f);
         if (int e = launch_status("fill_kernel")) return e;
     }
-    reproject_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
-        d_distance_in, d_distance_out, cols, rows, to_intr(*intrinsics), translation[0], translation[1],
-        translation[2]);
+    ReprojParams p{};
+    p.cols = cols;
+    p.rows = rows;
+    p.references = 1;
+    p.k[0] = to_intr(*intrinsics);
+    std::memcpy(p.t[0], translation, sizeof(float) * 3);
+    reproject_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(p, d_distance_in,
+                                                                                       d_distance_out);
+    return launch_status("reproject_kernel");
+}
+
+extern "C" int ssg_reproject_distance_batch(const float* d_distance_in, float* d_distance_out, int cols, int rows,
+                                            int instances, int references, const ssg_intrinsics* intrinsics,
+                                            const float* translations, int fill, void* stream)
+{
+    SSG_REQUIRE(d_distance_in && d_distance_out && translations, "null pointer");
+    SSG_REQUIRE(d_distance_in != d_distance_out, "input and output maps must differ");
+    SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
+    SSG_REQUIRE(references >= 1 && references <= SSG_MAX_REFERENCES, "references out of range");
+    SSG_REQUIRE(instances >= 1 && instances <= 65535 && instances % references == 0,
+                "instances must be a positive multiple of references");
+    if (int e = check_intrinsics(intrinsics, references)) return e;
+    const int64_t P = (int64_t)cols * rows;
+    if (fill) {
+        fill_kernel<<<grid_1d(P * instances, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+            d_distance_out, P * instances, 1e8f);
+        if (int e = launch_status("fill_kernel")) return e;
+    }
+    ReprojParams p{};
+    p.cols = cols;
+    p.rows = rows;
+    p.references = references;
+    for (int r = 0; r < references; ++r) {
+        p.k[r] = to_intr(intrinsics[r]);
+        std::memcpy(p.t[r], translations + 3 * r, sizeof(float) * 3);
+    }
+    dim3 grid(grid_1d(P, kStitchBlock), instances);
+    reproject_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(p, d_distance_in, d_distance_out);
     return launch_status("reproject_kernel");
 }
 
 extern "C" int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scratch, int cols, int rows,
                            double max_dist, int iterations, void* stream)
 {
+    return ssg_inpaint_batch(d_distance, d_table, d_scratch, cols, rows, 1, 1, max_dist, iterations, stream);
+}
+
+extern "C" int ssg_inpaint_batch(float* d_distance, const uint8_t* d_tables, float* d_scratch, int cols, int rows,
+                                 int instances, int references, double max_dist, int iterations, void* stream)
+{
+    const uint8_t* d_table = d_tables;
     SSG_REQUIRE(d_distance && d_table && d_scratch && d_distance != d_scratch, "null or aliased pointer");
     SSG_REQUIRE(cols > 0 && rows > 0 && iterations >= 0, "invalid sizes");
+    SSG_REQUIRE(references >= 1 && instances >= 1 && instances <= 65535 && instances % references == 0,
+                "instances must be a positive multiple of references");
     if (int e = enable_inpaint_smem()) return e;
     // hole: distance >= MAX_DIST + 0.1 (double, stitcher.cu:287); usable neighbour:
     // distance <= MAX_DIST + 0.1f (stitcher.cu:311)
     const float hole = float_at_least(max_dist + 0.1);
     const float ok = float_at_most(max_dist + (double)0.1f);
-    dim3 grid((cols + kTileW - 1) / kTileW, (rows + kTileH - 1) / kTileH);
+    dim3 grid((cols + kTileW - 1) / kTileW, (rows + kTileH - 1) / kTileH, instances);
     float* a = d_distance;
     float* b = d_scratch;
     for (int done = 0; done < iterations;) {
         const int steps = iterations - done < kHalo ? iterations - done : kHalo;
         inpaint_tile_kernel<<<grid, kInpaintBlock, kInpaintSmem, as_stream(stream)>>>(
-            a, b, reinterpret_cast<const uchar2*>(d_table), cols, rows, steps, hole, ok);
+            a, b, reinterpret_cast<const uchar2*>(d_table), cols, rows, references, steps, hole, ok);
         if (int e = launch_status("inpaint_tile_kernel")) return e;
         float* t = a;
         a = b;
@@ -495,8 +563,8 @@ extern "C" int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_s
         done += steps;
     }
     if (a != d_distance) {
-        cudaError_t e = cudaMemcpyAsync(d_distance, a, sizeof(float) * (size_t)cols * rows, cudaMemcpyDeviceToDevice,
-                                        as_stream(stream));
+        cudaError_t e = cudaMemcpyAsync(d_distance, a, sizeof(float) * (size_t)cols * rows * instances,
+                                        cudaMemcpyDeviceToDevice, as_stream(stream));
         if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemcpyAsync: %s", cudaGetErrorString(e));
     }
     return SSG_OK;
@@ -508,6 +576,18 @@ extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, co
                                   int cols, int rows, int pano_cols, int pano_rows, float* d_distance_panorama,
                                   uint8_t* d_rgb_panorama, void* stream)
 {
+    return ssg_merge_panorama_batch(d_lut, d_weights, d_reprojected, d_distances, d_images, image_rows, image_cols,
+                                    translations, intrinsics, reference_count, cols, rows, pano_cols, pano_rows, 1,
+                                    d_distance_panorama, d_rgb_panorama, stream);
+}
+
+extern "C" int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                                        const float* d_distances, const uint8_t* d_images, int image_rows,
+                                        int image_cols, const float* translations, const ssg_intrinsics* intrinsics,
+                                        int reference_count, int cols, int rows, int pano_cols, int pano_rows,
+                                        int frames, float* d_distance_panorama, uint8_t* d_rgb_panorama, void* stream)
+{
+    SSG_REQUIRE(frames >= 1 && frames <= 65535, "frames out of range");
     SSG_REQUIRE(d_lut && d_weights && d_reprojected && d_distances && d_images && translations &&
                     d_distance_panorama && d_rgb_panorama,
                 "null pointer");
@@ -531,7 +611,8 @@ extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, co
         std::memcpy(p.t[r], translations + 3 * r, sizeof(float) * 3);
     }
     const int64_t Q = (int64_t)pano_cols * pano_rows;
-    merge_kernel<<<grid_1d(Q, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
+    dim3 grid(grid_1d(Q, kStitchBlock), frames);
+    merge_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(
         p, reinterpret_cast<const float2*>(d_lut), d_weights, d_reprojected, d_distances, d_images,
         d_distance_panorama, d_rgb_panorama);
     return launch_status("merge_kernel");

@@ -36,7 +36,8 @@ def distance_candidates(min_dist, max_dist, candidate_count) -> torch.Tensor:
 
 class RGBD_Estimator:
     def __init__(self, calibrations, min_dist, max_dist, candidate_count, references_indices, reprojection_viewpoint,
-                 masks, matching_resolution, rgb_to_stitch_resolution, panorama_resolution, sigma_i, sigma_s, device):
+                 masks, matching_resolution, rgb_to_stitch_resolution, panorama_resolution, sigma_i, sigma_s, device,
+                 *, cost_storage="fp32", max_batch=1, cuda_graphs=True):
         """Prepare RGB-D estimation: camera selection for adaptive matching, filters, stitcher.
 
         Args:
@@ -52,6 +53,11 @@ class RGBD_Estimator:
             sigma_i: edge preservation of the cost filter (lower preserves edges more)
             sigma_s: smoothing of the cost filter (higher favours coarser scales)
             device: CUDA device
+            cost_storage (keyword only, not in the reference): "fp32" runs the reference's
+                arithmetic bit for bit against the oracle; "fp16" / "unorm16" store the cost
+                volume with 16 bits per candidate (fp32 arithmetic) and run frames in batches
+            max_batch (keyword only): largest batch of ``estimate_RGBD_panoramas``
+            cuda_graphs (keyword only): replay each batch from a captured CUDA graph
         """
         device = torch.device(device)
         if device.type != "cuda":
@@ -90,7 +96,8 @@ class RGBD_Estimator:
         self.distance_candidates_host = distance_candidates(min_dist, max_dist, candidate_count)
         self._candidates = N.floats(self.distance_candidates_host.tolist())
         self._cams = N.cameras_array([camera_struct(c) for c in calibrations])
-        self._poses = {r: N.floats(relative_poses(calibrations, r)) for r in self.references_indices}
+        self._poses_list = {r: relative_poses(calibrations, r) for r in self.references_indices}
+        self._poses = {r: N.floats(v) for r, v in self._poses_list.items()}
         cols, rows = self.matching_resolution
         self._shapes = level_shapes(self.matching_resolution)
         self._guide = torch.empty([rows, cols, 3], dtype=torch.uint8, device=device)
@@ -101,6 +108,57 @@ class RGBD_Estimator:
         # per reference: the selected candidate index (torch.min's index, depth_estimation.py:180)
         self.index_maps = torch.empty([len(self.references_indices), rows, cols], dtype=torch.int32, device=device)
         self.select_camera(masks)
+        if cost_storage not in ("fp32", "fp16", "unorm16"):
+            raise ValueError("cost_storage must be 'fp32', 'fp16' or 'unorm16'")
+        self.cost_storage = cost_storage
+        self.max_batch = int(max_batch)
+        self.cuda_graphs = bool(cuda_graphs)
+        self._pipeline = None
+
+    def set_rig_tables(self, selected_cameras=None, relative_poses=None):
+        """Replace the per-rig tables computed at construction (no counterpart in the reference,
+        which recomputes poses with torch on every call).
+
+        Args:
+            selected_cameras: per reference, [1, rows, cols] or [rows, cols] integer camera
+                indices (-1 = none), e.g. another implementation's ``selected_cameras``
+            relative_poses: per reference, camera_count x 12 floats: rows 0..2 of
+                inverse(camera.rt) @ reference.rt (python/depth_estimation.py:156)
+        The tables are host-computed with float32 linear algebra whose last bit depends on the
+        platform's BLAS; the selection compares displacements and can flip on exact ties, so
+        parity checks against another platform's outputs pass that platform's tables in here.
+        """
+        cols, rows = self.matching_resolution
+        if selected_cameras is not None:
+            if len(selected_cameras) != len(self.references_indices):
+                raise ValueError("one selection map per reference is required")
+            sel8 = []
+            for s_ in selected_cameras:
+                t = torch.as_tensor(s_).reshape(rows, cols).to(self.device)
+                if t.min() < -1 or t.max() >= len(self.calibrations):
+                    raise ValueError("camera indices out of range")
+                sel8.append(t.to(torch.int8).contiguous())
+            self._selected = sel8
+            self.selected_cameras = [t.long().unsqueeze(0) for t in sel8]
+        if relative_poses is not None:
+            if len(relative_poses) != len(self.references_indices):
+                raise ValueError("one pose table per reference is required")
+            for r, v in zip(self.references_indices, relative_poses):
+                v = [float(x) for x in torch.as_tensor(v).reshape(-1).tolist()]
+                if len(v) != 12 * len(self.calibrations):
+                    raise ValueError("each pose table needs camera_count x 12 floats")
+                self._poses_list[r] = v
+                self._poses[r] = N.floats(v)
+        self._pipeline = None
+
+    def pipeline(self):
+        """The batched 16-bit pipeline (built on first use)."""
+        if self._pipeline is None:
+            from .pipeline import BatchPipeline
+
+            storage = "fp16" if self.cost_storage == "fp32" else self.cost_storage
+            self._pipeline = BatchPipeline(self, self.max_batch, storage, self.cuda_graphs)
+        return self._pipeline
 
     # --------------------------------------------------------------------------------------
     def select_camera(self, masks):
@@ -199,6 +257,11 @@ class RGBD_Estimator:
         """
         cols, rows = self.matching_resolution
         st = self.fishey_stitcher
+        if self.cost_storage != "fp32":
+            match = torch.stack(list(images_to_match))[None]
+            stitch = torch.stack(list(images_to_stitch))[None]
+            rgb, distance = self.pipeline().run(match, stitch)
+            return rgb[0], distance[0]
         if len(images_to_match) != len(self.calibrations):
             raise ValueError(f"expected {len(self.calibrations)} images to match")
         if len(images_to_stitch) != len(self.references_indices):
@@ -211,3 +274,28 @@ class RGBD_Estimator:
         for slot, image in enumerate(images_to_stitch):
             st.images_to_stitch_list[slot].copy_(image)  # float -> uint8 truncation (depth_estimation.py:239-240)
         return st.stitch(st.images_to_stitch_list, st.distances_list)
+
+    def estimate_RGBD_panoramas(self, images_to_match, images_to_stitch):
+        """Batched ``estimate_RGBD_panorama`` (no counterpart in the reference, which takes one
+        frame per call) on the 16-bit pipeline.
+
+        Args:
+            images_to_match: [frames, cameras, matching_rows, matching_cols, 3] float32 in [0, 255]
+            images_to_stitch: [frames, references, rgb_stitching_rows, rgb_stitching_cols, 3]
+                float32 in [0, 255]
+        Returns:
+            rgb: [frames, rows, cols, 3] uint8, distance: [frames, rows, cols] float32 (views of
+            the pipeline's buffers, overwritten by the next call)
+        """
+        return self.pipeline().run(images_to_match, images_to_stitch)
+
+    @property
+    def batch_distance_maps(self):
+        """Filtered per-reference distance maps of the last batch, [frames, references, rows, cols]."""
+        return self.pipeline().distance
+
+    @property
+    def batch_index_maps(self):
+        """Selected candidate indices of the last batch, [frames, references, rows, cols]."""
+        p = self.pipeline()
+        return p.index.view(p.max_frames, p.R, p.rows, p.cols)

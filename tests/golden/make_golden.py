@@ -88,7 +88,7 @@ def make_pipeline(ref, cfg, filename, keep_volumes):
         "masks": np.stack(masks),
     }
     keep = ["rgb_panorama", "distance_panorama", "selected_cameras", "candidates", "index", "distance_raw",
-            "distance_filtered", "guide", "translations", "calibration_vectors", "viewpoint"]
+            "distance_filtered", "guide", "translations", "calibration_vectors", "viewpoint", "relative_poses"]
     if keep_volumes:
         keep += ["cost_raw", "cost_filtered", "blending_sampling", "guide_filtered_cost", "guide_filtered_distance",
                  "reprojected_distances", "blending_weights", "inpainting_tables"]
