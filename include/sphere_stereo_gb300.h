@@ -41,9 +41,10 @@ enum {
     SSG_ERR_UNSUPPORTED = 3       /* a size beyond a documented compile-time limit */
 };
 
-/* 16-bit cost storage of the batched path (the fp32 path keeps float32). */
+/* Cost storage of the batched path: the level-0 volume is 16-bit, coarser levels float32. */
 #define SSG_STORAGE_F16 0     /* IEEE half */
 #define SSG_STORAGE_UNORM16 1 /* uint16 q = round(cost * 65535 / 500), costs being in [0, 500] */
+#define SSG_STORAGE_F32 2     /* float32 (the coarse levels) */
 
 /* Compile-time limits (also reported by ssg_limits). */
 #define SSG_MAX_CAMERAS 16
@@ -202,8 +203,9 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
  * points have no single counterpart in the reference, which processes one frame and one
  * reference camera per call.
  *
- * Cost volumes of the batched path are stored with 16 bits per candidate (SSG_STORAGE_*) in
- * chunks of 8 candidates: per instance and level [ceil(N / 8)][pixels][8], all arithmetic fp32.
+ * Cost volumes of the batched path are stored in chunks of 8 candidates, per instance and level
+ * [ceil(N / 8)][pixels][8]: the level-0 volume with 16 bits per candidate (SSG_STORAGE_F16 /
+ * SSG_STORAGE_UNORM16), the coarser levels as float32; all arithmetic is fp32.
  * ------------------------------------------------------------------------------------------- */
 
 /* Image staging + guides: d_images frames x cameras x pixels x 3 float32 (the inputs of
@@ -222,7 +224,9 @@ SSG_API int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_coun
                                  const float* d_staged, const int8_t* d_selected, const float* candidates,
                                  int candidate_count, int storage, void* d_cost, void* stream);
 
-/* ISB down / up steps (python/isb_filter.cu:44-329) on `instances` contiguous levels. */
+/* ISB down / up steps (python/isb_filter.cu:44-329) on `instances` contiguous levels.  The
+ * downsampling reads a level stored as `storage` and writes float32; the upsampling reads and
+ * writes float32 levels (storage must be SSG_STORAGE_F32). */
 SSG_API int ssg_isb_downsample_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
                                      uint8_t* d_guide_out, void* d_cost_out, int rows_out, int cols_out,
                                      int candidate_count, int instances, int storage, float var_inv_i, void* stream);
@@ -232,7 +236,8 @@ SSG_API int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_cost
                                    float var_inv_i, void* stream);
 
 /* Last ISB level fused with distance selection (python/isb_filter.cu:132-329 +
- * python/depth_estimation.py:179-198): d_distance / d_index instances x fine pixels. */
+ * python/depth_estimation.py:179-198): float32 coarse level, fine (level-0) volume stored as
+ * `storage`; d_distance / d_index instances x fine pixels. */
 SSG_API int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
                                           uint8_t* d_guide_inout, const void* d_cost_fine, int rows_fine,
                                           int cols_fine, int candidate_count, int instances, int storage,

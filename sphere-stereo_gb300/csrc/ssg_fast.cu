@@ -11,10 +11,14 @@
 // candidates in order through the same running argmin as the fp32 path, without writing the
 // level-0 volume back.
 //
-// Storage types: __half (fp16) and unorm16 (uint16 q = round(c * 65535 / 500); costs are
-// clamped to [0, 500] by the sweep and the filter forms convex combinations, so every level
-// stays in range).  Arithmetic is fp32 with fused multiply-adds and fast transcendentals; the
-// fp32 path (ssg_sweep.cu, ssg_isb.cu) is the one that reproduces the reference bit for bit.
+// Storage: the level-0 volume (the sweep's output, the largest buffer) is 16-bit, __half (fp16)
+// or unorm16 (uint16 q = round(c * 65535 / 500); costs are clamped to [0, 500] by the sweep);
+// the coarser levels are float32.  Quantising the coarse levels moves the argmin: they are
+// averages whose differences between candidates are small next to their magnitude, and the
+// coarse scales carry much of the final weight.  Measured on the reference's golden frames:
+// 16-bit coarse levels keep 73-99 % of the reference's candidate indices, float32 coarse
+// levels 99.99-100 %.  Arithmetic is fp32 with fused multiply-adds and fast transcendentals;
+// the fp32 path (ssg_sweep.cu, ssg_isb.cu) is the one that reproduces the reference bit for bit.
 #include <cmath>
 
 #include "ssg_common.cuh"
@@ -86,7 +90,35 @@ struct Cell<uint16_t> {
     }
 };
 
+template <>
+struct Cell<float> {};
+
 __device__ __forceinline__ uint4 ldg16(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+
+// 8 consecutive candidates of one cell, any storage type
+template <typename T>
+__device__ __forceinline__ void load8(const T* __restrict__ p, float v[8])
+{
+    Cell<T>::unpack(ldg16(p), v);
+}
+template <>
+__device__ __forceinline__ void load8<float>(const float* __restrict__ p, float v[8])
+{
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+template <typename T>
+__device__ __forceinline__ void store8(T* p, const float v[8])
+{
+    reinterpret_cast<uint4*>(p)[0] = Cell<T>::pack(v);
+}
+template <>
+__device__ __forceinline__ void store8<float>(float* p, const float v[8])
+{
+    reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Image staging: HWC float32 -> RGBx float4 (16-byte texels for the sweep's bilinear taps), with
@@ -259,11 +291,11 @@ struct LevelGeom {
     int rows_in, cols_in, rows_out, cols_out;
 };
 
-template <typename T>
+template <typename Tin, typename Tout>
 __global__ void __launch_bounds__(kFastBlock) isb_down_fast_kernel(const uint8_t* __restrict__ guide_in,
-                                                                   const T* __restrict__ cost_in,
+                                                                   const Tin* __restrict__ cost_in,
                                                                    uint8_t* __restrict__ guide_out,
-                                                                   T* __restrict__ cost_out, LevelGeom g, int chunks,
+                                                                   Tout* __restrict__ cost_out, LevelGeom g, int chunks,
                                                                    float var_inv_i)
 {
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
@@ -302,16 +334,16 @@ __global__ void __launch_bounds__(kFastBlock) isb_down_fast_kernel(const uint8_t
 #pragma unroll
     for (int t = 0; t < 9; ++t) w[t] *= inv;
     for (int c = 0; c < chunks; ++c) {
-        const T* src = cost_in + (int64_t)c * pin * 8;
+        const Tin* src = cost_in + (int64_t)c * pin * 8;
         float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
         for (int t = 0; t < 9; ++t) {
             float v[8];
-            Cell<T>::unpack(ldg16(src + idx[t] * 8), v);
+            load8<Tin>(src + idx[t] * 8, v);
 #pragma unroll
             for (int j = 0; j < 8; ++j) acc[j] = fmaf(v[j], w[t], acc[j]);
         }
-        reinterpret_cast<uint4*>(cost_out + ((int64_t)c * pout + o) * 8)[0] = Cell<T>::pack(acc);
+        store8<Tout>(cost_out + ((int64_t)c * pout + o) * 8, acc);
     }
 }
 
@@ -414,20 +446,20 @@ __device__ __forceinline__ void fast_up_weights(const uint8_t* __restrict__ gin,
 }
 
 // 8 candidates of the four fine pixels from 9 coarse cells and the fine cells
-template <typename T>
-__device__ __forceinline__ void fast_up_chunk(const FastUp& u, const T* __restrict__ coarse,
-                                              const T* __restrict__ fine, float out[4][8])
+template <typename Tc, typename Tf>
+__device__ __forceinline__ void fast_up_chunk(const FastUp& u, const Tc* __restrict__ coarse,
+                                              const Tf* __restrict__ fine, float out[4][8])
 {
     float cd[9][8];
 #pragma unroll
-    for (int t = 0; t < 9; ++t) Cell<T>::unpack(ldg16(coarse + u.cidx[t] * 8), cd[t]);
+    for (int t = 0; t < 9; ++t) load8<Tc>(coarse + u.cidx[t] * 8, cd[t]);
     const float* c2[6] = SSG_T2(cd);
     const float* c3[6] = SSG_T3(cd);
     const float* c4[4] = SSG_T4(cd);
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
         float fv[8];
-        Cell<T>::unpack(ldg16(fine + u.fidx[f] * 8), fv);
+        load8<Tf>(fine + u.fidx[f] * 8, fv);
 #pragma unroll
         for (int j = 0; j < 8; ++j) out[f][j] = u.up[f] * fv[j];
     }
@@ -445,11 +477,10 @@ __device__ __forceinline__ void fast_up_chunk(const FastUp& u, const T* __restri
     }
 }
 
-template <typename T>
 __global__ void __launch_bounds__(kFastBlock) isb_up_fast_kernel(const uint8_t* __restrict__ guide_in,
-                                                                 const T* __restrict__ cost_in,
+                                                                 const float* __restrict__ cost_in,
                                                                  uint8_t* __restrict__ guide_io,
-                                                                 T* __restrict__ cost_io, LevelGeom g, int chunks,
+                                                                 float* __restrict__ cost_io, LevelGeom g, int chunks,
                                                                  float weight_up, float weight_down, float var_inv_i)
 {
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
@@ -465,11 +496,11 @@ __global__ void __launch_bounds__(kFastBlock) isb_up_fast_kernel(const uint8_t* 
                     var_inv_i, true, u);
     for (int c = 0; c < chunks; ++c) {
         float out[4][8];
-        T* fine = cost_io + (int64_t)c * pio * 8;
-        fast_up_chunk<T>(u, cost_in + (int64_t)c * pin * 8, fine, out);
+        float* fine = cost_io + (int64_t)c * pio * 8;
+        fast_up_chunk<float, float>(u, cost_in + (int64_t)c * pin * 8, fine, out);
 #pragma unroll
         for (int f = 0; f < 4; ++f)
-            if (u.set[f]) reinterpret_cast<uint4*>(fine + u.fidx[f] * 8)[0] = Cell<T>::pack(out[f]);
+            if (u.set[f]) store8<float>(fine + u.fidx[f] * 8, out[f]);
     }
 }
 
@@ -516,7 +547,7 @@ struct FastSelector {
 
 template <typename T>
 __global__ void __launch_bounds__(kFastBlock) isb_up_select_fast_kernel(
-    const uint8_t* __restrict__ guide_in, const T* __restrict__ cost_in, uint8_t* __restrict__ guide_io,
+    const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in, uint8_t* __restrict__ guide_io,
     const T* __restrict__ cost_fine, LevelGeom g, int chunks, int ncand, float weight_up, float weight_down,
     float var_inv_i, float d0, float dl, float q, float* __restrict__ distance, int32_t* __restrict__ index)
 {
@@ -536,7 +567,7 @@ __global__ void __launch_bounds__(kFastBlock) isb_up_select_fast_kernel(
     FastSelector s[4];
     for (int c = 0; c < chunks; ++c) {
         float out[4][8];
-        fast_up_chunk<T>(u, cost_in + (int64_t)c * pin * 8, cost_fine + (int64_t)c * pio * 8, out);
+        fast_up_chunk<float, T>(u, cost_in + (int64_t)c * pin * 8, cost_fine + (int64_t)c * pio * 8, out);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int k = c * 8 + j;
@@ -568,7 +599,7 @@ __global__ void __launch_bounds__(kFastBlock) select_fast_kernel(const T* __rest
     FastSelector s;
     for (int c = 0; c < chunks; ++c) {
         float v[8];
-        Cell<T>::unpack(ldg16(cost + ((int64_t)c * P + i) * 8), v);
+        load8<T>(cost + ((int64_t)c * P + i) * 8, v);
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (c * 8 + j < ncand) s.push(c * 8 + j, v[j]);
@@ -680,20 +711,24 @@ extern "C" int ssg_isb_downsample_batch(const uint8_t* d_guide_in, const void* d
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_out && d_cost_out, "null pointer");
     if (int e = check_levels(rows_in, cols_in, rows_out, cols_out)) return e;
-    if (int e = check_storage(storage)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
+                "unknown input storage %d", storage);
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
     const LevelGeom g{rows_in, cols_in, rows_out, cols_out};
     dim3 grid(grid_1d((int64_t)rows_out * cols_out, kFastBlock), instances);
     const int chunks = chunks_of(candidate_count);
+    float* out = static_cast<float*>(d_cost_out);
+    cudaStream_t st = as_stream(stream);
     if (storage == SSG_STORAGE_F16)
-        isb_down_fast_kernel<__half><<<grid, kFastBlock, 0, as_stream(stream)>>>(
-            d_guide_in, static_cast<const __half*>(d_cost_in), d_guide_out, static_cast<__half*>(d_cost_out), g, chunks,
-            var_inv_i);
+        isb_down_fast_kernel<__half, float><<<grid, kFastBlock, 0, st>>>(
+            d_guide_in, static_cast<const __half*>(d_cost_in), d_guide_out, out, g, chunks, var_inv_i);
+    else if (storage == SSG_STORAGE_UNORM16)
+        isb_down_fast_kernel<uint16_t, float><<<grid, kFastBlock, 0, st>>>(
+            d_guide_in, static_cast<const uint16_t*>(d_cost_in), d_guide_out, out, g, chunks, var_inv_i);
     else
-        isb_down_fast_kernel<uint16_t><<<grid, kFastBlock, 0, as_stream(stream)>>>(
-            d_guide_in, static_cast<const uint16_t*>(d_cost_in), d_guide_out, static_cast<uint16_t*>(d_cost_out), g,
-            chunks, var_inv_i);
+        isb_down_fast_kernel<float, float><<<grid, kFastBlock, 0, st>>>(
+            d_guide_in, static_cast<const float*>(d_cost_in), d_guide_out, out, g, chunks, var_inv_i);
     return launch_status("isb_down_fast_kernel");
 }
 
@@ -704,20 +739,14 @@ extern "C" int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_c
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_inout, "null pointer");
     if (int e = check_levels(rows_inout, cols_inout, rows_in, cols_in)) return e;
-    if (int e = check_storage(storage)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F32, "coarse levels are float32 (storage must be SSG_STORAGE_F32)");
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
     const LevelGeom g{rows_in, cols_in, rows_inout, cols_inout};
     dim3 grid(grid_1d((int64_t)rows_in * cols_in, kFastBlock), instances);
-    const int chunks = chunks_of(candidate_count);
-    if (storage == SSG_STORAGE_F16)
-        isb_up_fast_kernel<__half><<<grid, kFastBlock, 0, as_stream(stream)>>>(
-            d_guide_in, static_cast<const __half*>(d_cost_in), d_guide_inout, static_cast<__half*>(d_cost_inout), g,
-            chunks, weight_up, weight_down, var_inv_i);
-    else
-        isb_up_fast_kernel<uint16_t><<<grid, kFastBlock, 0, as_stream(stream)>>>(
-            d_guide_in, static_cast<const uint16_t*>(d_cost_in), d_guide_inout, static_cast<uint16_t*>(d_cost_inout),
-            g, chunks, weight_up, weight_down, var_inv_i);
+    isb_up_fast_kernel<<<grid, kFastBlock, 0, as_stream(stream)>>>(
+        d_guide_in, static_cast<const float*>(d_cost_in), d_guide_inout, static_cast<float*>(d_cost_inout), g,
+        chunks_of(candidate_count), weight_up, weight_down, var_inv_i);
     return launch_status("isb_up_fast_kernel");
 }
 
@@ -730,22 +759,28 @@ extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const vo
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_fine && d_distance && candidates, "null pointer");
     if (int e = check_levels(rows_fine, cols_fine, rows_in, cols_in)) return e;
-    if (int e = check_storage(storage)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
+                "unknown fine-level storage %d", storage);
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
     const LevelGeom g{rows_in, cols_in, rows_fine, cols_fine};
     dim3 grid(grid_1d((int64_t)rows_in * cols_in, kFastBlock), instances);
     const int chunks = chunks_of(candidate_count);
     const float d0 = candidates[0], dl = candidates[candidate_count - 1], q = d0 / dl - 1.0f;
+    const float* coarse = static_cast<const float*>(d_cost_in);
+    cudaStream_t st = as_stream(stream);
     if (storage == SSG_STORAGE_F16)
-        isb_up_select_fast_kernel<__half><<<grid, kFastBlock, 0, as_stream(stream)>>>(
-            d_guide_in, static_cast<const __half*>(d_cost_in), d_guide_inout, static_cast<const __half*>(d_cost_fine),
-            g, chunks, candidate_count, weight_up, weight_down, var_inv_i, d0, dl, q, d_distance, d_index);
+        isb_up_select_fast_kernel<__half><<<grid, kFastBlock, 0, st>>>(
+            d_guide_in, coarse, d_guide_inout, static_cast<const __half*>(d_cost_fine), g, chunks, candidate_count,
+            weight_up, weight_down, var_inv_i, d0, dl, q, d_distance, d_index);
+    else if (storage == SSG_STORAGE_UNORM16)
+        isb_up_select_fast_kernel<uint16_t><<<grid, kFastBlock, 0, st>>>(
+            d_guide_in, coarse, d_guide_inout, static_cast<const uint16_t*>(d_cost_fine), g, chunks, candidate_count,
+            weight_up, weight_down, var_inv_i, d0, dl, q, d_distance, d_index);
     else
-        isb_up_select_fast_kernel<uint16_t><<<grid, kFastBlock, 0, as_stream(stream)>>>(
-            d_guide_in, static_cast<const uint16_t*>(d_cost_in), d_guide_inout,
-            static_cast<const uint16_t*>(d_cost_fine), g, chunks, candidate_count, weight_up, weight_down, var_inv_i,
-            d0, dl, q, d_distance, d_index);
+        isb_up_select_fast_kernel<float><<<grid, kFastBlock, 0, st>>>(
+            d_guide_in, coarse, d_guide_inout, static_cast<const float*>(d_cost_fine), g, chunks, candidate_count,
+            weight_up, weight_down, var_inv_i, d0, dl, q, d_distance, d_index);
     return launch_status("isb_up_select_fast_kernel");
 }
 
@@ -756,15 +791,19 @@ extern "C" int ssg_select_distance_batch(const void* d_cost, int candidate_count
     SSG_REQUIRE(d_cost && d_distance && candidates, "null pointer");
     SSG_REQUIRE(pixels > 0 && instances >= 1 && instances <= 65535, "invalid sizes");
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
-    if (int e = check_storage(storage)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
+                "unknown storage %d", storage);
     const float d0 = candidates[0], dl = candidates[candidate_count - 1], q = d0 / dl - 1.0f;
     dim3 grid(grid_1d(pixels, kFastBlock), instances);
     const int chunks = chunks_of(candidate_count);
     if (storage == SSG_STORAGE_F16)
         select_fast_kernel<__half><<<grid, kFastBlock, 0, as_stream(stream)>>>(
             static_cast<const __half*>(d_cost), pixels, chunks, candidate_count, d0, dl, q, d_distance, d_index);
-    else
+    else if (storage == SSG_STORAGE_UNORM16)
         select_fast_kernel<uint16_t><<<grid, kFastBlock, 0, as_stream(stream)>>>(
             static_cast<const uint16_t*>(d_cost), pixels, chunks, candidate_count, d0, dl, q, d_distance, d_index);
+    else
+        select_fast_kernel<float><<<grid, kFastBlock, 0, as_stream(stream)>>>(
+            static_cast<const float*>(d_cost), pixels, chunks, candidate_count, d0, dl, q, d_distance, d_index);
     return launch_status("select_fast_kernel");
 }

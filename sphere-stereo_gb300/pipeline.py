@@ -1,5 +1,5 @@
-"""Batched frame pipeline: many frames of one rig per launch sequence, 16-bit cost storage with
-fp32 arithmetic, optional CUDA-graph capture.
+"""Batched frame pipeline: many frames of one rig per launch sequence, a 16-bit level-0 cost
+volume (coarser levels float32) with fp32 arithmetic, optional CUDA-graph capture.
 
 One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_panorama
 (python/depth_estimation.py:205-242) for all F x R (frame, reference) instances at once:
@@ -25,6 +25,7 @@ from . import _native as N
 from .isb_filter import level_shapes, level_weights
 
 STORAGE = {"fp16": 0, "unorm16": 1}
+F32 = 2
 
 
 class BatchPipeline:
@@ -57,7 +58,9 @@ class BatchPipeline:
         i16 = dict(dtype=torch.int16, device=dev)
         self.staged = torch.empty(F * C * P * 4, **f32)
         self.guides = [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes]
-        self.costs = [torch.empty(F * R * self.chunks * r * c * 8, **i16) for r, c in self.shapes]
+        # level 0 (the sweep's output) 16-bit, coarser levels float32
+        self.costs = [torch.empty(F * R * self.chunks * r * c * 8, **(i16 if l == 0 else f32))
+                      for l, (r, c) in enumerate(self.shapes)]
         self.df_guides = [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes]
         self.df_costs = [torch.empty(F * R * r * c, **f32) for r, c in self.shapes[1:]]
         self.distance_raw = torch.empty(F * R * P, **f32)
@@ -91,13 +94,13 @@ class BatchPipeline:
             for s in range(1, L):
                 (ri, ci), (ro, co) = self.shapes[s - 1], self.shapes[s]
                 N.call("ssg_isb_downsample_batch", self.guides[s - 1].data_ptr(), self.costs[s - 1].data_ptr(), ri, ci,
-                       self.guides[s].data_ptr(), self.costs[s].data_ptr(), ro, co, self.N, inst, self.storage,
-                       var_inv_i, stream)
+                       self.guides[s].data_ptr(), self.costs[s].data_ptr(), ro, co, self.N, inst,
+                       self.storage if s == 1 else F32, var_inv_i, stream)
             for s in range(L - 2, 0, -1):
                 (rc, cc), (rf, cf) = self.shapes[s + 1], self.shapes[s]
                 wu, wd = weights[s]
                 N.call("ssg_isb_upsample_batch", self.guides[s + 1].data_ptr(), self.costs[s + 1].data_ptr(), rc, cc,
-                       self.guides[s].data_ptr(), self.costs[s].data_ptr(), rf, cf, self.N, inst, self.storage, wu, wd,
+                       self.guides[s].data_ptr(), self.costs[s].data_ptr(), rf, cf, self.N, inst, F32, wu, wd,
                        var_inv_i, stream)
             (rc, cc) = self.shapes[1]
             wu, wd = weights[0]
