@@ -186,6 +186,22 @@ SSG_API int ssg_reproject_distance(const float* d_distance_in, float* d_distance
 SSG_API int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scratch, int cols, int rows, double max_dist,
                 int iterations, void* stream);
 
+/* Hole filling exactly as ssg_inpaint, for callers that cannot allocate device memory (a plugin
+ * inside a host application whose memory manager owns the device heap, or a hard real-time loop
+ * in which cudaMalloc may synchronise the device): the scratch map lives in a fixed 4 MiB array
+ * inside the library, held by every GPU that loads the library until the process exits.  The
+ * caller passes only the map and the table.  No counterpart in the reference.
+ *   - Maps of up to 1,048,576 pixels (e.g. 1024 x 1024); larger maps return
+ *     SSG_ERR_UNSUPPORTED without launching anything.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ *     and enables the kernel's shared memory; make that first call before any stream capture.
+ *   - Every call on a device shares the array: calls that overlap on the GPU (different streams
+ *     without ordering) race.  Each pass overwrites the whole scratch map it uses, so nothing a
+ *     previous call left there is read.
+ *   - No cudaMalloc / cudaFree or allocating library routine is called. */
+SSG_API int ssg_inpaint_noalloc(float* d_distance, const uint8_t* d_table, int cols, int rows, double max_dist,
+                                int iterations, void* stream);
+
 /* mergeRGBDPanoramaKernel, python/stitcher.cu:423-473.  d_reprojected, d_distances:
  * reference_count x rows x cols; d_images: reference_count x image_rows x image_cols x 3 uint8;
  * outputs pano_rows x pano_cols float32 distance and x 3 uint8 colour. */

@@ -79,6 +79,7 @@ SIGNATURES = {
     "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _P]),
     "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint_batch": (_I, [_P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
+    "ssg_inpaint_noalloc": (_I, [_P, _P, _I, _I, _D, _I, _P]),
     "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
 }
 
@@ -188,4 +189,6 @@ def kernels_launched(name: str, args) -> int:
         return -(-int(args[6]) // 16)
     if name == "ssg_inpaint_batch":
         return -(-int(args[8]) // 16)
+    if name == "ssg_inpaint_noalloc":
+        return -(-int(args[5]) // 16)
     return 1

@@ -617,3 +617,75 @@ extern "C" int ssg_merge_panorama_batch(const float* d_lut, const float* d_weigh
         d_distance_panorama, d_rgb_panorama);
     return launch_status("merge_kernel");
 }
+
+// ---------------------------------------------------------------------------------------------
+// Hole filling without any device allocation by the caller.
+//
+// ssg_inpaint alternates between the caller's map and a caller-owned scratch map.  Some callers
+// cannot allocate device memory for that scratch: a plugin inside a host application whose own
+// memory manager owns the device heap, or a hard real-time loop where cudaMalloc may synchronise
+// the device and stall it.  For them ssg_inpaint_noalloc keeps the scratch in this fixed array,
+// part of the library image: every GPU that loads the library holds these 4 MiB until the
+// process exits.  Maps up to kNoAllocMaxPixels pixels are accepted.
+// ---------------------------------------------------------------------------------------------
+namespace ssg {
+constexpr int64_t kNoAllocMaxPixels = int64_t(1) << 20;  // 4 MiB of float32, e.g. 1024 x 1024
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocMaxPixels];
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device (host
+// code only sees a host-side stand-in for the symbol, never its device address).
+static int noalloc_scratch_address(float** out)
+{
+    static std::atomic<float*> cached[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) return fail(SSG_ERR_UNSUPPORTED, "device ordinal %d beyond 63", dev);
+    float* p = cached[dev].load();
+    if (!p) {
+        e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_scratch);
+        if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+        cached[dev].store(p);
+    }
+    *out = p;
+    return SSG_OK;
+}
+}  // namespace ssg
+
+extern "C" int ssg_inpaint_noalloc(float* d_distance, const uint8_t* d_table, int cols, int rows, double max_dist,
+                                   int iterations, void* stream)
+{
+    SSG_REQUIRE(d_distance && d_table, "null pointer");
+    SSG_REQUIRE(cols > 0 && rows > 0 && iterations >= 0, "invalid sizes");
+    if ((int64_t)cols * rows > kNoAllocMaxPixels)
+        return fail(SSG_ERR_UNSUPPORTED,
+                    "ssg_inpaint_noalloc: a %d x %d map has %lld pixels, more than the %lld of its built-in scratch; "
+                    "use ssg_inpaint with a caller-allocated scratch map",
+                    cols, rows, (long long)cols * rows, (long long)kNoAllocMaxPixels);
+    float* scratch = nullptr;
+    if (int e = noalloc_scratch_address(&scratch)) return e;
+    if (int e = enable_inpaint_smem()) return e;
+    // every pass writes every pixel of its destination, so nothing left in the scratch by an
+    // earlier call is read
+    const float hole = float_at_least(max_dist + 0.1);
+    const float ok = float_at_most(max_dist + (double)0.1f);
+    dim3 grid((cols + kTileW - 1) / kTileW, (rows + kTileH - 1) / kTileH, 1);
+    float* a = d_distance;
+    float* b = scratch;
+    for (int done = 0; done < iterations;) {
+        const int steps = iterations - done < kHalo ? iterations - done : kHalo;
+        inpaint_tile_kernel<<<grid, kInpaintBlock, kInpaintSmem, as_stream(stream)>>>(
+            a, b, reinterpret_cast<const uchar2*>(d_table), cols, rows, 1, steps, hole, ok);
+        if (int e = launch_status("inpaint_tile_kernel")) return e;
+        float* t = a;
+        a = b;
+        b = t;
+        done += steps;
+    }
+    if (a != d_distance) {
+        cudaError_t e = cudaMemcpyAsync(d_distance, a, sizeof(float) * (size_t)cols * rows, cudaMemcpyDeviceToDevice,
+                                        as_stream(stream));
+        if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemcpyAsync: %s", cudaGetErrorString(e));
+    }
+    return SSG_OK;
+}
