@@ -304,7 +304,7 @@ def run_ours(args, rank, world, device, rendered):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
-        "roofline": {"bound": "hbm", "kernel": "sweep_fast_kernel", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "sweep_batch_kernel", "achieved": achieved, "peak": peak,
                      "peak_kind": f"{peak_kind} hbm_gbs (burst copy)", "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": None,
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms,

@@ -224,13 +224,18 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
  * SSG_STORAGE_UNORM16), the coarser levels as float32; all arithmetic is fp32.
  * ------------------------------------------------------------------------------------------- */
 
-/* Image staging + guides: d_images frames x cameras x pixels x 3 float32 (the inputs of
- * estimate_RGBD_panorama, python/depth_estimation.py:205-227) -> d_staged frames x cameras x
- * pixels float4 (RGB, 0) and d_guides frames x references x pixels x 3 uint8 (rgb2yCbCr + uint8
- * cast of each reference camera, python/utils.py:144-155). */
-SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int64_t pixels,
+/* Image staging + guides: d_images frames x cameras x rows x cols x 3, float32 (the inputs of
+ * estimate_RGBD_panorama, python/depth_estimation.py:205-227) or uint8 (the 8-bit images those
+ * inputs are made from, python/main.py:84-100) -> d_staged frames x cameras x (rows + 2) x
+ * (cols + 2) float4 texels (R, G, B, 0) with a one-texel border that the caller zeroes once and
+ * that is never written, and d_guides frames x references x rows x cols x 3 uint8 (rgb2yCbCr +
+ * uint8 cast of each reference camera, python/utils.py:144-155). */
+SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                              const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
                              void* stream);
+SSG_API int ssg_stage_images_u8(const uint8_t* d_images, int frames, int cameras, int cols, int rows,
+                                const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
+                                void* stream);
 
 /* Sphere sweep + cost for every instance (python/depth_estimation.py:141-175), 16-bit output.
  * relative_poses: references x cameras x 12 floats (host); d_selected: references x pixels
@@ -289,6 +294,59 @@ SSG_API int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights,
                                      int image_cols, const float* translations, const ssg_intrinsics* intrinsics,
                                      int reference_count, int cols, int rows, int pano_cols, int pano_rows, int frames,
                                      float* d_distance_panorama, uint8_t* d_rgb_panorama, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Differentiable sweep (no counterpart in the reference, whose selection is a hard argmin with
+ * a parabolic step, python/depth_estimation.py:179-198).  Forward: the fp32 sweep and ISB filter
+ * above, then a soft-argmin inverse distance q = sum_k softmax(-F_k / temperature) / d_k over the
+ * filtered costs F, fused with the last filter level.  Backward: the transposes of those linear
+ * steps (the filter's weights come from uint8 guides and receive no gradient) and of the sweep.
+ * Gradient buffers are float32 planar volumes like the forward's; atomic adds make the sums'
+ * order, and so their last bits, run-dependent.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Last ISB level (level 1 -> 0) fused with the soft-argmin: d_inverse_distance fine pixels. */
+SSG_API int ssg_isb_upsample_softargmin(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in, int cols_in,
+                                        const uint8_t* d_guide_fine, const float* d_cost_fine, int rows_fine,
+                                        int cols_fine, int candidate_count, float weight_up, float weight_down,
+                                        float var_inv_i, const float* candidates, float temperature,
+                                        float* d_inverse_distance, void* stream);
+
+/* Backward of ssg_isb_upsample_softargmin: writes dL/d(level-0 cost) (own-pixel part) and adds
+ * dL/d(filtered level 1) into d_grad_filtered_coarse (zero it first). */
+SSG_API int ssg_isb_upsample_softargmin_backward(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in,
+                                                 int cols_in, const uint8_t* d_guide_fine, const float* d_cost_fine,
+                                                 int rows_fine, int cols_fine, int candidate_count, float weight_up,
+                                                 float weight_down, float var_inv_i, const float* candidates,
+                                                 float temperature, const float* d_grad_inverse_distance,
+                                                 float* d_grad_cost_fine, float* d_grad_filtered_coarse,
+                                                 void* stream);
+
+/* Transpose of one upsampling step (python/isb_filter.cu:132-329): adds the own-pixel part of
+ * dL/d(filtered fine level) to d_grad_cost_fine and its coarse-tap part to
+ * d_grad_filtered_coarse.  d_guide_coarse: filtered coarse guide; d_guide_fine: the fine guide
+ * before its own upsampling step. */
+SSG_API int ssg_isb_upsample_transpose(const uint8_t* d_guide_coarse, int rows_in, int cols_in,
+                                       const uint8_t* d_guide_fine, int rows_fine, int cols_fine,
+                                       int candidate_count, float weight_up, float weight_down, float var_inv_i,
+                                       const float* d_grad_filtered_fine, float* d_grad_cost_fine,
+                                       float* d_grad_filtered_coarse, void* stream);
+
+/* Transpose of one downsampling step (python/isb_filter.cu:44-119): adds the coarse gradient,
+ * spread over the 3 x 3 taps, into d_grad_cost_fine. */
+SSG_API int ssg_isb_downsample_transpose(const uint8_t* d_guide_in, int rows_in, int cols_in, int rows_out,
+                                         int cols_out, int candidate_count, float var_inv_i,
+                                         const float* d_grad_cost_coarse, float* d_grad_cost_fine, void* stream);
+
+/* Backward of ssg_sweep_cost (python/depth_estimation.py:141-175): adds dL/d(image) into
+ * d_grad_images (camera_count device pointers, rows x cols x 3 float32) and the per-camera
+ * 6-DoF gradient into d_grad_pose (camera_count x 6 float64: rotation, then translation, of a
+ * right perturbation T <- T [Exp(omega), v] evaluated at zero). */
+SSG_API int ssg_sweep_cost_backward(int cols, int rows, int camera_count, const ssg_camera* cameras, int reference,
+                                    const float* relative_poses, const float* const* d_images,
+                                    float* const* d_grad_images, const int8_t* d_selected, const float* candidates,
+                                    int candidate_count, const float* d_grad_cost, double* d_grad_pose,
+                                    void* stream);
 
 #ifdef __cplusplus
 }

@@ -752,3 +752,118 @@ void sso_merge(const REAL* lut, const REAL* weights, const REAL* reproj, const R
         for (int ch = 0; ch < 3; ++ch) rgb_pano[3 * i + ch] = (uint8_t)(rgb[ch] > 255 ? 255 : rgb[ch]);
     }
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * ISB_Filter.apply as explicit linear operators on the cost (isb_filter.py:72-136): for a given
+ * guide the filter is linear in the cost, with weights from the guide pyramid.  Exported for
+ * the float64 autograd restatement of the differentiable sweep.
+ *   down level s = 1..L-1, coarse pixel o:  c_s[o] = sum_t down_w[s][9o+t] c_{s-1}[down_idx[s][9o+t]]
+ *   up step s = L-2..0, fine pixel p (level s):
+ *       f_s[p] = up_own[s][p] c_s[p] + sum_t up_w[s][9p+t] f_{s+1}[up_idx[s][9p+t]]
+ * with f_{L-1} = c_{L-1}.  Arrays are indexed by level; unused taps have weight 0.  The guide
+ * pyramid is updated exactly as the filter updates it.
+ * ------------------------------------------------------------------------------------------- */
+void sso_isb_operators(const uint8_t* guide, int rows, int cols, double sigma_i, double sigma_s,
+                       int32_t* const* down_idx, REAL* const* down_w, int32_t* const* up_idx, REAL* const* up_w,
+                       REAL* const* up_own)
+{
+    const int L = sso_isb_scale_count(cols, rows);
+    if (L < 2) return;
+    int r[64], c[64];
+    uint8_t* g[64];
+    for (int s = 0; s < L; ++s) {
+        r[s] = (int)ceil(rows / pow(2.0, s));
+        c[s] = (int)ceil(cols / pow(2.0, s));
+        g[s] = (uint8_t*)calloc((size_t)r[s] * c[s] * 3, 1);
+    }
+    memcpy(g[0], guide, (size_t)rows * cols * 3);
+    const double vs = 1 / (2 * sigma_s * sigma_s), vi = 1 / (2 * sigma_i * sigma_i);
+    const REAL var_inv_i = (REAL)(IS_F32 ? (double)(float)vi : vi);
+    for (int s = 1; s < L; ++s) {
+        const int ci = c[s - 1], ri = r[s - 1], co = c[s];
+        const long pout = (long)r[s] * co;
+        for (long o = 0; o < pout; ++o) {
+            int x = (int)(o % co), y = (int)(o / co);
+            int x2 = 2 * x, y2 = 2 * y;
+            int px = x2 + 1 < ci ? x2 + 1 : ci - 1, py = y2 + 1 < ri ? y2 + 1 : ri - 1;
+            int mx = x2 - 1 >= 0 ? x2 - 1 : 0, my = y2 - 1 >= 0 ? y2 - 1 : 0;
+            const long idx[9] = {(long)y2 * ci + x2, (long)my * ci + mx, (long)y2 * ci + mx, (long)py * ci + mx,
+                                 (long)py * ci + x2, (long)py * ci + px, (long)y2 * ci + px, (long)my * ci + px,
+                                 (long)my * ci + x2};
+            const uint8_t* gi = g[s - 1];
+            REAL cur[3] = {gi[3 * idx[0]], gi[3 * idx[0] + 1], gi[3 * idx[0] + 2]};
+            REAL w[9] = {1, 0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f};
+            REAL wsum = 1, gs[3] = {cur[0], cur[1], cur[2]};
+            for (int t = 1; t < 9; ++t) {
+                REAL nb[3] = {gi[3 * idx[t]], gi[3 * idx[t] + 1], gi[3 * idx[t] + 2]};
+                REAL d = abs_sum3(cur, nb);
+                w[t] = w[t] * (r_exp(-d * d * var_inv_i) + ISB_EPS);
+                wsum = wsum + w[t];
+                for (int ch = 0; ch < 3; ++ch) gs[ch] = gs[ch] + nb[ch] * w[t];
+            }
+            REAL den = 1 / wsum;
+            for (int ch = 0; ch < 3; ++ch) g[s][3 * o + ch] = (uint8_t)(gs[ch] * den);
+            for (int t = 0; t < 9; ++t) {
+                down_idx[s][9 * o + t] = (int32_t)idx[t];
+                down_w[s][9 * o + t] = w[t] / wsum;
+            }
+        }
+    }
+    static const int t1[9][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 0}, {1, 1}, {1, 2}, {2, 0}, {2, 1}, {2, 2}};
+    static const int t2[6][2] = {{1, 1}, {2, 1}, {1, 0}, {2, 0}, {1, 2}, {2, 2}};
+    static const int t3[6][2] = {{1, 1}, {1, 2}, {0, 1}, {0, 2}, {2, 1}, {2, 2}};
+    static const int t4[4][2] = {{1, 1}, {1, 2}, {2, 1}, {2, 2}};
+    static const REAL b1[9] = {1, 1, 1, 1, 8, 1, 1, 1, 1}, b2[6] = {8, 8, 1, 1, 1, 1},
+                      b3[6] = {8, 8, 1, 1, 1, 1}, b4[4] = {1, 1, 1, 1};
+    const int (*taps[4])[2] = {t1, t2, t3, t4};
+    const REAL* base[4] = {b1, b2, b3, b4};
+    const int ntap[4] = {9, 6, 6, 4};
+    for (int s = L - 2; s >= 0; --s) {
+        const double dist = pow(2.0, s) - 0.5;
+        const double wd = exp(-(dist * dist) * vs);
+        const REAL weight_down = (REAL)wd, weight_up = (REAL)(1 - wd);
+        const int ci = c[s + 1], ri = r[s + 1], cio = c[s], rio = r[s];
+        const long pf = (long)rio * cio;
+        for (long p = 0; p < pf * 9; ++p) { up_idx[s][p] = 0; up_w[s][p] = 0; }
+        uint8_t* gnew = (uint8_t*)malloc((size_t)pf * 3);
+        memcpy(gnew, g[s], (size_t)pf * 3);
+        for (long o = 0; o < (long)ri * ci; ++o) {
+            int x = (int)(o % ci), y = (int)(o / ci);
+            int mdx = x - 1 >= 0 ? x - 1 : 0, mdy = y - 1 >= 0 ? y - 1 : 0;
+            int pdx = x + 1 < ci ? x + 1 : ci - 1, pdy = y + 1 < ri ? y + 1 : ri - 1;
+            int x2 = 2 * x, y2 = 2 * y;
+            int pux = x2 + 1 < cio ? x2 + 1 : cio - 1, puy = y2 + 1 < rio ? y2 + 1 : rio - 1;
+            const int rr[3] = {mdy, y, pdy}, cc[3] = {mdx, x, pdx};
+            const long fidx[4] = {(long)y2 * cio + x2, (long)puy * cio + x2, (long)y2 * cio + pux, (long)puy * cio + pux};
+            const int set[4] = {1, y2 != puy, x2 != pux, (y2 != puy) && (x2 != pux)};
+            for (int f = 0; f < 4; ++f) {
+                const uint8_t* gf = g[s] + 3 * fidx[f];
+                REAL up[3] = {gf[0], gf[1], gf[2]};
+                REAL gs[3] = {weight_up * up[0], weight_up * up[1], weight_up * up[2]};
+                REAL wsum = weight_up, w[9];
+                long cidx[9];
+                for (int i = 0; i < ntap[f]; ++i) {
+                    const int a = taps[f][i][0], b = taps[f][i][1];
+                    cidx[i] = (long)rr[a] * ci + cc[b];
+                    const uint8_t* gc = g[s + 1] + 3 * cidx[i];
+                    REAL nb[3] = {gc[0], gc[1], gc[2]};
+                    REAL d = abs_sum3(nb, up);
+                    w[i] = base[f][i] * (weight_down * (r_exp(-d * d * var_inv_i) + ISB_EPS));
+                    for (int ch = 0; ch < 3; ++ch) gs[ch] = gs[ch] + nb[ch] * w[i];
+                    wsum = wsum + w[i];
+                }
+                if (!set[f]) continue;
+                REAL inv = 1 / wsum;
+                for (int ch = 0; ch < 3; ++ch) gnew[3 * fidx[f] + ch] = (uint8_t)(gs[ch] * inv);
+                up_own[s][fidx[f]] = weight_up * inv;
+                for (int i = 0; i < ntap[f]; ++i) {
+                    up_idx[s][9 * fidx[f] + i] = (int32_t)cidx[i];
+                    up_w[s][9 * fidx[f] + i] = w[i] * inv;
+                }
+            }
+        }
+        memcpy(g[s], gnew, (size_t)pf * 3);
+        free(gnew);
+    }
+    for (int s = 0; s < L; ++s) free(g[s]);
+}

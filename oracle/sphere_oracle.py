@@ -77,6 +77,7 @@ def _signatures(real):
         "sso_inpaint": [_P, _P, _I, _I, _D, _I],
         "sso_merge": [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P],
         "sso_set_exp_mode": [_I],
+        "sso_isb_operators": [_P, _I, _I, _D, _D, _P, _P, _P, _P, _P],
         "sso_cw_expf": [ctypes.c_float],
     }
 
@@ -167,6 +168,25 @@ class Oracle:
         n, rows, cols = cost.shape
         self.lib.sso_isb_apply(_ptr(guide), _ptr(cost), n, rows, cols, sigma_i, sigma_s)
         return cost, guide
+
+    def isb_operators(self, guide, sigma_i, sigma_s):
+        """The filter of isb_apply for this guide as explicit sparse operators (see
+        sso_isb_operators): dict with per-level lists down_idx/down_w ([P_s, 9], s >= 1) and
+        up_idx/up_w ([P_s, 9]) / up_own ([P_s]) (s <= L - 2), plus the level shapes."""
+        self.lib.sso_set_exp_mode(self.exp_mode)
+        guide = np.ascontiguousarray(guide, np.uint8)
+        rows, cols = guide.shape[:2]
+        L = self.isb_scale_count(cols, rows)
+        shapes = [(int(math.ceil(rows / 2 ** s)), int(math.ceil(cols / 2 ** s))) for s in range(L)]
+        di = [np.zeros((max(1, r * c), 9), np.int32) for r, c in shapes]
+        dw = [np.zeros((max(1, r * c), 9), self.dtype) for r, c in shapes]
+        ui = [np.zeros((max(1, r * c), 9), np.int32) for r, c in shapes]
+        uw = [np.zeros((max(1, r * c), 9), self.dtype) for r, c in shapes]
+        uo = [np.zeros((max(1, r * c),), self.dtype) for r, c in shapes]
+        arr = lambda xs: (ctypes.c_void_p * len(xs))(*[x.ctypes.data for x in xs])  # noqa: E731
+        self.lib.sso_isb_operators(_ptr(guide), rows, cols, sigma_i, sigma_s, arr(di), arr(dw), arr(ui), arr(uw),
+                                   arr(uo))
+        return {"shapes": shapes, "down_idx": di, "down_w": dw, "up_idx": ui, "up_w": uw, "up_own": uo}
 
     def isb_scale_count(self, cols, rows):
         return self.lib.sso_isb_scale_count(cols, rows)

@@ -9,9 +9,10 @@ The public names mirror the reference's modules; the compute runs in libsphere_s
 """
 from . import _native
 from .depth_estimation import RGBD_Estimator, distance_candidates
+from .differentiable import DifferentiableSweep
 from .isb_filter import ISB_Filter
 from .stitcher import Stitcher, vectorize_calibration
 from .utils import Calibration, parse_json_calib, project, rgb2yCbCr, rgb_to_guide, unproject
 
 __all__ = ["RGBD_Estimator", "ISB_Filter", "Stitcher", "Calibration", "parse_json_calib", "unproject", "project",
-           "rgb2yCbCr", "rgb_to_guide", "vectorize_calibration", "distance_candidates"]
+           "rgb2yCbCr", "rgb_to_guide", "vectorize_calibration", "distance_candidates", "DifferentiableSweep"]

@@ -70,7 +70,8 @@ SIGNATURES = {
     "ssg_reproject_distance": (_I, [_P, _P, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint": (_I, [_P, _P, _P, _I, _I, _D, _I, _P]),
     "ssg_merge_panorama": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P]),
-    "ssg_stage_images": (_I, [_P, _I, _I, _I64, _P, _I, _P, _P, _P]),
+    "ssg_stage_images": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P]),
+    "ssg_stage_images_u8": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P]),
     "ssg_sweep_cost_batch": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "ssg_isb_downsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _P]),
     "ssg_isb_upsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P]),
@@ -80,6 +81,12 @@ SIGNATURES = {
     "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint_batch": (_I, [_P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
     "ssg_inpaint_noalloc": (_I, [_P, _P, _I, _I, _D, _I, _P]),
+    "ssg_isb_upsample_softargmin": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P]),
+    "ssg_isb_upsample_softargmin_backward": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P, _P,
+                                                  _P]),
+    "ssg_isb_upsample_transpose": (_I, [_P, _I, _I, _P, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P]),
+    "ssg_isb_downsample_transpose": (_I, [_P, _I, _I, _I, _I, _I, _F, _P, _P, _P]),
+    "ssg_sweep_cost_backward": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
 }
 

@@ -1,327 +1,283 @@
 // ISB multiscale edge-aware cost filter (python/isb_filter.cu, python/isb_filter.py) and the
-// distance selection of python/depth_estimation.py:179-198, fp32 planar cost volumes
-// [candidates][rows][cols] as the reference's API has them.
+// distance selection of python/depth_estimation.py:179-198, for one cost volume in the reference's
+// planar layout [candidates][rows][cols] and for batches of volumes in the chunked layout of
+// ssg_cells.cuh.
 //
-// One thread per coarse pixel, as in the reference: the range weights of its 3x3 neighbourhood
-// are computed once from the uint8 guides and shared by all candidates.  Consecutive threads
-// touch consecutive pixels of each candidate plane, so loads and stores coalesce.  Arithmetic
-// is the reference's, in its order, with the exponential of ssg_common.cuh.
+// Both layouts run the same kernels, templated on the cell width W (1 = planar, 8 = chunked):
+//   - downsampling: one thread per coarse pixel; its 3x3 range weights are computed once from the
+//     uint8 guides and shared by all candidates;
+//   - upsampling: one thread per fine pixel, with the coarse neighbourhood of a block staged in
+//     shared memory per chunk of candidates;
+//   - the last upsampling step can be fused with the selection, so that the filtered level-0
+//     volume is never written.
+// Guides, range weights and cost sums use the reference's arithmetic in its order
+// (ssg_isb_common.cuh), so both layouts give the same bits; the batched path differs from the
+// reference only by the 16-bit rounding of its level-0 volume.
 #include <cmath>
 
-#include "ssg_common.cuh"
+#include "ssg_cells.cuh"
+#include "ssg_isb_common.cuh"
 
 namespace ssg {
 
-constexpr int kIsbBlock = 256;
-constexpr float kIsbEps = 0.01f;  // isb_filter.cu:32
+// ---------------------------------------------------------------------------------------------
+// ISB filter on the chunked layout. Guides and range weights come from the same device functions
+// as the fp32 path (ssg_isb_common.cuh), so the guide pyramid is bit-identical to it: the uint8
+// truncation of the filtered guide turns a one-ulp change of a weight into a step of one grey
+// level on a sizeable share of coarse pixels, which then moves the argmin. The costs are summed
+// in the fp32 path's order as well; the level-0 rounding is the only difference.
+// ---------------------------------------------------------------------------------------------
+struct LevelGeom {
+    int rows_in, cols_in, rows_out, cols_out;
+};
 
-__device__ __forceinline__ float range_weight(float d, float var_inv_i)
+// Downsampling, one thread per coarse pixel; level 0 (any storage) or a float32 level in,
+// float32 out.
+template <int W, typename Tin>
+__global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __restrict__ guide_in,
+                                                                   const Tin* __restrict__ cost_in,
+                                                                   uint8_t* __restrict__ guide_out,
+                                                                   float* __restrict__ cost_out, LevelGeom g,
+                                                                   int chunks, float var_inv_i)
 {
-    // __expf(-diff * diff * varInvI) + EPS  (isb_filter.cu:87, :229)
-    return fadd(cw_expf(fmul(fmul(-d, d), var_inv_i)), kIsbEps);
-}
-
-__device__ __forceinline__ float abs_sum(const float a[3], const float b[3])
-{
-    return fadd(fadd(fabsf(fsub(a[0], b[0])), fabsf(fsub(a[1], b[1]))), fabsf(fsub(a[2], b[2])));
-}
-
-__device__ __forceinline__ void load_guide(const uint8_t* __restrict__ g, int64_t idx, float out[3])
-{
-    out[0] = (float)g[3 * idx];
-    out[1] = (float)g[3 * idx + 1];
-    out[2] = (float)g[3 * idx + 2];
-}
-
-// guideDownsample2xKernel, isb_filter.cu:44-119
-__global__ void __launch_bounds__(kIsbBlock) isb_down_kernel(const uint8_t* __restrict__ guide_in,
-                                                             const float* __restrict__ cost_in, int rows_in,
-                                                             int cols_in, uint8_t* __restrict__ guide_out,
-                                                             float* __restrict__ cost_out, int rows_out,
-                                                             int cols_out, int ncand, float var_inv_i)
-{
-    const int64_t pout = (int64_t)rows_out * cols_out, pin = (int64_t)rows_in * cols_in;
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pout) return;
-    // blockIdx.y: instance of a batch of equally sized, contiguous levels
-    guide_in += (int64_t)blockIdx.y * pin * 3;
-    guide_out += (int64_t)blockIdx.y * pout * 3;
-    cost_in += (int64_t)blockIdx.y * ncand * pin;
-    cost_out += (int64_t)blockIdx.y * ncand * pout;
-    const int x = (int)(o % cols_out), y = (int)(o / cols_out);
-    const int x2 = 2 * x, y2 = 2 * y;
-    const int px = min(x2 + 1, cols_in - 1), py = min(y2 + 1, rows_in - 1);
-    const int mx = max(x2 - 1, 0), my = max(y2 - 1, 0);
-    const int64_t idx[8] = {(int64_t)my * cols_in + mx, (int64_t)y2 * cols_in + mx, (int64_t)py * cols_in + mx,
-                            (int64_t)py * cols_in + x2, (int64_t)py * cols_in + px, (int64_t)y2 * cols_in + px,
-                            (int64_t)my * cols_in + px, (int64_t)my * cols_in + x2};
-    const int64_t ic = (int64_t)y2 * cols_in + x2;
-    float cur[3];
-    load_guide(guide_in, ic, cur);
-    float w[8] = {0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f};
-    float wsum = 1.0f, g[3] = {cur[0], cur[1], cur[2]};
+    const int inst = blockIdx.y;
+    guide_in += (int64_t)inst * pin * 3;
+    guide_out += (int64_t)inst * pout * 3;
+    cost_in += (int64_t)inst * chunks * pin * W;
+    cost_out += (int64_t)inst * chunks * pout * W;
+    DownTapsT<int> t;
+    down_weights(guide_in, g.rows_in, g.cols_in, (int)(o % g.cols_out), (int)(o / g.cols_out), var_inv_i,
+                 guide_out + 3 * o, t);
+    for (int c = 0; c < chunks; ++c) {
+        const Tin* src = cost_in + (int64_t)c * pin * W;
+        float acc[W];
+        CellIO<W, Tin>::load(src + (int64_t)t.centre * W, acc);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        float nb[3];
-        load_guide(guide_in, idx[i], nb);
-        w[i] = fmul(w[i], range_weight(abs_sum(cur, nb), var_inv_i));
-        wsum = fadd(wsum, w[i]);
+        for (int i = 0; i < 8; ++i) {
+            float v[W];
+            CellIO<W, Tin>::load(src + (int64_t)t.idx[i] * W, v);
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul(nb[ch], w[i]));
-    }
-    const float den = fdiv(1.0f, wsum);
+            for (int j = 0; j < W; ++j) acc[j] = fadd(acc[j], fmul(v[j], t.w[i]));
+        }
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) guide_out[3 * o + ch] = (uint8_t)__float2uint_rz(fmul(g[ch], den));
-    for (int z = 0; z < ncand; ++z) {
-        const float* c = cost_in + (int64_t)z * pin;
-        float s = __ldg(c + ic);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) s = fadd(s, fmul(__ldg(c + idx[i]), w[i]));
-        cost_out[(int64_t)z * pout + o] = fdiv(s, wsum);
+        for (int j = 0; j < W; ++j) acc[j] = fdiv(acc[j], t.wsum);
+        CellIO<W, float>::store(cost_out + ((int64_t)c * pout + o) * W, acc);
     }
 }
 
-// Weights of the four fine pixels of one coarse pixel (isb_filter.cu:142-267): taps index the
-// 3x3 coarse neighbourhood [row][col] flattened as 3 * row + col.
-struct UpWeights {
-    float w1[9], w2[6], w3[6], w4[4];
-    float inv[4];
-    int64_t cidx[9];
-    int64_t fidx[4];
-    bool set[4];
+// ---------------------------------------------------------------------------------------------
+// Upsampling, one thread per fine pixel.  A block covers kUpTileX coarse pixels of one coarse
+// row: warp w takes fine pixel F = w % 4 (UpTaps<F>) of coarse pixels 32 * (w / 4) + lane, so
+// that all lanes of a warp follow one tap list.  The coarse costs of the block's 3 x (kUpTileX + 2)
+// neighbourhood (edge-clamped, as the taps are) are staged per chunk in shared memory with
+// cp.async, double-buffered: each coarse cell is read from memory once per block instead of
+// once per tap, and the next chunk streams in while this one is filtered.
+// ---------------------------------------------------------------------------------------------
+constexpr int kUpTileX = kBatchBlock / 4;
+constexpr int kUpTileCols = kUpTileX + 2;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+// Tile of one chunk: [part][row 0..2][col 0..kUpTileCols-1] with parts of 4 floats (W = 8: two
+// parts, float4 elements) or one part of single floats (W = 1).
+template <int W>
+struct UpTile {
+    static constexpr int parts = W == 8 ? 2 : 1;
+    static constexpr int elem = W == 8 ? 4 : 1;
+    static constexpr int floats = parts * 3 * kUpTileCols * elem;
 };
 
-// Tap lists of the fine pixels below, right and below-right (isb_filter.cu:185-208), as indices
-// into the flattened 3x3 neighbourhood; written out so that every index is a compile-time
-// constant and the neighbourhood stays in registers.
-#define SSG_TAPS2(a) {a[4], a[7], a[3], a[6], a[5], a[8]}  // (1,1),(2,1),(1,0),(2,0),(1,2),(2,2)
-#define SSG_TAPS3(a) {a[4], a[5], a[1], a[2], a[7], a[8]}  // (1,1),(1,2),(0,1),(0,2),(2,1),(2,2)
-#define SSG_TAPS4(a) {a[4], a[5], a[7], a[8]}              // (1,1),(1,2),(2,1),(2,2)
-
-__device__ __forceinline__ void up_weights(const uint8_t* __restrict__ guide_in, int rows_in, int cols_in,
-                                           uint8_t* __restrict__ guide_io, int rows_io, int cols_io, int x, int y,
-                                           float weight_up, float weight_down, float var_inv_i, UpWeights& u)
+template <int W>
+__device__ __forceinline__ void load_tile_async(float* __restrict__ buf, const float* __restrict__ chunk,
+                                                int rows_in, int cols_in, int x0, int y)
 {
-    const int mdx = max(x - 1, 0), mdy = max(y - 1, 0);
-    const int pdx = min(x + 1, cols_in - 1), pdy = min(y + 1, rows_in - 1);
-    const int x2 = 2 * x, y2 = 2 * y;
-    const int pux = min(x2 + 1, cols_io - 1), puy = min(y2 + 1, rows_io - 1);
-    const int rr[3] = {mdy, y, pdy}, cc[3] = {mdx, x, pdx};
-    float gd[9][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            u.cidx[3 * a + b] = (int64_t)rr[a] * cols_in + cc[b];
-            load_guide(guide_in, u.cidx[3 * a + b], gd[3 * a + b]);
-        }
-    u.fidx[0] = (int64_t)y2 * cols_io + x2;
-    u.fidx[1] = (int64_t)puy * cols_io + x2;
-    u.fidx[2] = (int64_t)y2 * cols_io + pux;
-    u.fidx[3] = (int64_t)puy * cols_io + pux;
-    u.set[0] = true;
-    u.set[1] = y2 != puy;
-    u.set[2] = x2 != pux;
-    u.set[3] = u.set[1] && u.set[2];
-    float up[4][3];
-#pragma unroll
-    for (int f = 0; f < 4; ++f) load_guide(guide_io, u.fidx[f], up[f]);
-    const float b1[9] = {1, 1, 1, 1, 8, 1, 1, 1, 1};
-    const float b23[6] = {8, 8, 1, 1, 1, 1};
-    float g[4][3], ws[4];
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        ws[f] = weight_up;
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[f][ch] = fmul(weight_up, up[f][ch]);
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-        const float* nb = gd[i];
-        u.w1[i] = fmul(b1[i], fmul(weight_down, range_weight(abs_sum(nb, up[0]), var_inv_i)));
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[0][ch] = fadd(g[0][ch], fmul(nb[ch], u.w1[i]));
-        ws[0] = fadd(ws[0], u.w1[i]);
-    }
-    const float* g2[6] = SSG_TAPS2(gd);
-    const float* g3[6] = SSG_TAPS3(gd);
-    const float* g4[4] = SSG_TAPS4(gd);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const float* nb2 = g2[i];
-        u.w2[i] = fmul(b23[i], fmul(weight_down, range_weight(abs_sum(nb2, up[1]), var_inv_i)));
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[1][ch] = fadd(g[1][ch], fmul(nb2[ch], u.w2[i]));
-        ws[1] = fadd(ws[1], u.w2[i]);
-        const float* nb3 = g3[i];
-        u.w3[i] = fmul(b23[i], fmul(weight_down, range_weight(abs_sum(nb3, up[2]), var_inv_i)));
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[2][ch] = fadd(g[2][ch], fmul(nb3[ch], u.w3[i]));
-        ws[2] = fadd(ws[2], u.w3[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const float* nb = g4[i];
-        u.w4[i] = fmul(weight_down, range_weight(abs_sum(nb, up[3]), var_inv_i));
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[3][ch] = fadd(g[3][ch], fmul(nb[ch], u.w4[i]));
-        ws[3] = fadd(ws[3], u.w4[i]);
-    }
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        u.inv[f] = fdiv(1.0f, ws[f]);
-        if (u.set[f])
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch)
-                guide_io[3 * u.fidx[f] + ch] = (uint8_t)__float2uint_rz(fmul(g[f][ch], u.inv[f]));
+    constexpr int cells = 3 * kUpTileCols;
+    for (int e = threadIdx.x; e < UpTile<W>::parts * cells; e += blockDim.x) {
+        const int part = e / cells, rc = e % cells;
+        const int row = rc / kUpTileCols, col = rc % kUpTileCols;
+        const int gx = min(max(x0 - 1 + col, 0), cols_in - 1), gy = min(max(y - 1 + row, 0), rows_in - 1);
+        const float* src = chunk + ((int64_t)gy * cols_in + gx) * W + part * 4;
+        if constexpr (W == 8)
+            cp_async16(buf + e * 4, src);
+        else
+            cp_async4(buf + e, src);
     }
 }
 
-// Filtered fine costs of one candidate plane (isb_filter.cu:270-327)
-__device__ __forceinline__ void up_costs(const UpWeights& u, const float* __restrict__ c,
-                                         const float* __restrict__ fine, float weight_up, float out[4])
+// coarse tap (row a, col b) of local coarse column lx, all W candidates
+template <int W>
+__device__ __forceinline__ void tile_tap(const float* __restrict__ buf, int a, int b, int lx, float v[W])
 {
-    float cd[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) cd[t] = __ldg(c + u.cidx[t]);
-    float s = fmul(weight_up, fine[u.fidx[0]]);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) s = fadd(s, fmul(u.w1[i], cd[i]));
-    out[0] = fmul(s, u.inv[0]);
-    const float c2[6] = SSG_TAPS2(cd);
-    const float c3[6] = SSG_TAPS3(cd);
-    const float c4[4] = SSG_TAPS4(cd);
-    if (u.set[1]) {
-        s = fmul(weight_up, fine[u.fidx[1]]);
-#pragma unroll
-        for (int i = 0; i < 6; ++i) s = fadd(s, fmul(u.w2[i], c2[i]));
-        out[1] = fmul(s, u.inv[1]);
-    }
-    if (u.set[2]) {
-        s = fmul(weight_up, fine[u.fidx[2]]);
-#pragma unroll
-        for (int i = 0; i < 6; ++i) s = fadd(s, fmul(u.w3[i], c3[i]));
-        out[2] = fmul(s, u.inv[2]);
-    }
-    if (u.set[3]) {
-        s = fmul(weight_up, fine[u.fidx[3]]);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) s = fadd(s, fmul(u.w4[i], c4[i]));
-        out[3] = fmul(s, u.inv[3]);
+    const int cell = a * kUpTileCols + lx + b;
+    if constexpr (W == 8) {
+        const float4 lo = reinterpret_cast<const float4*>(buf)[cell];
+        const float4 hi = reinterpret_cast<const float4*>(buf)[3 * kUpTileCols + cell];
+        v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
+        v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
+    } else {
+        v[0] = buf[cell];
     }
 }
 
-// guideUpsample2xKernel, isb_filter.cu:132-329
-__global__ void __launch_bounds__(kIsbBlock) isb_up_kernel(const uint8_t* __restrict__ guide_in,
-                                                           const float* __restrict__ cost_in, int rows_in,
-                                                           int cols_in, uint8_t* __restrict__ guide_io,
-                                                           float* __restrict__ cost_io, int rows_io, int cols_io,
-                                                           int ncand, float weight_up, float weight_down,
-                                                           float var_inv_i)
+// filtered costs of fine pixel F (the arithmetic and order of up_costs)
+template <int F, int W>
+__device__ __forceinline__ void tile_filter(const float* __restrict__ buf, int lx, const float (&w)[9], float inv,
+                                            float weight_up, float acc[W])
 {
-    const int64_t pin = (int64_t)rows_in * cols_in, pio = (int64_t)rows_io * cols_io;
-    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= pin) return;
-    guide_in += (int64_t)blockIdx.y * pin * 3;
-    guide_io += (int64_t)blockIdx.y * pio * 3;
-    cost_in += (int64_t)blockIdx.y * ncand * pin;
-    cost_io += (int64_t)blockIdx.y * ncand * pio;
-    UpWeights u;
-    up_weights(guide_in, rows_in, cols_in, guide_io, rows_io, cols_io, (int)(o % cols_in), (int)(o / cols_in),
-               weight_up, weight_down, var_inv_i, u);
-    for (int z = 0; z < ncand; ++z) {
-        float* fine = cost_io + (int64_t)z * pio;
-        float out[4];
-        up_costs(u, cost_in + (int64_t)z * pin, fine, weight_up, out);
 #pragma unroll
-        for (int f = 0; f < 4; ++f)
-            if (u.set[f]) fine[u.fidx[f]] = out[f];
+    for (int j = 0; j < W; ++j) acc[j] = fmul(weight_up, acc[j]);
+#pragma unroll
+    for (int i = 0; i < UpTaps<F>::n; ++i) {
+        const int t = UpTaps<F>::tap(i);
+        float v[W];
+        tile_tap<W>(buf, t / 3, t % 3, lx, v);
+#pragma unroll
+        for (int j = 0; j < W; ++j) acc[j] = fadd(acc[j], fmul(w[i], v[j]));
     }
+#pragma unroll
+    for (int j = 0; j < W; ++j) acc[j] = fmul(acc[j], inv);
 }
 
-// Running argmin / max with the neighbours of the argmin (depth_estimation.py:180-187):
-// the first minimum wins ties, as torch.min(dim) does.
-struct Selector {
-    float m, M, L, R, prev;
-    int idx;
-    bool need_right;
-    __device__ __forceinline__ void push(int z, float c)
-    {
-        if (z == 0) {
-            m = M = L = prev = c;
-            idx = 0;
-            need_right = true;
-            return;
-        }
-        if (need_right) {
-            R = c;
-            need_right = false;
-        }
-        if (c < m) {
-            m = c;
-            idx = z;
-            L = prev;
-            need_right = true;
-        }
-        if (c > M) M = c;
-        prev = c;
-    }
+template <int F>
+__device__ __forceinline__ float fine_weights_padded(const float (&gd)[9][3], const float up[3], float weight_up,
+                                                     float weight_down, float var_inv_i, float (&w)[9], float g[3])
+{
+    float wf[UpTaps<F>::n];
+    const float inv = fine_weights<F>(gd, up, weight_up, weight_down, var_inv_i, wf, g);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) w[i] = i < UpTaps<F>::n ? wf[i < UpTaps<F>::n ? i : 0] : 0.0f;  // (no dead-branch index past n)
+    return inv;
+}
+
+struct SelectOut {
+    float d0, dl, q;
+    float* distance;
+    int32_t* index;
+    bool write_guide;  // the selecting step also writes the filtered level-0 guide
 };
 
-// depth_estimation.py:188-198
-__device__ __forceinline__ float select_from(Selector s, int ncand, float d0, float dl, float q)
+// kSelect = false: coarse float32 -> fine float32 in place (and the fine guide);
+// kSelect = true: the last step, fine level-0 costs of type Tf in, the selection out.
+template <int W, typename Tf, bool kSelect>
+__global__ void __launch_bounds__(kBatchBlock) isb_up_kernel(const uint8_t* __restrict__ guide_in,
+                                                                 const float* __restrict__ cost_in,
+                                                                 uint8_t* __restrict__ guide_io,
+                                                                 Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
+                                                                 int ncand, float weight_up, float weight_down,
+                                                                 float var_inv_i, SelectOut so)
 {
-    if (s.need_right) s.R = s.m;  // argmin at the last candidate: clamp(idx + 1) = idx
-    float var = fdiv(fmul(0.5f, fsub(s.L, s.R)), fadd(fsub(fadd(s.L, s.R), fmul(2.0f, s.m)), 1e-8f));
-    var = var < -0.5f ? -0.5f : (var > 0.5f ? 0.5f : var);
-    if (s.idx == ncand - 1 || s.idx == 0) var = 0.0f;
-    float sel = fadd((float)s.idx, var);
-    if (s.M == s.m) sel = (float)(ncand - 1);
-    float d = fdiv(d0, fadd(fdiv(fmul(q, sel), (float)(ncand - 1)), 1.0f));
-    if (fabsf(fsub(s.M, s.m)) < 1e-8f) d = dl;
-    return d;
+    __shared__ __align__(16) float tile[2][UpTile<W>::floats];
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
+    const int inst = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kUpTileX;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int F = warp & 3;
+    const int lx = (warp >> 2) * 32 + lane, x = x0 + lx;
+    guide_in += (int64_t)inst * pin * 3;
+    guide_io += (int64_t)inst * pio * 3;
+    cost_in += (int64_t)inst * chunks * pin * W;
+    cost_fine += (int64_t)inst * chunks * pio * W;
+    const int fx = 2 * x + (F >= 2 ? 1 : 0), fy = 2 * y + (F & 1);
+    // a fine pixel outside the level is the clamped duplicate of another one and is skipped
+    const bool active = x < g.cols_in && fx < g.cols_out && fy < g.rows_out;
+    const int fi = fy * g.cols_out + fx;
+    float w[9], inv = 0.0f;
+    if (active) {
+        int ci[9];
+        float gd[9][3], up[3], gsum[3];
+        coarse_neighbourhood(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+        load_guide(guide_io, fi, up);
+        switch (F) {
+            case 0: inv = fine_weights_padded<0>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
+            case 1: inv = fine_weights_padded<1>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
+            case 2: inv = fine_weights_padded<2>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
+            default: inv = fine_weights_padded<3>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
+        }
+        if (!kSelect || so.write_guide)
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) guide_io[3 * fi + ch] = (uint8_t)__float2uint_rz(fmul(gsum[ch], inv));
+    }
+    Selector s;
+    load_tile_async<W>(tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
+    cp_async_commit();
+    for (int c = 0; c < chunks; ++c) {
+        if (c + 1 < chunks)
+            load_tile_async<W>(tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in, x0, y);
+        cp_async_commit();
+        cp_async_wait_one();  // this chunk's tile has landed
+        __syncthreads();
+        if (active) {
+            Tf* fc = cost_fine + ((int64_t)c * pio + fi) * W;
+            const float* buf = tile[c & 1];
+            float acc[W];
+            CellIO<W, Tf>::load(fc, acc);
+            switch (F) {
+                case 0: tile_filter<0, W>(buf, lx, w, inv, weight_up, acc); break;
+                case 1: tile_filter<1, W>(buf, lx, w, inv, weight_up, acc); break;
+                case 2: tile_filter<2, W>(buf, lx, w, inv, weight_up, acc); break;
+                default: tile_filter<3, W>(buf, lx, w, inv, weight_up, acc); break;
+            }
+            if constexpr (kSelect) {
+#pragma unroll
+                for (int j = 0; j < W; ++j)
+                    if (c * W + j < ncand) s.push(c * W + j, acc[j]);
+            } else {
+                CellIO<W, float>::store(reinterpret_cast<float*>(fc), acc);
+            }
+        }
+        __syncthreads();  // the tile is refilled two chunks on
+    }
+    if constexpr (kSelect) {
+        if (active) {
+            so.distance[(int64_t)inst * pio + fi] = select_from(s, ncand, so.d0, so.dl, so.q);
+            if (so.index) so.index[(int64_t)inst * pio + fi] = s.idx;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(kIsbBlock) select_distance_kernel(const float* __restrict__ cost, int ncand,
-                                                                    int64_t P, float d0, float dl, float q,
-                                                                    float* __restrict__ distance,
-                                                                    int32_t* __restrict__ index)
+// Selection from an unfiltered level-0 volume (pyramids of fewer than two levels, or the
+// reference's own select_distance on a filtered planar volume)
+template <int W, typename T>
+__global__ void __launch_bounds__(kBatchBlock) select_kernel(const T* __restrict__ cost, int64_t P, int chunks,
+                                                            int ncand, float d0, float dl, float q,
+                                                            float* __restrict__ distance,
+                                                            int32_t* __restrict__ index)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
+    const int inst = blockIdx.y;
+    cost += (int64_t)inst * chunks * P * W;
     Selector s;
-    for (int z = 0; z < ncand; ++z) s.push(z, __ldg(cost + (int64_t)z * P + i));
-    distance[i] = select_from(s, ncand, d0, dl, q);
-    if (index) index[i] = s.idx;
+    for (int c = 0; c < chunks; ++c) {
+        float v[W];
+        CellIO<W, T>::load(cost + ((int64_t)c * P + i) * W, v);
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+            if (c * W + j < ncand) s.push(c * W + j, v[j]);
+    }
+    distance[(int64_t)inst * P + i] = select_from(s, ncand, d0, dl, q);
+    if (index) index[(int64_t)inst * P + i] = s.idx;
 }
 
-// Last upsampling step fused with the selection: the level-0 filtered costs stay in registers
-__global__ void __launch_bounds__(kIsbBlock) isb_up_select_kernel(
-    const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in, int rows_in, int cols_in,
-    uint8_t* __restrict__ guide_io, const float* __restrict__ cost_fine, int rows_io, int cols_io, int ncand,
-    float weight_up, float weight_down, float var_inv_i, float d0, float dl, float q, float* __restrict__ distance,
-    int32_t* __restrict__ index)
+static int chunks_of(int n) { return (n + 7) / 8; }
+
+// blocks of kUpTileX coarse pixels of one coarse row, per instance
+static dim3 up_grid(int cols_in, int rows_in, int instances)
 {
-    const int64_t pin = (int64_t)rows_in * cols_in, pio = (int64_t)rows_io * cols_io;
-    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= pin) return;
-    UpWeights u;
-    up_weights(guide_in, rows_in, cols_in, guide_io, rows_io, cols_io, (int)(o % cols_in), (int)(o / cols_in),
-               weight_up, weight_down, var_inv_i, u);
-    Selector s[4];
-    for (int z = 0; z < ncand; ++z) {
-        float out[4];
-        up_costs(u, cost_in + (int64_t)z * pin, cost_fine + (int64_t)z * pio, weight_up, out);
-#pragma unroll
-        for (int f = 0; f < 4; ++f)
-            if (u.set[f]) s[f].push(z, out[f]);
-    }
-#pragma unroll
-    for (int f = 0; f < 4; ++f)
-        if (u.set[f]) {
-            distance[u.fidx[f]] = select_from(s[f], ncand, d0, dl, q);
-            if (index) index[u.fidx[f]] = s[f].idx;
-        }
+    return dim3((unsigned)((cols_in + kUpTileX - 1) / kUpTileX), (unsigned)rows_in, (unsigned)instances);
 }
 
 static int level_rows(int rows, int s) { return (int)std::ceil(rows / std::pow(2.0, s)); }
@@ -346,17 +302,92 @@ static Levels isb_constants(int level_count, double sigma_i, double sigma_s)
     return l;
 }
 
-static void candidate_constants(const float* candidates, int ncand, float& d0, float& dl, float& q)
+// (candidates[0] / candidates[-1] - 1) in float32, depth_estimation.py:195-196
+static SelectOut select_constants(const float* candidates, int ncand, float* distance, int32_t* index,
+                                  bool write_guide)
 {
-    d0 = candidates[0];
-    dl = candidates[ncand - 1];
-    q = d0 / dl - 1.0f;  // (candidates[0] / candidates[-1] - 1), float32
+    const float d0 = candidates[0], dl = candidates[ncand - 1];
+    return SelectOut{d0, dl, d0 / dl - 1.0f, distance, index, write_guide};
+}
+
+static int check_levels(int rows_in, int cols_in, int rows_out, int cols_out)
+{
+    SSG_REQUIRE(rows_in > 0 && cols_in > 0 && rows_out > 0 && cols_out > 0, "sizes must be positive");
+    SSG_REQUIRE((int64_t)rows_in * cols_in < ((int64_t)1 << 31) && rows_in <= 65535 && rows_out <= 65535,
+                "a level of %dx%d pixels is too large", rows_in, cols_in);
+    SSG_REQUIRE(2 * (rows_out - 1) < rows_in && 2 * (cols_out - 1) < cols_in && (rows_in + 1) / 2 <= rows_out &&
+                    (cols_in + 1) / 2 <= cols_out,
+                "level %dx%d is not the 2x downsampling of %dx%d", rows_out, cols_out, rows_in, cols_in);
+    return SSG_OK;
+}
+
+// --- launches shared by both layouts ---------------------------------------------------------
+template <int W, typename Tin>
+static int launch_down(const uint8_t* gi, const Tin* ci, int ri, int cl_i, uint8_t* go, float* co, int ro, int cl_o,
+                       int chunks, int instances, float var_inv_i, cudaStream_t st)
+{
+    const LevelGeom g{ri, cl_i, ro, cl_o};
+    const dim3 grid(grid_1d((int64_t)ro * cl_o, kBatchBlock), instances);
+    isb_down_kernel<W, Tin><<<grid, kBatchBlock, 0, st>>>(gi, ci, go, co, g, chunks, var_inv_i);
+    return launch_status("isb_down_kernel");
+}
+
+template <int W, typename Tf, bool kSelect>
+static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t* gio, Tf* cf, int rf, int cf_cols,
+                     int chunks, int ncand, int instances, float wu, float wd, float var_inv_i, const SelectOut& so,
+                     cudaStream_t st)
+{
+    const LevelGeom g{rc, cc, rf, cf_cols};
+    isb_up_kernel<W, Tf, kSelect><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks,
+                                                                                      ncand, wu, wd, var_inv_i, so);
+    return launch_status(kSelect ? "isb_up_kernel<select>" : "isb_up_kernel");
+}
+
+// the whole filter on planar levels (W = 1, chunks = candidates): python/isb_filter.py:72-136
+static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
+                        int candidate_count, int instances, double sigma_i, double sigma_s, cudaStream_t st)
+{
+    const Levels c = isb_constants(level_count, sigma_i, sigma_s);
+    for (int s = 1; s < level_count; ++s) {
+        const int ri = level_rows(rows, s - 1), ci = level_rows(cols, s - 1), ro = level_rows(rows, s),
+                  co = level_rows(cols, s);
+        if (int e = check_levels(ri, ci, ro, co)) return e;
+        if (int e = launch_down<1, float>(d_guides[s - 1], d_costs[s - 1], ri, ci, d_guides[s], d_costs[s], ro, co,
+                                          candidate_count, instances, c.var_inv_i, st))
+            return e;
+    }
+    for (int s = level_count - 2; s >= 0; --s) {
+        const int rc = level_rows(rows, s + 1), cc = level_rows(cols, s + 1), rf = level_rows(rows, s),
+                  cf = level_rows(cols, s);
+        if (int e = launch_up<1, float, false>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s], rf, cf,
+                                               candidate_count, candidate_count, instances, c.weight_up[s],
+                                               c.weight_down[s], c.var_inv_i, SelectOut{}, st))
+            return e;
+    }
+    return SSG_OK;
+}
+
+static int check_apply_args(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
+                            int candidate_count, double sigma_i, double sigma_s)
+{
+    SSG_REQUIRE(d_guides && d_costs, "null level arrays");
+    const int expected = cols > 0 && rows > 0 ? (int)(std::fmin(std::log2((double)cols), std::log2((double)rows)) - 1) : 0;
+    SSG_REQUIRE(level_count == expected, "level_count %d differs from the pyramid of a %dx%d image (%d)", level_count,
+                cols, rows, expected);
+    SSG_REQUIRE(level_count <= SSG_MAX_LEVELS, "too many levels");
+    SSG_REQUIRE(candidate_count >= 1 && candidate_count <= 65535, "candidate_count out of range");
+    SSG_REQUIRE(sigma_i > 0 && sigma_s > 0, "sigmas must be positive");
+    for (int s = 0; s < level_count; ++s) SSG_REQUIRE(d_guides[s] && d_costs[s], "level %d is NULL", s);
+    return SSG_OK;
 }
 
 }  // namespace ssg
 
 using namespace ssg;
 
+// ---------------------------------------------------------------------------------------------
+// One planar volume, the reference's layout (python/isb_filter.py, depth_estimation.py:179-198)
+// ---------------------------------------------------------------------------------------------
 extern "C" int ssg_isb_level_count(int cols, int rows)
 {
     if (cols <= 0 || rows <= 0) return 0;
@@ -368,15 +399,10 @@ extern "C" int ssg_isb_downsample(const uint8_t* d_guide_in, const float* d_cost
                                   int candidate_count, float var_inv_i, void* stream)
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_out && d_cost_out, "null device pointer");
-    SSG_REQUIRE(rows_in > 0 && cols_in > 0 && rows_out > 0 && cols_out > 0, "sizes must be positive");
-    SSG_REQUIRE(2 * (rows_out - 1) < rows_in && 2 * (cols_out - 1) < cols_in,
-                "output %dx%d is not a 2x downsampling of %dx%d", rows_out, cols_out, rows_in, cols_in);
+    if (int e = check_levels(rows_in, cols_in, rows_out, cols_out)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    const int64_t pout = (int64_t)rows_out * cols_out;
-    isb_down_kernel<<<grid_1d(pout, kIsbBlock), kIsbBlock, 0, as_stream(stream)>>>(
-        d_guide_in, d_cost_in, rows_in, cols_in, d_guide_out, d_cost_out, rows_out, cols_out, candidate_count,
-        var_inv_i);
-    return launch_status("isb_down_kernel");
+    return launch_down<1, float>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_out, d_cost_out, rows_out, cols_out,
+                                 candidate_count, 1, var_inv_i, as_stream(stream));
 }
 
 extern "C" int ssg_isb_upsample(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in, int cols_in,
@@ -385,77 +411,31 @@ extern "C" int ssg_isb_upsample(const uint8_t* d_guide_in, const float* d_cost_i
                                 void* stream)
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_inout, "null device pointer");
-    SSG_REQUIRE(rows_in > 0 && cols_in > 0 && rows_inout > 0 && cols_inout > 0, "sizes must be positive");
-    SSG_REQUIRE(2 * (rows_in - 1) < rows_inout && 2 * (cols_in - 1) < cols_inout,
-                "coarse %dx%d is not the 2x downsampling of %dx%d", rows_in, cols_in, rows_inout, cols_inout);
-    SSG_REQUIRE((rows_inout + 1) / 2 <= rows_in && (cols_inout + 1) / 2 <= cols_in,
-                "coarse %dx%d does not cover fine %dx%d", rows_in, cols_in, rows_inout, cols_inout);
+    if (int e = check_levels(rows_inout, cols_inout, rows_in, cols_in)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    const int64_t pin = (int64_t)rows_in * cols_in;
-    isb_up_kernel<<<grid_1d(pin, kIsbBlock), kIsbBlock, 0, as_stream(stream)>>>(
-        d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout, d_cost_inout, rows_inout, cols_inout, candidate_count,
-        weight_up, weight_down, var_inv_i);
-    return launch_status("isb_up_kernel");
+    return launch_up<1, float, false>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout, d_cost_inout,
+                                      rows_inout, cols_inout, candidate_count, candidate_count, 1, weight_up,
+                                      weight_down, var_inv_i, SelectOut{}, as_stream(stream));
 }
 
 extern "C" int ssg_isb_apply(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
                              int candidate_count, double sigma_i, double sigma_s, void* stream)
 {
-    SSG_REQUIRE(d_guides && d_costs, "null level arrays");
-    SSG_REQUIRE(level_count == ssg_isb_level_count(cols, rows),
-                "level_count %d differs from the pyramid of a %dx%d image (%d)", level_count, cols, rows,
-                ssg_isb_level_count(cols, rows));
-    SSG_REQUIRE(level_count <= SSG_MAX_LEVELS, "too many levels");
-    SSG_REQUIRE(sigma_i > 0 && sigma_s > 0, "sigmas must be positive");
-    for (int s = 0; s < level_count; ++s) SSG_REQUIRE(d_guides[s] && d_costs[s], "level %d is NULL", s);
-    const Levels c = isb_constants(level_count, sigma_i, sigma_s);
-    for (int s = 1; s < level_count; ++s) {
-        int e = ssg_isb_downsample(d_guides[s - 1], d_costs[s - 1], level_rows(rows, s - 1), level_rows(cols, s - 1),
-                                   d_guides[s], d_costs[s], level_rows(rows, s), level_rows(cols, s), candidate_count,
-                                   c.var_inv_i, stream);
-        if (e) return e;
-    }
-    for (int s = level_count - 2; s >= 0; --s) {
-        int e = ssg_isb_upsample(d_guides[s + 1], d_costs[s + 1], level_rows(rows, s + 1), level_rows(cols, s + 1),
-                                 d_guides[s], d_costs[s], level_rows(rows, s), level_rows(cols, s), candidate_count,
-                                 c.weight_up[s], c.weight_down[s], c.var_inv_i, stream);
-        if (e) return e;
-    }
-    return SSG_OK;
+    if (int e = check_apply_args(d_guides, d_costs, level_count, rows, cols, candidate_count, sigma_i, sigma_s))
+        return e;
+    return apply_planar(d_guides, d_costs, level_count, rows, cols, candidate_count, 1, sigma_i, sigma_s,
+                        as_stream(stream));
 }
 
 extern "C" int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows,
                                    int cols, int candidate_count, int instances, double sigma_i, double sigma_s,
                                    void* stream)
 {
-    SSG_REQUIRE(d_guides && d_costs, "null level arrays");
-    SSG_REQUIRE(level_count == ssg_isb_level_count(cols, rows),
-                "level_count %d differs from the pyramid of a %dx%d image (%d)", level_count, cols, rows,
-                ssg_isb_level_count(cols, rows));
-    SSG_REQUIRE(level_count <= SSG_MAX_LEVELS, "too many levels");
+    if (int e = check_apply_args(d_guides, d_costs, level_count, rows, cols, candidate_count, sigma_i, sigma_s))
+        return e;
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
-    SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    SSG_REQUIRE(sigma_i > 0 && sigma_s > 0, "sigmas must be positive");
-    for (int s = 0; s < level_count; ++s) SSG_REQUIRE(d_guides[s] && d_costs[s], "level %d is NULL", s);
-    const Levels c = isb_constants(level_count, sigma_i, sigma_s);
-    cudaStream_t st = as_stream(stream);
-    for (int s = 1; s < level_count; ++s) {
-        const int ri = level_rows(rows, s - 1), ci = level_rows(cols, s - 1), ro = level_rows(rows, s),
-                  co = level_rows(cols, s);
-        dim3 grid(grid_1d((int64_t)ro * co, kIsbBlock), instances);
-        isb_down_kernel<<<grid, kIsbBlock, 0, st>>>(d_guides[s - 1], d_costs[s - 1], ri, ci, d_guides[s], d_costs[s], ro,
-                                                    co, candidate_count, c.var_inv_i);
-        if (int e = launch_status("isb_down_kernel")) return e;
-    }
-    for (int s = level_count - 2; s >= 0; --s) {
-        const int rc = level_rows(rows, s + 1), cc = level_rows(cols, s + 1), rf = level_rows(rows, s),
-                  cf = level_rows(cols, s);
-        dim3 grid(grid_1d((int64_t)rc * cc, kIsbBlock), instances);
-        isb_up_kernel<<<grid, kIsbBlock, 0, st>>>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s], rf,
-                                                  cf, candidate_count, c.weight_up[s], c.weight_down[s], c.var_inv_i);
-        if (int e = launch_status("isb_up_kernel")) return e;
-    }
-    return SSG_OK;
+    return apply_planar(d_guides, d_costs, level_count, rows, cols, candidate_count, instances, sigma_i, sigma_s,
+                        as_stream(stream));
 }
 
 extern "C" int ssg_select_distance(const float* d_cost, int candidate_count, int64_t pixels, const float* candidates,
@@ -465,11 +445,10 @@ extern "C" int ssg_select_distance(const float* d_cost, int candidate_count, int
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
     SSG_REQUIRE(pixels >= 0, "negative pixel count");
     if (pixels == 0) return SSG_OK;
-    float d0, dl, q;
-    candidate_constants(candidates, candidate_count, d0, dl, q);
-    select_distance_kernel<<<grid_1d(pixels, kIsbBlock), kIsbBlock, 0, as_stream(stream)>>>(
-        d_cost, candidate_count, pixels, d0, dl, q, d_distance, d_index);
-    return launch_status("select_distance_kernel");
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, false);
+    select_kernel<1, float><<<dim3(grid_1d(pixels, kBatchBlock), 1), kBatchBlock, 0, as_stream(stream)>>>(
+        d_cost, pixels, candidate_count, candidate_count, so.d0, so.dl, so.q, d_distance, d_index);
+    return launch_status("select_kernel");
 }
 
 extern "C" int ssg_isb_upsample_select(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in, int cols_in,
@@ -479,16 +458,112 @@ extern "C" int ssg_isb_upsample_select(const uint8_t* d_guide_in, const float* d
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_fine && d_distance && candidates,
                 "null pointer");
-    SSG_REQUIRE(rows_in > 0 && cols_in > 0 && rows_fine > 0 && cols_fine > 0, "sizes must be positive");
-    SSG_REQUIRE(2 * (rows_in - 1) < rows_fine && 2 * (cols_in - 1) < cols_fine &&
-                    (rows_fine + 1) / 2 <= rows_in && (cols_fine + 1) / 2 <= cols_in,
-                "coarse %dx%d does not match fine %dx%d", rows_in, cols_in, rows_fine, cols_fine);
+    if (int e = check_levels(rows_fine, cols_fine, rows_in, cols_in)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    float d0, dl, q;
-    candidate_constants(candidates, candidate_count, d0, dl, q);
-    const int64_t pin = (int64_t)rows_in * cols_in;
-    isb_up_select_kernel<<<grid_1d(pin, kIsbBlock), kIsbBlock, 0, as_stream(stream)>>>(
-        d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout, d_cost_fine, rows_fine, cols_fine, candidate_count,
-        weight_up, weight_down, var_inv_i, d0, dl, q, d_distance, d_index);
-    return launch_status("isb_up_select_kernel");
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, true);
+    return launch_up<1, float, true>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout,
+                                     const_cast<float*>(d_cost_fine), rows_fine, cols_fine, candidate_count,
+                                     candidate_count, 1, weight_up, weight_down, var_inv_i, so, as_stream(stream));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batches of chunked volumes (the batched path)
+// ---------------------------------------------------------------------------------------------
+extern "C" int ssg_isb_downsample_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
+                                        uint8_t* d_guide_out, void* d_cost_out, int rows_out, int cols_out,
+                                        int candidate_count, int instances, int storage, float var_inv_i,
+                                        void* stream)
+{
+    SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_out && d_cost_out, "null pointer");
+    if (int e = check_levels(rows_in, cols_in, rows_out, cols_out)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
+                "unknown input storage %d", storage);
+    SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
+    SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    const int chunks = chunks_of(candidate_count);
+    float* out = static_cast<float*>(d_cost_out);
+    cudaStream_t st = as_stream(stream);
+    if (storage == SSG_STORAGE_F16)
+        return launch_down<8, __half>(d_guide_in, static_cast<const __half*>(d_cost_in), rows_in, cols_in, d_guide_out,
+                                      out, rows_out, cols_out, chunks, instances, var_inv_i, st);
+    if (storage == SSG_STORAGE_UNORM16)
+        return launch_down<8, uint16_t>(d_guide_in, static_cast<const uint16_t*>(d_cost_in), rows_in, cols_in,
+                                        d_guide_out, out, rows_out, cols_out, chunks, instances, var_inv_i, st);
+    return launch_down<8, float>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in, d_guide_out, out,
+                                 rows_out, cols_out, chunks, instances, var_inv_i, st);
+}
+
+extern "C" int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
+                                      uint8_t* d_guide_inout, void* d_cost_inout, int rows_inout, int cols_inout,
+                                      int candidate_count, int instances, int storage, float weight_up,
+                                      float weight_down, float var_inv_i, void* stream)
+{
+    SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_inout, "null pointer");
+    if (int e = check_levels(rows_inout, cols_inout, rows_in, cols_in)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F32, "coarse levels are float32 (storage must be SSG_STORAGE_F32)");
+    SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
+    SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    const int chunks = chunks_of(candidate_count);
+    return launch_up<8, float, false>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in,
+                                      d_guide_inout, static_cast<float*>(d_cost_inout), rows_inout, cols_inout, chunks,
+                                      chunks * 8, instances, weight_up, weight_down, var_inv_i, SelectOut{},
+                                      as_stream(stream));
+}
+
+extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in,
+                                             int cols_in, uint8_t* d_guide_inout, const void* d_cost_fine,
+                                             int rows_fine, int cols_fine, int candidate_count, int instances,
+                                             int storage, float weight_up, float weight_down, float var_inv_i,
+                                             const float* candidates, float* d_distance, int32_t* d_index,
+                                             void* stream)
+{
+    SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_fine && d_distance && candidates, "null pointer");
+    if (int e = check_levels(rows_fine, cols_fine, rows_in, cols_in)) return e;
+    SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
+                "unknown fine-level storage %d", storage);
+    SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
+    SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    const int chunks = chunks_of(candidate_count);
+    // the level-0 guide is not needed after the selection and is left as it was
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, false);
+    const float* coarse = static_cast<const float*>(d_cost_in);
+    void* fine = const_cast<void*>(d_cost_fine);  // read only in the selecting variant
+    cudaStream_t st = as_stream(stream);
+    if (storage == SSG_STORAGE_F16)
+        return launch_up<8, __half, true>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout,
+                                          static_cast<__half*>(fine), rows_fine, cols_fine, chunks, candidate_count,
+                                          instances, weight_up, weight_down, var_inv_i, so, st);
+    if (storage == SSG_STORAGE_UNORM16)
+        return launch_up<8, uint16_t, true>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout,
+                                            static_cast<uint16_t*>(fine), rows_fine, cols_fine, chunks,
+                                            candidate_count, instances, weight_up, weight_down, var_inv_i, so, st);
+    return launch_up<8, float, true>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout, static_cast<float*>(fine),
+                                     rows_fine, cols_fine, chunks, candidate_count, instances, weight_up, weight_down,
+                                     var_inv_i, so, st);
+}
+
+extern "C" int ssg_select_distance_batch(const void* d_cost, int candidate_count, int64_t pixels, int instances,
+                                         int storage, const float* candidates, float* d_distance, int32_t* d_index,
+                                         void* stream)
+{
+    SSG_REQUIRE(d_cost && d_distance && candidates, "null pointer");
+    SSG_REQUIRE(pixels > 0 && instances >= 1 && instances <= 65535, "invalid sizes");
+    SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
+    SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
+                "unknown storage %d", storage);
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, false);
+    const dim3 grid(grid_1d(pixels, kBatchBlock), instances);
+    const int chunks = chunks_of(candidate_count);
+    cudaStream_t st = as_stream(stream);
+    if (storage == SSG_STORAGE_F16)
+        select_kernel<8, __half><<<grid, kBatchBlock, 0, st>>>(static_cast<const __half*>(d_cost), pixels, chunks,
+                                                               candidate_count, so.d0, so.dl, so.q, d_distance, d_index);
+    else if (storage == SSG_STORAGE_UNORM16)
+        select_kernel<8, uint16_t><<<grid, kBatchBlock, 0, st>>>(static_cast<const uint16_t*>(d_cost), pixels, chunks,
+                                                                 candidate_count, so.d0, so.dl, so.q, d_distance,
+                                                                 d_index);
+    else
+        select_kernel<8, float><<<grid, kBatchBlock, 0, st>>>(static_cast<const float*>(d_cost), pixels, chunks,
+                                                              candidate_count, so.d0, so.dl, so.q, d_distance, d_index);
+    return launch_status("select_kernel");
 }

@@ -210,8 +210,44 @@ __global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_co
 constexpr int kTileW = 64, kTileH = 32, kHalo = 16;
 constexpr int kRegW = kTileW + 2 * kHalo, kRegH = kTileH + 2 * kHalo;
 constexpr int kInpaintBlock = 512;
-constexpr size_t kInpaintSmem = sizeof(float) * 2 * kRegW * kRegH + sizeof(uchar2) * kRegW * kRegH;
+constexpr size_t kInpaintSmem =
+    sizeof(float) * 2 * kRegW * kRegH + sizeof(uchar2) * kRegW * kRegH + sizeof(uint16_t) * kRegW * kRegH;
 
+// One Jacobi step of inpaintKernel (stitcher.cu:283-323) at region cell j, reading `cur`.
+__device__ __forceinline__ float inpaint_cell(const float* cur, const uchar2* tab, int j, float hole_at_least,
+                                              float valid_at_most)
+{
+    const float v = cur[j];
+    if (!(v >= hole_at_least)) return v;  // filled in an earlier step
+    const uchar2 t = tab[j];
+    const int n0 = j + ((t.x & 12) / 4 - 1) * kRegW + ((t.x & 3) - 1);
+    const int n1 = j + ((t.y & 12) / 4 - 1) * kRegW + ((t.y & 3) - 1);
+    // an offset field of 3 (a step of 2) never comes out of the table kernel; such a neighbour is
+    // ignored instead of read outside the 3x3 neighbourhood
+    const bool ok0 = (t.x & 3) != 3 && (t.x & 12) != 12, ok1 = (t.y & 3) != 3 && (t.y & 12) != 12;
+    const float w0 = ok0 ? (float)(t.x & 240) : 0.0f, w1 = ok1 ? (float)(t.y & 240) : 0.0f;
+    float val = 0.0f, ws = 0.0f;
+    if (w0 > 0.0f) {
+        const float sd = cur[n0];
+        if (sd <= valid_at_most) {
+            val = fadd(val, fmul(w0, sd));
+            ws = fadd(ws, w0);
+        }
+    }
+    if (w1 > 0.0f) {
+        const float sd = cur[n1];
+        if (sd <= valid_at_most) {
+            val = fadd(val, fmul(w1, sd));
+            ws = fadd(ws, w1);
+        }
+    }
+    return ws > 0.0f ? fdiv(val, ws) : v;
+}
+
+// `steps` Jacobi steps on a 64 x 32 output tile from its region with a 16-pixel halo held in
+// shared memory.  Only hole pixels change, and a pixel that is not a hole never becomes one, so
+// the block lists the region's holes once and updates only those; a tile without holes copies
+// its input through.
 __global__ void __launch_bounds__(kInpaintBlock) inpaint_tile_kernel(const float* __restrict__ src,
                                                                      float* __restrict__ dst,
                                                                      const uchar2* __restrict__ table, int cols,
@@ -219,6 +255,7 @@ __global__ void __launch_bounds__(kInpaintBlock) inpaint_tile_kernel(const float
                                                                      float hole_at_least, float valid_at_most)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int hole_count;
     // blockIdx.z: instance (frame * references + reference slot); tables are per slot
     const int64_t P = (int64_t)cols * rows;
     src += (int64_t)blockIdx.z * P;
@@ -227,59 +264,46 @@ __global__ void __launch_bounds__(kInpaintBlock) inpaint_tile_kernel(const float
     float* buf0 = reinterpret_cast<float*>(smem);
     float* buf1 = buf0 + kRegW * kRegH;
     uchar2* tab = reinterpret_cast<uchar2*>(buf1 + kRegW * kRegH);
+    uint16_t* holes = reinterpret_cast<uint16_t*>(tab + kRegW * kRegH);
     const int ox = blockIdx.x * kTileW - kHalo, oy = blockIdx.y * kTileH - kHalo;
+    if (threadIdx.x == 0) hole_count = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    // kRegW * kRegH is a multiple of the block size: every warp runs whole iterations
     for (int j = threadIdx.x; j < kRegW * kRegH; j += blockDim.x) {
-        const int x = ox + j % kRegW, y = oy + j / kRegW;
+        const int lx = j % kRegW, ly = j / kRegW;
+        const int x = ox + lx, y = oy + ly;
         const bool in = x >= 0 && x < cols && y >= 0 && y < rows;
         const int64_t g = (int64_t)y * cols + x;
-        buf0[j] = in ? src[g] : 0.0f;
+        const float v = in ? src[g] : 0.0f;
+        buf0[j] = v;
+        buf1[j] = v;
         tab[j] = in ? table[g] : make_uchar2(0, 0);
+        // hole test of stitcher.cu:287 and the interior test of :291; neighbours must lie inside
+        // the region (pixels whose neighbours do not are farther than `steps` from the outputs)
+        const bool hole = in && v >= hole_at_least && x >= 1 && y >= 1 && x < cols - 1 && y < rows - 1 && lx >= 1 &&
+                          ly >= 1 && lx < kRegW - 1 && ly < kRegH - 1;
+        const unsigned mask = __ballot_sync(0xffffffffu, hole);
+        int base = 0;
+        if (lane == 0 && mask) base = atomicAdd(&hole_count, __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (hole) holes[base + __popc(mask & ((1u << lane) - 1))] = (uint16_t)j;
     }
     __syncthreads();
+    const int n = hole_count;
     float* cur = buf0;
     float* nxt = buf1;
-    for (int s = 0; s < steps; ++s) {
-        for (int j = threadIdx.x; j < kRegW * kRegH; j += blockDim.x) {
-            const float v = cur[j];
-            float out = v;
-            const int lx = j % kRegW, ly = j / kRegW;
-            const int x = ox + lx, y = oy + ly;
-            // hole test of stitcher.cu:287 and the interior test of :291; neighbours must lie
-            // inside the region (pixels whose neighbours do not are farther than `steps` from
-            // the tile's outputs and never reach them)
-            if (v >= hole_at_least && x >= 1 && y >= 1 && x < cols - 1 && y < rows - 1 && lx >= 1 && ly >= 1 &&
-                lx < kRegW - 1 && ly < kRegH - 1) {
-                const uchar2 t = tab[j];
-                const int n0 = j + ((t.x & 12) / 4 - 1) * kRegW + ((t.x & 3) - 1);
-                const int n1 = j + ((t.y & 12) / 4 - 1) * kRegW + ((t.y & 3) - 1);
-                // an offset field of 3 (a step of 2) never comes out of the table kernel; such a
-                // neighbour is ignored instead of read outside the 3x3 neighbourhood
-                const bool ok0 = (t.x & 3) != 3 && (t.x & 12) != 12, ok1 = (t.y & 3) != 3 && (t.y & 12) != 12;
-                const float w0 = ok0 ? (float)(t.x & 240) : 0.0f, w1 = ok1 ? (float)(t.y & 240) : 0.0f;
-                float val = 0.0f, ws = 0.0f;
-                if (w0 > 0.0f) {
-                    const float sd = cur[n0];
-                    if (sd <= valid_at_most) {
-                        val = fadd(val, fmul(w0, sd));
-                        ws = fadd(ws, w0);
-                    }
-                }
-                if (w1 > 0.0f) {
-                    const float sd = cur[n1];
-                    if (sd <= valid_at_most) {
-                        val = fadd(val, fmul(w1, sd));
-                        ws = fadd(ws, w1);
-                    }
-                }
-                if (ws > 0.0f) out = fdiv(val, ws);
+    if (n > 0)
+        for (int s = 0; s < steps; ++s) {
+            for (int h = threadIdx.x; h < n; h += blockDim.x) {
+                const int j = holes[h];
+                nxt[j] = inpaint_cell(cur, tab, j, hole_at_least, valid_at_most);
             }
-            nxt[j] = out;
+            __syncthreads();
+            float* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
         }
-        __syncthreads();
-        float* tmp = cur;
-        cur = nxt;
-        nxt = tmp;
-    }
     for (int j = threadIdx.x; j < kTileW * kTileH; j += blockDim.x) {
         const int lx = kHalo + j % kTileW, ly = kHalo + j / kTileW;
         const int x = ox + lx, y = oy + ly;

@@ -280,9 +280,10 @@ class RGBD_Estimator:
         frame per call) on the 16-bit pipeline.
 
         Args:
-            images_to_match: [frames, cameras, matching_rows, matching_cols, 3] float32 in [0, 255]
+            images_to_match: [frames, cameras, matching_rows, matching_cols, 3] float32 in [0, 255],
+                or uint8 (the 8-bit images the float inputs are made from)
             images_to_stitch: [frames, references, rgb_stitching_rows, rgb_stitching_cols, 3]
-                float32 in [0, 255]
+                float32 in [0, 255], or uint8
         Returns:
             rgb: [frames, rows, cols, 3] uint8, distance: [frames, rows, cols] float32 (views of
             the pipeline's buffers, overwritten by the next call)

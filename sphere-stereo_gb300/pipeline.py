@@ -4,7 +4,7 @@ volume (coarser levels float32) with fp32 arithmetic, optional CUDA-graph captur
 One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_panorama
 (python/depth_estimation.py:205-242) for all F x R (frame, reference) instances at once:
 
-    ssg_stage_images               inputs -> float4 texels + guides of the references   1 launch
+    ssg_stage_images[_u8]          inputs -> float4 texels + guides of the references   1 launch
     ssg_sweep_cost_batch           sweep + cost, 16-bit chunked volume                  1
     ssg_isb_downsample_batch       L - 1 levels                                         L - 1
     ssg_isb_upsample_batch         levels L - 2 .. 1                                    L - 2
@@ -56,7 +56,8 @@ class BatchPipeline:
         u8 = dict(dtype=torch.uint8, device=dev)
         f32 = dict(dtype=torch.float32, device=dev)
         i16 = dict(dtype=torch.int16, device=dev)
-        self.staged = torch.empty(F * C * P * 4, **f32)
+        # float4 texel planes with a zero border, (rows + 2) x (cols + 2); the border is never written
+        self.staged = torch.zeros(F * C * (self.rows + 2) * (self.cols + 2) * 4, **f32)
         self.guides = [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes]
         # level 0 (the sweep's output) 16-bit, coarser levels float32
         self.costs = [torch.empty(F * R * self.chunks * r * c * 8, **(i16 if l == 0 else f32))
@@ -82,7 +83,8 @@ class BatchPipeline:
         e, st = self.e, self.st
         inst = frames * self.R
         cols, rows, P = self.cols, self.rows, self.P
-        N.call("ssg_stage_images", match.data_ptr(), frames, self.C, P, self._refs, self.R, self.staged.data_ptr(),
+        stage = "ssg_stage_images_u8" if match.dtype == torch.uint8 else "ssg_stage_images"
+        N.call(stage, match.data_ptr(), frames, self.C, cols, rows, self._refs, self.R, self.staged.data_ptr(),
                self.guides[0].data_ptr(), stream)
         N.call("ssg_sweep_cost_batch", cols, rows, frames, self.C, e._cams, self.R, self._refs, self._poses,
                self.staged.data_ptr(), self.selected.data_ptr(), e._candidates, self.N, self.storage,
@@ -119,30 +121,35 @@ class BatchPipeline:
                    N.pointers([dist.data_ptr()] + [c.data_ptr() for c in self.df_costs]), L, rows, cols, 1, inst,
                    float(e.sigma_i) / 2, float(e.sigma_s) / 2, stream)
         # stitch (python/stitcher.py:166-220)
-        self.images_u8[:frames].copy_(stitch[:frames])  # float -> uint8 truncation (depth_estimation.py:239)
+        if stitch.dtype == torch.uint8:
+            images_u8 = stitch
+        else:
+            images_u8 = self.images_u8
+            images_u8[:frames].copy_(stitch[:frames])  # float -> uint8 truncation (depth_estimation.py:239)
         N.call("ssg_reproject_distance_batch", dist.data_ptr(), self.reprojected.data_ptr(), cols, rows, inst, self.R,
                st._intr, st._trans, 1, stream)
         N.call("ssg_inpaint_batch", self.reprojected.data_ptr(), self.tables.data_ptr(), self.scratch.data_ptr(), cols,
                rows, inst, self.R, st.max_dist, st.inpainting_iterations, stream)
         N.call("ssg_merge_panorama_batch", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
-               self.reprojected.data_ptr(), dist.data_ptr(), self.images_u8.data_ptr(), st.image_rows, st.image_cols,
+               self.reprojected.data_ptr(), dist.data_ptr(), images_u8.data_ptr(), st.image_rows, st.image_cols,
                st._trans, st._intr, self.R, cols, rows, st.pano_cols, st.pano_rows, frames,
                self.pano_distance.data_ptr(), self.rgb.data_ptr(), stream)
 
     def run(self, match: torch.Tensor, stitch: torch.Tensor):
-        """match: [F, C, rows, cols, 3] float32, stitch: [F, R, image_rows, image_cols, 3] float32,
-        both contiguous on the pipeline's device.  Returns views of the outputs for F frames."""
+        """match: [F, C, rows, cols, 3], stitch: [F, R, image_rows, image_cols, 3], each float32 or
+        uint8 (8-bit images: a quarter of the upload, no conversion pass), contiguous on the
+        pipeline's device.  Returns views of the outputs for F frames."""
         frames = match.shape[0]
         if not 1 <= frames <= self.max_frames:
             raise ValueError(f"batch of {frames} frames outside [1, {self.max_frames}]")
         st = self.st
-        N.require(match, "images_to_match", torch.float32, (frames, self.C, self.rows, self.cols, 3), self.device)
-        N.require(stitch, "images_to_stitch", torch.float32, (frames, self.R, st.image_rows, st.image_cols, 3),
-                  self.device)
+        for name, t, shape in (("images_to_match", match, (frames, self.C, self.rows, self.cols, 3)),
+                               ("images_to_stitch", stitch, (frames, self.R, st.image_rows, st.image_cols, 3))):
+            N.require(t, name, torch.uint8 if t.dtype == torch.uint8 else torch.float32, shape, self.device)
         if not self.cuda_graphs:
             self._launch(match, stitch, frames, N.stream_of(match))
         else:
-            key = (match.data_ptr(), stitch.data_ptr(), frames)
+            key = (match.data_ptr(), match.dtype, stitch.data_ptr(), stitch.dtype, frames)
             graph = self._graphs.get(key)
             if graph is None:
                 # one eager run (first-use set-up such as shared-memory opt-in happens outside capture)

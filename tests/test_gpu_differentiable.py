@@ -1,0 +1,136 @@
+"""The differentiable sweep (soft-argmin inverse distance, gradients with respect to the images
+and to each camera's 6-DoF pose delta) against a float64 torch autograd restatement
+(oracle/diff_reference.py) and central finite differences.
+
+Setting, after the differentiable-sweep configuration at reduced size: the synthetic rig's
+extrinsics perturbed by a seeded 0.5 deg rotation and 5 mm translation, images ray-cast with
+the true rig, loss = L1 between the soft-argmin inverse distance and the ray-cast ground truth.
+
+The cost is an L1 of bilinear samples with a clamp: piecewise linear in the pose, so a central
+difference with a pose step of 1e-4 rad / 1e-4 m crosses many of its kinks and differs from the
+derivative by a few percent; with a step of 1e-7 the differences converge to the derivative.
+Image steps of 1e-4 (intensity units) cross almost none.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+@pytest.fixture(scope="module")
+def setting(ss, native, synthetic, oracle_mod):
+    import diff_reference
+
+    res = (96, 96)
+    true_cams = synthetic.square_rig(192)
+    rng = np.random.Generator(np.random.PCG64(synthetic.frame_seed(4, 0)))
+    scene = synthetic.random_scene(rng)
+    frame = synthetic.render_frame(scene, true_cams, res, res, [2, 3])
+    noisy = synthetic.perturb_rig(true_cams, np.random.Generator(np.random.PCG64(4000)), 0.5, 0.005)
+    calibration = synthetic.basalt_calibration(noisy)
+    calibs = ss.parse_json_calib(calibration, res, DEV)
+    masks = [torch.ones(1, res[1], res[0], device=DEV) for _ in calibs]
+    kw = dict(min_dist=0.55, max_dist=100.0, candidate_count=16, references_indices=[2, 3], sigma_i=10.0,
+              sigma_s=6.25)
+    sweep = ss.DifferentiableSweep(calibs, kw["min_dist"], kw["max_dist"], kw["candidate_count"],
+                                   kw["references_indices"], masks, res, kw["sigma_i"], kw["sigma_s"], DEV,
+                                   temperature=2.0)
+    images = np.stack(frame.images_to_match).astype(np.float32)
+    gt = np.stack([frame.inv_distance[r] for r in kw["references_indices"]])
+    guides = [oracle_mod.Oracle("f32", exp_mode="device").rgb2ycbcr(images[r]) for r in kw["references_indices"]]
+    ref = diff_reference.DiffReference(calibration, matching_resolution=res, selected=[s.cpu().numpy()
+                                                                                       for s in sweep.selected],
+                                       guides=guides, temperature=2.0, **kw)
+    return sweep, ref, images, gt
+
+
+def _loss(q, gt):
+    valid = gt > 0
+    return (q - gt).abs()[valid].mean()
+
+
+def test_forward_matches_float64(setting):
+    """fp32 evaluation of the float64 formula: the relative poses are rounded to float32, which
+    moves samples by ~1e-5 px and costs (magnitude ~100) by ~1e-3; through softmax(-F / 2) that
+    is a relative weight change of ~5e-4 on an inverse distance range of 1.8, so the bound is
+    3e-5 absolute (1.7e-5 of the range)."""
+    sweep, ref, images, gt = setting
+    q = sweep(torch.as_tensor(images, device=DEV)).cpu().double()
+    q64 = ref.inverse_distance(torch.as_tensor(images, dtype=torch.float64), torch.zeros(4, 6, dtype=torch.float64))
+    err = (q - q64).abs().max().item()
+    print(f"\nsoft-argmin inverse distance vs float64: max abs error {err:.2e}")
+    assert err <= 3e-5
+
+
+def test_gradients_match_float64_autograd_and_finite_differences(setting):
+    sweep, ref, images, gt = setting
+    gt_t = torch.as_tensor(gt)
+    im = torch.as_tensor(images, device=DEV).requires_grad_()
+    de = torch.zeros(4, 6, dtype=torch.float64, device=DEV, requires_grad=True)
+    loss = _loss(sweep(im, de).double().cpu(), gt_t)
+    loss.backward()
+    g_im, g_de = im.grad.double().cpu(), de.grad.cpu()
+
+    im64 = torch.as_tensor(images, dtype=torch.float64).requires_grad_()
+    de64 = torch.zeros(4, 6, dtype=torch.float64, requires_grad=True)
+    loss64 = _loss(ref.inverse_distance(im64, de64), gt_t)
+    loss64.backward()
+    r_pose = ((g_de - de64.grad).norm() / de64.grad.norm()).item()
+    r_img = ((g_im - im64.grad).norm() / im64.grad.norm()).item()
+
+    def f64(im_, de_):
+        with torch.no_grad():
+            return _loss(ref.inverse_distance(im_, de_), gt_t).item()
+
+    base_im = im64.detach()
+    zero = torch.zeros(4, 6, dtype=torch.float64)
+    fd = {}
+    for h in (1e-4, 1e-7):
+        d = torch.zeros(4, 6, dtype=torch.float64)
+        for c in range(4):
+            for j in range(6):
+                e = zero.clone()
+                e[c, j] = h
+                d[c, j] = (f64(base_im, e) - f64(base_im, -e)) / (2 * h)
+        fd[h] = ((g_de - d).norm() / d.norm()).item()
+    rng = np.random.default_rng(1)
+    nz = torch.nonzero(im64.grad.abs() > 1e-8)
+    picks = [tuple(nz[i].tolist()) for i in rng.choice(len(nz), 96, replace=False)]
+    fd_img, ana = [], []
+    for (c, y, x, ch) in picks:
+        e = torch.zeros_like(base_im)
+        e[c, y, x, ch] = 1e-4
+        fd_img.append((f64(base_im + e, zero) - f64(base_im - e, zero)) / 2e-4)
+        ana.append(g_im[c, y, x, ch].item())
+    fd_img, ana = np.array(fd_img), np.array(ana)
+    r_fd_img = float(np.linalg.norm(fd_img - ana) / np.linalg.norm(fd_img))
+    print(f"\nrelative error vs float64 autograd: poses {r_pose:.2e}, images {r_img:.2e}; vs central differences: "
+          f"poses (step 1e-4) {fd[1e-4]:.2e}, poses (step 1e-7) {fd[1e-7]:.2e}, images (step 1e-4) {r_fd_img:.2e}")
+    assert r_pose <= 1e-3 and r_img <= 1e-3
+    assert fd[1e-7] <= 1e-3
+    assert r_fd_img <= 1e-3
+    assert math.isfinite(fd[1e-4])
+
+
+def test_descent_on_pose_deltas_reduces_the_loss(setting):
+    """A few gradient steps on the pose deltas (calibration refinement) lower the loss."""
+    sweep, _, images, gt = setting
+    gt_t = torch.as_tensor(gt)
+    im = torch.as_tensor(images, device=DEV)
+    de = torch.zeros(4, 6, dtype=torch.float64, device=DEV, requires_grad=True)
+    opt = torch.optim.Adam([de], lr=2e-3)
+    losses = []
+    for _ in range(8):
+        opt.zero_grad()
+        loss = _loss(sweep(im, de).double().cpu(), gt_t)
+        loss.backward()
+        opt.step()
+        losses.append(loss.item())
+    print("\nloss during refinement:", " ".join(f"{v:.4f}" for v in losses))
+    assert losses[-1] < losses[0]
