@@ -226,10 +226,12 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
 
 /* Image staging + guides: d_images frames x cameras x rows x cols x 3, float32 (the inputs of
  * estimate_RGBD_panorama, python/depth_estimation.py:205-227) or uint8 (the 8-bit images those
- * inputs are made from, python/main.py:84-100) -> d_staged frames x cameras x (rows + 2) x
- * (cols + 2) float4 texels (R, G, B, 0) with a one-texel border that the caller zeroes once and
- * that is never written, and d_guides frames x references x rows x cols x 3 uint8 (rgb2yCbCr +
- * uint8 cast of each reference camera, python/utils.py:144-155). */
+ * inputs are made from, python/utils.py:157-205) -> d_staged frames x cameras x (rows + 2) x
+ * (cols + 2) 16-byte entries, entry (y + 1, x) holding texels x - 1 and x of row y as fp16 RGB
+ * (exact for 8-bit values; other floats are rounded to fp16), with a border that the caller
+ * zeroes once and that is never written; and d_guides frames x references x rows x cols x 3
+ * uint8 (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from the
+ * float values). */
 SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                              const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
                              void* stream);

@@ -69,14 +69,19 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __
 }
 
 // ---------------------------------------------------------------------------------------------
-// Upsampling, one thread per fine pixel.  A block covers kUpTileX coarse pixels of one coarse
-// row: warp w takes fine pixel F = w % 4 (UpTaps<F>) of coarse pixels 32 * (w / 4) + lane, so
-// that all lanes of a warp follow one tap list.  The coarse costs of the block's 3 x (kUpTileX + 2)
-// neighbourhood (edge-clamped, as the taps are) are staged per chunk in shared memory with
-// cp.async, double-buffered: each coarse cell is read from memory once per block instead of
-// once per tap, and the next chunk streams in while this one is filtered.
+// Upsampling.  A coarse pixel (x, y) owns four fine pixels F = 0 (2x, 2y), 1 (2x, 2y + 1),
+// 2 (2x + 1, 2y), 3 (2x + 1, 2y + 1), each filtered from its own list of the coarse 3x3 taps
+// (UpTaps<F>: 9, 6, 6 and 4 taps).  A thread takes two of them, so that every thread has about
+// the same work and shares its tap loads between its two pixels: kind 0 takes F = 0 and 3
+// (13 taps, 9 distinct), kind 1 takes F = 1 and 2 (12 taps, 8 distinct).  A block of 256 threads
+// covers kUpTileX = 128 coarse pixels of one coarse row: warps 0-3 are kind 0, warps 4-7 kind 1,
+// so every warp follows one tap list.  The coarse costs of the block's 3 x (kUpTileX + 2)
+// neighbourhood, edge-clamped as the taps are, are staged per chunk of candidates in shared
+// memory with cp.async, double-buffered: each coarse cell is read from memory once per block,
+// and the next chunk streams in while this one is filtered.  Candidates are processed in parts
+// of 4 (W = 8) or 1 (W = 1) to bound the registers that hold the taps.
 // ---------------------------------------------------------------------------------------------
-constexpr int kUpTileX = kBatchBlock / 4;
+constexpr int kUpTileX = kBatchBlock / 2;
 constexpr int kUpTileCols = kUpTileX + 2;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
@@ -92,13 +97,13 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
 
-// Tile of one chunk: [part][row 0..2][col 0..kUpTileCols-1] with parts of 4 floats (W = 8: two
-// parts, float4 elements) or one part of single floats (W = 1).
+// A chunk's tile: [part][row 0..2][col 0..kUpTileCols-1][E floats], parts of E = 4 candidates
+// (W = 8, two parts) or of one candidate (W = 1).
 template <int W>
 struct UpTile {
     static constexpr int parts = W == 8 ? 2 : 1;
-    static constexpr int elem = W == 8 ? 4 : 1;
-    static constexpr int floats = parts * 3 * kUpTileCols * elem;
+    static constexpr int E = W == 8 ? 4 : 1;
+    static constexpr int floats = parts * 3 * kUpTileCols * E;
 };
 
 template <int W>
@@ -118,38 +123,71 @@ __device__ __forceinline__ void load_tile_async(float* __restrict__ buf, const f
     }
 }
 
-// coarse tap (row a, col b) of local coarse column lx, all W candidates
-template <int W>
-__device__ __forceinline__ void tile_tap(const float* __restrict__ buf, int a, int b, int lx, float v[W])
-{
-    const int cell = a * kUpTileCols + lx + b;
-    if constexpr (W == 8) {
-        const float4 lo = reinterpret_cast<const float4*>(buf)[cell];
-        const float4 hi = reinterpret_cast<const float4*>(buf)[3 * kUpTileCols + cell];
-        v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
-        v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
-    } else {
-        v[0] = buf[cell];
+// One fine cell held in registers as loaded (prefetched a chunk ahead), read out in parts of E
+// candidates; and the store of a float32 part.
+template <int W, typename T>
+struct RawCell;
+template <>
+struct RawCell<8, __half> {
+    uint4 q;
+    __device__ __forceinline__ void load(const __half* cell) { q = __ldg(reinterpret_cast<const uint4*>(cell)); }
+    __device__ __forceinline__ void part(int p, float v[4]) const
+    {
+        const uint32_t lo = p == 0 ? q.x : q.z, hi = p == 0 ? q.y : q.w;
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&lo));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&hi));
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
     }
+};
+template <>
+struct RawCell<8, uint16_t> {
+    uint4 q;
+    __device__ __forceinline__ void load(const uint16_t* cell) { q = __ldg(reinterpret_cast<const uint4*>(cell)); }
+    __device__ __forceinline__ void part(int p, float v[4]) const
+    {
+        const uint32_t lo = p == 0 ? q.x : q.z, hi = p == 0 ? q.y : q.w;
+        v[0] = (float)(lo & 0xFFFFu) * kUnormInv;
+        v[1] = (float)(lo >> 16) * kUnormInv;
+        v[2] = (float)(hi & 0xFFFFu) * kUnormInv;
+        v[3] = (float)(hi >> 16) * kUnormInv;
+    }
+};
+template <>
+struct RawCell<8, float> {
+    float4 a, b;
+    __device__ __forceinline__ void load(const float* cell)
+    {
+        a = __ldg(reinterpret_cast<const float4*>(cell));
+        b = __ldg(reinterpret_cast<const float4*>(cell) + 1);
+    }
+    __device__ __forceinline__ void part(int p, float v[4]) const
+    {
+        const float4 q = p == 0 ? a : b;
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+};
+template <>
+struct RawCell<1, float> {
+    float a;
+    __device__ __forceinline__ void load(const float* cell) { a = __ldg(cell); }
+    __device__ __forceinline__ void part(int, float v[1]) const { v[0] = a; }
+};
+
+template <int E>
+__device__ __forceinline__ void store_part(float* cell, int p, const float v[E])
+{
+    if constexpr (E == 4)
+        reinterpret_cast<float4*>(cell + 4 * p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    else
+        cell[0] = v[0];
 }
 
-// filtered costs of fine pixel F (the arithmetic and order of up_costs)
-template <int F, int W>
-__device__ __forceinline__ void tile_filter(const float* __restrict__ buf, int lx, const float (&w)[9], float inv,
-                                            float weight_up, float acc[W])
+template <int F>
+__device__ __forceinline__ constexpr bool uses_tap(int t)
 {
-#pragma unroll
-    for (int j = 0; j < W; ++j) acc[j] = fmul(weight_up, acc[j]);
-#pragma unroll
-    for (int i = 0; i < UpTaps<F>::n; ++i) {
-        const int t = UpTaps<F>::tap(i);
-        float v[W];
-        tile_tap<W>(buf, t / 3, t % 3, lx, v);
-#pragma unroll
-        for (int j = 0; j < W; ++j) acc[j] = fadd(acc[j], fmul(w[i], v[j]));
-    }
-#pragma unroll
-    for (int j = 0; j < W; ++j) acc[j] = fmul(acc[j], inv);
+    for (int i = 0; i < UpTaps<F>::n; ++i)
+        if (UpTaps<F>::tap(i) == t) return true;
+    return false;
 }
 
 template <int F>
@@ -159,8 +197,23 @@ __device__ __forceinline__ float fine_weights_padded(const float (&gd)[9][3], co
     float wf[UpTaps<F>::n];
     const float inv = fine_weights<F>(gd, up, weight_up, weight_down, var_inv_i, wf, g);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) w[i] = i < UpTaps<F>::n ? wf[i < UpTaps<F>::n ? i : 0] : 0.0f;  // (no dead-branch index past n)
+    for (int i = 0; i < 9; ++i) w[i] = i < UpTaps<F>::n ? wf[i < UpTaps<F>::n ? i : 0] : 0.0f;
     return inv;
+}
+
+// filtered costs of fine pixel F from the staged taps (the arithmetic and order of up_costs)
+template <int F, int E>
+__device__ __forceinline__ void filter_part(const float (&tap)[9][E], const float (&w)[9], float inv, float weight_up,
+                                            float acc[E])
+{
+#pragma unroll
+    for (int e = 0; e < E; ++e) acc[e] = fmul(weight_up, acc[e]);
+#pragma unroll
+    for (int i = 0; i < UpTaps<F>::n; ++i)
+#pragma unroll
+        for (int e = 0; e < E; ++e) acc[e] = fadd(acc[e], fmul(w[i], tap[UpTaps<F>::tap(i)][e]));
+#pragma unroll
+    for (int e = 0; e < E; ++e) acc[e] = fmul(acc[e], inv);
 }
 
 struct SelectOut {
@@ -170,80 +223,162 @@ struct SelectOut {
     bool write_guide;  // the selecting step also writes the filtered level-0 guide
 };
 
-// kSelect = false: coarse float32 -> fine float32 in place (and the fine guide);
+// State of one fine pixel of a thread
+struct FinePixel {
+    float w[9];
+    float inv;
+    int index;  // fine pixel index in its level
+    bool active;
+};
+
+template <int F>
+__device__ __forceinline__ void fine_setup(const float (&gd)[9][3], const uint8_t* __restrict__ guide_io,
+                                           const LevelGeom& g, int x, int y, bool coarse_ok, float weight_up,
+                                           float weight_down, float var_inv_i, bool write_guide, FinePixel& px)
+{
+    const int fx = 2 * x + (F >= 2 ? 1 : 0), fy = 2 * y + (F & 1);
+    // a fine pixel outside the level is the clamped duplicate of another one and is skipped
+    px.active = coarse_ok && fx < g.cols_out && fy < g.rows_out;
+    px.index = fy * g.cols_out + fx;
+    px.inv = 0.0f;
+    if (!px.active) return;
+    float up[3], gsum[3];
+    load_guide(guide_io, px.index, up);
+    px.inv = fine_weights_padded<F>(gd, up, weight_up, weight_down, var_inv_i, px.w, gsum);
+    if (write_guide)
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch)
+            const_cast<uint8_t*>(guide_io)[3 * px.index + ch] = (uint8_t)__float2uint_rz(fmul(gsum[ch], px.inv));
+}
+
+// filter one part of fine pixel F and select or store it
+template <int F, int W, typename Tf, bool kSelect>
+__device__ __forceinline__ void up_part(const float (&tap)[9][UpTile<W>::E], const FinePixel& px,
+                                        const RawCell<W, Tf>& raw, int part, int k0, bool full, int ncand,
+                                        float weight_up, Tf* __restrict__ fine_chunk, Selector& s)
+{
+    constexpr int E = UpTile<W>::E;
+    float acc[E];
+    raw.part(part, acc);
+    filter_part<F, E>(tap, px.w, px.inv, weight_up, acc);
+    if constexpr (kSelect) {
+        if (full) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) s.push(k0 + e, acc[e]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e)
+                if (k0 + e < ncand) s.push(k0 + e, acc[e]);
+        }
+    } else {
+        store_part<E>(reinterpret_cast<float*>(fine_chunk + (int64_t)px.index * W), part, acc);
+    }
+}
+
+// one chunk for the two fine pixels FA, FB of a thread, from their prefetched fine cells
+template <int FA, int FB, int W, typename Tf, bool kSelect>
+__device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, Tf* __restrict__ fine_chunk, int c,
+                                         int ncand, float weight_up, const FinePixel& pa, const FinePixel& pb,
+                                         const RawCell<W, Tf>& ra, const RawCell<W, Tf>& rb, Selector& sa,
+                                         Selector& sb)
+{
+    constexpr int E = UpTile<W>::E;
+    const bool full = (c + 1) * W <= ncand;
+#pragma unroll
+    for (int part = 0; part < UpTile<W>::parts; ++part) {
+        float tap[9][E];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            if (uses_tap<FA>(t) || uses_tap<FB>(t)) {
+                const int cell = (part * 3 + t / 3) * kUpTileCols + lx + t % 3;
+                if constexpr (E == 4) {
+                    const float4 q = reinterpret_cast<const float4*>(buf)[cell];
+                    tap[t][0] = q.x; tap[t][1] = q.y; tap[t][2] = q.z; tap[t][3] = q.w;
+                } else {
+                    tap[t][0] = buf[cell];
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; ++e) tap[t][e] = 0.0f;
+            }
+        }
+        const int k0 = c * W + part * E;
+        if (pa.active) up_part<FA, W, Tf, kSelect>(tap, pa, ra, part, k0, full, ncand, weight_up, fine_chunk, sa);
+        if (pb.active) up_part<FB, W, Tf, kSelect>(tap, pb, rb, part, k0, full, ncand, weight_up, fine_chunk, sb);
+    }
+}
+
+// kSelect = false: coarse float32 -> fine float32 in place (and the fine guides);
 // kSelect = true: the last step, fine level-0 costs of type Tf in, the selection out.
 template <int W, typename Tf, bool kSelect>
-__global__ void __launch_bounds__(kBatchBlock) isb_up_kernel(const uint8_t* __restrict__ guide_in,
-                                                                 const float* __restrict__ cost_in,
-                                                                 uint8_t* __restrict__ guide_io,
-                                                                 Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
-                                                                 int ncand, float weight_up, float weight_down,
-                                                                 float var_inv_i, SelectOut so)
+__global__ void __launch_bounds__(kBatchBlock, 2) isb_up_kernel(const uint8_t* __restrict__ guide_in,
+                                                            const float* __restrict__ cost_in,
+                                                            uint8_t* __restrict__ guide_io,
+                                                            Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
+                                                            int ncand, float weight_up, float weight_down,
+                                                            float var_inv_i, SelectOut so)
 {
     __shared__ __align__(16) float tile[2][UpTile<W>::floats];
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
     const int inst = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kUpTileX;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int F = warp & 3;
-    const int lx = (warp >> 2) * 32 + lane, x = x0 + lx;
+    const int kind = warp >> 2;  // warp-uniform
+    const int lx = (warp & 3) * 32 + lane, x = x0 + lx;
     guide_in += (int64_t)inst * pin * 3;
     guide_io += (int64_t)inst * pio * 3;
     cost_in += (int64_t)inst * chunks * pin * W;
     cost_fine += (int64_t)inst * chunks * pio * W;
-    const int fx = 2 * x + (F >= 2 ? 1 : 0), fy = 2 * y + (F & 1);
-    // a fine pixel outside the level is the clamped duplicate of another one and is skipped
-    const bool active = x < g.cols_in && fx < g.cols_out && fy < g.rows_out;
-    const int fi = fy * g.cols_out + fx;
-    float w[9], inv = 0.0f;
-    if (active) {
+    const bool coarse_ok = x < g.cols_in;
+    const bool write_guide = !kSelect || so.write_guide;
+    FinePixel pa, pb;
+    {
         int ci[9];
-        float gd[9][3], up[3], gsum[3];
-        coarse_neighbourhood(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
-        load_guide(guide_io, fi, up);
-        switch (F) {
-            case 0: inv = fine_weights_padded<0>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
-            case 1: inv = fine_weights_padded<1>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
-            case 2: inv = fine_weights_padded<2>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
-            default: inv = fine_weights_padded<3>(gd, up, weight_up, weight_down, var_inv_i, w, gsum); break;
+        float gd[9][3];
+        if (coarse_ok) coarse_neighbourhood(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+        if (kind == 0) {
+            fine_setup<0>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pa);
+            fine_setup<3>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pb);
+        } else {
+            fine_setup<1>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pa);
+            fine_setup<2>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pb);
         }
-        if (!kSelect || so.write_guide)
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) guide_io[3 * fi + ch] = (uint8_t)__float2uint_rz(fmul(gsum[ch], inv));
     }
-    Selector s;
+    Selector sa, sb;
     load_tile_async<W>(tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
     cp_async_commit();
+    // fine cells are read once, from memory: prefetched a chunk ahead of their use
+    RawCell<W, Tf> ra, rb;
+    if (pa.active) ra.load(cost_fine + (int64_t)pa.index * W);
+    if (pb.active) rb.load(cost_fine + (int64_t)pb.index * W);
     for (int c = 0; c < chunks; ++c) {
         if (c + 1 < chunks)
             load_tile_async<W>(tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in, x0, y);
         cp_async_commit();
+        RawCell<W, Tf> na = ra, nb = rb;
+        if (c + 1 < chunks) {
+            const Tf* next = cost_fine + (int64_t)(c + 1) * pio * W;
+            if (pa.active) na.load(next + (int64_t)pa.index * W);
+            if (pb.active) nb.load(next + (int64_t)pb.index * W);
+        }
         cp_async_wait_one();  // this chunk's tile has landed
         __syncthreads();
-        if (active) {
-            Tf* fc = cost_fine + ((int64_t)c * pio + fi) * W;
-            const float* buf = tile[c & 1];
-            float acc[W];
-            CellIO<W, Tf>::load(fc, acc);
-            switch (F) {
-                case 0: tile_filter<0, W>(buf, lx, w, inv, weight_up, acc); break;
-                case 1: tile_filter<1, W>(buf, lx, w, inv, weight_up, acc); break;
-                case 2: tile_filter<2, W>(buf, lx, w, inv, weight_up, acc); break;
-                default: tile_filter<3, W>(buf, lx, w, inv, weight_up, acc); break;
-            }
-            if constexpr (kSelect) {
-#pragma unroll
-                for (int j = 0; j < W; ++j)
-                    if (c * W + j < ncand) s.push(c * W + j, acc[j]);
-            } else {
-                CellIO<W, float>::store(reinterpret_cast<float*>(fc), acc);
-            }
-        }
+        Tf* fine_chunk = cost_fine + (int64_t)c * pio * W;
+        if (kind == 0)
+            up_chunk<0, 3, W, Tf, kSelect>(tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+        else
+            up_chunk<1, 2, W, Tf, kSelect>(tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
         __syncthreads();  // the tile is refilled two chunks on
+        ra = na;
+        rb = nb;
     }
     if constexpr (kSelect) {
-        if (active) {
-            so.distance[(int64_t)inst * pio + fi] = select_from(s, ncand, so.d0, so.dl, so.q);
-            if (so.index) so.index[(int64_t)inst * pio + fi] = s.idx;
+        if (pa.active) {
+            so.distance[(int64_t)inst * pio + pa.index] = select_from(sa, ncand, so.d0, so.dl, so.q);
+            if (so.index) so.index[(int64_t)inst * pio + pa.index] = sa.idx;
+        }
+        if (pb.active) {
+            so.distance[(int64_t)inst * pio + pb.index] = select_from(sb, ncand, so.d0, so.dl, so.q);
+            if (so.index) so.index[(int64_t)inst * pio + pb.index] = sb.idx;
         }
     }
 }

@@ -228,30 +228,23 @@ __device__ __forceinline__ void up_costs(const UpWeights& u, const float* __rest
 }
 
 // Running argmin / max with the neighbours of the argmin (depth_estimation.py:180-187):
-// the first minimum wins ties, as torch.min(dim) does.
+// the first minimum wins ties, as torch.min(dim) does.  Candidates are pushed in order
+// z = 0, 1, ...; L is the value before the argmin (read only when the argmin is not the first
+// candidate), R the value after it (read only when it is not the last).  Branch-free: every
+// push is a handful of compares and selects.  Costs are finite (the sweep clamps them).
 struct Selector {
-    float m, M, L, R, prev;
-    int idx;
-    bool need_right;
+    float m = __builtin_huge_valf(), M = -__builtin_huge_valf(), L = 0.0f, R = 0.0f, prev = 0.0f;
+    int idx = 0;
+    bool need_right = false;
     __device__ __forceinline__ void push(int z, float c)
     {
-        if (z == 0) {
-            m = M = L = prev = c;
-            idx = 0;
-            need_right = true;
-            return;
-        }
-        if (need_right) {
-            R = c;
-            need_right = false;
-        }
-        if (c < m) {
-            m = c;
-            idx = z;
-            L = prev;
-            need_right = true;
-        }
-        if (c > M) M = c;
+        R = need_right ? c : R;
+        const bool lt = c < m;
+        m = lt ? c : m;
+        idx = lt ? z : idx;
+        L = lt ? prev : L;
+        need_right = lt;
+        M = c > M ? c : M;
         prev = c;
     }
 };

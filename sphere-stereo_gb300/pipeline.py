@@ -4,7 +4,7 @@ volume (coarser levels float32) with fp32 arithmetic, optional CUDA-graph captur
 One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_panorama
 (python/depth_estimation.py:205-242) for all F x R (frame, reference) instances at once:
 
-    ssg_stage_images[_u8]          inputs -> float4 texels + guides of the references   1 launch
+    ssg_stage_images[_u8]          inputs -> fp16 texel pairs + guides of the references 1 launch
     ssg_sweep_cost_batch           sweep + cost, 16-bit chunked volume                  1
     ssg_isb_downsample_batch       L - 1 levels                                         L - 1
     ssg_isb_upsample_batch         levels L - 2 .. 1                                    L - 2
@@ -56,7 +56,8 @@ class BatchPipeline:
         u8 = dict(dtype=torch.uint8, device=dev)
         f32 = dict(dtype=torch.float32, device=dev)
         i16 = dict(dtype=torch.int16, device=dev)
-        # float4 texel planes with a zero border, (rows + 2) x (cols + 2); the border is never written
+        # planes of 16-byte texel-pair entries with a zero border, (rows + 2) x (cols + 2); the
+        # border is never written
         self.staged = torch.zeros(F * C * (self.rows + 2) * (self.cols + 2) * 4, **f32)
         self.guides = [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes]
         # level 0 (the sweep's output) 16-bit, coarser levels float32

@@ -193,3 +193,24 @@ def test_bench_configuration_against_fp32_path(ss, native, synthetic):
         assert same >= 0.999
         assert mae_raw <= 1e-4 and mae_p <= 1e-4
         assert p >= 50
+
+
+def test_non_integer_inputs_against_fp32_path(ss, native, golden_c1):
+    """Inputs that are not 8-bit values (the reference resizes float images, python/utils.py:198)
+    are staged as fp16: the 16-bit path still keeps the fp32 path's index on >= 99.9 % of pixels."""
+    g = golden_c1
+    rng = np.random.default_rng(7)
+    noisy = {**g, "images_to_match": (g["images_to_match"].astype(np.float32)
+                                      + rng.uniform(0, 1, g["images_to_match"].shape).astype(np.float32)),
+             "images_to_stitch": g["images_to_stitch"].astype(np.float32)}
+    exact, cfg = _estimator(ss, noisy, "fp32")
+    match = [torch.as_tensor(im, device=DEV) for im in noisy["images_to_match"]]
+    stitch = [torch.as_tensor(im, device=DEV) for im in noisy["images_to_stitch"]]
+    exact.estimate_RGBD_panorama(match, stitch)
+    idx32 = exact.index_maps.cpu().numpy()
+    fast, _ = _estimator(ss, noisy, "fp16")
+    fast.estimate_RGBD_panoramas(torch.stack(match)[None].contiguous(), torch.stack(stitch)[None].contiguous())
+    torch.cuda.synchronize()
+    same = (fast.batch_index_maps[0].cpu().numpy() == idx32).mean()
+    print(f"\nnon-integer inputs, fp16 vs fp32 path: same index {same:.6f}")
+    assert same >= 0.999
