@@ -39,6 +39,10 @@ WORKLOAD_NAME = ("4 double-sphere fisheye cameras (fx=0.28W, xi=-0.2, alpha=0.6)
 METRIC = "RGB-D panoramas/s @1024² match, 32 cand"
 UNIT = "panoramas/s"
 DATA = "synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast per frame (seed 2000+frame)"
+# DRAM bytes (read + write) of sweep_batch_kernel per (frame, reference) instance with fp16 storage,
+# measured by ncu on one launch of an 8-frame batch of this workload (571,416,576 B read +
+# 1,022,696,704 B written for 16 instances)
+SWEEP_DRAM_BYTES_PER_INSTANCE = (571416576 + 1022696704) // 16
 
 
 def _env_int(name, default):
@@ -297,6 +301,31 @@ def run_ours(args, rank, world, device, rendered):
     sweep_ms = rec.mean_ms()
     sweep_bytes = B * len(WORKLOAD["refs"]) * sweep_bytes_per_launch(mw, mh, 4, WORKLOAD["candidates"], 2, staged=True)
     achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9 if sweep_ms else None
+    instances = B * len(WORKLOAD["refs"])
+    traffic = (SWEEP_DRAM_BYTES_PER_INSTANCE * instances
+               if SWEEP_DRAM_BYTES_PER_INSTANCE is not None and args.storage == "fp16" else None)
+
+    # the same batches through the 8-bit inputs the float images are made from (a quarter of the
+    # upload): end to end, uploads overlapped as above
+    e2e_u8 = None
+    if not args.no_u8:
+        pinned = [(torch.as_tensor(m.astype(np.uint8)).pin_memory(), torch.as_tensor(st.astype(np.uint8)).pin_memory())
+                  for m, st in host_batches]
+        staging = [(torch.empty_like(pinned[0][0], device=device), torch.empty_like(pinned[0][1], device=device))
+                   for _ in range(2)]
+        h2d_u8 = sum(t.numel() * t.element_size() for t in pinned[0])
+        e2e(args.warmup)
+        torch.cuda.synchronize()
+        barrier(world)
+        s3, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s3.record()
+        e2e(args.steps)
+        e3.record()
+        torch.cuda.synchronize()
+        u8_ms = max_over_ranks(s3.elapsed_time(e3) / args.steps, world, device)
+        e2e_u8 = {"value": world * B * 1000.0 / u8_ms, "unit": UNIT, "h2d_bytes_per_step": h2d_u8,
+                  "d2h_bytes_per_step": d2h, "ms_per_step": u8_ms,
+                  "inputs": "uint8 images (the 8-bit data the float32 inputs hold)"}
     return {
         "value": world * B * 1000.0 / ms,
         "ms_per_step": ms,
@@ -306,10 +335,37 @@ def run_ours(args, rank, world, device, rendered):
         "clocks": clocks.summary(),
         "roofline": {"bound": "hbm", "kernel": "sweep_batch_kernel", "achieved": achieved, "peak": peak,
                      "peak_kind": f"{peak_kind} hbm_gbs (burst copy)", "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                       "batch, profiles/sweep_batch_kernel_1024_n32.md",
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms,
                      "launches_timed": len(rec.events)},
+        "e2e_u8": e2e_u8,
     }
+
+
+def run_plain_fp32(args, device, rendered, frames_timed: int):
+    """The plain fp32 path on the same GPU: one frame per call of estimate_RGBD_panorama, float32
+    cost volume, the reference's arithmetic bit for bit (no batching, no CUDA graph)."""
+    import torch
+
+    ss = importlib.import_module(PACKAGE)
+    calibration, frames = rendered
+    est = _estimator(ss, calibration, device, "fp32", 1, False)
+    inputs = [([torch.as_tensor(im.astype(np.float32), device=device) for im in f.images_to_match],
+               [torch.as_tensor(im.astype(np.float32), device=device) for im in f.images_to_stitch]) for f in frames]
+    for i in range(args.warmup):
+        est.estimate_RGBD_panorama(*inputs[i % len(inputs)])
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for i in range(frames_timed):
+        est.estimate_RGBD_panorama(*inputs[i % len(inputs)])
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / frames_timed
+    return {"value": 1000.0 / ms, "unit": UNIT, "ms_per_frame": ms, "frames": frames_timed,
+            "mode": "fp32 cost volume, one frame per estimate_RGBD_panorama call, eager launches"}
 
 
 def cpu_baseline(frames_calib, sample_frames: int):
@@ -364,6 +420,8 @@ def main():
     ap.add_argument("--unique-frames", type=int, default=2, help="distinct rendered frames batches are built from")
     ap.add_argument("--cpu-frames", type=int, default=8, help="frames timed for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-u8", action="store_true", help="skip the uint8-input end-to-end leg")
+    ap.add_argument("--plain-frames", type=int, default=32, help="frames timed on the plain fp32 path (0 = skip)")
     args = ap.parse_args()
 
     world = _env_int("WORLD_SIZE", 1)
@@ -401,6 +459,9 @@ def main():
         if world > 1:
             torch.distributed.destroy_process_group()
         return
+    plain = run_plain_fp32(args, device, rendered, args.plain_frames) if args.plain_frames > 0 else None
+    if plain is not None:
+        plain["batched_over_plain"] = ours["value"] / (world * plain["value"])
     base = None
     if not args.no_cpu_baseline:
         base = cpu_baseline((rendered[0], rendered[1][:1]), args.cpu_frames)
@@ -412,7 +473,8 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"each step reads a {args.batch}-frame batch of inputs ({args.batch} x 83 MB), "
                              "alternating between two batches; both far exceed the 126 MB L2"},
-            "e2e": ours["e2e"], "gpu_launches": ours["gpu_launches"], "clocks": ours["clocks"],
+            "e2e": ours["e2e"], "e2e_u8": ours["e2e_u8"], "plain_fp32_gpu": plain,
+            "gpu_launches": ours["gpu_launches"], "clocks": ours["clocks"],
             "roofline": ours["roofline"], "cpu_baseline": base}
     print(json.dumps(line))
     if world > 1:

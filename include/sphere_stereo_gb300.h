@@ -22,6 +22,7 @@
 #ifndef SPHERE_STEREO_GB300_H
 #define SPHERE_STEREO_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #if defined(__GNUC__)
@@ -289,6 +290,18 @@ SSG_API int ssg_reproject_distance_batch(const float* d_distance_in, float* d_di
 SSG_API int ssg_inpaint_batch(float* d_distance, const uint8_t* d_tables, float* d_scratch, int cols, int rows,
                               int instances, int references, double max_dist, int iterations, void* stream);
 
+/* Hole filling of `instances` maps with the result of ssg_inpaint_batch (the Jacobi steps of
+ * inpaintKernel, python/stitcher.cu:283-323, bit for bit), in place and over lists of holes: a
+ * scan stamps every pixel (d_stamps, instances x rows x cols bytes: 0 not a hole, 255 an open
+ * hole, s filled at step s); step 1 visits every fillable hole, and step s > 1 only the open holes
+ * that read a pixel filled at step s - 1.
+ * d_holes: caller-owned int32 scratch of 3 x instances x rows x cols + 4 entries (3 rotating
+ * counts, two lists, a claim word per pixel); instances x rows x cols < 2^31; iterations <= 254.
+ * Launches 1 + iterations kernels after a 16-byte memset. */
+SSG_API int ssg_inpaint_holes_batch(float* d_distance, const uint8_t* d_tables, uint8_t* d_stamps, int32_t* d_holes,
+                                    int cols, int rows, int instances, int references, double max_dist,
+                                    int iterations, void* stream);
+
 /* Merge (python/stitcher.cu:423-473) of `frames` frames: maps frames x references x rows x
  * cols, images frames x references x image_rows x image_cols x 3, panoramas per frame. */
 SSG_API int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
@@ -296,6 +309,16 @@ SSG_API int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights,
                                      int image_cols, const float* translations, const ssg_intrinsics* intrinsics,
                                      int reference_count, int cols, int rows, int pano_cols, int pano_rows, int frames,
                                      float* d_distance_panorama, uint8_t* d_rgb_panorama, void* stream);
+
+/* ssg_merge_panorama_batch with fused multiply-adds and approximate square roots and
+ * reciprocals in the same steps (the batched 16-bit path, whose panoramas are checked against the
+ * fp32 path within tolerances: PSNR >= 50 dB, inverse-distance MAE <= 1e-4 of the range). */
+SSG_API int ssg_merge_panorama_batch_approx(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                                            const float* d_distances, const uint8_t* d_images, int image_rows,
+                                            int image_cols, const float* translations,
+                                            const ssg_intrinsics* intrinsics, int reference_count, int cols, int rows,
+                                            int pano_cols, int pano_rows, int frames, float* d_distance_panorama,
+                                            uint8_t* d_rgb_panorama, void* stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Differentiable sweep (no counterpart in the reference, whose selection is a hard argmin with
@@ -349,6 +372,70 @@ SSG_API int ssg_sweep_cost_backward(int cols, int rows, int camera_count, const 
                                     float* const* d_grad_images, const int8_t* d_selected, const float* candidates,
                                     int candidate_count, const float* d_grad_cost, double* d_grad_pose,
                                     void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Uneven batches (no counterpart in the reference, which estimates one rig's frame per call of
+ * estimate_RGBD_panorama, python/depth_estimation.py:205-242): many RGB-D panorama jobs of
+ * different rigs, matching resolutions and candidate counts in one fixed sequence of launches --
+ * one persistent sweep launch over every instance (a work queue of 256-pixel tiles, largest
+ * instances first), one launch per cost-filter step, one fused selection, one launch per
+ * post-filter step, then fill, reprojection, hole filling and merge over every job.  The 16-bit
+ * path's arithmetic (ssg_sweep_cost_batch, ssg_isb_*_batch, ssg_merge_panorama_batch_approx).
+ * ------------------------------------------------------------------------------------------- */
+
+/* One instance: one reference camera of one rig, with its own buffers (device pointers, the
+ * layouts of the batched functions above for one instance). */
+typedef struct {
+    int cols, rows;               /* matching resolution; at least 2 filter levels */
+    int camera_count;             /* cameras of the rig */
+    int reference_camera;         /* the reference camera, in [0, camera_count) */
+    int candidate_count;
+    const ssg_camera* cameras;    /* host, camera_count */
+    const float* relative_poses;  /* host, camera_count x 12: rows 0..2 of inverse(camera.rt) @ reference.rt */
+    const float* candidates;      /* host, candidate_count distances */
+    double sigma_i, sigma_s;      /* cost filter; the distance post-filter uses half of each */
+    const float* d_staged;        /* the rig frame's planes from ssg_stage_images (camera_count planes) */
+    const int8_t* d_selected;     /* rows x cols selected cameras */
+    uint8_t* const* d_guides;     /* host array of level_count pointers: the guide pyramid (level 0 staged) */
+    void* const* d_costs;         /* host array: level 0 16-bit chunked (written by the sweep), others float32 */
+    uint8_t* const* d_df_guides;  /* host array of level_count pointers: post-filter guides (level 0 may be
+                                     d_guides[0], which the 16-bit selection leaves unchanged) */
+    float* const* d_df_costs;     /* host array of level_count - 1 pointers: post-filter levels 1.. */
+    float* d_distance_raw;        /* rows x cols: the selection's distance */
+    float* d_distance;            /* rows x cols: the filtered distance */
+    int32_t* d_index;             /* rows x cols selected candidate index, or NULL */
+} ssg_uneven_instance;
+
+/* One job: the stitch of one rig's instances (python/stitcher.py:166-220). */
+typedef struct {
+    int cols, rows, references, pano_cols, pano_rows, image_cols, image_rows;
+    const ssg_intrinsics* intrinsics; /* host, references */
+    const float* translations;        /* host, references x 3 */
+    const float* d_distance;          /* references x rows x cols: the instances' d_distance maps, contiguous */
+    const uint8_t* d_tables;          /* references x rows x cols x 2 inpainting tables */
+    const float* d_lut;               /* references x pano_rows x pano_cols x 2 */
+    const float* d_weights;           /* references x pano_rows x pano_cols */
+    const uint8_t* d_images;          /* references x image_rows x image_cols x 3 */
+    float* d_pano_distance;           /* pano_rows x pano_cols */
+    uint8_t* d_rgb;                   /* pano_rows x pano_cols x 3 */
+} ssg_uneven_job;
+
+typedef struct ssg_uneven_batch ssg_uneven_batch;
+
+/* Validates the instances and jobs and lays out their descriptors; gives the sizes of the device
+ * plan and scratch the caller allocates (256-byte aligned).  storage: SSG_STORAGE_F16 or
+ * SSG_STORAGE_UNORM16.  The host arrays are read during the call only. */
+SSG_API int ssg_uneven_create(const ssg_uneven_instance* instances, int instance_count, const ssg_uneven_job* jobs,
+                              int job_count, int storage, double max_dist, int inpainting_iterations,
+                              size_t* plan_bytes, size_t* scratch_bytes, ssg_uneven_batch** batch);
+/* Writes the descriptors into d_plan (synchronising `stream`: call it at set-up, outside a
+ * capture) and binds d_scratch (the sweep's work counter, the reprojected maps, hole lists). */
+SSG_API int ssg_uneven_upload(ssg_uneven_batch* batch, void* d_plan, void* d_scratch, void* stream);
+/* Enqueues the batch's launches on `stream` (capturable in a CUDA graph). */
+SSG_API int ssg_uneven_run(const ssg_uneven_batch* batch, void* stream);
+/* Kernels one ssg_uneven_run launches. */
+SSG_API int ssg_uneven_launches(const ssg_uneven_batch* batch);
+SSG_API void ssg_uneven_destroy(ssg_uneven_batch* batch);
 
 #ifdef __cplusplus
 }

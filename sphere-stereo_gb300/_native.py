@@ -43,6 +43,25 @@ class ssg_intrinsics(ctypes.Structure):
                 ("xi", ctypes.c_float), ("alpha", ctypes.c_float)]
 
 
+class ssg_uneven_instance(ctypes.Structure):
+    _fields_ = [("cols", ctypes.c_int), ("rows", ctypes.c_int), ("camera_count", ctypes.c_int),
+                ("reference_camera", ctypes.c_int), ("candidate_count", ctypes.c_int),
+                ("cameras", ctypes.c_void_p), ("relative_poses", ctypes.c_void_p), ("candidates", ctypes.c_void_p),
+                ("sigma_i", ctypes.c_double), ("sigma_s", ctypes.c_double),
+                ("d_staged", ctypes.c_void_p), ("d_selected", ctypes.c_void_p), ("d_guides", ctypes.c_void_p),
+                ("d_costs", ctypes.c_void_p), ("d_df_guides", ctypes.c_void_p), ("d_df_costs", ctypes.c_void_p),
+                ("d_distance_raw", ctypes.c_void_p), ("d_distance", ctypes.c_void_p), ("d_index", ctypes.c_void_p)]
+
+
+class ssg_uneven_job(ctypes.Structure):
+    _fields_ = [("cols", ctypes.c_int), ("rows", ctypes.c_int), ("references", ctypes.c_int),
+                ("pano_cols", ctypes.c_int), ("pano_rows", ctypes.c_int), ("image_cols", ctypes.c_int),
+                ("image_rows", ctypes.c_int), ("intrinsics", ctypes.c_void_p), ("translations", ctypes.c_void_p),
+                ("d_distance", ctypes.c_void_p), ("d_tables", ctypes.c_void_p), ("d_lut", ctypes.c_void_p),
+                ("d_weights", ctypes.c_void_p), ("d_images", ctypes.c_void_p), ("d_pano_distance", ctypes.c_void_p),
+                ("d_rgb", ctypes.c_void_p)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _I64 = ctypes.c_int64
@@ -80,6 +99,7 @@ SIGNATURES = {
     "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _P]),
     "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint_batch": (_I, [_P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
+    "ssg_inpaint_holes_batch": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
     "ssg_inpaint_noalloc": (_I, [_P, _P, _I, _I, _D, _I, _P]),
     "ssg_isb_upsample_softargmin": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P]),
     "ssg_isb_upsample_softargmin_backward": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P, _P,
@@ -88,6 +108,12 @@ SIGNATURES = {
     "ssg_isb_downsample_transpose": (_I, [_P, _I, _I, _I, _I, _I, _F, _P, _P, _P]),
     "ssg_sweep_cost_backward": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "ssg_uneven_create": (_I, [_P, _I, _P, _I, _I, _D, _I, _P, _P, _P]),
+    "ssg_uneven_upload": (_I, [_P, _P, _P, _P]),
+    "ssg_uneven_run": (_I, [_P, _P]),
+    "ssg_uneven_launches": (_I, [_P]),
+    "ssg_uneven_destroy": (None, [_P]),
+    "ssg_merge_panorama_batch_approx": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
 }
 
 _lock = threading.Lock()
@@ -194,6 +220,9 @@ def kernels_launched(name: str, args) -> int:
         return 2 if args[8] else 1
     if name == "ssg_inpaint":
         return -(-int(args[6]) // 16)
+    if name == "ssg_inpaint_holes_batch":
+        it = int(args[9])
+        return 0 if it == 0 else 1 + it
     if name == "ssg_inpaint_batch":
         return -(-int(args[8]) // 16)
     if name == "ssg_inpaint_noalloc":

@@ -10,6 +10,19 @@
 namespace ssg {
 
 constexpr int kBatchBlock = 256;
+
+// Double-sphere camera of the batched sweep (utils.py:75-94 constants in float32)
+struct FastCam {
+    float fx, fy, cx, cy, xi, alpha, one_minus_alpha;
+};
+
+// Packed pairs of fp32 values: one Blackwell instruction performs a rounded-to-nearest operation
+// on both halves (two candidates of one pixel), which halves the issue slots of the batched
+// kernels' arithmetic.
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 constexpr float kUnormScale = 65535.0f / 500.0f;
 constexpr float kUnormInv = 500.0f / 65535.0f;
 

@@ -37,6 +37,21 @@ __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b)
 __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
+// The hardware's approximate square root and reciprocal (PTX sqrt.approx / rcp.approx, a few ulp):
+// used only by the batched 16-bit path, whose outputs are compared within tolerances.
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Exponential by Cody-Waite range reduction and a degree-7 Taylor polynomial (W. J. Cody and
 // W. Waite, "Software Manual for the Elementary Functions", 1980): x = n ln2 + r with
 // |r| <= ln2 / 2, e^r by Horner's scheme in fused multiply-adds, then scaling by 2^n.  Every

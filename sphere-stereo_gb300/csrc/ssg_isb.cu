@@ -17,6 +17,7 @@
 
 #include "ssg_cells.cuh"
 #include "ssg_isb_common.cuh"
+#include "ssg_uneven.cuh"
 
 namespace ssg {
 
@@ -27,30 +28,24 @@ namespace ssg {
 // level on a sizeable share of coarse pixels, which then moves the argmin. The costs are summed
 // in the fp32 path's order as well; the level-0 rounding is the only difference.
 // ---------------------------------------------------------------------------------------------
-struct LevelGeom {
-    int rows_in, cols_in, rows_out, cols_out;
-};
 
 // Downsampling, one thread per coarse pixel; level 0 (any storage) or a float32 level in,
 // float32 out.
+// One coarse pixel o of a level: pointers are the instance's own; `lut` is the block's filled
+// range table.
 template <int W, typename Tin>
-__global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __restrict__ guide_in,
-                                                                   const Tin* __restrict__ cost_in,
-                                                                   uint8_t* __restrict__ guide_out,
-                                                                   float* __restrict__ cost_out, LevelGeom g,
-                                                                   int chunks, float var_inv_i)
+__device__ __forceinline__ void isb_down_pixel(const uint8_t* __restrict__ guide_in, const Tin* __restrict__ cost_in,
+                                               uint8_t* __restrict__ guide_out, float* __restrict__ cost_out,
+                                               const LevelGeom& g, int chunks, int64_t o, const float* lut)
 {
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
-    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= pout) return;
-    const int inst = blockIdx.y;
-    guide_in += (int64_t)inst * pin * 3;
-    guide_out += (int64_t)inst * pout * 3;
-    cost_in += (int64_t)inst * chunks * pin * W;
-    cost_out += (int64_t)inst * chunks * pout * W;
     DownTapsT<int> t;
-    down_weights(guide_in, g.rows_in, g.cols_in, (int)(o % g.cols_out), (int)(o / g.cols_out), var_inv_i,
+    down_weights(guide_in, g.rows_in, g.cols_in, (int)(o % g.cols_out), (int)(o / g.cols_out), LutRange{lut},
                  guide_out + 3 * o, t);
+    // the chunked (16-bit) path sums with fused multiply-adds and scales by the reciprocal; the
+    // planar path keeps the reference's separate products and its division
+    constexpr bool kFast = W == 8;
+    const float rsum = kFast ? __frcp_rn(t.wsum) : 0.0f;
     for (int c = 0; c < chunks; ++c) {
         const Tin* src = cost_in + (int64_t)c * pin * W;
         float acc[W];
@@ -60,12 +55,33 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __
             float v[W];
             CellIO<W, Tin>::load(src + (int64_t)t.idx[i] * W, v);
 #pragma unroll
-            for (int j = 0; j < W; ++j) acc[j] = fadd(acc[j], fmul(v[j], t.w[i]));
+            for (int j = 0; j < W; ++j) acc[j] = kFast ? fmaf(v[j], t.w[i], acc[j]) : fadd(acc[j], fmul(v[j], t.w[i]));
         }
 #pragma unroll
-        for (int j = 0; j < W; ++j) acc[j] = fdiv(acc[j], t.wsum);
+        for (int j = 0; j < W; ++j) acc[j] = kFast ? acc[j] * rsum : fdiv(acc[j], t.wsum);
         CellIO<W, float>::store(cost_out + ((int64_t)c * pout + o) * W, acc);
     }
+}
+
+// Downsampling, one thread per coarse pixel; level 0 (any storage) or a float32 level in,
+// float32 out.  blockIdx.y: instance of contiguous levels.
+template <int W, typename Tin>
+__global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __restrict__ guide_in,
+                                                                   const Tin* __restrict__ cost_in,
+                                                                   uint8_t* __restrict__ guide_out,
+                                                                   float* __restrict__ cost_out, LevelGeom g,
+                                                                   int chunks, float var_inv_i)
+{
+    __shared__ float lut[kRangeLutSize];
+    fill_range_lut(lut, var_inv_i);
+    __syncthreads();
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= pout) return;
+    const int inst = blockIdx.y;
+    isb_down_pixel<W, Tin>(guide_in + (int64_t)inst * pin * 3, cost_in + (int64_t)inst * chunks * pin * W,
+                           guide_out + (int64_t)inst * pout * 3, cost_out + (int64_t)inst * chunks * pout * W, g,
+                           chunks, o, lut);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -191,18 +207,20 @@ __device__ __forceinline__ constexpr bool uses_tap(int t)
 }
 
 template <int F>
-__device__ __forceinline__ float fine_weights_padded(const float (&gd)[9][3], const float up[3], float weight_up,
-                                                     float weight_down, float var_inv_i, float (&w)[9], float g[3])
+__device__ __forceinline__ float fine_weights_padded(const int (&gd)[9][3], const int up[3], float weight_up,
+                                                     float weight_down, const LutRange& range, float (&w)[9],
+                                                     float g[3])
 {
     float wf[UpTaps<F>::n];
-    const float inv = fine_weights<F>(gd, up, weight_up, weight_down, var_inv_i, wf, g);
+    const float inv = fine_weights<F>(gd, up, weight_up, weight_down, range, wf, g);
 #pragma unroll
     for (int i = 0; i < 9; ++i) w[i] = i < UpTaps<F>::n ? wf[i < UpTaps<F>::n ? i : 0] : 0.0f;
     return inv;
 }
 
-// filtered costs of fine pixel F from the staged taps (the arithmetic and order of up_costs)
-template <int F, int E>
+// filtered costs of fine pixel F from the staged taps: the arithmetic and order of up_costs, or
+// (kFast, the chunked 16-bit path) the same sum with fused multiply-adds
+template <int F, int E, bool kFast>
 __device__ __forceinline__ void filter_part(const float (&tap)[9][E], const float (&w)[9], float inv, float weight_up,
                                             float acc[E])
 {
@@ -211,17 +229,13 @@ __device__ __forceinline__ void filter_part(const float (&tap)[9][E], const floa
 #pragma unroll
     for (int i = 0; i < UpTaps<F>::n; ++i)
 #pragma unroll
-        for (int e = 0; e < E; ++e) acc[e] = fadd(acc[e], fmul(w[i], tap[UpTaps<F>::tap(i)][e]));
+        for (int e = 0; e < E; ++e)
+            acc[e] = kFast ? fmaf(w[i], tap[UpTaps<F>::tap(i)][e], acc[e])
+                           : fadd(acc[e], fmul(w[i], tap[UpTaps<F>::tap(i)][e]));
 #pragma unroll
     for (int e = 0; e < E; ++e) acc[e] = fmul(acc[e], inv);
 }
 
-struct SelectOut {
-    float d0, dl, q;
-    float* distance;
-    int32_t* index;
-    bool write_guide;  // the selecting step also writes the filtered level-0 guide
-};
 
 // State of one fine pixel of a thread
 struct FinePixel {
@@ -231,10 +245,10 @@ struct FinePixel {
     bool active;
 };
 
-template <int F>
-__device__ __forceinline__ void fine_setup(const float (&gd)[9][3], const uint8_t* __restrict__ guide_io,
+template <int F, bool kWriteGuide>
+__device__ __forceinline__ void fine_setup(const int (&gd)[9][3], const uint8_t* __restrict__ guide_io,
                                            const LevelGeom& g, int x, int y, bool coarse_ok, float weight_up,
-                                           float weight_down, float var_inv_i, bool write_guide, FinePixel& px)
+                                           float weight_down, const LutRange& range, FinePixel& px)
 {
     const int fx = 2 * x + (F >= 2 ? 1 : 0), fy = 2 * y + (F & 1);
     // a fine pixel outside the level is the clamped duplicate of another one and is skipped
@@ -242,10 +256,11 @@ __device__ __forceinline__ void fine_setup(const float (&gd)[9][3], const uint8_
     px.index = fy * g.cols_out + fx;
     px.inv = 0.0f;
     if (!px.active) return;
-    float up[3], gsum[3];
+    int up[3];
+    float gsum[3];
     load_guide(guide_io, px.index, up);
-    px.inv = fine_weights_padded<F>(gd, up, weight_up, weight_down, var_inv_i, px.w, gsum);
-    if (write_guide)
+    px.inv = fine_weights_padded<F>(gd, up, weight_up, weight_down, range, px.w, gsum);
+    if (kWriteGuide)
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch)
             const_cast<uint8_t*>(guide_io)[3 * px.index + ch] = (uint8_t)__float2uint_rz(fmul(gsum[ch], px.inv));
@@ -260,7 +275,7 @@ __device__ __forceinline__ void up_part(const float (&tap)[9][UpTile<W>::E], con
     constexpr int E = UpTile<W>::E;
     float acc[E];
     raw.part(part, acc);
-    filter_part<F, E>(tap, px.w, px.inv, weight_up, acc);
+    filter_part<F, E, W == 8>(tap, px.w, px.inv, weight_up, acc);
     if constexpr (kSelect) {
         if (full) {
 #pragma unroll
@@ -308,43 +323,48 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
     }
 }
 
+// Shared memory of one upsampling block
+template <int W>
+struct UpShared {
+    __align__(16) float tile[2][UpTile<W>::floats];
+    float lut[kRangeLutSize];
+};
+
+// One block of an upsampling step: coarse pixels x0 .. x0 + kUpTileX - 1 of coarse row y, their
+// fine pixels.  Pointers are the instance's own (so.distance / so.index / so.distance2 included);
+// sh.lut is filled with the level's range weights and the block synchronised before the call.
 // kSelect = false: coarse float32 -> fine float32 in place (and the fine guides);
 // kSelect = true: the last step, fine level-0 costs of type Tf in, the selection out.
 template <int W, typename Tf, bool kSelect>
-__global__ void __launch_bounds__(kBatchBlock, 2) isb_up_kernel(const uint8_t* __restrict__ guide_in,
-                                                            const float* __restrict__ cost_in,
-                                                            uint8_t* __restrict__ guide_io,
-                                                            Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
-                                                            int ncand, float weight_up, float weight_down,
-                                                            float var_inv_i, SelectOut so)
+__device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
+                                             uint8_t* __restrict__ guide_io, Tf* __restrict__ cost_fine,
+                                             const LevelGeom& g, int chunks, int ncand, float weight_up,
+                                             float weight_down, const SelectOut& so, int x0, int y, UpShared<W>& sh)
 {
-    __shared__ __align__(16) float tile[2][UpTile<W>::floats];
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
-    const int inst = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kUpTileX;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int kind = warp >> 2;  // warp-uniform
     const int lx = (warp & 3) * 32 + lane, x = x0 + lx;
-    guide_in += (int64_t)inst * pin * 3;
-    guide_io += (int64_t)inst * pio * 3;
-    cost_in += (int64_t)inst * chunks * pin * W;
-    cost_fine += (int64_t)inst * chunks * pio * W;
     const bool coarse_ok = x < g.cols_in;
-    const bool write_guide = !kSelect || so.write_guide;
+    // the planar selecting step writes the filtered level-0 guide as the reference's filter does;
+    // the chunked one leaves it, as nothing reads it after the selection
+    constexpr bool kWriteGuide = !kSelect || W == 1;
+    const LutRange range{sh.lut};
     FinePixel pa, pb;
     {
         int ci[9];
-        float gd[9][3];
+        int gd[9][3];
         if (coarse_ok) coarse_neighbourhood(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
         if (kind == 0) {
-            fine_setup<0>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pa);
-            fine_setup<3>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pb);
+            fine_setup<0, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<3, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
         } else {
-            fine_setup<1>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pa);
-            fine_setup<2>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, var_inv_i, write_guide, pb);
+            fine_setup<1, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<2, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
         }
     }
     Selector sa, sb;
-    load_tile_async<W>(tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
+    load_tile_async<W>(sh.tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
     cp_async_commit();
     // fine cells are read once, from memory: prefetched a chunk ahead of their use
     RawCell<W, Tf> ra, rb;
@@ -352,7 +372,8 @@ __global__ void __launch_bounds__(kBatchBlock, 2) isb_up_kernel(const uint8_t* _
     if (pb.active) rb.load(cost_fine + (int64_t)pb.index * W);
     for (int c = 0; c < chunks; ++c) {
         if (c + 1 < chunks)
-            load_tile_async<W>(tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in, x0, y);
+            load_tile_async<W>(sh.tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in, x0,
+                               y);
         cp_async_commit();
         RawCell<W, Tf> na = ra, nb = rb;
         if (c + 1 < chunks) {
@@ -364,23 +385,52 @@ __global__ void __launch_bounds__(kBatchBlock, 2) isb_up_kernel(const uint8_t* _
         __syncthreads();
         Tf* fine_chunk = cost_fine + (int64_t)c * pio * W;
         if (kind == 0)
-            up_chunk<0, 3, W, Tf, kSelect>(tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+            up_chunk<0, 3, W, Tf, kSelect>(sh.tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
         else
-            up_chunk<1, 2, W, Tf, kSelect>(tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+            up_chunk<1, 2, W, Tf, kSelect>(sh.tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
         __syncthreads();  // the tile is refilled two chunks on
         ra = na;
         rb = nb;
     }
     if constexpr (kSelect) {
         if (pa.active) {
-            so.distance[(int64_t)inst * pio + pa.index] = select_from(sa, ncand, so.d0, so.dl, so.q);
-            if (so.index) so.index[(int64_t)inst * pio + pa.index] = sa.idx;
+            const float d = select_from(sa, ncand, so.d0, so.dl, so.q);
+            so.distance[pa.index] = d;
+            if (so.distance2) so.distance2[pa.index] = d;
+            if (so.index) so.index[pa.index] = sa.idx;
         }
         if (pb.active) {
-            so.distance[(int64_t)inst * pio + pb.index] = select_from(sb, ncand, so.d0, so.dl, so.q);
-            if (so.index) so.index[(int64_t)inst * pio + pb.index] = sb.idx;
+            const float d = select_from(sb, ncand, so.d0, so.dl, so.q);
+            so.distance[pb.index] = d;
+            if (so.distance2) so.distance2[pb.index] = d;
+            if (so.index) so.index[pb.index] = sb.idx;
         }
     }
+}
+
+// blockIdx.z: instance of contiguous levels.  (3 blocks per SM for the single-candidate filter,
+// 2 for the chunked volumes, whose taps need the registers.)
+template <int W, typename Tf, bool kSelect>
+__global__ void __launch_bounds__(kBatchBlock, W == 1 ? 3 : 2) isb_up_kernel(const uint8_t* __restrict__ guide_in,
+                                                            const float* __restrict__ cost_in,
+                                                            uint8_t* __restrict__ guide_io,
+                                                            Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
+                                                            int ncand, float weight_up, float weight_down,
+                                                            float var_inv_i, SelectOut so)
+{
+    __shared__ UpShared<W> sh;
+    fill_range_lut(sh.lut, var_inv_i);
+    __syncthreads();  // the range table is filled
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
+    const int inst = blockIdx.z;
+    if (kSelect) {
+        so.distance += (int64_t)inst * pio;
+        if (so.distance2) so.distance2 += (int64_t)inst * pio;
+        if (so.index) so.index += (int64_t)inst * pio;
+    }
+    isb_up_block<W, Tf, kSelect>(guide_in + (int64_t)inst * pin * 3, cost_in + (int64_t)inst * chunks * pin * W,
+                                 guide_io + (int64_t)inst * pio * 3, cost_fine + (int64_t)inst * chunks * pio * W, g,
+                                 chunks, ncand, weight_up, weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh);
 }
 
 // Selection from an unfiltered level-0 volume (pyramids of fewer than two levels, or the
@@ -407,6 +457,74 @@ __global__ void __launch_bounds__(kBatchBlock) select_kernel(const T* __restrict
     if (index) index[(int64_t)inst * P + i] = s.idx;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Uneven batches: one launch per filter step over the instances that have the step, each block
+// reading its instance's LevelDesc (blockIdx.y / blockIdx.z); blocks beyond an instance's level
+// size return before touching shared memory.
+// ---------------------------------------------------------------------------------------------
+template <int W, typename Tin>
+__global__ void __launch_bounds__(kBatchBlock) isb_down_uneven_kernel(const LevelDesc* __restrict__ descs)
+{
+    const LevelDesc& d = descs[blockIdx.y];
+    const LevelGeom g = d.g;
+    const int64_t pout = (int64_t)g.rows_out * g.cols_out;
+    if ((int64_t)blockIdx.x * blockDim.x >= pout) return;
+    __shared__ float lut[kRangeLutSize];
+    fill_range_lut(lut, d.var_inv_i);
+    __syncthreads();
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= pout) return;
+    isb_down_pixel<W, Tin>(d.guide_in, static_cast<const Tin*>(d.cost_in), d.guide_out, static_cast<float*>(d.cost_out),
+                           g, d.chunks, o, lut);
+}
+
+template <int W, typename Tf, bool kSelect>
+__global__ void __launch_bounds__(kBatchBlock, W == 1 ? 3 : 2) isb_up_uneven_kernel(const LevelDesc* __restrict__ descs)
+{
+    const LevelDesc& d = descs[blockIdx.z];
+    const LevelGeom g = d.g;
+    const int x0 = blockIdx.x * kUpTileX, y = blockIdx.y;
+    if (x0 >= g.cols_in || y >= g.rows_in) return;
+    __shared__ UpShared<W> sh;
+    fill_range_lut(sh.lut, d.var_inv_i);
+    __syncthreads();
+    isb_up_block<W, Tf, kSelect>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
+                                 static_cast<Tf*>(d.cost_out), g, d.chunks, d.ncand, d.weight_up, d.weight_down, d.so,
+                                 x0, y, sh);
+}
+
+int launch_down_uneven(const LevelDesc* d_descs, int count, int max_rows_out, int max_cols_out, int width,
+                       int storage_in, cudaStream_t st)
+{
+    SSG_REQUIRE(count >= 1 && count <= 65535, "instances out of range");
+    const dim3 grid(grid_1d((int64_t)max_rows_out * max_cols_out, kBatchBlock), count);
+    if (width == 1)
+        isb_down_uneven_kernel<1, float><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else if (storage_in == SSG_STORAGE_F16)
+        isb_down_uneven_kernel<8, __half><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else if (storage_in == SSG_STORAGE_UNORM16)
+        isb_down_uneven_kernel<8, uint16_t><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else
+        isb_down_uneven_kernel<8, float><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    return launch_status("isb_down_uneven_kernel");
+}
+
+int launch_up_uneven(const LevelDesc* d_descs, int count, int max_rows_in, int max_cols_in, int width,
+                     int storage_fine, bool select, cudaStream_t st)
+{
+    SSG_REQUIRE(count >= 1 && count <= 65535 && max_rows_in <= 65535, "sizes out of range");
+    const dim3 grid((unsigned)((max_cols_in + kUpTileX - 1) / kUpTileX), (unsigned)max_rows_in, (unsigned)count);
+    if (width == 1)
+        isb_up_uneven_kernel<1, float, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else if (!select)
+        isb_up_uneven_kernel<8, float, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else if (storage_fine == SSG_STORAGE_F16)
+        isb_up_uneven_kernel<8, __half, true><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else
+        isb_up_uneven_kernel<8, uint16_t, true><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    return launch_status("isb_up_uneven_kernel");
+}
+
 static int chunks_of(int n) { return (n + 7) / 8; }
 
 // blocks of kUpTileX coarse pixels of one coarse row, per instance
@@ -415,15 +533,10 @@ static dim3 up_grid(int cols_in, int rows_in, int instances)
     return dim3((unsigned)((cols_in + kUpTileX - 1) / kUpTileX), (unsigned)rows_in, (unsigned)instances);
 }
 
-static int level_rows(int rows, int s) { return (int)std::ceil(rows / std::pow(2.0, s)); }
-
-struct Levels {
-    float var_inv_i;
-    float weight_up[SSG_MAX_LEVELS], weight_down[SSG_MAX_LEVELS];
-};
+int level_rows(int rows, int s) { return (int)std::ceil(rows / std::pow(2.0, s)); }
 
 // python/isb_filter.py:87-88, :110-112 in double, rounded to float32 as cupy.float32 does
-static Levels isb_constants(int level_count, double sigma_i, double sigma_s)
+Levels isb_constants(int level_count, double sigma_i, double sigma_s)
 {
     Levels l{};
     const double vs = 1 / (2 * sigma_s * sigma_s), vi = 1 / (2 * sigma_i * sigma_i);
@@ -438,11 +551,10 @@ static Levels isb_constants(int level_count, double sigma_i, double sigma_s)
 }
 
 // (candidates[0] / candidates[-1] - 1) in float32, depth_estimation.py:195-196
-static SelectOut select_constants(const float* candidates, int ncand, float* distance, int32_t* index,
-                                  bool write_guide)
+SelectOut select_constants(const float* candidates, int ncand, float* distance, int32_t* index)
 {
     const float d0 = candidates[0], dl = candidates[ncand - 1];
-    return SelectOut{d0, dl, d0 / dl - 1.0f, distance, index, write_guide};
+    return SelectOut{d0, dl, d0 / dl - 1.0f, distance, index, nullptr};
 }
 
 static int check_levels(int rows_in, int cols_in, int rows_out, int cols_out)
@@ -580,7 +692,7 @@ extern "C" int ssg_select_distance(const float* d_cost, int candidate_count, int
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
     SSG_REQUIRE(pixels >= 0, "negative pixel count");
     if (pixels == 0) return SSG_OK;
-    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, false);
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
     select_kernel<1, float><<<dim3(grid_1d(pixels, kBatchBlock), 1), kBatchBlock, 0, as_stream(stream)>>>(
         d_cost, pixels, candidate_count, candidate_count, so.d0, so.dl, so.q, d_distance, d_index);
     return launch_status("select_kernel");
@@ -595,7 +707,7 @@ extern "C" int ssg_isb_upsample_select(const uint8_t* d_guide_in, const float* d
                 "null pointer");
     if (int e = check_levels(rows_fine, cols_fine, rows_in, cols_in)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, true);
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
     return launch_up<1, float, true>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout,
                                      const_cast<float*>(d_cost_fine), rows_fine, cols_fine, candidate_count,
                                      candidate_count, 1, weight_up, weight_down, var_inv_i, so, as_stream(stream));
@@ -659,8 +771,7 @@ extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const vo
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
     const int chunks = chunks_of(candidate_count);
-    // the level-0 guide is not needed after the selection and is left as it was
-    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, false);
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
     const float* coarse = static_cast<const float*>(d_cost_in);
     void* fine = const_cast<void*>(d_cost_fine);  // read only in the selecting variant
     cudaStream_t st = as_stream(stream);
@@ -686,7 +797,7 @@ extern "C" int ssg_select_distance_batch(const void* d_cost, int candidate_count
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
                 "unknown storage %d", storage);
-    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index, false);
+    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
     const dim3 grid(grid_1d(pixels, kBatchBlock), instances);
     const int chunks = chunks_of(candidate_count);
     cudaStream_t st = as_stream(stream);

@@ -9,6 +9,20 @@ namespace ssg {
 
 constexpr float kIsbEps = 0.01f;  // isb_filter.cu:32
 
+// Sizes of a level pair (down: in = fine, out = coarse; up: in = coarse, out = fine)
+struct LevelGeom {
+    int rows_in, cols_in, rows_out, cols_out;
+};
+
+// Outputs of the selecting step (depth_estimation.py:179-198): d0, dl the first and last
+// candidates, q = d0 / dl - 1
+struct SelectOut {
+    float d0, dl, q;
+    float* distance;
+    int32_t* index;
+    float* distance2;  // optional second copy of the distance
+};
+
 __device__ __forceinline__ float range_weight(float d, float var_inv_i)
 {
     // __expf(-diff * diff * varInvI) + EPS  (isb_filter.cu:87, :229)
@@ -27,6 +41,41 @@ __device__ __forceinline__ void load_guide(const uint8_t* __restrict__ g, int64_
     out[2] = (float)g[3 * idx + 2];
 }
 
+__device__ __forceinline__ void load_guide(const uint8_t* __restrict__ g, int64_t idx, int out[3])
+{
+    out[0] = g[3 * idx];
+    out[1] = g[3 * idx + 1];
+    out[2] = g[3 * idx + 2];
+}
+
+// Guides are 8-bit, so the colour distance of two guide pixels, |a0 - b0| + |a1 - b1| + |a2 - b2|,
+// is an integer in [0, 765]: the reference computes it in float32 exactly, and a range weight is
+// a function of that integer alone.  The forward kernels therefore read range weights from a
+// shared-memory table of all 766 values, filled per block with range_weight, which gives the
+// same bits as evaluating the exponential per tap.
+constexpr int kRangeLutSize = 766;
+
+__device__ __forceinline__ int colour_distance(const int a[3], const int b[3])
+{
+    return abs(a[0] - b[0]) + abs(a[1] - b[1]) + abs(a[2] - b[2]);
+}
+
+struct ExpRange {  // evaluates the weight of a colour distance
+    float var_inv_i;
+    __device__ __forceinline__ float operator()(int d) const { return range_weight((float)d, var_inv_i); }
+};
+
+struct LutRange {  // reads it from the block's table
+    const float* lut;
+    __device__ __forceinline__ float operator()(int d) const { return lut[d]; }
+};
+
+// fills the table of a block (the caller synchronises the block before reading it)
+__device__ __forceinline__ void fill_range_lut(float* lut, float var_inv_i)
+{
+    for (int d = threadIdx.x; d < kRangeLutSize; d += blockDim.x) lut[d] = range_weight((float)d, var_inv_i);
+}
+
 // Guide weights of one coarse pixel of guideDownsample2xKernel (isb_filter.cu:44-119): the
 // centre tap (weight 1) and its 8 neighbours in the reference's order, edge-clamped. Writes the
 // coarse guide (uint8 truncation, isb_filter.cu:93).
@@ -39,9 +88,9 @@ struct DownTapsT {
 };
 using DownTaps = DownTapsT<int64_t>;
 
-template <typename I>
+template <typename I, typename RW>
 __device__ __forceinline__ void down_weights(const uint8_t* __restrict__ guide_in, int rows_in, int cols_in, int x,
-                                             int y, float var_inv_i, uint8_t* __restrict__ guide_out,
+                                             int y, const RW& range, uint8_t* __restrict__ guide_out,
                                              DownTapsT<I>& t)
 {
     const int x2 = 2 * x, y2 = 2 * y;
@@ -50,19 +99,19 @@ __device__ __forceinline__ void down_weights(const uint8_t* __restrict__ guide_i
     const int rows8[8] = {my, y2, py, py, py, y2, my, my};
     const int cols8[8] = {mx, mx, mx, x2, px, px, px, x2};
     t.centre = (I)y2 * cols_in + x2;
-    float cur[3];
+    int cur[3];
     load_guide(guide_in, t.centre, cur);
     const float base[8] = {0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f};
-    float wsum = 1.0f, g[3] = {cur[0], cur[1], cur[2]};
+    float wsum = 1.0f, g[3] = {(float)cur[0], (float)cur[1], (float)cur[2]};
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         t.idx[i] = (I)rows8[i] * cols_in + cols8[i];
-        float nb[3];
+        int nb[3];
         load_guide(guide_in, t.idx[i], nb);
-        t.w[i] = fmul(base[i], range_weight(abs_sum(cur, nb), var_inv_i));
+        t.w[i] = fmul(base[i], range(colour_distance(cur, nb)));
         wsum = fadd(wsum, t.w[i]);
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul(nb[ch], t.w[i]));
+        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul((float)nb[ch], t.w[i]));
     }
     t.wsum = wsum;
     const float den = fdiv(1.0f, wsum);
@@ -107,21 +156,21 @@ struct UpTaps<3> {  // (1,1),(1,2),(2,1),(2,2)
 
 // Range weights of fine pixel F from the coarse guides `gd` and its own guide `up`; returns
 // 1 / (sum of weights) and the weighted guide sum `g` (isb_filter.cu:142-267).
-template <int F>
-__device__ __forceinline__ float fine_weights(const float (&gd)[9][3], const float up[3], float weight_up,
-                                              float weight_down, float var_inv_i, float (&w)[UpTaps<F>::n],
+template <int F, typename RW>
+__device__ __forceinline__ float fine_weights(const int (&gd)[9][3], const int up[3], float weight_up,
+                                              float weight_down, const RW& range, float (&w)[UpTaps<F>::n],
                                               float g[3])
 {
     float ws = weight_up;
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) g[ch] = fmul(weight_up, up[ch]);
+    for (int ch = 0; ch < 3; ++ch) g[ch] = fmul(weight_up, (float)up[ch]);
 #pragma unroll
     for (int i = 0; i < UpTaps<F>::n; ++i) {
-        const float* nb = gd[UpTaps<F>::tap(i)];
-        const float rw = fmul(weight_down, range_weight(abs_sum(nb, up), var_inv_i));
+        const int* nb = gd[UpTaps<F>::tap(i)];
+        const float rw = fmul(weight_down, range(colour_distance(nb, up)));
         w[i] = UpTaps<F>::weighted ? fmul(UpTaps<F>::base(i), rw) : rw;
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul(nb[ch], w[i]));
+        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul((float)nb[ch], w[i]));
         ws = fadd(ws, w[i]);
     }
     return fdiv(1.0f, ws);
@@ -130,7 +179,7 @@ __device__ __forceinline__ float fine_weights(const float (&gd)[9][3], const flo
 // Coarse 3x3 neighbourhood of (x, y), edge-clamped: flat indices and guides
 template <typename I>
 __device__ __forceinline__ void coarse_neighbourhood(const uint8_t* __restrict__ guide_in, int rows_in, int cols_in,
-                                                     int x, int y, I (&cidx)[9], float (&gd)[9][3])
+                                                     int x, int y, I (&cidx)[9], int (&gd)[9][3])
 {
     const int rr[3] = {max(y - 1, 0), y, min(y + 1, rows_in - 1)};
     const int cc[3] = {max(x - 1, 0), x, min(x + 1, cols_in - 1)};
@@ -164,7 +213,7 @@ __device__ __forceinline__ void up_weights(const uint8_t* __restrict__ guide_in,
                                            float weight_up, float weight_down, float var_inv_i, bool write_guide,
                                            UpWeights& u)
 {
-    float gd[9][3];
+    int gd[9][3];
     coarse_neighbourhood(guide_in, rows_in, cols_in, x, y, u.cidx, gd);
     const int x2 = 2 * x, y2 = 2 * y;
     const int pux = min(x2 + 1, cols_io - 1), puy = min(y2 + 1, rows_io - 1);
@@ -176,14 +225,15 @@ __device__ __forceinline__ void up_weights(const uint8_t* __restrict__ guide_in,
     u.set[1] = y2 != puy;
     u.set[2] = x2 != pux;
     u.set[3] = u.set[1] && u.set[2];
-    float up[4][3];
+    int up[4][3];
 #pragma unroll
     for (int f = 0; f < 4; ++f) load_guide(guide_io, u.fidx[f], up[f]);
     float g[4][3];
-    u.inv[0] = fine_weights<0>(gd, up[0], weight_up, weight_down, var_inv_i, u.w1, g[0]);
-    u.inv[1] = fine_weights<1>(gd, up[1], weight_up, weight_down, var_inv_i, u.w2, g[1]);
-    u.inv[2] = fine_weights<2>(gd, up[2], weight_up, weight_down, var_inv_i, u.w3, g[2]);
-    u.inv[3] = fine_weights<3>(gd, up[3], weight_up, weight_down, var_inv_i, u.w4, g[3]);
+    const ExpRange range{var_inv_i};
+    u.inv[0] = fine_weights<0>(gd, up[0], weight_up, weight_down, range, u.w1, g[0]);
+    u.inv[1] = fine_weights<1>(gd, up[1], weight_up, weight_down, range, u.w2, g[1]);
+    u.inv[2] = fine_weights<2>(gd, up[2], weight_up, weight_down, range, u.w3, g[2]);
+    u.inv[3] = fine_weights<3>(gd, up[3], weight_up, weight_down, range, u.w4, g[3]);
     if (write_guide)
 #pragma unroll
         for (int f = 0; f < 4; ++f)

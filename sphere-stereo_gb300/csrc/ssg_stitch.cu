@@ -16,10 +16,28 @@
 #include <cstring>
 
 #include "ssg_common.cuh"
+#include "ssg_uneven.cuh"
 
 namespace ssg {
 
 constexpr int kStitchBlock = 256;
+
+// smallest float f with (double)f >= v, and largest float f with (double)f <= v
+static float float_at_least(double v)
+{
+    float f = (float)v;
+    while ((double)f < v) f = std::nextafter(f, INFINITY);
+    while ((double)std::nextafter(f, -INFINITY) >= v) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+static float float_at_most(double v)
+{
+    float f = (float)v;
+    while ((double)f > v) f = std::nextafter(f, -INFINITY);
+    while ((double)std::nextafter(f, INFINITY) <= v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
 
 // createInpaintingWeightsKernel, stitcher.cu:212-272
 __global__ void __launch_bounds__(kStitchBlock) inpainting_table_kernel(int cols, int rows, Intr k, float tx,
@@ -177,26 +195,17 @@ struct ReprojParams {
     float t[SSG_MAX_REFERENCES][3];
 };
 
-// reprojectDistanceKernel, stitcher.cu:181-204, as a z-buffer on the float bits.
-// blockIdx.y: instance (frame * references + reference slot) of contiguous maps.
-__global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_constant__ ReprojParams p,
-                                                                 const float* __restrict__ din,
-                                                                 float* __restrict__ dout)
+// reprojectDistanceKernel, stitcher.cu:181-204, as a z-buffer on the float bits: pixel i of one
+// map (din -> dout, P pixels, `cols` wide)
+__device__ __forceinline__ void reproject_pixel(const Intr& k, const float* t, const float* __restrict__ din,
+                                                float* __restrict__ dout, int cols, int64_t P, int64_t i)
 {
-    const int cols = p.cols;
-    const int64_t P = (int64_t)cols * p.rows;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
-    const int slot = blockIdx.y % p.references;
-    din += (int64_t)blockIdx.y * P;
-    dout += (int64_t)blockIdx.y * P;
-    const Intr& k = p.k[slot];
     float pt[3];
     unproject_cu((float)(i % cols), (float)(i / cols), k, pt);
     const float d = din[i];
-    pt[0] = fsub(fmul(d, pt[0]), p.t[slot][0]);
-    pt[1] = fsub(fmul(d, pt[1]), p.t[slot][1]);
-    pt[2] = fsub(fmul(d, pt[2]), p.t[slot][2]);
+    pt[0] = fsub(fmul(d, pt[0]), t[0]);
+    pt[1] = fsub(fmul(d, pt[1]), t[1]);
+    pt[2] = fsub(fmul(d, pt[2]), t[2]);
     float o[2];
     project_cu(pt, k, o, nullptr);
     const float dist = norm3df(pt[0], pt[1], pt[2]);
@@ -204,6 +213,18 @@ __global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_co
     const int idx = (int)((unsigned)__float2int_rn(o[1]) * (unsigned)cols + (unsigned)__float2int_rn(o[0]));
     if (idx < 0 || (int64_t)idx >= P || !(dist >= 0.0f)) return;
     atomicMin(reinterpret_cast<int*>(dout) + idx, __float_as_int(dist));
+}
+
+// blockIdx.y: instance (frame * references + reference slot) of contiguous maps.
+__global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_constant__ ReprojParams p,
+                                                                 const float* __restrict__ din,
+                                                                 float* __restrict__ dout)
+{
+    const int64_t P = (int64_t)p.cols * p.rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int slot = blockIdx.y % p.references;
+    reproject_pixel(p.k[slot], p.t[slot], din + (int64_t)blockIdx.y * P, dout + (int64_t)blockIdx.y * P, p.cols, P, i);
 }
 
 // Tiled Jacobi inpainting: kTileW x kTileH outputs, a halo of kHalo >= steps pixels.
@@ -311,6 +332,285 @@ __global__ void __launch_bounds__(kInpaintBlock) inpaint_tile_kernel(const float
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Hole filling over lists of holes (the batched path), with the result of the Jacobi steps above.
+// Only holes change, a filled hole keeps its value from then on, and a hole whose two table
+// weights are 0 (outside the model's valid area) never changes.  Every pixel gets a one-byte
+// stamp: 0 for a pixel that is not a hole, kUnfilled for a hole, s for a hole filled at step s.
+// Step s reads a neighbour only when its stamp is below s, i.e. as it was before the step (a
+// neighbour filled in the same step has stamp s and counts as a hole, as in a Jacobi step on a
+// copy), and writes each filled hole's value and stamp in place: one map, no copy.
+//   * Step 1 visits every fillable hole (listed by a scan).
+//   * A hole that step 1 leaves open can only be filled at step s > 1 through a neighbour filled
+//     at step s - 1 (a neighbour filled earlier would have filled it earlier), so step s visits the
+//     holes that read a pixel filled at step s - 1: the work of a step is its frontier.  A claim
+//     word per pixel (the last step that queued it) keeps a hole from being visited twice.
+// ---------------------------------------------------------------------------------------------
+constexpr uint8_t kUnfilled = 255;
+constexpr int kMaxListIterations = 254;
+
+struct HoleOffsets {
+    int64_t n0, n1;
+    float w0, w1;
+};
+
+// the two weighted neighbours a table entry encodes (stitcher.cu:297-316); a weight is 0 where
+// the offset field is 3 (never written by the table kernel)
+__device__ __forceinline__ HoleOffsets hole_offsets(uchar2 t, int64_t g, int cols)
+{
+    HoleOffsets h;
+    h.n0 = g + ((t.x & 12) / 4 - 1) * (int64_t)cols + ((t.x & 3) - 1);
+    h.n1 = g + ((t.y & 12) / 4 - 1) * (int64_t)cols + ((t.y & 3) - 1);
+    const bool ok0 = (t.x & 3) != 3 && (t.x & 12) != 12, ok1 = (t.y & 3) != 3 && (t.y & 12) != 12;
+    h.w0 = ok0 ? (float)(t.x & 240) : 0.0f;
+    h.w1 = ok1 ? (float)(t.y & 240) : 0.0f;
+    return h;
+}
+
+__device__ __forceinline__ bool fillable(uchar2 t)
+{
+    const HoleOffsets h = hole_offsets(t, 0, 1);
+    return h.w0 > 0.0f || h.w1 > 0.0f;
+}
+
+// Jacobi step `step` of hole g: fills it (value and stamp) when a usable neighbour exists
+__device__ __forceinline__ bool fill_hole(float* __restrict__ map, uint8_t* __restrict__ stamp, int64_t g,
+                                         const HoleOffsets& h, int step, float valid_at_most)
+{
+    float val = 0.0f, ws = 0.0f;
+    if (h.w0 > 0.0f && stamp[h.n0] < step) {
+        const float sd = map[h.n0];
+        if (sd <= valid_at_most) {
+            val = fadd(val, fmul(h.w0, sd));
+            ws = fadd(ws, h.w0);
+        }
+    }
+    if (h.w1 > 0.0f && stamp[h.n1] < step) {
+        const float sd = map[h.n1];
+        if (sd <= valid_at_most) {
+            val = fadd(val, fmul(h.w1, sd));
+            ws = fadd(ws, h.w1);
+        }
+    }
+    if (!(ws > 0.0f)) return false;
+    map[g] = fdiv(val, ws);
+    stamp[g] = (uint8_t)step;
+    return true;
+}
+
+// Appends `item` (where `take`) to the list counted by *count with one atomic per block: every
+// thread of the block calls it (block-uniform control flow; blockDim.x == kStitchBlock).
+__device__ __forceinline__ void block_append(bool take, int32_t item, int32_t* count, int32_t* list)
+{
+    __shared__ int warp_base[kStitchBlock / 32];
+    __shared__ int block_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned mask = __ballot_sync(0xffffffffu, take);
+    if (lane == 0) warp_base[warp] = __popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int w = 0; w < kStitchBlock / 32; ++w) {
+            const int n = warp_base[w];
+            warp_base[w] = total;
+            total += n;
+        }
+        block_base = total ? atomicAdd(count, total) : 0;
+    }
+    __syncthreads();
+    if (take) list[block_base + warp_base[warp] + __popc(mask & ((1u << lane) - 1))] = item;
+    __syncthreads();  // warp_base and block_base are reused by the next call
+}
+
+// Reserves `n` entries per thread in a list counted by *count, with one atomic per block: returns
+// the thread's first entry.  Every thread of the block calls it (block-uniform control flow;
+// blockDim.x == kStitchBlock).
+__device__ __forceinline__ int block_reserve(int n, int32_t* count)
+{
+    __shared__ int warp_base[kStitchBlock / 32];
+    __shared__ int block_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = n;  // inclusive scan over the warp
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    if (lane == 31) warp_base[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int w = 0; w < kStitchBlock / 32; ++w) {
+            const int c = warp_base[w];
+            warp_base[w] = total;
+            total += c;
+        }
+        block_base = total ? atomicAdd(count, total) : 0;
+    }
+    __syncthreads();
+    const int first = block_base + warp_base[warp] + incl - n;
+    __syncthreads();  // warp_base and block_base are reused by the next call
+    return first;
+}
+
+// Where a flat map pixel g lives: its map's size, its position in the map, its table entry.
+struct MapPixel {
+    int cols, rows, x, y;
+    const uchar2* table;  // the map's inpainting table (entry of pixel (x, y): table[y * cols + x])
+};
+
+// `instances` maps of one size, tables per reference slot (the uniform batch)
+struct UniformMaps {
+    int cols, rows, references;
+    const uchar2* tables;
+    __device__ __forceinline__ MapPixel at(int64_t g) const
+    {
+        const int64_t P = (int64_t)cols * rows;
+        const int64_t inst = g / P, j = g - inst * P;
+        return MapPixel{cols, rows, (int)(j % cols), (int)(j / cols), tables + (inst % references) * P};
+    }
+};
+
+// Scan: stamps map pixels [begin, end) of the flat index space, clears their claims and lists
+// the fillable holes in `list` (counted by *count).
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_scan_kernel(const Maps maps, int64_t total,
+                                                                 const float* __restrict__ map,
+                                                                 uint8_t* __restrict__ stamp,
+                                                                 int32_t* __restrict__ claim, float hole_at_least,
+                                                                 int32_t* __restrict__ count,
+                                                                 int32_t* __restrict__ list)
+{
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool take = false;
+    if (g < total) {
+        const bool hole = map[g] >= hole_at_least;  // stitcher.cu:287
+        stamp[g] = hole ? kUnfilled : 0;
+        claim[g] = 0;
+        if (hole) {
+            const MapPixel m = maps.at(g);
+            // interior test of stitcher.cu:291
+            take = m.x >= 1 && m.y >= 1 && m.x < m.cols - 1 && m.y < m.rows - 1 &&
+                   fillable(m.table[(int64_t)m.y * m.cols + m.x]);
+        }
+    }
+    block_append(take, (int32_t)g, count, list);
+}
+
+// Step 1 on every listed hole; lists the holes it fills.  counts[3] rotate: counts[(s - 1) % 3]
+// counts step s's input list, counts[s % 3] its output (zeroed by step s - 1 or the set-up), and
+// step s zeroes counts[(s + 1) % 3].
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Maps maps, float* __restrict__ map,
+                                                                       uint8_t* __restrict__ stamp,
+                                                                       int32_t* __restrict__ counts,
+                                                                       const int32_t* __restrict__ list_in,
+                                                                       int32_t* __restrict__ list_out,
+                                                                       float valid_at_most)
+{
+    const int n = counts[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[2] = 0;
+    const int stride = gridDim.x * blockDim.x;
+    // whole blocks iterate together (block_append is block-collective)
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int h = base + (int)threadIdx.x;
+        bool filled = false;
+        int32_t g = 0;
+        if (h < n) {
+            g = list_in[h];
+            const MapPixel m = maps.at(g);
+            const uchar2 t = m.table[(int64_t)m.y * m.cols + m.x];
+            filled = fill_hole(map, stamp, g, hole_offsets(t, g, m.cols), 1, valid_at_most);
+        }
+        block_append(filled, g, counts + 1, list_out);
+    }
+}
+
+// Step `step` >= 2: visits the open holes next to the pixels filled at step - 1 (list_in) that read
+// one of them, fills those it can and lists them (one reservation per block and pass).
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const Maps maps, float* __restrict__ map,
+                                                                          uint8_t* __restrict__ stamp,
+                                                                          int32_t* __restrict__ claim, int step,
+                                                                          int32_t* __restrict__ counts,
+                                                                          const int32_t* __restrict__ list_in,
+                                                                          int32_t* __restrict__ list_out,
+                                                                          float valid_at_most)
+{
+    const int n = counts[(step - 1) % 3];
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[(step + 1) % 3] = 0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int h = base + (int)threadIdx.x;
+        unsigned filled = 0;  // bit k: neighbour k (3 x 3, row-major) filled
+        int64_t p = 0;
+        int cols = 1;
+        if (h < n) {
+            p = list_in[h];
+            const MapPixel m = maps.at(p);
+            cols = m.cols;
+#pragma unroll 1
+            for (int k = 0; k < 9; ++k) {
+                const int qx = m.x + k % 3 - 1, qy = m.y + k / 3 - 1;
+                if (k == 4 || qx < 1 || qy < 1 || qx >= m.cols - 1 || qy >= m.rows - 1) continue;
+                const int64_t q = p + (int64_t)(k / 3 - 1) * m.cols + (k % 3 - 1);
+                if (stamp[q] != kUnfilled) continue;
+                const HoleOffsets o = hole_offsets(m.table[(int64_t)qy * m.cols + qx], q, m.cols);
+                // q reads p, and no other thread has queued q for this step
+                if (((o.w0 > 0.0f && o.n0 == p) || (o.w1 > 0.0f && o.n1 == p)) && atomicMax(claim + q, step) < step &&
+                    fill_hole(map, stamp, q, o, step, valid_at_most))
+                    filled |= 1u << k;
+            }
+        }
+        int at = block_reserve(__popc(filled), counts + step % 3);
+        for (int k = 0; k < 9; ++k)
+            if (filled & (1u << k)) list_out[at++] = (int32_t)(p + (int64_t)(k / 3 - 1) * cols + (k % 3 - 1));
+    }
+}
+
+// blocks of a grid-stride launch: a few per SM
+static int resident_grid(int per_sm)
+{
+    static std::atomic<int> sms[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152 * per_sm;
+    int n = sms[dev].load();
+    if (n == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        sms[dev].store(n);
+    }
+    return n * per_sm;
+}
+
+// The hole filling of `total` flat map pixels (see above): d_holes holds 3 rotating counts (+ 1),
+// two lists and a claim word per pixel
+template <typename Maps>
+static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t* d_stamps, int32_t* d_holes,
+                         double max_dist, int iterations, cudaStream_t st)
+{
+    if (iterations == 0) return SSG_OK;
+    const float hole = float_at_least(max_dist + 0.1);
+    const float ok = float_at_most(max_dist + (double)0.1f);
+    int32_t* counts = d_holes;
+    int32_t* lists[2] = {d_holes + 4, d_holes + 4 + total};
+    int32_t* claims = d_holes + 4 + 2 * total;
+    const cudaError_t e = cudaMemsetAsync(counts, 0, 4 * sizeof(int32_t), st);
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    hole_scan_kernel<Maps><<<grid_1d(total, kStitchBlock), kStitchBlock, 0, st>>>(maps, total, d_map, d_stamps,
+                                                                                  claims, hole, counts, lists[0]);
+    if (int err = launch_status("hole_scan_kernel")) return err;
+    const int grid = resident_grid(4);
+    hole_first_step_kernel<Maps><<<grid, kStitchBlock, 0, st>>>(maps, d_map, d_stamps, counts, lists[0], lists[1],
+                                                                ok);
+    if (int err = launch_status("hole_first_step_kernel")) return err;
+    for (int s = 2; s <= iterations; ++s) {
+        hole_frontier_step_kernel<Maps><<<grid, kStitchBlock, 0, st>>>(maps, d_map, d_stamps, claims, s, counts,
+                                                                       lists[(s - 1) % 2], lists[s % 2], ok);
+        if (int err = launch_status("hole_frontier_step_kernel")) return err;
+    }
+    return SSG_OK;
+}
+
 struct MergeParams {
     int cols, rows, pano_cols, pano_rows, nref, image_rows, image_cols;
     float ratio_x, ratio_y;
@@ -332,6 +632,61 @@ __device__ __forceinline__ void interp_rgb(const uint8_t* __restrict__ img, floa
     for (int ch = 0; ch < 3; ++ch)
         out[ch] = fadd(fadd(fadd(fmul((float)p1[ch], w1), fmul((float)p2[ch], w2)), fmul((float)p3[ch], w3)),
                        fmul((float)p4[ch], w4));
+}
+
+// Bilinear sample of a float map and of uint8 RGB (interpF, interp: stitcher.cu:56-116) in
+// fused multiply-adds, for the batched 16-bit path's merge
+__device__ __forceinline__ float interp_f_fast(const float* __restrict__ s, float u, float v, int cols)
+{
+    const float u1f = floorf(u), v1f = floorf(v);
+    const int u1 = (int)u1f, v1 = (int)v1f;
+    const float fu = u - u1f, fv = v - v1f;
+    const float* r0 = s + (int64_t)v1 * cols + u1;
+    const float p1 = __ldg(r0), p3 = __ldg(r0 + 1), p2 = __ldg(r0 + cols), p4 = __ldg(r0 + cols + 1);
+    const float top = fmaf(fu, p3 - p1, p1), bot = fmaf(fu, p4 - p2, p2);
+    return fmaf(fv, bot - top, top);
+}
+
+__device__ __forceinline__ void interp_rgb_fast(const uint8_t* __restrict__ img, float u, float v, int cols,
+                                                float out[3])
+{
+    const float u1f = floorf(u), v1f = floorf(v);
+    const int u1 = (int)u1f, v1 = (int)v1f;
+    const float fu = u - u1f, fv = v - v1f;
+    const uint8_t* p1 = img + 3 * ((int64_t)v1 * cols + u1);
+    const uint8_t* p2 = p1 + 3 * (int64_t)cols;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const float a = p1[ch], b = p1[3 + ch], c = p2[ch], d = p2[3 + ch];
+        const float top = fmaf(fu, b - a, a), bot = fmaf(fu, d - c, c);
+        out[ch] = fmaf(fv, bot - top, top);
+    }
+}
+
+// Double-sphere unprojection / projection of the stitcher (stitcher.cu:121-168) with
+// approximate square roots and reciprocals
+__device__ __forceinline__ void unproject_fast(float u, float v, const Intr& k, float p[3])
+{
+    const float mx = (u - k.cx) / k.fx, my = (v - k.cy) / k.fy;
+    const float r2 = fmaf(my, my, mx * mx);
+    const float mz = (1.0f - k.alpha * k.alpha * r2) *
+                     rcp_approx(fmaf(k.alpha, sqrt_approx(1.0f - (2.0f * k.alpha - 1.0f) * r2), 1.0f - k.alpha));
+    const float mz2 = mz * mz;
+    const float s = fmaf(mz, k.xi, sqrt_approx(fmaf(1.0f - k.xi * k.xi, r2, mz2))) * rcp_approx(mz2 + r2);
+    p[0] = mx * s;
+    p[1] = my * s;
+    p[2] = fmaf(mz, s, -k.xi);
+}
+
+__device__ __forceinline__ void project_fast(const float p[3], const Intr& k, float uv[2])
+{
+    const float rxy = fmaf(p[1], p[1], p[0] * p[0]);
+    const float d1 = sqrt_approx(fmaf(p[2], p[2], rxy));
+    const float c = fmaf(k.xi, d1, p[2]);
+    const float d2 = sqrt_approx(fmaf(c, c, rxy));
+    const float den = rcp_approx(fmaf(k.alpha, d2, (1.0f - k.alpha) * c));
+    uv[0] = fmaf(k.fx * p[0], den, k.cx);
+    uv[1] = fmaf(k.fy * p[1], den, k.cy);
 }
 
 // mergeRGBDPanoramaKernel, stitcher.cu:423-473
@@ -389,20 +744,70 @@ __global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_consta
     for (int ch = 0; ch < 3; ++ch) rgb_pano[3 * i + ch] = (uint8_t)__float2uint_rz(fminf(rgb[ch], 255.0f));
 }
 
-// smallest float f with (double)f >= v, and largest float f with (double)f <= v
-static float float_at_least(double v)
+// The approximate merge for a batch of frames of one rig: the blending table, the weights and the
+// unprojected ray of each (panorama pixel, reference) are the same for every frame, so a thread
+// reads and unprojects them once and applies them to kMergeFrames frames (blockIdx.y: group of
+// frames), which also gives it that many independent gathers in flight.
+constexpr int kMergeFrames = 4;
+
+__global__ void __launch_bounds__(kStitchBlock) merge_frames_kernel(const __grid_constant__ MergeParams p,
+                                                                    int frames, const float2* __restrict__ lut,
+                                                                    const float* __restrict__ weights,
+                                                                    const float* __restrict__ reproj,
+                                                                    const float* __restrict__ dists,
+                                                                    const uint8_t* __restrict__ images,
+                                                                    float* __restrict__ dist_pano,
+                                                                    uint8_t* __restrict__ rgb_pano)
 {
-    float f = (float)v;
-    while ((double)f < v) f = std::nextafter(f, INFINITY);
-    while ((double)std::nextafter(f, -INFINITY) >= v) f = std::nextafter(f, -INFINITY);
-    return f;
-}
-static float float_at_most(double v)
-{
-    float f = (float)v;
-    while ((double)f > v) f = std::nextafter(f, -INFINITY);
-    while ((double)std::nextafter(f, INFINITY) <= v) f = std::nextafter(f, INFINITY);
-    return f;
+    const int64_t Q = (int64_t)p.pano_cols * p.pano_rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q) return;
+    const int f0 = blockIdx.y * kMergeFrames;
+    const int nf = min(kMergeFrames, frames - f0);
+    const int64_t map_frame = (int64_t)p.nref * p.cols * p.rows;
+    const int64_t image_frame = (int64_t)p.nref * p.image_cols * p.image_rows * 3;
+    reproj += f0 * map_frame;
+    dists += f0 * map_frame;
+    images += f0 * image_frame;
+    float inv[kMergeFrames], rgb[kMergeFrames][3];
+#pragma unroll
+    for (int f = 0; f < kMergeFrames; ++f) inv[f] = rgb[f][0] = rgb[f][1] = rgb[f][2] = 0.0f;
+    const float colsm = fsub((float)p.image_cols, 1.1f), rowsm = fsub((float)p.image_rows, 1.1f);
+    for (int r = 0; r < p.nref; ++r) {
+        const float w = weights[(int64_t)r * Q + i];
+        float2 uv = lut[(int64_t)r * Q + i];
+        uv.x = fminf(fmaxf(uv.x, 0.1f), fsub((float)p.cols, 1.1f));
+        uv.y = fminf(fmaxf(uv.y, 0.1f), fsub((float)p.rows, 1.1f));
+        const float vo = fadd(uv.y, (float)(r * p.rows));
+        float ray[3];
+        unproject_fast(uv.x, uv.y, p.k[r], ray);
+#pragma unroll
+        for (int f = 0; f < kMergeFrames; ++f) {
+            if (f < nf) {
+                const float rd = interp_f_fast(reproj + f * map_frame, uv.x, vo, p.cols);
+                inv[f] = fmaf(w, rcp_approx(rd), inv[f]);
+                const float dc = fminf(rd, interp_f_fast(dists + f * map_frame, uv.x, vo, p.cols));
+                float pt[3], o[2], c[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) pt[a] = fmaf(dc, ray[a], p.t[r][a]);
+                project_fast(pt, p.k[r], o);
+                o[0] = fminf(fmaxf(fmul(o[0], p.ratio_x), 0.1f), colsm);
+                o[1] = fadd(fminf(fmaxf(fmul(o[1], p.ratio_y), 0.1f), rowsm), (float)(r * p.image_rows));
+                interp_rgb_fast(images + f * image_frame, o[0], o[1], p.image_cols, c);
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) rgb[f][ch] = fmaf(c[ch], w, rgb[f][ch]);
+            }
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < kMergeFrames; ++f) {
+        if (f < nf) {
+            const int64_t o = (int64_t)(f0 + f) * Q + i;
+            dist_pano[o] = rcp_approx(inv[f]);
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) rgb_pano[3 * o + ch] = (uint8_t)__float2uint_rz(fminf(rgb[f][ch], 255.0f));
+        }
+    }
 }
 
 // The tile kernel needs more than 48 KB of dynamic shared memory: opt in once per device.
@@ -594,6 +999,115 @@ extern "C" int ssg_inpaint_batch(float* d_distance, const uint8_t* d_tables, flo
     return SSG_OK;
 }
 
+namespace ssg {
+
+// ---------------------------------------------------------------------------------------------
+// Stitch of an uneven batch: every job has its own rig, map and panorama sizes; its maps are
+// concatenated job by job (StitchJob::map_begin).
+// ---------------------------------------------------------------------------------------------
+struct JobMaps {
+    const StitchJob* jobs;
+    int n;
+    __device__ __forceinline__ MapPixel at(int64_t g) const
+    {
+        int lo = 0, hi = n - 1;  // the last job whose maps begin at or before g
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].map_begin <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        const StitchJob& J = jobs[lo];
+        const int64_t P = (int64_t)J.cols * J.rows, off = g - J.map_begin, slot = off / P, j = off - slot * P;
+        return MapPixel{J.cols, J.rows, (int)(j % J.cols), (int)(j / J.cols),
+                        reinterpret_cast<const uchar2*>(J.tables) + slot * P};
+    }
+};
+
+// blockIdx.y: job * max_references + reference slot
+__global__ void __launch_bounds__(kStitchBlock) reproject_uneven_kernel(const StitchJob* __restrict__ jobs,
+                                                                        int max_references)
+{
+    const StitchJob& J = jobs[blockIdx.y / max_references];
+    const int slot = blockIdx.y % max_references;
+    const int64_t P = (int64_t)J.cols * J.rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= J.references || i >= P) return;
+    reproject_pixel(J.k[slot], J.t[slot], J.distance + slot * P, J.reprojected + slot * P, J.cols, P, i);
+}
+
+// the approximate merge (merge_frames_kernel's arithmetic) of one job's panorama; blockIdx.y: job
+__global__ void __launch_bounds__(kStitchBlock) merge_uneven_kernel(const StitchJob* __restrict__ jobs)
+{
+    const StitchJob& J = jobs[blockIdx.y];
+    const int64_t Q = (int64_t)J.pano_cols * J.pano_rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q) return;
+    const int cols = J.cols, rows = J.rows;
+    float inv = 0.0f, rgb[3] = {0.0f, 0.0f, 0.0f};
+    const float colsm = fsub((float)J.image_cols, 1.1f), rowsm = fsub((float)J.image_rows, 1.1f);
+    for (int r = 0; r < J.references; ++r) {
+        const float w = J.weights[(int64_t)r * Q + i];
+        float2 uv = J.lut[(int64_t)r * Q + i];
+        uv.x = fminf(fmaxf(uv.x, 0.1f), fsub((float)cols, 1.1f));
+        uv.y = fminf(fmaxf(uv.y, 0.1f), fsub((float)rows, 1.1f));
+        const float vo = fadd(uv.y, (float)(r * rows));
+        float ray[3], pt[3], o[2], c[3];
+        unproject_fast(uv.x, uv.y, J.k[r], ray);
+        const float rd = interp_f_fast(J.reprojected, uv.x, vo, cols);
+        inv = fmaf(w, rcp_approx(rd), inv);
+        const float dc = fminf(rd, interp_f_fast(J.distance, uv.x, vo, cols));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pt[a] = fmaf(dc, ray[a], J.t[r][a]);
+        project_fast(pt, J.k[r], o);
+        o[0] = fminf(fmaxf(fmul(o[0], J.ratio_x), 0.1f), colsm);
+        o[1] = fadd(fminf(fmaxf(fmul(o[1], J.ratio_y), 0.1f), rowsm), (float)(r * J.image_rows));
+        interp_rgb_fast(J.images, o[0], o[1], J.image_cols, c);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) rgb[ch] = fmaf(c[ch], w, rgb[ch]);
+    }
+    J.pano_distance[i] = rcp_approx(inv);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) J.rgb[3 * i + ch] = (uint8_t)__float2uint_rz(fminf(rgb[ch], 255.0f));
+}
+
+int launch_stitch_uneven(const StitchJob* d_jobs, int jobs, float* d_maps, int64_t total_map_pixels,
+                         int max_map_pixels, int max_pano_pixels, int max_references, double max_dist,
+                         int iterations, uint8_t* d_stamps, int32_t* d_holes, cudaStream_t st)
+{
+    SSG_REQUIRE(iterations >= 0 && iterations <= kMaxListIterations, "iterations %d outside [0, %d]", iterations,
+                kMaxListIterations);
+    SSG_REQUIRE(total_map_pixels < ((int64_t)1 << 31), "too many map pixels");
+    fill_kernel<<<grid_1d(total_map_pixels, kStitchBlock), kStitchBlock, 0, st>>>(d_maps, total_map_pixels, 1e8f);
+    if (int e = launch_status("fill_kernel")) return e;
+    reproject_uneven_kernel<<<dim3(grid_1d(max_map_pixels, kStitchBlock), jobs * max_references), kStitchBlock, 0,
+                              st>>>(d_jobs, max_references);
+    if (int e = launch_status("reproject_uneven_kernel")) return e;
+    if (int e = inpaint_lists(JobMaps{d_jobs, jobs}, total_map_pixels, d_maps, d_stamps, d_holes, max_dist,
+                              iterations, st))
+        return e;
+    merge_uneven_kernel<<<dim3(grid_1d(max_pano_pixels, kStitchBlock), jobs), kStitchBlock, 0, st>>>(d_jobs);
+    return launch_status("merge_uneven_kernel");
+}
+
+}  // namespace ssg
+
+extern "C" int ssg_inpaint_holes_batch(float* d_distance, const uint8_t* d_tables, uint8_t* d_stamps,
+                                       int32_t* d_holes, int cols, int rows, int instances, int references,
+                                       double max_dist, int iterations, void* stream)
+{
+    SSG_REQUIRE(d_distance && d_tables && d_stamps && d_holes, "null pointer");
+    SSG_REQUIRE(cols > 0 && rows > 0, "invalid sizes");
+    SSG_REQUIRE(iterations >= 0 && iterations <= kMaxListIterations, "iterations %d outside [0, %d]", iterations,
+                kMaxListIterations);
+    SSG_REQUIRE(references >= 1 && instances >= 1 && instances <= 65535 && instances % references == 0,
+                "instances must be a positive multiple of references");
+    SSG_REQUIRE((int64_t)cols * rows * instances < ((int64_t)1 << 31), "%d maps of %dx%d pixels are too many",
+                instances, cols, rows);
+    const UniformMaps maps{cols, rows, references, reinterpret_cast<const uchar2*>(d_tables)};
+    return inpaint_lists(maps, (int64_t)cols * rows * instances, d_distance, d_stamps, d_holes, max_dist, iterations,
+                         as_stream(stream));
+}
+
 extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, const float* d_reprojected,
                                   const float* d_distances, const uint8_t* d_images, int image_rows, int image_cols,
                                   const float* translations, const ssg_intrinsics* intrinsics, int reference_count,
@@ -605,11 +1119,12 @@ extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, co
                                     d_distance_panorama, d_rgb_panorama, stream);
 }
 
-extern "C" int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
-                                        const float* d_distances, const uint8_t* d_images, int image_rows,
-                                        int image_cols, const float* translations, const ssg_intrinsics* intrinsics,
-                                        int reference_count, int cols, int rows, int pano_cols, int pano_rows,
-                                        int frames, float* d_distance_panorama, uint8_t* d_rgb_panorama, void* stream)
+template <bool kFast>
+static int merge_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                       const float* d_distances, const uint8_t* d_images, int image_rows, int image_cols,
+                       const float* translations, const ssg_intrinsics* intrinsics, int reference_count, int cols,
+                       int rows, int pano_cols, int pano_rows, int frames, float* d_distance_panorama,
+                       uint8_t* d_rgb_panorama, void* stream)
 {
     SSG_REQUIRE(frames >= 1 && frames <= 65535, "frames out of range");
     SSG_REQUIRE(d_lut && d_weights && d_reprojected && d_distances && d_images && translations &&
@@ -636,10 +1151,42 @@ extern "C" int ssg_merge_panorama_batch(const float* d_lut, const float* d_weigh
     }
     const int64_t Q = (int64_t)pano_cols * pano_rows;
     dim3 grid(grid_1d(Q, kStitchBlock), frames);
-    merge_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(
-        p, reinterpret_cast<const float2*>(d_lut), d_weights, d_reprojected, d_distances, d_images,
-        d_distance_panorama, d_rgb_panorama);
-    return launch_status("merge_kernel");
+    if constexpr (kFast) {
+        const dim3 fgrid(grid_1d(Q, kStitchBlock), (frames + kMergeFrames - 1) / kMergeFrames);
+        merge_frames_kernel<<<fgrid, kStitchBlock, 0, as_stream(stream)>>>(
+            p, frames, reinterpret_cast<const float2*>(d_lut), d_weights, d_reprojected, d_distances, d_images,
+            d_distance_panorama, d_rgb_panorama);
+        return launch_status("merge_frames_kernel");
+    } else {
+        merge_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(
+            p, reinterpret_cast<const float2*>(d_lut), d_weights, d_reprojected, d_distances, d_images,
+            d_distance_panorama, d_rgb_panorama);
+        return launch_status("merge_kernel");
+    }
+}
+
+extern "C" int ssg_merge_panorama_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
+                                        const float* d_distances, const uint8_t* d_images, int image_rows,
+                                        int image_cols, const float* translations, const ssg_intrinsics* intrinsics,
+                                        int reference_count, int cols, int rows, int pano_cols, int pano_rows,
+                                        int frames, float* d_distance_panorama, uint8_t* d_rgb_panorama, void* stream)
+{
+    return merge_batch<false>(d_lut, d_weights, d_reprojected, d_distances, d_images, image_rows, image_cols,
+                              translations, intrinsics, reference_count, cols, rows, pano_cols, pano_rows, frames,
+                              d_distance_panorama, d_rgb_panorama, stream);
+}
+
+extern "C" int ssg_merge_panorama_batch_approx(const float* d_lut, const float* d_weights,
+                                               const float* d_reprojected, const float* d_distances,
+                                               const uint8_t* d_images, int image_rows, int image_cols,
+                                               const float* translations, const ssg_intrinsics* intrinsics,
+                                               int reference_count, int cols, int rows, int pano_cols,
+                                               int pano_rows, int frames, float* d_distance_panorama,
+                                               uint8_t* d_rgb_panorama, void* stream)
+{
+    return merge_batch<true>(d_lut, d_weights, d_reprojected, d_distances, d_images, image_rows, image_cols,
+                             translations, intrinsics, reference_count, cols, rows, pano_cols, pano_rows, frames,
+                             d_distance_panorama, d_rgb_panorama, stream);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -12,21 +12,10 @@
 #include <cmath>
 
 #include "ssg_cells.cuh"
+#include "ssg_uneven.cuh"
 
 namespace ssg {
 
-__device__ __forceinline__ float sqrt_approx(float x)
-{
-    float r;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float rcp_approx(float x)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 
 // ---------------------------------------------------------------------------------------------
 // Image staging.  The sweep reads each bilinear sample as two 16-byte loads, one per image row:
@@ -101,9 +90,6 @@ __device__ __forceinline__ void unpack_entry(uint4 q, float lo[3], float hi[3])
 // ---------------------------------------------------------------------------------------------
 // Sweep + cost, batched, 16-bit output
 // ---------------------------------------------------------------------------------------------
-struct FastCam {
-    float fx, fy, cx, cy, xi, alpha, one_minus_alpha;
-};
 
 struct FastSweepParams {
     int cols, rows, cameras, references, ncand, chunks;
@@ -111,49 +97,129 @@ struct FastSweepParams {
     int ref_index[SSG_MAX_REFERENCES];
     FastCam cam[SSG_MAX_CAMERAS];
     float pose[SSG_MAX_REFERENCES][SSG_MAX_CAMERAS][12];  // reference -> camera, rows 0..2
-    float cand[SSG_MAX_CANDIDATES];  // padded to whole chunks with the last candidate
+    alignas(8) float cand[SSG_MAX_CANDIDATES];  // padded to whole chunks with the last candidate
 };
 
-// Double-sphere projection (utils.py:75-94) with approximate square roots and reciprocal: a
-// relative error of a few 1e-7 in the sample position, well below the 16-bit rounding of the
-// cost it feeds.
-__device__ __forceinline__ void fast_project(float x, float y, float z, const FastCam& k, float& u, float& v)
+// Double-sphere projection (utils.py:75-94) of two points with approximate square roots and
+// reciprocal: a relative error of a few 1e-7 in the sample position, well below the 16-bit
+// rounding of the cost it feeds.
+__device__ __forceinline__ void project_pair(float2 x, float2 y, float2 z, const FastCam& k, float2& u, float2& v)
 {
-    const float rxy = fmaf(y, y, x * x);
-    const float d1 = sqrt_approx(fmaf(z, z, rxy));
-    const float c = fmaf(k.xi, d1, z);
-    const float d2 = sqrt_approx(fmaf(c, c, rxy));
-    const float inv = rcp_approx(fmaf(k.alpha, d2, k.one_minus_alpha * c));
-    u = fmaf(k.fx * x, inv, k.cx);
-    v = fmaf(k.fy * y, inv, k.cy);
+    const float2 rxy = fma2(y, y, mul2(x, x));
+    const float2 s1 = fma2(z, z, rxy);
+    const float2 d1 = make_float2(sqrt_approx(s1.x), sqrt_approx(s1.y));
+    const float2 c = fma2(splat(k.xi), d1, z);
+    const float2 s2 = fma2(c, c, rxy);
+    const float2 d2 = make_float2(sqrt_approx(s2.x), sqrt_approx(s2.y));
+    const float2 n = fma2(splat(k.alpha), d2, mul2(splat(k.one_minus_alpha), c));
+    const float2 inv = make_float2(rcp_approx(n.x), rcp_approx(n.y));
+    u = fma2(mul2(splat(k.fx), x), inv, splat(k.cx));
+    v = fma2(mul2(splat(k.fy), y), inv, splat(k.cy));
 }
 
-// Bilinear sample with zero padding (torch grid_sample, align_corners=False, taps nw, ne, sw,
-// se) from a bordered plane of texel pairs; `img` points at the entry of texels (-1, 0), (0, 0),
-// `pitch` = cols + 2.
-__device__ __forceinline__ void fast_sample(const uint4* __restrict__ img, int pitch, int cols, int rows, float ix,
-                                            float iy, float& s0, float& s1, float& s2)
+// Bilinear samples with zero padding (torch grid_sample, align_corners=False, taps nw, ne, sw,
+// se) at two positions, from a bordered plane of texel pairs; `img` points at the entry of texels
+// (-1, 0), (0, 0), `pitch` = cols + 2.  The coordinates are clamped to [-1, cols] x [-1, rows]
+// (a NaN to -1): a sample whose four taps all lie outside the image then reads border zeros, or
+// has weight 0 on its in-image taps, so it is exactly 0 as grid_sample's, without a branch.  The
+// bottom tap row is clamped to the last border row for a sample at row `rows` (its weight is 0).
+__device__ __forceinline__ void sample_pair(const uint4* __restrict__ img, int pitch, float colsf, float rowsf,
+                                            int rows, float2 ix, float2 iy, float (&s)[2][3])
 {
-    const float x0 = floorf(ix), y0 = floorf(iy);
-    // saturating conversions (NaN converts to 0 and is rejected by the x0 == x0 tests)
-    const int xi = __float2int_rz(x0), yi = __float2int_rz(y0);
-    s0 = s1 = s2 = 0.0f;
-    // all four taps outside (or a NaN coordinate): zero.  -1 <= xi <= cols - 1 as one unsigned test
-    if (!((unsigned)xi + 1u <= (unsigned)cols && (unsigned)yi + 1u <= (unsigned)rows && x0 == x0 && y0 == y0)) return;
-    const uint4* t = img + yi * pitch + xi + 1;  // entry of texels (xi, yi), (xi + 1, yi)
-    float a[3], b[3], c[3], d[3];
-    unpack_entry(__ldg(t), a, b);
-    unpack_entry(__ldg(t + pitch), c, d);
-    const float fx = ix - x0, fy = iy - y0;
-    const float gx = 1.0f - fx, gy = 1.0f - fy;
-    const float wa = gx * gy, wb = fx * gy, wc = gx * fy, wd = fx * fy;
-    s0 = fmaf(d[0], wd, fmaf(c[0], wc, fmaf(b[0], wb, a[0] * wa)));
-    s1 = fmaf(d[1], wd, fmaf(c[1], wc, fmaf(b[1], wb, a[1] * wa)));
-    s2 = fmaf(d[2], wd, fmaf(c[2], wc, fmaf(b[2], wb, a[2] * wa)));
+    ix = make_float2(fminf(fmaxf(ix.x, -1.0f), colsf), fminf(fmaxf(ix.y, -1.0f), colsf));
+    iy = make_float2(fminf(fmaxf(iy.x, -1.0f), rowsf), fminf(fmaxf(iy.y, -1.0f), rowsf));
+    const float2 x0 = make_float2(floorf(ix.x), floorf(ix.y)), y0 = make_float2(floorf(iy.x), floorf(iy.y));
+    const float2 fx = add2(ix, make_float2(-x0.x, -x0.y)), fy = add2(iy, make_float2(-y0.x, -y0.y));
+    const float2 gx = add2(splat(1.0f), make_float2(-fx.x, -fx.y)), gy = add2(splat(1.0f), make_float2(-fy.x, -fy.y));
+    // weights of the taps of both samples: (nw, ne, sw, se)
+    const float2 wa = mul2(gx, gy), wb = mul2(fx, gy), wc = mul2(gx, fy), wd = mul2(fx, fy);
+    float t[2][4][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int xi = (int)(h ? x0.y : x0.x), yi = (int)(h ? y0.y : y0.x);
+        const uint4* top = img + yi * pitch + xi + 1;  // entry of texels (xi, yi), (xi + 1, yi)
+        const uint4* bot = img + min(yi + 1, rows) * pitch + xi + 1;
+        unpack_entry(__ldg(top), t[h][0], t[h][1]);
+        unpack_entry(__ldg(bot), t[h][2], t[h][3]);
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        float2 v = mul2(wa, make_float2(t[0][0][ch], t[1][0][ch]));
+        v = fma2(wb, make_float2(t[0][1][ch], t[1][1][ch]), v);
+        v = fma2(wc, make_float2(t[0][2][ch], t[1][2][ch]), v);
+        v = fma2(wd, make_float2(t[0][3][ch], t[1][3][ch]), v);
+        s[0][ch] = v.x;
+        s[1][ch] = v.y;
+    }
 }
+
+// Sweep + cost of one reference pixel (x, y) over all candidates, into its cells (`out`, chunk
+// stride `chunk_stride`).  `V` gives the instance's constants: ref_cam(), cam(c), pose(c) (12
+// floats), cand(k) (pairs are read as float2) and cameras(), chunks().  `frame_img` points at row
+// 0, entry 0 of the frame's camera 0 plane; planes are `plane` entries apart.
+template <typename T, typename V>
+__device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restrict__ frame_img, int plane,
+                                            int ref_camera, int cols, int rows, int x, int y, int sel,
+                                            T* __restrict__ out, int64_t chunk_stride)
+{
+    const int pitch = cols + 2;
+    float rp[3], unused[3];
+    unpack_entry(__ldg(frame_img + (int64_t)ref_camera * plane + y * pitch + x + 1), rp, unused);
+    const int chunks = view.chunks();
+    if (sel < 0 || sel >= view.cameras()) {
+        // no camera sees the point: grid_sample of an all-zero image (depth_estimation.py:166)
+        float c = fminf(fabsf(rp[0]) + fabsf(rp[1]) + fabsf(rp[2]), 500.0f);
+        float cc[8] = {c, c, c, c, c, c, c, c};
+        const uint4 v = Cell<T>::pack(cc);
+        for (int ch = 0; ch < chunks; ++ch) reinterpret_cast<uint4*>(out + ch * chunk_stride)[0] = v;
+        return;
+    }
+    float pu[3];
+    unproject_torch((float)x, (float)y, view.ref_cam(), pu);
+    float m[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) m[j] = view.pose(sel, j);
+    // p_cam = R (d u) + t = d (R u) + t
+    const float2 ax = splat(fmaf(m[2], pu[2], fmaf(m[1], pu[1], m[0] * pu[0])));
+    const float2 ay = splat(fmaf(m[6], pu[2], fmaf(m[5], pu[1], m[4] * pu[0])));
+    const float2 az = splat(fmaf(m[10], pu[2], fmaf(m[9], pu[1], m[8] * pu[0])));
+    const float2 tx = splat(m[3]), ty = splat(m[7]), tz = splat(m[11]);
+    const FastCam k = view.cam(sel);
+    const uint4* img = frame_img + (int64_t)sel * plane;
+    const float colsf = (float)cols, rowsf = (float)rows;
+    for (int ch = 0; ch < chunks; ++ch) {
+        uint32_t packed[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+            const float2 d = view.cand2(ch * 8 + j);
+            float2 u, v;
+            project_pair(fma2(d, ax, tx), fma2(d, ay, ty), fma2(d, az, tz), k, u, v);
+            float s[2][3];
+            sample_pair(img, pitch, colsf, rowsf, rows, u, v, s);
+            float c2[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                c2[h] = fminf(fabsf(s[h][0] - rp[0]) + fabsf(s[h][1] - rp[1]) + fabsf(s[h][2] - rp[2]), 500.0f);
+            packed[j / 2] = Cell<T>::pack2(c2[0], c2[1]);
+        }
+        reinterpret_cast<uint4*>(out + ch * chunk_stride)[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
+}
+
+// the constants of one reference slot of a uniform batch (kernel parameters)
+struct UniformView {
+    const FastSweepParams& p;
+    int slot;
+    __device__ __forceinline__ int chunks() const { return p.chunks; }
+    __device__ __forceinline__ int cameras() const { return p.cameras; }
+    __device__ __forceinline__ const TorchCam& ref_cam() const { return p.ref_cam[slot]; }
+    __device__ __forceinline__ float pose(int c, int j) const { return p.pose[slot][c][j]; }
+    __device__ __forceinline__ FastCam cam(int c) const { return p.cam[c]; }
+    __device__ __forceinline__ float2 cand2(int k) const { return *reinterpret_cast<const float2*>(&p.cand[k]); }
+};
 
 template <typename T>
-__global__ void __launch_bounds__(kBatchBlock) sweep_batch_kernel(const __grid_constant__ FastSweepParams p,
+__global__ void __launch_bounds__(kBatchBlock, 4) sweep_batch_kernel(const __grid_constant__ FastSweepParams p,
                                                                 const uint4* __restrict__ staged,
                                                                 const int8_t* __restrict__ selected,
                                                                 T* __restrict__ cost)
@@ -166,48 +232,71 @@ __global__ void __launch_bounds__(kBatchBlock) sweep_batch_kernel(const __grid_c
     const int frame = inst / p.references, slot = inst % p.references;
     const int plane = pitch * (rows + 2);
     const uint4* frame_img = staged + (int64_t)frame * p.cameras * plane + pitch;  // row 0, entry 0 of camera 0
-    const int x = i % cols, y = i / cols;
-    float rp[3], unused[3];
-    unpack_entry(__ldg(frame_img + (int64_t)p.ref_index[slot] * plane + y * pitch + x + 1), rp, unused);
     T* out = cost + (int64_t)inst * p.chunks * P * 8 + (int64_t)i * 8;
-    const int64_t chunk_stride = (int64_t)P * 8;
-    const int sel = selected[(int64_t)slot * P + i];
-    if (sel < 0 || sel >= p.cameras) {
-        // no camera sees the point: grid_sample of an all-zero image (depth_estimation.py:166)
-        float c = fminf(fabsf(rp[0]) + fabsf(rp[1]) + fabsf(rp[2]), 500.0f);
-        float cc[8] = {c, c, c, c, c, c, c, c};
-        const uint4 v = Cell<T>::pack(cc);
-        for (int ch = 0; ch < p.chunks; ++ch) reinterpret_cast<uint4*>(out + ch * chunk_stride)[0] = v;
-        return;
-    }
-    float pu[3];
-    unproject_torch((float)x, (float)y, p.ref_cam[slot], pu);
-    const float* m = p.pose[slot][sel];
-    // p_cam = R (d u) + t = d (R u) + t
-    const float ax = fmaf(m[2], pu[2], fmaf(m[1], pu[1], m[0] * pu[0]));
-    const float ay = fmaf(m[6], pu[2], fmaf(m[5], pu[1], m[4] * pu[0]));
-    const float az = fmaf(m[10], pu[2], fmaf(m[9], pu[1], m[8] * pu[0]));
-    const float tx = m[3], ty = m[7], tz = m[11];
-    const FastCam k = p.cam[sel];
-    const uint4* img = frame_img + (int64_t)sel * plane;
-    for (int ch = 0; ch < p.chunks; ++ch) {
-        uint32_t packed[4];
-#pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-            float c2[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int kk = ch * 8 + j + h;
-                const float d = p.cand[kk];
-                float u, v, s0, s1, s2;
-                fast_project(fmaf(d, ax, tx), fmaf(d, ay, ty), fmaf(d, az, tz), k, u, v);
-                fast_sample(img, pitch, cols, rows, u, v, s0, s1, s2);
-                c2[h] = fminf(fabsf(s0 - rp[0]) + fabsf(s1 - rp[1]) + fabsf(s2 - rp[2]), 500.0f);
+    sweep_pixel<T>(UniformView{p, slot}, frame_img, plane, p.ref_index[slot], cols, rows, i % cols, i / cols,
+                   selected[(int64_t)slot * P + i], out, (int64_t)P * 8);
+}
+
+// the constants of one instance of an uneven batch (device memory)
+struct InstView {
+    const SweepInst* I;
+    __device__ __forceinline__ int chunks() const { return I->chunks; }
+    __device__ __forceinline__ int cameras() const { return I->cameras; }
+    __device__ __forceinline__ const TorchCam& ref_cam() const { return I->ref_cam; }
+    __device__ __forceinline__ float pose(int c, int j) const { return __ldg(&I->pose[c][j]); }
+    __device__ __forceinline__ FastCam cam(int c) const { return I->cam[c]; }
+    __device__ __forceinline__ float2 cand2(int k) const { return __ldg(reinterpret_cast<const float2*>(&I->cand[k])); }
+};
+
+// Persistent sweep over an uneven batch: each block takes work items (kSweepTile reference pixels
+// of one instance) from a queue (*counter, zeroed before the launch) until the batch is done.
+template <typename T>
+__global__ void __launch_bounds__(kBatchBlock, 4) sweep_uneven_kernel(const SweepInst* __restrict__ insts,
+                                                                 int instances, int total_tiles,
+                                                                 int* __restrict__ counter)
+{
+    __shared__ int s_tile, s_inst;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int t = atomicAdd(counter, 1);
+            int lo = 0, hi = instances - 1;  // the last instance whose tiles begin at or before t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (insts[mid].tile_begin <= t) lo = mid;
+                else hi = mid - 1;
             }
-            packed[j / 2] = Cell<T>::pack2(c2[0], c2[1]);
+            s_tile = t;
+            s_inst = lo;
         }
-        reinterpret_cast<uint4*>(out + ch * chunk_stride)[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        __syncthreads();
+        const int t = s_tile, k = s_inst;
+        __syncthreads();  // s_tile and s_inst are rewritten by the next take
+        if (t >= total_tiles) return;
+        const SweepInst* I = insts + k;
+        const int cols = I->cols, rows = I->rows, P = cols * rows;
+        const int i = (t - I->tile_begin) * kSweepTile + threadIdx.x;
+        if (i < P) {
+            const int plane = (cols + 2) * (rows + 2);
+            T* out = static_cast<T*>(I->cost) + (int64_t)i * 8;
+            sweep_pixel<T>(InstView{I}, I->staged, plane, I->ref_camera, cols, rows, i % cols, i / cols,
+                           I->selected[i], out, (int64_t)P * 8);
+        }
     }
+}
+
+int launch_sweep_uneven(const SweepInst* d_insts, int instances, int total_tiles, int storage, int* d_counter,
+                        cudaStream_t st)
+{
+    const cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = sms * 4;  // resident blocks (4 per SM at the kernel's register bound)
+    if (storage == SSG_STORAGE_F16)
+        sweep_uneven_kernel<__half><<<grid, kBatchBlock, 0, st>>>(d_insts, instances, total_tiles, d_counter);
+    else
+        sweep_uneven_kernel<uint16_t><<<grid, kBatchBlock, 0, st>>>(d_insts, instances, total_tiles, d_counter);
+    return launch_status("sweep_uneven_kernel");
 }
 
 static int check_storage(int storage)

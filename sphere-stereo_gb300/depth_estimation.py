@@ -85,8 +85,12 @@ class RGBD_Estimator:
         self.sigma_i = sigma_i
         self.sigma_s = sigma_s
 
-        self.cost_filter = ISB_Filter(candidate_count, matching_resolution, device)
-        self.distance_filter = ISB_Filter(1, matching_resolution, device)
+        if cost_storage not in ("fp32", "fp16", "unorm16"):
+            raise ValueError("cost_storage must be 'fp32', 'fp16' or 'unorm16'")
+        # the fp32 path's filters (pyramids of candidate_count float32 planes) are allocated on
+        # first use: the 16-bit paths have their own buffers
+        self._cost_filter = None
+        self._distance_filter = None
         calibrations_for_stitch = [calibrations[r] for r in self.references_indices]
         masks_for_stitching = [masks[r] for r in self.references_indices]
         self.fishey_stitcher = Stitcher(calibrations_for_stitch, reprojection_viewpoint, masks_for_stitching, min_dist,
@@ -101,19 +105,29 @@ class RGBD_Estimator:
         cols, rows = self.matching_resolution
         self._shapes = level_shapes(self.matching_resolution)
         self._guide = torch.empty([rows, cols, 3], dtype=torch.uint8, device=device)
-        self._cost0 = self.cost_filter.costs[0]
-        self._guide0 = self.cost_filter.guides[0]
         # per reference: the distance map before the post-filter (depth_estimation.py:196-198)
         self.distance_raw_maps = torch.empty([len(self.references_indices), rows, cols], device=device)
         # per reference: the selected candidate index (torch.min's index, depth_estimation.py:180)
         self.index_maps = torch.empty([len(self.references_indices), rows, cols], dtype=torch.int32, device=device)
         self.select_camera(masks)
-        if cost_storage not in ("fp32", "fp16", "unorm16"):
-            raise ValueError("cost_storage must be 'fp32', 'fp16' or 'unorm16'")
         self.cost_storage = cost_storage
         self.max_batch = int(max_batch)
         self.cuda_graphs = bool(cuda_graphs)
         self._pipeline = None
+
+    @property
+    def cost_filter(self) -> ISB_Filter:
+        """The fp32 path's cost filter (python/depth_estimation.py:67)."""
+        if self._cost_filter is None:
+            self._cost_filter = ISB_Filter(self.candidate_count, self.matching_resolution, self.device)
+        return self._cost_filter
+
+    @property
+    def distance_filter(self) -> ISB_Filter:
+        """The fp32 path's distance post-filter (python/depth_estimation.py:68)."""
+        if self._distance_filter is None:
+            self._distance_filter = ISB_Filter(1, self.matching_resolution, self.device)
+        return self._distance_filter
 
     def set_rig_tables(self, selected_cameras=None, relative_poses=None):
         """Replace the per-rig tables computed at construction (no counterpart in the reference,
@@ -190,8 +204,8 @@ class RGBD_Estimator:
         n = self.candidate_count
         stream = N.stream_of(guide)
         cf = self.cost_filter
-        cost = self._cost0
-        guides = [self._guide0] + cf.guides[1:]
+        cost = cf.costs[0]
+        guides = cf.guides
         costs = [cost] + cf.costs[1:]
         N.call("ssg_sweep_cost", cols, rows, len(self.calibrations), self._cams, reference, self._poses[reference],
                N.pointers([im.data_ptr() for im in images]), self._selected[slot].data_ptr(), self._candidates, n,

@@ -11,10 +11,10 @@ One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_p
     ssg_isb_upsample_select_batch  last level + argmin / sub-candidate step             1
     ssg_isb_apply_batch            distance post-filter, fp32, N = 1                    2L - 2
     ssg_reproject_distance_batch   fill + z-buffer                                      2
-    ssg_inpaint_batch              hole filling, 32 Jacobi steps in 2 tiled passes      2
-    ssg_merge_panorama_batch       panoramas                                            1
+    ssg_inpaint_holes_batch        hole filling: a scan, then 32 steps on hole lists    33
+    ssg_merge_panorama_batch_approx panoramas                                           1
 
-so the launch count does not grow with F (about 40 at 1024^2).  Buffers are allocated once for
+so the launch count does not grow with F (about 70 at 1024^2).  Buffers are allocated once for
 the largest batch; outputs alias them, as the reference's outputs alias its stitcher buffers.
 """
 from __future__ import annotations
@@ -63,13 +63,16 @@ class BatchPipeline:
         # level 0 (the sweep's output) 16-bit, coarser levels float32
         self.costs = [torch.empty(F * R * self.chunks * r * c * 8, **(i16 if l == 0 else f32))
                       for l, (r, c) in enumerate(self.shapes)]
-        self.df_guides = [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes]
+        # the distance post-filter's guide pyramid; its level 0 is the unfiltered guide itself,
+        # which the batched cost filter leaves as it was
+        self.df_guides = [self.guides[0]] + [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes[1:]]
         self.df_costs = [torch.empty(F * R * r * c, **f32) for r, c in self.shapes[1:]]
         self.distance_raw = torch.empty(F * R * P, **f32)
         self.index = torch.empty(F * R * P, dtype=torch.int32, device=dev)
         self.distance = torch.empty(F, R, self.rows, self.cols, **f32)
         self.reprojected = torch.empty(F * R * P, **f32)
-        self.scratch = torch.empty(F * R * P, **f32)
+        self.stamps = torch.empty(F * R * P, **u8)
+        self.holes = torch.empty(3 * F * R * P + 4, dtype=torch.int32, device=dev)
         self.images_u8 = torch.empty(F, R, st.image_rows, st.image_cols, 3, **u8)
         self.rgb = torch.empty(F, st.pano_rows, st.pano_cols, 3, **u8)
         self.pano_distance = torch.empty(F, st.pano_rows, st.pano_cols, **f32)
@@ -117,7 +120,6 @@ class BatchPipeline:
         dist = self.distance.view(-1)[: inst * P]
         dist.copy_(self.distance_raw[: inst * P])
         if L >= 2:
-            self.df_guides[0][: inst * P * 3].copy_(self.guides[0][: inst * P * 3])
             N.call("ssg_isb_apply_batch", N.pointers([g.data_ptr() for g in self.df_guides]),
                    N.pointers([dist.data_ptr()] + [c.data_ptr() for c in self.df_costs]), L, rows, cols, 1, inst,
                    float(e.sigma_i) / 2, float(e.sigma_s) / 2, stream)
@@ -129,9 +131,9 @@ class BatchPipeline:
             images_u8[:frames].copy_(stitch[:frames])  # float -> uint8 truncation (depth_estimation.py:239)
         N.call("ssg_reproject_distance_batch", dist.data_ptr(), self.reprojected.data_ptr(), cols, rows, inst, self.R,
                st._intr, st._trans, 1, stream)
-        N.call("ssg_inpaint_batch", self.reprojected.data_ptr(), self.tables.data_ptr(), self.scratch.data_ptr(), cols,
-               rows, inst, self.R, st.max_dist, st.inpainting_iterations, stream)
-        N.call("ssg_merge_panorama_batch", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
+        N.call("ssg_inpaint_holes_batch", self.reprojected.data_ptr(), self.tables.data_ptr(), self.stamps.data_ptr(),
+               self.holes.data_ptr(), cols, rows, inst, self.R, st.max_dist, st.inpainting_iterations, stream)
+        N.call("ssg_merge_panorama_batch_approx", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
                self.reprojected.data_ptr(), dist.data_ptr(), images_u8.data_ptr(), st.image_rows, st.image_cols,
                st._trans, st._intr, self.R, cols, rows, st.pano_cols, st.pano_rows, frames,
                self.pano_distance.data_ptr(), self.rgb.data_ptr(), stream)
@@ -172,5 +174,6 @@ class BatchPipeline:
         L = self.L
         isb = (L - 1) + (L - 2) + 1 if L >= 2 else 1
         post = 2 * (L - 1) if L >= 2 else 0
-        inpaint = -(-self.st.inpainting_iterations // 16)
+        it = self.st.inpainting_iterations
+        inpaint = 0 if it == 0 else 1 + it
         return 2 + isb + post + 2 + inpaint + 1
