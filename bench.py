@@ -40,9 +40,9 @@ METRIC = "RGB-D panoramas/s @1024² match, 32 cand"
 UNIT = "panoramas/s"
 DATA = "synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast per frame (seed 2000+frame)"
 # DRAM bytes (read + write) of sweep_batch_kernel per (frame, reference) instance with fp16 storage,
-# measured by ncu on one launch of an 8-frame batch of this workload (571,416,576 B read +
-# 1,022,696,704 B written for 16 instances)
-SWEEP_DRAM_BYTES_PER_INSTANCE = (571416576 + 1022696704) // 16
+# measured by ncu on one launch of an 8-frame batch of this workload (579,591,936 B read +
+# 1,029,880,576 B written for 16 instances)
+SWEEP_DRAM_BYTES_PER_INSTANCE = (579591936 + 1029880576) // 16
 
 
 def _env_int(name, default):
@@ -186,7 +186,7 @@ def sweep_bytes_per_launch(cols: int, rows: int, cameras: int, candidates: int, 
     return texel * P + texel * P * (cameras - 1) + P + cost_bytes * candidates * P
 
 
-def _estimator(ss, calibration, device, storage, batch, graphs):
+def _estimator(ss, calibration, device, storage, batch, graphs, tuner=None):
     import torch
 
     W = WORKLOAD
@@ -198,7 +198,7 @@ def _estimator(ss, calibration, device, storage, batch, graphs):
     masks = [torch.ones(1, mh, mw, device=device) for _ in calibs]
     return ss.RGBD_Estimator(calibs, W["min_dist"], W["max_dist"], W["candidates"], W["refs"], vp, masks,
                              W["matching"], W["stitch"], W["panorama"], W["sigma_i"], W["sigma_s"], device,
-                             cost_storage=storage, max_batch=batch, cuda_graphs=graphs)
+                             cost_storage=storage, max_batch=batch, cuda_graphs=graphs, tuner=tuner)
 
 
 def run_ours(args, rank, world, device, rendered):
@@ -208,7 +208,9 @@ def run_ours(args, rank, world, device, rendered):
     native = ss._native
     calibration, frames = rendered
     B = args.batch
-    est = _estimator(ss, calibration, device, args.storage, B, True)
+    autotune = importlib.import_module(PACKAGE + ".autotune")
+    tuner = None if args.no_autotune else autotune.Tuner()
+    est = _estimator(ss, calibration, device, args.storage, B, True, tuner)
     pipe = est.pipeline()
     mw, mh = WORKLOAD["matching"]
 
@@ -341,6 +343,7 @@ def run_ours(args, rank, world, device, rendered):
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms,
                      "launches_timed": len(rec.events)},
         "e2e_u8": e2e_u8,
+        "tuned": pipe.tuned,
     }
 
 
@@ -391,6 +394,118 @@ def cpu_baseline(frames_calib, sample_frames: int):
                       f"{os.cpu_count()} threads), camera selection and stitcher tables excluded"}
 
 
+UNEVEN_METRIC = "RGB-D panoramas/s, uneven batch (matching {512,768,1024}^2, {32,64,96} candidates, 3-6 cameras)"
+
+
+def uneven_jobs(count: int, seed: int = 5000):
+    """The uneven workload: ``count`` jobs, each a rig of 3-6 double-sphere cameras on a ring of
+    radius 0.1-0.3 m (xi in [-0.3, 0], alpha in [0.5, 0.7]), matching resolution drawn from
+    {512^2, 768^2, 1024^2}, candidates from {32, 64, 96}, references cameras 0 and C // 2,
+    rgb_to_stitch = matching resolution, panorama 2W x H.  Seeded per job."""
+    syn = importlib.import_module(PACKAGE + ".synthetic")
+    jobs = []
+    for k in range(count):
+        rng = np.random.Generator(np.random.PCG64(seed + k))
+        width = int(rng.choice([512, 768, 1024]))
+        cands = int(rng.choice([32, 64, 96]))
+        cams = int(rng.integers(3, 7))
+        jobs.append(dict(width=width, candidates=cands, rig=syn.ring_rig(rng, width, cams), refs=[0, cams // 2]))
+    return jobs
+
+
+def uneven_images(jobs, seed: int = 5000):
+    """Images of the uneven workload: one seeded scene rendered once per resolution by a 6-camera
+    ring, shared by the jobs of that resolution (their own rigs set the work; the image content
+    only moves costs and holes around)."""
+    syn = importlib.import_module(PACKAGE + ".synthetic")
+    pool = {}
+    for width in sorted({j["width"] for j in jobs}):
+        rng = np.random.Generator(np.random.PCG64(seed + width))
+        cams = syn.ring_rig(rng, width, 6)
+        scene = syn.random_scene(rng)
+        pool[width] = [syn.render_fisheye(scene, c, width, width)[0] for c in cams]
+    return [(np.stack(pool[j["width"]][:len(j["rig"])]), np.stack([pool[j["width"]][r] for r in j["refs"]]))
+            for j in jobs]
+
+
+def run_uneven(args, device):
+    import torch
+
+    ss = importlib.import_module(PACKAGE)
+    syn = importlib.import_module(PACKAGE + ".synthetic")
+    uneven = importlib.import_module(PACKAGE + ".uneven")
+    autotune = importlib.import_module(PACKAGE + ".autotune")
+    jobs = uneven_jobs(args.jobs)
+    images = uneven_images(jobs)
+    estimators = []
+    for j in jobs:
+        w = j["width"]
+        calibs = ss.parse_json_calib(syn.basalt_calibration(j["rig"]), (w, w), device)
+        vp = torch.zeros(3, device=device)
+        for r in j["refs"]:
+            vp += calibs[r].rt[:3, 3] / len(j["refs"])
+        masks = [torch.ones(1, w, w, device=device) for _ in j["rig"]]
+        estimators.append(ss.RGBD_Estimator(calibs, 0.55, 100.0, j["candidates"], j["refs"], vp, masks, (w, w),
+                                            (w, w), (2 * w, w), 10.0, 25.0, device, cost_storage=args.storage))
+    tuner = autotune.Tuner() if not args.no_autotune else None
+    batch = uneven.UnevenBatch(estimators, storage=args.storage, cuda_graphs=True, input_dtype=torch.uint8,
+                               tuner=tuner)
+    for k, (m, st) in enumerate(images):
+        batch.match_inputs[k].copy_(torch.as_tensor(m))
+        batch.stitch_inputs[k].copy_(torch.as_tensor(st))
+    for _ in range(args.warmup):
+        batch.run()
+    torch.cuda.synchronize()
+    with ClockSampler(device.index) as clocks:
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(args.steps):
+            batch.run()
+        end.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / args.steps
+    # end to end: uint8 inputs from pinned host memory, panoramas back, every step
+    pinned = [(torch.as_tensor(m).pin_memory(), torch.as_tensor(st).pin_memory()) for m, st in images]
+    outs = batch.run()
+    host_out = [(torch.empty(r.shape, dtype=r.dtype).pin_memory(), torch.empty(d.shape).pin_memory()) for r, d in outs]
+    h2d = sum(a.numel() + b.numel() for a, b in pinned)
+    d2h = sum(a.numel() + 4 * b.numel() for a, b in host_out)
+
+    def e2e():
+        for k, (m, st) in enumerate(pinned):
+            batch.match_inputs[k].copy_(m, non_blocking=True)
+            batch.stitch_inputs[k].copy_(st, non_blocking=True)
+        for (r, d), (hr, hd) in zip(batch.run(), host_out):
+            hr.copy_(r, non_blocking=True)
+            hd.copy_(d, non_blocking=True)
+
+    e2e()
+    torch.cuda.synchronize()
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record()
+    for _ in range(args.steps):
+        e2e()
+    e2.record()
+    torch.cuda.synchronize()
+    e2e_ms = s2.elapsed_time(e2) / args.steps
+    mix = {}
+    for j in jobs:
+        key = f"{j['width']}^2/{j['candidates']}"
+        mix[key] = mix.get(key, 0) + 1
+    line = {"metric": UNEVEN_METRIC, "value": len(jobs) * 1000.0 / ms, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": f"{args.storage} storage, f32 arithmetic",
+            "data": "synthetic: seeded ring rigs per job; one seeded scene per resolution, 8-bit images",
+            "config": {"workload": f"{len(jobs)} jobs in one uneven batch, 2 references per rig, panorama 2W x H",
+                       "jobs_by_resolution_and_candidates": mix,
+                       "instances": batch.instance_count, "launches_per_step": batch.launches(),
+                       "mode": "persistent sweep over all instances, CUDA-graph replay", "tuned": batch.tuned},
+            "e2e": {"value": len(jobs) * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": batch.launches() * args.steps, "clocks": clocks.summary()}
+    print(json.dumps(line))
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -422,6 +537,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-u8", action="store_true", help="skip the uint8-input end-to-end leg")
     ap.add_argument("--plain-frames", type=int, default=32, help="frames timed on the plain fp32 path (0 = skip)")
+    ap.add_argument("--workload", choices=["prototype", "uneven"], default="prototype",
+                    help="prototype: the headline 1024^2 / 32-candidate workload; uneven: a mixed batch of jobs")
+    ap.add_argument("--jobs", type=int, default=128, help="jobs of the uneven workload")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
     args = ap.parse_args()
 
     world = _env_int("WORLD_SIZE", 1)
@@ -453,6 +572,11 @@ def main():
         dist.init_process_group("nccl")
     device = torch.device("cuda", local_rank)
     torch.cuda.set_device(device)
+    if args.workload == "uneven":
+        if world > 1:
+            raise SystemExit("the uneven workload runs on one GPU")
+        run_uneven(args, device)
+        return
     rendered = render_pool(args.unique_frames, rank, world)
     ours = run_ours(args, rank, world, device, rendered)
     if rank != 0:
@@ -470,6 +594,7 @@ def main():
             "vs_baseline": None, "dtype": f"{args.storage} storage, f32 arithmetic", "data": DATA,
             "config": {"workload": WORKLOAD_NAME, "batch_frames": args.batch,
                        "mode": f"batched, {args.storage} cost volume, fp32 arithmetic, CUDA-graph replay",
+                       "tuned": ours["tuned"],
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"each step reads a {args.batch}-frame batch of inputs ({args.batch} x 83 MB), "
                              "alternating between two batches; both far exceed the 126 MB L2"},

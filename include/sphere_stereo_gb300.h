@@ -68,6 +68,21 @@ typedef struct {
     float fx, fy, cx, cy, xi, alpha;
 } ssg_intrinsics;
 
+/* Launch-shape knobs of the batched kernels (no counterpart in the reference), picked per
+ * workload by the Python autotuner (sphere-stereo_gb300/autotune.py).  Process-wide; read when a
+ * launch is enqueued, so a captured CUDA graph keeps the values it was captured with. */
+#define SSG_TUNE_SWEEP_VARIANT 0      /* sweep block shape: 0 = 256 threads x 4 blocks/SM (64 registers),
+                                         1 = 256 x 3 (80 registers), 2 = 128 x 8 (64 registers) */
+#define SSG_TUNE_HOLE_BLOCKS_PER_SM 1 /* blocks per SM of the hole-filling steps: 2, 4, 8 */
+#define SSG_TUNE_MERGE_FRAMES 2       /* frames one thread of the batched merge handles: 2, 4, 8 */
+#define SSG_TUNE_UNEVEN_SPAN 3        /* 256-pixel tiles per work item of the uneven sweep: 1, 2, 4 */
+#define SSG_TUNE_ISB_UP_BLOCKS 4      /* blocks per SM the chunked ISB upsampling is register-bounded for: 2, 3 */
+SSG_API int ssg_tuning_set(int knob, int value);
+/* The knob's current value (-1 for an unknown knob). */
+SSG_API int ssg_tuning_get(int knob);
+/* Writes up to `capacity` allowed values of a knob; returns how many it has (0 if unknown). */
+SSG_API int ssg_tuning_choices(int knob, int32_t* values, int capacity);
+
 /* Message of the calling thread's last failed call ("" if none). */
 SSG_API const char* ssg_last_error(void);
 /* Library version, major * 10000 + minor * 100 + patch. */
@@ -222,7 +237,10 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
  *
  * Cost volumes of the batched path are stored in chunks of 8 candidates, per instance and level
  * [ceil(N / 8)][pixels][8]: the level-0 volume with 16 bits per candidate (SSG_STORAGE_F16 /
- * SSG_STORAGE_UNORM16), the coarser levels as float32; all arithmetic is fp32.
+ * SSG_STORAGE_UNORM16), the coarser levels as float32; all arithmetic is fp32.  Guides of the
+ * batched path are one 32-bit word per pixel, bytes (Y, Cb, Cr, 0) (the reference's 3-byte
+ * pixels padded: one load per pixel, the colour distance in one byte-wise absolute-difference
+ * sum), rows x cols words per instance and level.
  * ------------------------------------------------------------------------------------------- */
 
 /* Image staging + guides: d_images frames x cameras x rows x cols x 3, float32 (the inputs of
@@ -230,9 +248,9 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
  * inputs are made from, python/utils.py:157-205) -> d_staged frames x cameras x (rows + 2) x
  * (cols + 2) 16-byte entries, entry (y + 1, x) holding texels x - 1 and x of row y as fp16 RGB
  * (exact for 8-bit values; other floats are rounded to fp16), with a border that the caller
- * zeroes once and that is never written; and d_guides frames x references x rows x cols x 3
- * uint8 (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from the
- * float values). */
+ * zeroes once and that is never written; and d_guides frames x references x rows x cols 32-bit
+ * guide words (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from
+ * the float values). */
 SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                              const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
                              void* stream);
@@ -274,7 +292,7 @@ SSG_API int ssg_select_distance_batch(const void* d_cost, int candidate_count, i
                                       void* stream);
 
 /* ISB_Filter.apply (python/isb_filter.py:72-136) on `instances` contiguous float32 pyramids:
- * level l holds instances x (guide ceil(rows/2^l) x ceil(cols/2^l) x 3) and instances x
+ * level l holds instances x ceil(rows/2^l) x ceil(cols/2^l) 32-bit guide words and instances x
  * (candidate_count x ... ) costs. */
 SSG_API int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
                                 int candidate_count, int instances, double sigma_i, double sigma_s, void* stream);

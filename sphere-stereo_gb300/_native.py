@@ -23,6 +23,11 @@ MAX_CAMERAS = 16
 MAX_CANDIDATES = 256
 MAX_REFERENCES = 16
 MAX_LEVELS = 24
+TUNE_SWEEP_VARIANT = 0
+TUNE_HOLE_BLOCKS_PER_SM = 1
+TUNE_MERGE_FRAMES = 2
+TUNE_UNEVEN_SPAN = 3
+TUNE_ISB_UP_BLOCKS = 4
 
 
 class NativeLibraryError(RuntimeError):
@@ -108,6 +113,9 @@ SIGNATURES = {
     "ssg_isb_downsample_transpose": (_I, [_P, _I, _I, _I, _I, _I, _F, _P, _P, _P]),
     "ssg_sweep_cost_backward": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "ssg_tuning_set": (_I, [_I, _I]),
+    "ssg_tuning_get": (_I, [_I]),
+    "ssg_tuning_choices": (_I, [_I, _P, _I]),
     "ssg_uneven_create": (_I, [_P, _I, _P, _I, _I, _D, _I, _P, _P, _P]),
     "ssg_uneven_upload": (_I, [_P, _P, _P, _P]),
     "ssg_uneven_run": (_I, [_P, _P]),
@@ -210,7 +218,8 @@ def pointers(values) -> ctypes.Array:
 
 def kernels_launched(name: str, args) -> int:
     """Number of kernels one call of entry point ``name`` with ``args`` launches."""
-    if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count"):
+    if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count", "ssg_tuning_set",
+                "ssg_tuning_get", "ssg_tuning_choices"):
         return 0
     if name in ("ssg_isb_apply", "ssg_isb_apply_batch"):
         return 2 * max(0, int(args[2]) - 1)

@@ -1,5 +1,6 @@
 // Library-wide plumbing of the C ABI: per-thread error messages, version, limits, and the
 // host-side derivation of the torch-form camera constants.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -51,9 +52,62 @@ TorchCam make_torch_cam(const ssg_camera& c)
     return k;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Launch-shape knobs (chosen by the Python autotuner): process-wide, read when a launch is
+// enqueued, so a CUDA graph keeps the values it was captured with.
+// ---------------------------------------------------------------------------------------------
+namespace {
+struct Knob {
+    const int* values;
+    int count;
+    std::atomic<int> value;
+};
+constexpr int kSweepVariants[] = {0, 1, 2};
+constexpr int kHoleBlocks[] = {2, 4, 8};
+constexpr int kMergeFramesValues[] = {2, 4, 8};
+constexpr int kUnevenSpans[] = {1, 2, 4};
+constexpr int kIsbUpBlocks[] = {2, 3};
+Knob g_knobs[] = {
+    {kSweepVariants, 3, {0}},      // SSG_TUNE_SWEEP_VARIANT
+    {kHoleBlocks, 3, {4}},         // SSG_TUNE_HOLE_BLOCKS_PER_SM
+    {kMergeFramesValues, 3, {4}},  // SSG_TUNE_MERGE_FRAMES
+    {kUnevenSpans, 3, {1}},        // SSG_TUNE_UNEVEN_SPAN
+    {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_UP_BLOCKS
+};
+constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
+}  // namespace
+
+int tuning(int knob) { return g_knobs[knob].value.load(std::memory_order_relaxed); }
+
 }  // namespace ssg
 
 extern "C" {
+
+int ssg_tuning_set(int knob, int value)
+{
+    SSG_REQUIRE(knob >= 0 && knob < ssg::kKnobCount, "unknown tuning knob %d", knob);
+    ssg::Knob& k = ssg::g_knobs[knob];
+    for (int i = 0; i < k.count; ++i)
+        if (k.values[i] == value) {
+            k.value.store(value);
+            return SSG_OK;
+        }
+    return ssg::fail(SSG_ERR_INVALID_ARGUMENT, "value %d is not a choice of tuning knob %d", value, knob);
+}
+
+int ssg_tuning_get(int knob)
+{
+    if (knob < 0 || knob >= ssg::kKnobCount) return -1;
+    return ssg::tuning(knob);
+}
+
+int ssg_tuning_choices(int knob, int32_t* values, int capacity)
+{
+    if (knob < 0 || knob >= ssg::kKnobCount) return 0;
+    const ssg::Knob& k = ssg::g_knobs[knob];
+    for (int i = 0; i < k.count && i < capacity && values; ++i) values[i] = k.values[i];
+    return k.count;
+}
 
 const char* ssg_last_error(void) { return ssg::g_error; }
 

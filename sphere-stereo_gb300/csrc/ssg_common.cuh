@@ -25,6 +25,8 @@ void clear_error();
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+int tuning(int knob);  // current value of an SSG_TUNE_* knob (ssg_api.cu)
+
 // ---------------------------------------------------------------------------------------------
 // IEEE round-to-nearest arithmetic that the compiler never contracts into FMAs.  The exact
 // (fp32) kernels use these so that every operation is the one the reference performs, in the

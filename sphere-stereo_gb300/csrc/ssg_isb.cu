@@ -33,15 +33,15 @@ namespace ssg {
 // float32 out.
 // One coarse pixel o of a level: pointers are the instance's own; `lut` is the block's filled
 // range table.
-template <int W, typename Tin>
+template <int W, typename Tin, typename GL>
 __device__ __forceinline__ void isb_down_pixel(const uint8_t* __restrict__ guide_in, const Tin* __restrict__ cost_in,
                                                uint8_t* __restrict__ guide_out, float* __restrict__ cost_out,
                                                const LevelGeom& g, int chunks, int64_t o, const float* lut)
 {
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
     DownTapsT<int> t;
-    down_weights(guide_in, g.rows_in, g.cols_in, (int)(o % g.cols_out), (int)(o / g.cols_out), LutRange{lut},
-                 guide_out + 3 * o, t);
+    down_weights<int, LutRange, GL>(guide_in, g.rows_in, g.cols_in, (int)(o % g.cols_out), (int)(o / g.cols_out),
+                                    LutRange{lut}, guide_out, o, t);
     // the chunked (16-bit) path sums with fused multiply-adds and scales by the reciprocal; the
     // planar path keeps the reference's separate products and its division
     constexpr bool kFast = W == 8;
@@ -64,8 +64,8 @@ __device__ __forceinline__ void isb_down_pixel(const uint8_t* __restrict__ guide
 }
 
 // Downsampling, one thread per coarse pixel; level 0 (any storage) or a float32 level in,
-// float32 out.  blockIdx.y: instance of contiguous levels.
-template <int W, typename Tin>
+// float32 out.  blockIdx.y: instance of contiguous levels; GL: the guides' layout.
+template <int W, typename Tin, typename GL>
 __global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __restrict__ guide_in,
                                                                    const Tin* __restrict__ cost_in,
                                                                    uint8_t* __restrict__ guide_out,
@@ -79,9 +79,9 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pout) return;
     const int inst = blockIdx.y;
-    isb_down_pixel<W, Tin>(guide_in + (int64_t)inst * pin * 3, cost_in + (int64_t)inst * chunks * pin * W,
-                           guide_out + (int64_t)inst * pout * 3, cost_out + (int64_t)inst * chunks * pout * W, g,
-                           chunks, o, lut);
+    isb_down_pixel<W, Tin, GL>(guide_in + (int64_t)inst * pin * GL::bytes, cost_in + (int64_t)inst * chunks * pin * W,
+                               guide_out + (int64_t)inst * pout * GL::bytes, cost_out + (int64_t)inst * chunks * pout * W,
+                               g, chunks, o, lut);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -206,13 +206,13 @@ __device__ __forceinline__ constexpr bool uses_tap(int t)
     return false;
 }
 
-template <int F>
-__device__ __forceinline__ float fine_weights_padded(const int (&gd)[9][3], const int up[3], float weight_up,
-                                                     float weight_down, const LutRange& range, float (&w)[9],
-                                                     float g[3])
+template <int F, typename GL>
+__device__ __forceinline__ float fine_weights_padded(const typename GL::Pix (&gd)[9], const typename GL::Pix& up,
+                                                     float weight_up, float weight_down, const LutRange& range,
+                                                     float (&w)[9], float g[3])
 {
     float wf[UpTaps<F>::n];
-    const float inv = fine_weights<F>(gd, up, weight_up, weight_down, range, wf, g);
+    const float inv = fine_weights<F, LutRange, GL>(gd, up, weight_up, weight_down, range, wf, g);
 #pragma unroll
     for (int i = 0; i < 9; ++i) w[i] = i < UpTaps<F>::n ? wf[i < UpTaps<F>::n ? i : 0] : 0.0f;
     return inv;
@@ -245,8 +245,8 @@ struct FinePixel {
     bool active;
 };
 
-template <int F, bool kWriteGuide>
-__device__ __forceinline__ void fine_setup(const int (&gd)[9][3], const uint8_t* __restrict__ guide_io,
+template <int F, bool kWriteGuide, typename GL>
+__device__ __forceinline__ void fine_setup(const typename GL::Pix (&gd)[9], const uint8_t* __restrict__ guide_io,
                                            const LevelGeom& g, int x, int y, bool coarse_ok, float weight_up,
                                            float weight_down, const LutRange& range, FinePixel& px)
 {
@@ -256,14 +256,15 @@ __device__ __forceinline__ void fine_setup(const int (&gd)[9][3], const uint8_t*
     px.index = fy * g.cols_out + fx;
     px.inv = 0.0f;
     if (!px.active) return;
-    int up[3];
     float gsum[3];
-    load_guide(guide_io, px.index, up);
-    px.inv = fine_weights_padded<F>(gd, up, weight_up, weight_down, range, px.w, gsum);
-    if (kWriteGuide)
+    const typename GL::Pix up = GL::load(guide_io, px.index);
+    px.inv = fine_weights_padded<F, GL>(gd, up, weight_up, weight_down, range, px.w, gsum);
+    if (kWriteGuide) {
+        uint32_t v[3];
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch)
-            const_cast<uint8_t*>(guide_io)[3 * px.index + ch] = (uint8_t)__float2uint_rz(fmul(gsum[ch], px.inv));
+        for (int ch = 0; ch < 3; ++ch) v[ch] = __float2uint_rz(fmul(gsum[ch], px.inv));
+        GL::store(const_cast<uint8_t*>(guide_io), px.index, v);
+    }
 }
 
 // filter one part of fine pixel F and select or store it
@@ -335,7 +336,7 @@ struct UpShared {
 // sh.lut is filled with the level's range weights and the block synchronised before the call.
 // kSelect = false: coarse float32 -> fine float32 in place (and the fine guides);
 // kSelect = true: the last step, fine level-0 costs of type Tf in, the selection out.
-template <int W, typename Tf, bool kSelect>
+template <int W, typename Tf, bool kSelect, typename GL>
 __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
                                              uint8_t* __restrict__ guide_io, Tf* __restrict__ cost_fine,
                                              const LevelGeom& g, int chunks, int ncand, float weight_up,
@@ -353,14 +354,14 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     FinePixel pa, pb;
     {
         int ci[9];
-        int gd[9][3];
-        if (coarse_ok) coarse_neighbourhood(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+        typename GL::Pix gd[9];
+        if (coarse_ok) coarse_neighbourhood<int, GL>(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
         if (kind == 0) {
-            fine_setup<0, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
-            fine_setup<3, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
+            fine_setup<0, kWriteGuide, GL>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<3, kWriteGuide, GL>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
         } else {
-            fine_setup<1, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
-            fine_setup<2, kWriteGuide>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
+            fine_setup<1, kWriteGuide, GL>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<2, kWriteGuide, GL>(gd, guide_io, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
         }
     }
     Selector sa, sb;
@@ -408,10 +409,11 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     }
 }
 
-// blockIdx.z: instance of contiguous levels.  (3 blocks per SM for the single-candidate filter,
-// 2 for the chunked volumes, whose taps need the registers.)
-template <int W, typename Tf, bool kSelect>
-__global__ void __launch_bounds__(kBatchBlock, W == 1 ? 3 : 2) isb_up_kernel(const uint8_t* __restrict__ guide_in,
+// blockIdx.z: instance of contiguous levels.  kBlocks: blocks per SM the registers are bounded
+// for (3 for the single-candidate filter; 2 or 3 for the chunked volumes, SSG_TUNE_ISB_UP_BLOCKS:
+// 3 spills a few of the taps' registers for more resident warps).
+template <int W, typename Tf, bool kSelect, typename GL, int kBlocks = (W == 1 ? 3 : 2)>
+__global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint8_t* __restrict__ guide_in,
                                                             const float* __restrict__ cost_in,
                                                             uint8_t* __restrict__ guide_io,
                                                             Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
@@ -428,9 +430,11 @@ __global__ void __launch_bounds__(kBatchBlock, W == 1 ? 3 : 2) isb_up_kernel(con
         if (so.distance2) so.distance2 += (int64_t)inst * pio;
         if (so.index) so.index += (int64_t)inst * pio;
     }
-    isb_up_block<W, Tf, kSelect>(guide_in + (int64_t)inst * pin * 3, cost_in + (int64_t)inst * chunks * pin * W,
-                                 guide_io + (int64_t)inst * pio * 3, cost_fine + (int64_t)inst * chunks * pio * W, g,
-                                 chunks, ncand, weight_up, weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh);
+    isb_up_block<W, Tf, kSelect, GL>(guide_in + (int64_t)inst * pin * GL::bytes,
+                                     cost_in + (int64_t)inst * chunks * pin * W,
+                                     guide_io + (int64_t)inst * pio * GL::bytes,
+                                     cost_fine + (int64_t)inst * chunks * pio * W, g, chunks, ncand, weight_up,
+                                     weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh);
 }
 
 // Selection from an unfiltered level-0 volume (pyramids of fewer than two levels, or the
@@ -474,12 +478,12 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_uneven_kernel(const Leve
     __syncthreads();
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pout) return;
-    isb_down_pixel<W, Tin>(d.guide_in, static_cast<const Tin*>(d.cost_in), d.guide_out, static_cast<float*>(d.cost_out),
-                           g, d.chunks, o, lut);
+    isb_down_pixel<W, Tin, G4>(d.guide_in, static_cast<const Tin*>(d.cost_in), d.guide_out,
+                               static_cast<float*>(d.cost_out), g, d.chunks, o, lut);
 }
 
-template <int W, typename Tf, bool kSelect>
-__global__ void __launch_bounds__(kBatchBlock, W == 1 ? 3 : 2) isb_up_uneven_kernel(const LevelDesc* __restrict__ descs)
+template <int W, typename Tf, bool kSelect, int kBlocks = (W == 1 ? 3 : 2)>
+__global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_uneven_kernel(const LevelDesc* __restrict__ descs)
 {
     const LevelDesc& d = descs[blockIdx.z];
     const LevelGeom g = d.g;
@@ -488,9 +492,9 @@ __global__ void __launch_bounds__(kBatchBlock, W == 1 ? 3 : 2) isb_up_uneven_ker
     __shared__ UpShared<W> sh;
     fill_range_lut(sh.lut, d.var_inv_i);
     __syncthreads();
-    isb_up_block<W, Tf, kSelect>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
-                                 static_cast<Tf*>(d.cost_out), g, d.chunks, d.ncand, d.weight_up, d.weight_down, d.so,
-                                 x0, y, sh);
+    isb_up_block<W, Tf, kSelect, G4>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
+                                     static_cast<Tf*>(d.cost_out), g, d.chunks, d.ncand, d.weight_up, d.weight_down,
+                                     d.so, x0, y, sh);
 }
 
 int launch_down_uneven(const LevelDesc* d_descs, int count, int max_rows_out, int max_cols_out, int width,
@@ -514,14 +518,18 @@ int launch_up_uneven(const LevelDesc* d_descs, int count, int max_rows_in, int m
 {
     SSG_REQUIRE(count >= 1 && count <= 65535 && max_rows_in <= 65535, "sizes out of range");
     const dim3 grid((unsigned)((max_cols_in + kUpTileX - 1) / kUpTileX), (unsigned)max_rows_in, (unsigned)count);
+    const bool three = tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3;
     if (width == 1)
         isb_up_uneven_kernel<1, float, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
     else if (!select)
-        isb_up_uneven_kernel<8, float, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
+        three ? isb_up_uneven_kernel<8, float, false, 3><<<grid, kBatchBlock, 0, st>>>(d_descs)
+              : isb_up_uneven_kernel<8, float, false, 2><<<grid, kBatchBlock, 0, st>>>(d_descs);
     else if (storage_fine == SSG_STORAGE_F16)
-        isb_up_uneven_kernel<8, __half, true><<<grid, kBatchBlock, 0, st>>>(d_descs);
+        three ? isb_up_uneven_kernel<8, __half, true, 3><<<grid, kBatchBlock, 0, st>>>(d_descs)
+              : isb_up_uneven_kernel<8, __half, true, 2><<<grid, kBatchBlock, 0, st>>>(d_descs);
     else
-        isb_up_uneven_kernel<8, uint16_t, true><<<grid, kBatchBlock, 0, st>>>(d_descs);
+        three ? isb_up_uneven_kernel<8, uint16_t, true, 3><<<grid, kBatchBlock, 0, st>>>(d_descs)
+              : isb_up_uneven_kernel<8, uint16_t, true, 2><<<grid, kBatchBlock, 0, st>>>(d_descs);
     return launch_status("isb_up_uneven_kernel");
 }
 
@@ -569,28 +577,33 @@ static int check_levels(int rows_in, int cols_in, int rows_out, int cols_out)
 }
 
 // --- launches shared by both layouts ---------------------------------------------------------
-template <int W, typename Tin>
+template <int W, typename Tin, typename GL>
 static int launch_down(const uint8_t* gi, const Tin* ci, int ri, int cl_i, uint8_t* go, float* co, int ro, int cl_o,
                        int chunks, int instances, float var_inv_i, cudaStream_t st)
 {
     const LevelGeom g{ri, cl_i, ro, cl_o};
     const dim3 grid(grid_1d((int64_t)ro * cl_o, kBatchBlock), instances);
-    isb_down_kernel<W, Tin><<<grid, kBatchBlock, 0, st>>>(gi, ci, go, co, g, chunks, var_inv_i);
+    isb_down_kernel<W, Tin, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, go, co, g, chunks, var_inv_i);
     return launch_status("isb_down_kernel");
 }
 
-template <int W, typename Tf, bool kSelect>
+template <int W, typename Tf, bool kSelect, typename GL>
 static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t* gio, Tf* cf, int rf, int cf_cols,
                      int chunks, int ncand, int instances, float wu, float wd, float var_inv_i, const SelectOut& so,
                      cudaStream_t st)
 {
     const LevelGeom g{rc, cc, rf, cf_cols};
-    isb_up_kernel<W, Tf, kSelect><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks,
-                                                                                      ncand, wu, wd, var_inv_i, so);
+    if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
+        isb_up_kernel<W, Tf, kSelect, GL, 3><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
+            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, so);
+    else
+        isb_up_kernel<W, Tf, kSelect, GL><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
+            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, so);
     return launch_status(kSelect ? "isb_up_kernel<select>" : "isb_up_kernel");
 }
 
 // the whole filter on planar levels (W = 1, chunks = candidates): python/isb_filter.py:72-136
+template <typename GL>
 static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
                         int candidate_count, int instances, double sigma_i, double sigma_s, cudaStream_t st)
 {
@@ -599,16 +612,16 @@ static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int lev
         const int ri = level_rows(rows, s - 1), ci = level_rows(cols, s - 1), ro = level_rows(rows, s),
                   co = level_rows(cols, s);
         if (int e = check_levels(ri, ci, ro, co)) return e;
-        if (int e = launch_down<1, float>(d_guides[s - 1], d_costs[s - 1], ri, ci, d_guides[s], d_costs[s], ro, co,
-                                          candidate_count, instances, c.var_inv_i, st))
+        if (int e = launch_down<1, float, GL>(d_guides[s - 1], d_costs[s - 1], ri, ci, d_guides[s], d_costs[s], ro,
+                                              co, candidate_count, instances, c.var_inv_i, st))
             return e;
     }
     for (int s = level_count - 2; s >= 0; --s) {
         const int rc = level_rows(rows, s + 1), cc = level_rows(cols, s + 1), rf = level_rows(rows, s),
                   cf = level_rows(cols, s);
-        if (int e = launch_up<1, float, false>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s], rf, cf,
-                                               candidate_count, candidate_count, instances, c.weight_up[s],
-                                               c.weight_down[s], c.var_inv_i, SelectOut{}, st))
+        if (int e = launch_up<1, float, false, GL>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s],
+                                                   rf, cf, candidate_count, candidate_count, instances,
+                                                   c.weight_up[s], c.weight_down[s], c.var_inv_i, SelectOut{}, st))
             return e;
     }
     return SSG_OK;
@@ -648,7 +661,7 @@ extern "C" int ssg_isb_downsample(const uint8_t* d_guide_in, const float* d_cost
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_out && d_cost_out, "null device pointer");
     if (int e = check_levels(rows_in, cols_in, rows_out, cols_out)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    return launch_down<1, float>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_out, d_cost_out, rows_out, cols_out,
+    return launch_down<1, float, G3>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_out, d_cost_out, rows_out, cols_out,
                                  candidate_count, 1, var_inv_i, as_stream(stream));
 }
 
@@ -660,7 +673,7 @@ extern "C" int ssg_isb_upsample(const uint8_t* d_guide_in, const float* d_cost_i
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_inout, "null device pointer");
     if (int e = check_levels(rows_inout, cols_inout, rows_in, cols_in)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    return launch_up<1, float, false>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout, d_cost_inout,
+    return launch_up<1, float, false, G3>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout, d_cost_inout,
                                       rows_inout, cols_inout, candidate_count, candidate_count, 1, weight_up,
                                       weight_down, var_inv_i, SelectOut{}, as_stream(stream));
 }
@@ -670,7 +683,7 @@ extern "C" int ssg_isb_apply(uint8_t* const* d_guides, float* const* d_costs, in
 {
     if (int e = check_apply_args(d_guides, d_costs, level_count, rows, cols, candidate_count, sigma_i, sigma_s))
         return e;
-    return apply_planar(d_guides, d_costs, level_count, rows, cols, candidate_count, 1, sigma_i, sigma_s,
+    return apply_planar<G3>(d_guides, d_costs, level_count, rows, cols, candidate_count, 1, sigma_i, sigma_s,
                         as_stream(stream));
 }
 
@@ -681,7 +694,7 @@ extern "C" int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_cos
     if (int e = check_apply_args(d_guides, d_costs, level_count, rows, cols, candidate_count, sigma_i, sigma_s))
         return e;
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
-    return apply_planar(d_guides, d_costs, level_count, rows, cols, candidate_count, instances, sigma_i, sigma_s,
+    return apply_planar<G4>(d_guides, d_costs, level_count, rows, cols, candidate_count, instances, sigma_i, sigma_s,
                         as_stream(stream));
 }
 
@@ -708,7 +721,7 @@ extern "C" int ssg_isb_upsample_select(const uint8_t* d_guide_in, const float* d
     if (int e = check_levels(rows_fine, cols_fine, rows_in, cols_in)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
     const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
-    return launch_up<1, float, true>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout,
+    return launch_up<1, float, true, G3>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_inout,
                                      const_cast<float*>(d_cost_fine), rows_fine, cols_fine, candidate_count,
                                      candidate_count, 1, weight_up, weight_down, var_inv_i, so, as_stream(stream));
 }
@@ -731,12 +744,12 @@ extern "C" int ssg_isb_downsample_batch(const uint8_t* d_guide_in, const void* d
     float* out = static_cast<float*>(d_cost_out);
     cudaStream_t st = as_stream(stream);
     if (storage == SSG_STORAGE_F16)
-        return launch_down<8, __half>(d_guide_in, static_cast<const __half*>(d_cost_in), rows_in, cols_in, d_guide_out,
+        return launch_down<8, __half, G4>(d_guide_in, static_cast<const __half*>(d_cost_in), rows_in, cols_in, d_guide_out,
                                       out, rows_out, cols_out, chunks, instances, var_inv_i, st);
     if (storage == SSG_STORAGE_UNORM16)
-        return launch_down<8, uint16_t>(d_guide_in, static_cast<const uint16_t*>(d_cost_in), rows_in, cols_in,
+        return launch_down<8, uint16_t, G4>(d_guide_in, static_cast<const uint16_t*>(d_cost_in), rows_in, cols_in,
                                         d_guide_out, out, rows_out, cols_out, chunks, instances, var_inv_i, st);
-    return launch_down<8, float>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in, d_guide_out, out,
+    return launch_down<8, float, G4>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in, d_guide_out, out,
                                  rows_out, cols_out, chunks, instances, var_inv_i, st);
 }
 
@@ -751,7 +764,7 @@ extern "C" int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_c
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
     const int chunks = chunks_of(candidate_count);
-    return launch_up<8, float, false>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in,
+    return launch_up<8, float, false, G4>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in,
                                       d_guide_inout, static_cast<float*>(d_cost_inout), rows_inout, cols_inout, chunks,
                                       chunks * 8, instances, weight_up, weight_down, var_inv_i, SelectOut{},
                                       as_stream(stream));
@@ -776,14 +789,14 @@ extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const vo
     void* fine = const_cast<void*>(d_cost_fine);  // read only in the selecting variant
     cudaStream_t st = as_stream(stream);
     if (storage == SSG_STORAGE_F16)
-        return launch_up<8, __half, true>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout,
+        return launch_up<8, __half, true, G4>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout,
                                           static_cast<__half*>(fine), rows_fine, cols_fine, chunks, candidate_count,
                                           instances, weight_up, weight_down, var_inv_i, so, st);
     if (storage == SSG_STORAGE_UNORM16)
-        return launch_up<8, uint16_t, true>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout,
+        return launch_up<8, uint16_t, true, G4>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout,
                                             static_cast<uint16_t*>(fine), rows_fine, cols_fine, chunks,
                                             candidate_count, instances, weight_up, weight_down, var_inv_i, so, st);
-    return launch_up<8, float, true>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout, static_cast<float*>(fine),
+    return launch_up<8, float, true, G4>(d_guide_in, coarse, rows_in, cols_in, d_guide_inout, static_cast<float*>(fine),
                                      rows_fine, cols_fine, chunks, candidate_count, instances, weight_up, weight_down,
                                      var_inv_i, so, st);
 }

@@ -60,6 +60,44 @@ __device__ __forceinline__ int colour_distance(const int a[3], const int b[3])
     return abs(a[0] - b[0]) + abs(a[1] - b[1]) + abs(a[2] - b[2]);
 }
 
+// Guide layouts.  G3: [rows][cols][3] bytes, the reference's (isb_filter.py:64).  G4: one 32-bit
+// word per pixel, bytes (Y, Cb, Cr, 0): one load per pixel, and the colour distance of two pixels
+// is one sum of absolute byte differences (__vsadu4), equal to G3's since the fourth bytes are 0.
+struct G3 {
+    struct Pix {
+        int c[3];
+    };
+    static constexpr int bytes = 3;
+    __device__ static __forceinline__ Pix load(const uint8_t* __restrict__ g, int64_t idx)
+    {
+        Pix p;
+        load_guide(g, idx, p.c);
+        return p;
+    }
+    __device__ static __forceinline__ int dist(const Pix& a, const Pix& b) { return colour_distance(a.c, b.c); }
+    __device__ static __forceinline__ int ch(const Pix& p, int k) { return p.c[k]; }
+    __device__ static __forceinline__ void store(uint8_t* __restrict__ g, int64_t idx, const uint32_t v[3])
+    {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) g[3 * idx + k] = (uint8_t)v[k];
+    }
+};
+
+struct G4 {
+    using Pix = uint32_t;
+    static constexpr int bytes = 4;
+    __device__ static __forceinline__ Pix load(const uint8_t* __restrict__ g, int64_t idx)
+    {
+        return reinterpret_cast<const uint32_t*>(g)[idx];
+    }
+    __device__ static __forceinline__ int dist(Pix a, Pix b) { return (int)__vsadu4(a, b); }
+    __device__ static __forceinline__ int ch(Pix p, int k) { return (int)((p >> (8 * k)) & 255u); }
+    __device__ static __forceinline__ void store(uint8_t* __restrict__ g, int64_t idx, const uint32_t v[3])
+    {
+        reinterpret_cast<uint32_t*>(g)[idx] = v[0] | (v[1] << 8) | (v[2] << 16);
+    }
+};
+
 struct ExpRange {  // evaluates the weight of a colour distance
     float var_inv_i;
     __device__ __forceinline__ float operator()(int d) const { return range_weight((float)d, var_inv_i); }
@@ -88,9 +126,10 @@ struct DownTapsT {
 };
 using DownTaps = DownTapsT<int64_t>;
 
-template <typename I, typename RW>
+// guide_out points at the layout's array; the coarse pixel's index is o
+template <typename I, typename RW, typename GL = G3>
 __device__ __forceinline__ void down_weights(const uint8_t* __restrict__ guide_in, int rows_in, int cols_in, int x,
-                                             int y, const RW& range, uint8_t* __restrict__ guide_out,
+                                             int y, const RW& range, uint8_t* __restrict__ guide_out, int64_t o,
                                              DownTapsT<I>& t)
 {
     const int x2 = 2 * x, y2 = 2 * y;
@@ -99,24 +138,24 @@ __device__ __forceinline__ void down_weights(const uint8_t* __restrict__ guide_i
     const int rows8[8] = {my, y2, py, py, py, y2, my, my};
     const int cols8[8] = {mx, mx, mx, x2, px, px, px, x2};
     t.centre = (I)y2 * cols_in + x2;
-    int cur[3];
-    load_guide(guide_in, t.centre, cur);
+    const typename GL::Pix cur = GL::load(guide_in, t.centre);
     const float base[8] = {0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f};
-    float wsum = 1.0f, g[3] = {(float)cur[0], (float)cur[1], (float)cur[2]};
+    float wsum = 1.0f, g[3] = {(float)GL::ch(cur, 0), (float)GL::ch(cur, 1), (float)GL::ch(cur, 2)};
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         t.idx[i] = (I)rows8[i] * cols_in + cols8[i];
-        int nb[3];
-        load_guide(guide_in, t.idx[i], nb);
-        t.w[i] = fmul(base[i], range(colour_distance(cur, nb)));
+        const typename GL::Pix nb = GL::load(guide_in, t.idx[i]);
+        t.w[i] = fmul(base[i], range(GL::dist(cur, nb)));
         wsum = fadd(wsum, t.w[i]);
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul((float)nb[ch], t.w[i]));
+        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul((float)GL::ch(nb, ch), t.w[i]));
     }
     t.wsum = wsum;
     const float den = fdiv(1.0f, wsum);
+    uint32_t v[3];
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) guide_out[ch] = (uint8_t)__float2uint_rz(fmul(g[ch], den));
+    for (int ch = 0; ch < 3; ++ch) v[ch] = __float2uint_rz(fmul(g[ch], den));
+    GL::store(guide_out, o, v);
 }
 
 // The four fine pixels of a coarse pixel (x, y) of guideUpsample2xKernel (isb_filter.cu:142-267):
@@ -156,30 +195,30 @@ struct UpTaps<3> {  // (1,1),(1,2),(2,1),(2,2)
 
 // Range weights of fine pixel F from the coarse guides `gd` and its own guide `up`; returns
 // 1 / (sum of weights) and the weighted guide sum `g` (isb_filter.cu:142-267).
-template <int F, typename RW>
-__device__ __forceinline__ float fine_weights(const int (&gd)[9][3], const int up[3], float weight_up,
-                                              float weight_down, const RW& range, float (&w)[UpTaps<F>::n],
-                                              float g[3])
+template <int F, typename RW, typename GL = G3>
+__device__ __forceinline__ float fine_weights(const typename GL::Pix (&gd)[9], const typename GL::Pix& up,
+                                              float weight_up, float weight_down, const RW& range,
+                                              float (&w)[UpTaps<F>::n], float g[3])
 {
     float ws = weight_up;
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) g[ch] = fmul(weight_up, (float)up[ch]);
+    for (int ch = 0; ch < 3; ++ch) g[ch] = fmul(weight_up, (float)GL::ch(up, ch));
 #pragma unroll
     for (int i = 0; i < UpTaps<F>::n; ++i) {
-        const int* nb = gd[UpTaps<F>::tap(i)];
-        const float rw = fmul(weight_down, range(colour_distance(nb, up)));
+        const typename GL::Pix& nb = gd[UpTaps<F>::tap(i)];
+        const float rw = fmul(weight_down, range(GL::dist(nb, up)));
         w[i] = UpTaps<F>::weighted ? fmul(UpTaps<F>::base(i), rw) : rw;
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul((float)nb[ch], w[i]));
+        for (int ch = 0; ch < 3; ++ch) g[ch] = fadd(g[ch], fmul((float)GL::ch(nb, ch), w[i]));
         ws = fadd(ws, w[i]);
     }
     return fdiv(1.0f, ws);
 }
 
 // Coarse 3x3 neighbourhood of (x, y), edge-clamped: flat indices and guides
-template <typename I>
+template <typename I, typename GL = G3>
 __device__ __forceinline__ void coarse_neighbourhood(const uint8_t* __restrict__ guide_in, int rows_in, int cols_in,
-                                                     int x, int y, I (&cidx)[9], int (&gd)[9][3])
+                                                     int x, int y, I (&cidx)[9], typename GL::Pix (&gd)[9])
 {
     const int rr[3] = {max(y - 1, 0), y, min(y + 1, rows_in - 1)};
     const int cc[3] = {max(x - 1, 0), x, min(x + 1, cols_in - 1)};
@@ -188,7 +227,7 @@ __device__ __forceinline__ void coarse_neighbourhood(const uint8_t* __restrict__
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             cidx[3 * a + b] = (I)rr[a] * cols_in + cc[b];
-            load_guide(guide_in, cidx[3 * a + b], gd[3 * a + b]);
+            gd[3 * a + b] = GL::load(guide_in, cidx[3 * a + b]);
         }
 }
 
@@ -213,8 +252,8 @@ __device__ __forceinline__ void up_weights(const uint8_t* __restrict__ guide_in,
                                            float weight_up, float weight_down, float var_inv_i, bool write_guide,
                                            UpWeights& u)
 {
-    int gd[9][3];
-    coarse_neighbourhood(guide_in, rows_in, cols_in, x, y, u.cidx, gd);
+    G3::Pix gd[9];
+    coarse_neighbourhood<int64_t, G3>(guide_in, rows_in, cols_in, x, y, u.cidx, gd);
     const int x2 = 2 * x, y2 = 2 * y;
     const int pux = min(x2 + 1, cols_io - 1), puy = min(y2 + 1, rows_io - 1);
     u.fidx[0] = (int64_t)y2 * cols_io + x2;
@@ -225,15 +264,15 @@ __device__ __forceinline__ void up_weights(const uint8_t* __restrict__ guide_in,
     u.set[1] = y2 != puy;
     u.set[2] = x2 != pux;
     u.set[3] = u.set[1] && u.set[2];
-    int up[4][3];
+    G3::Pix up[4];
 #pragma unroll
-    for (int f = 0; f < 4; ++f) load_guide(guide_io, u.fidx[f], up[f]);
+    for (int f = 0; f < 4; ++f) up[f] = G3::load(guide_io, u.fidx[f]);
     float g[4][3];
     const ExpRange range{var_inv_i};
-    u.inv[0] = fine_weights<0>(gd, up[0], weight_up, weight_down, range, u.w1, g[0]);
-    u.inv[1] = fine_weights<1>(gd, up[1], weight_up, weight_down, range, u.w2, g[1]);
-    u.inv[2] = fine_weights<2>(gd, up[2], weight_up, weight_down, range, u.w3, g[2]);
-    u.inv[3] = fine_weights<3>(gd, up[3], weight_up, weight_down, range, u.w4, g[3]);
+    u.inv[0] = fine_weights<0, ExpRange, G3>(gd, up[0], weight_up, weight_down, range, u.w1, g[0]);
+    u.inv[1] = fine_weights<1, ExpRange, G3>(gd, up[1], weight_up, weight_down, range, u.w2, g[1]);
+    u.inv[2] = fine_weights<2, ExpRange, G3>(gd, up[2], weight_up, weight_down, range, u.w3, g[2]);
+    u.inv[3] = fine_weights<3, ExpRange, G3>(gd, up[3], weight_up, weight_down, range, u.w4, g[3]);
     if (write_guide)
 #pragma unroll
         for (int f = 0; f < 4; ++f)

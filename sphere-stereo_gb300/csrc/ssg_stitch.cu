@@ -422,37 +422,6 @@ __device__ __forceinline__ void block_append(bool take, int32_t item, int32_t* c
     __syncthreads();  // warp_base and block_base are reused by the next call
 }
 
-// Reserves `n` entries per thread in a list counted by *count, with one atomic per block: returns
-// the thread's first entry.  Every thread of the block calls it (block-uniform control flow;
-// blockDim.x == kStitchBlock).
-__device__ __forceinline__ int block_reserve(int n, int32_t* count)
-{
-    __shared__ int warp_base[kStitchBlock / 32];
-    __shared__ int block_base;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int incl = n;  // inclusive scan over the warp
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += v;
-    }
-    if (lane == 31) warp_base[warp] = incl;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int total = 0;
-        for (int w = 0; w < kStitchBlock / 32; ++w) {
-            const int c = warp_base[w];
-            warp_base[w] = total;
-            total += c;
-        }
-        block_base = total ? atomicAdd(count, total) : 0;
-    }
-    __syncthreads();
-    const int first = block_base + warp_base[warp] + incl - n;
-    __syncthreads();  // warp_base and block_base are reused by the next call
-    return first;
-}
-
 // Where a flat map pixel g lives: its map's size, its position in the map, its table entry.
 struct MapPixel {
     int cols, rows, x, y;
@@ -527,7 +496,9 @@ __global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Map
 }
 
 // Step `step` >= 2: visits the open holes next to the pixels filled at step - 1 (list_in) that read
-// one of them, fills those it can and lists them (one reservation per block and pass).
+// one of them, fills those it can and lists them.  One thread per (filled pixel, neighbour): the
+// frontier is short after the first steps, and a thread's work is a chain of dependent loads, so
+// spreading the 8 neighbours over threads keeps a step's time near one chain's latency.
 template <typename Maps>
 __global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const Maps maps, float* __restrict__ map,
                                                                           uint8_t* __restrict__ stamp,
@@ -539,32 +510,31 @@ __global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const 
 {
     const int n = counts[(step - 1) % 3];
     if (blockIdx.x == 0 && threadIdx.x == 0) counts[(step + 1) % 3] = 0;
-    const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int h = base + (int)threadIdx.x;
-        unsigned filled = 0;  // bit k: neighbour k (3 x 3, row-major) filled
-        int64_t p = 0;
-        int cols = 1;
-        if (h < n) {
-            p = list_in[h];
+    const int64_t work = (int64_t)n * 8;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // whole blocks iterate together (block_append is block-collective)
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < work; base += stride) {
+        const int64_t h = base + threadIdx.x;
+        bool filled = false;
+        int64_t q = 0;
+        if (h < work) {
+            const int64_t p = list_in[h >> 3];
+            const int k = (int)(h & 7);
+            const int dx = k < 3 ? k - 1 : k == 3 ? -1 : k == 4 ? 1 : k - 6;  // the 8 neighbours
+            const int dy = k < 3 ? -1 : k < 5 ? 0 : 1;
             const MapPixel m = maps.at(p);
-            cols = m.cols;
-#pragma unroll 1
-            for (int k = 0; k < 9; ++k) {
-                const int qx = m.x + k % 3 - 1, qy = m.y + k / 3 - 1;
-                if (k == 4 || qx < 1 || qy < 1 || qx >= m.cols - 1 || qy >= m.rows - 1) continue;
-                const int64_t q = p + (int64_t)(k / 3 - 1) * m.cols + (k % 3 - 1);
-                if (stamp[q] != kUnfilled) continue;
-                const HoleOffsets o = hole_offsets(m.table[(int64_t)qy * m.cols + qx], q, m.cols);
-                // q reads p, and no other thread has queued q for this step
-                if (((o.w0 > 0.0f && o.n0 == p) || (o.w1 > 0.0f && o.n1 == p)) && atomicMax(claim + q, step) < step &&
-                    fill_hole(map, stamp, q, o, step, valid_at_most))
-                    filled |= 1u << k;
+            const int qx = m.x + dx, qy = m.y + dy;
+            if (qx >= 1 && qy >= 1 && qx < m.cols - 1 && qy < m.rows - 1) {
+                q = p + (int64_t)dy * m.cols + dx;
+                if (stamp[q] == kUnfilled) {
+                    const HoleOffsets o = hole_offsets(m.table[(int64_t)qy * m.cols + qx], q, m.cols);
+                    // q reads p, and no other thread has queued q for this step
+                    filled = ((o.w0 > 0.0f && o.n0 == p) || (o.w1 > 0.0f && o.n1 == p)) &&
+                             atomicMax(claim + q, step) < step && fill_hole(map, stamp, q, o, step, valid_at_most);
+                }
             }
         }
-        int at = block_reserve(__popc(filled), counts + step % 3);
-        for (int k = 0; k < 9; ++k)
-            if (filled & (1u << k)) list_out[at++] = (int32_t)(p + (int64_t)(k / 3 - 1) * cols + (k % 3 - 1));
+        block_append(filled, (int32_t)q, counts + step % 3, list_out);
     }
 }
 
@@ -599,7 +569,7 @@ static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t*
     hole_scan_kernel<Maps><<<grid_1d(total, kStitchBlock), kStitchBlock, 0, st>>>(maps, total, d_map, d_stamps,
                                                                                   claims, hole, counts, lists[0]);
     if (int err = launch_status("hole_scan_kernel")) return err;
-    const int grid = resident_grid(4);
+    const int grid = resident_grid(tuning(SSG_TUNE_HOLE_BLOCKS_PER_SM));
     hole_first_step_kernel<Maps><<<grid, kStitchBlock, 0, st>>>(maps, d_map, d_stamps, counts, lists[0], lists[1],
                                                                 ok);
     if (int err = launch_status("hole_first_step_kernel")) return err;
@@ -747,9 +717,8 @@ __global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_consta
 // The approximate merge for a batch of frames of one rig: the blending table, the weights and the
 // unprojected ray of each (panorama pixel, reference) are the same for every frame, so a thread
 // reads and unprojects them once and applies them to kMergeFrames frames (blockIdx.y: group of
-// frames), which also gives it that many independent gathers in flight.
-constexpr int kMergeFrames = 4;
-
+// frames; SSG_TUNE_MERGE_FRAMES), which also gives it that many independent gathers in flight.
+template <int kMergeFrames>
 __global__ void __launch_bounds__(kStitchBlock) merge_frames_kernel(const __grid_constant__ MergeParams p,
                                                                     int frames, const float2* __restrict__ lut,
                                                                     const float* __restrict__ weights,
@@ -1152,10 +1121,18 @@ static int merge_batch(const float* d_lut, const float* d_weights, const float* 
     const int64_t Q = (int64_t)pano_cols * pano_rows;
     dim3 grid(grid_1d(Q, kStitchBlock), frames);
     if constexpr (kFast) {
-        const dim3 fgrid(grid_1d(Q, kStitchBlock), (frames + kMergeFrames - 1) / kMergeFrames);
-        merge_frames_kernel<<<fgrid, kStitchBlock, 0, as_stream(stream)>>>(
-            p, frames, reinterpret_cast<const float2*>(d_lut), d_weights, d_reprojected, d_distances, d_images,
-            d_distance_panorama, d_rgb_panorama);
+        const int group = tuning(SSG_TUNE_MERGE_FRAMES);
+        const dim3 fgrid(grid_1d(Q, kStitchBlock), (frames + group - 1) / group);
+        const float2* lut = reinterpret_cast<const float2*>(d_lut);
+        if (group == 2)
+            merge_frames_kernel<2><<<fgrid, kStitchBlock, 0, as_stream(stream)>>>(
+                p, frames, lut, d_weights, d_reprojected, d_distances, d_images, d_distance_panorama, d_rgb_panorama);
+        else if (group == 8)
+            merge_frames_kernel<8><<<fgrid, kStitchBlock, 0, as_stream(stream)>>>(
+                p, frames, lut, d_weights, d_reprojected, d_distances, d_images, d_distance_panorama, d_rgb_panorama);
+        else
+            merge_frames_kernel<4><<<fgrid, kStitchBlock, 0, as_stream(stream)>>>(
+                p, frames, lut, d_weights, d_reprojected, d_distances, d_images, d_distance_panorama, d_rgb_panorama);
         return launch_status("merge_frames_kernel");
     } else {
         merge_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(

@@ -27,7 +27,7 @@ namespace ssg {
 // tap lies in [-1, cols - 1] x [-1, rows - 1] is a plain load and the border supplies
 // grid_sample's zero padding; the border rows and the last column are never written (the caller
 // zeroes the buffer once).  The guide of every reference camera (rgb2yCbCr + uint8 cast) is
-// written in the same pass, from the float values.
+// written in the same pass, from the float values, as one 32-bit word per pixel (Y, Cb, Cr, 0).
 // ---------------------------------------------------------------------------------------------
 struct StageParams {
     int cameras, references, cols, rows;
@@ -70,10 +70,12 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
         float yy = fadd(fadd(fadd(fmul(c0, 0.1826f), 16.0f), fmul(c1, 0.6142f)), fmul(c2, 0.062f));
         float cb = fadd(fsub(fsub(128.0f, fmul(c0, 0.1006f)), fmul(c1, 0.3386f)), fmul(c2, 0.4392f));
         float cr = fsub(fsub(fadd(fmul(c0, 0.4392f), 128.0f), fmul(c1, 0.3989f)), fmul(c2, 0.0403f));
-        uint8_t* g = guides + (((int64_t)frame * p.references + slot) * P + (int64_t)y * p.cols + e) * 3;
-        g[0] = (uint8_t)__float2uint_rz(fminf(fmaxf(yy, 16.0f), 235.0f));
-        g[1] = (uint8_t)__float2uint_rz(fminf(fmaxf(cb, 16.0f), 240.0f));
-        g[2] = (uint8_t)__float2uint_rz(fminf(fmaxf(cr, 16.0f), 240.0f));
+        // one 32-bit word per pixel: bytes (Y, Cb, Cr, 0)
+        const uint32_t g0 = __float2uint_rz(fminf(fmaxf(yy, 16.0f), 235.0f));
+        const uint32_t g1 = __float2uint_rz(fminf(fmaxf(cb, 16.0f), 240.0f));
+        const uint32_t g2 = __float2uint_rz(fminf(fmaxf(cr, 16.0f), 240.0f));
+        reinterpret_cast<uint32_t*>(guides)[((int64_t)frame * p.references + slot) * P + (int64_t)y * p.cols + e] =
+            g0 | (g1 << 8) | (g2 << 16);
     }
 }
 
@@ -218,8 +220,26 @@ struct UniformView {
     __device__ __forceinline__ float2 cand2(int k) const { return *reinterpret_cast<const float2*>(&p.cand[k]); }
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kBatchBlock, 4) sweep_batch_kernel(const __grid_constant__ FastSweepParams p,
+// Block shapes of the sweep (SSG_TUNE_SWEEP_VARIANT): threads per block and blocks per SM, which
+// bounds the registers (64, 80, 64)
+template <int V>
+struct SweepShape;
+template <>
+struct SweepShape<0> {
+    static constexpr int threads = 256, blocks = 4;
+};
+template <>
+struct SweepShape<1> {
+    static constexpr int threads = 256, blocks = 3;
+};
+template <>
+struct SweepShape<2> {
+    static constexpr int threads = 128, blocks = 8;
+};
+
+template <typename T, int V>
+__global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
+    sweep_batch_kernel(const __grid_constant__ FastSweepParams p,
                                                                 const uint4* __restrict__ staged,
                                                                 const int8_t* __restrict__ selected,
                                                                 T* __restrict__ cost)
@@ -248,39 +268,65 @@ struct InstView {
     __device__ __forceinline__ float2 cand2(int k) const { return __ldg(reinterpret_cast<const float2*>(&I->cand[k])); }
 };
 
-// Persistent sweep over an uneven batch: each block takes work items (kSweepTile reference pixels
-// of one instance) from a queue (*counter, zeroed before the launch) until the batch is done.
-template <typename T>
-__global__ void __launch_bounds__(kBatchBlock, 4) sweep_uneven_kernel(const SweepInst* __restrict__ insts,
-                                                                 int instances, int total_tiles,
-                                                                 int* __restrict__ counter)
+// Persistent sweep over an uneven batch: each block takes work items (`span` consecutive tiles of
+// kSweepTile reference pixels, in the instances' order) from a queue (*counter, zeroed before the
+// launch) until the batch is done; each tile belongs to one instance.
+template <typename T, int V>
+__global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
+    sweep_uneven_kernel(const SweepInst* __restrict__ insts, int instances, int total_tiles, int span,
+                        int* __restrict__ counter)
 {
-    __shared__ int s_tile, s_inst;
+    __shared__ int s_item;
+    __shared__ int s_inst[4];
     for (;;) {
-        if (threadIdx.x == 0) {
-            const int t = atomicAdd(counter, 1);
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int first = s_item * span;
+        if (threadIdx.x < span && first + (int)threadIdx.x < total_tiles) {
+            const int t = first + threadIdx.x;
             int lo = 0, hi = instances - 1;  // the last instance whose tiles begin at or before t
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
                 if (insts[mid].tile_begin <= t) lo = mid;
                 else hi = mid - 1;
             }
-            s_tile = t;
-            s_inst = lo;
+            s_inst[threadIdx.x] = lo;
         }
         __syncthreads();
-        const int t = s_tile, k = s_inst;
-        __syncthreads();  // s_tile and s_inst are rewritten by the next take
-        if (t >= total_tiles) return;
-        const SweepInst* I = insts + k;
-        const int cols = I->cols, rows = I->rows, P = cols * rows;
-        const int i = (t - I->tile_begin) * kSweepTile + threadIdx.x;
-        if (i < P) {
+        if (first >= total_tiles) return;
+        for (int u = 0; u < span && first + u < total_tiles; ++u) {
+            const SweepInst* I = insts + s_inst[u];
+            const int cols = I->cols, rows = I->rows, P = cols * rows;
             const int plane = (cols + 2) * (rows + 2);
-            T* out = static_cast<T*>(I->cost) + (int64_t)i * 8;
-            sweep_pixel<T>(InstView{I}, I->staged, plane, I->ref_camera, cols, rows, i % cols, i / cols,
-                           I->selected[i], out, (int64_t)P * 8);
+            for (int j = threadIdx.x; j < kSweepTile; j += blockDim.x) {
+                const int i = (first + u - I->tile_begin) * kSweepTile + j;
+                if (i < P) {
+                    T* out = static_cast<T*>(I->cost) + (int64_t)i * 8;
+                    sweep_pixel<T>(InstView{I}, I->staged, plane, I->ref_camera, cols, rows, i % cols, i / cols,
+                                   I->selected[i], out, (int64_t)P * 8);
+                }
+            }
         }
+        __syncthreads();  // s_item and s_inst are rewritten by the next take
+    }
+}
+
+template <typename T, int V>
+static void launch_sweep_uneven_shape(const SweepInst* d_insts, int instances, int total_tiles, int span,
+                                      int* d_counter, int sms, cudaStream_t st)
+{
+    sweep_uneven_kernel<T, V><<<sms * SweepShape<V>::blocks, SweepShape<V>::threads, 0, st>>>(
+        d_insts, instances, total_tiles, span, d_counter);
+}
+
+template <typename T>
+static void launch_sweep_uneven_t(const SweepInst* d_insts, int instances, int total_tiles, int span,
+                                  int* d_counter, int sms, cudaStream_t st)
+{
+    switch (tuning(SSG_TUNE_SWEEP_VARIANT)) {
+        case 1: launch_sweep_uneven_shape<T, 1>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
+        case 2: launch_sweep_uneven_shape<T, 2>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
+        default: launch_sweep_uneven_shape<T, 0>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
     }
 }
 
@@ -291,12 +337,32 @@ int launch_sweep_uneven(const SweepInst* d_insts, int instances, int total_tiles
     if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = sms * 4;  // resident blocks (4 per SM at the kernel's register bound)
+    const int span = tuning(SSG_TUNE_UNEVEN_SPAN);  // 1, 2 or 4 (<= the 4 entries of s_inst)
     if (storage == SSG_STORAGE_F16)
-        sweep_uneven_kernel<__half><<<grid, kBatchBlock, 0, st>>>(d_insts, instances, total_tiles, d_counter);
+        launch_sweep_uneven_t<__half>(d_insts, instances, total_tiles, span, d_counter, sms, st);
     else
-        sweep_uneven_kernel<uint16_t><<<grid, kBatchBlock, 0, st>>>(d_insts, instances, total_tiles, d_counter);
+        launch_sweep_uneven_t<uint16_t>(d_insts, instances, total_tiles, span, d_counter, sms, st);
     return launch_status("sweep_uneven_kernel");
+}
+
+template <typename T, int V>
+static void launch_sweep_shape(const FastSweepParams& p, const uint4* staged, const int8_t* selected, T* cost,
+                               int64_t P, int instances, cudaStream_t st)
+{
+    constexpr int threads = SweepShape<V>::threads;
+    const dim3 grid(grid_1d(P, threads), instances);
+    sweep_batch_kernel<T, V><<<grid, threads, 0, st>>>(p, staged, selected, cost);
+}
+
+template <typename T>
+static void launch_sweep(const FastSweepParams& p, const uint4* staged, const int8_t* selected, T* cost, int64_t P,
+                         int instances, cudaStream_t st)
+{
+    switch (tuning(SSG_TUNE_SWEEP_VARIANT)) {
+        case 1: launch_sweep_shape<T, 1>(p, staged, selected, cost, P, instances, st); break;
+        case 2: launch_sweep_shape<T, 2>(p, staged, selected, cost, P, instances, st); break;
+        default: launch_sweep_shape<T, 0>(p, staged, selected, cost, P, instances, st); break;
+    }
 }
 
 static int check_storage(int storage)
@@ -332,7 +398,8 @@ static int stage_images(const Tin* d_images, int frames, int cameras, int cols, 
     SSG_REQUIRE(cameras >= 1 && cameras <= SSG_MAX_CAMERAS && references >= 1 && references <= SSG_MAX_REFERENCES,
                 "camera or reference count out of range");
     if (int e = staged_plane_fits(cols, rows)) return e;
-    SSG_REQUIRE(((uintptr_t)d_staged & 15) == 0, "staged images must be 16-byte aligned");
+    SSG_REQUIRE(((uintptr_t)d_staged & 15) == 0 && ((uintptr_t)d_guides & 3) == 0,
+                "staged images must be 16-byte and guides 4-byte aligned");
     StageParams p{};
     p.cameras = cameras;
     p.references = references;
@@ -403,13 +470,12 @@ extern "C" int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_c
     }
     for (int k = 0; k < 8 * p.chunks; ++k) p.cand[k] = candidates[k < candidate_count ? k : candidate_count - 1];
     const int64_t P = (int64_t)cols * rows;
-    dim3 grid(grid_1d(P, kBatchBlock), frames * references);
     const uint4* staged = reinterpret_cast<const uint4*>(d_staged);
     if (storage == SSG_STORAGE_F16)
-        sweep_batch_kernel<__half><<<grid, kBatchBlock, 0, as_stream(stream)>>>(p, staged, d_selected,
-                                                                              static_cast<__half*>(d_cost));
+        launch_sweep<__half>(p, staged, d_selected, static_cast<__half*>(d_cost), P, frames * references,
+                             as_stream(stream));
     else
-        sweep_batch_kernel<uint16_t><<<grid, kBatchBlock, 0, as_stream(stream)>>>(p, staged, d_selected,
-                                                                                static_cast<uint16_t*>(d_cost));
+        launch_sweep<uint16_t>(p, staged, d_selected, static_cast<uint16_t*>(d_cost), P, frames * references,
+                               as_stream(stream));
     return launch_status("sweep_batch_kernel");
 }

@@ -37,7 +37,7 @@ def distance_candidates(min_dist, max_dist, candidate_count) -> torch.Tensor:
 class RGBD_Estimator:
     def __init__(self, calibrations, min_dist, max_dist, candidate_count, references_indices, reprojection_viewpoint,
                  masks, matching_resolution, rgb_to_stitch_resolution, panorama_resolution, sigma_i, sigma_s, device,
-                 *, cost_storage="fp32", max_batch=1, cuda_graphs=True):
+                 *, cost_storage="fp32", max_batch=1, cuda_graphs=True, tuner=None):
         """Prepare RGB-D estimation: camera selection for adaptive matching, filters, stitcher.
 
         Args:
@@ -58,6 +58,8 @@ class RGBD_Estimator:
                 volume with 16 bits per candidate (fp32 arithmetic) and run frames in batches
             max_batch (keyword only): largest batch of ``estimate_RGBD_panoramas``
             cuda_graphs (keyword only): replay each batch from a captured CUDA graph
+            tuner (keyword only): an autotune.Tuner that picks the batched kernels' launch
+                shapes on first use (None: the library's defaults)
         """
         device = torch.device(device)
         if device.type != "cuda":
@@ -113,6 +115,7 @@ class RGBD_Estimator:
         self.cost_storage = cost_storage
         self.max_batch = int(max_batch)
         self.cuda_graphs = bool(cuda_graphs)
+        self.tuner = tuner
         self._pipeline = None
 
     @property
@@ -171,7 +174,7 @@ class RGBD_Estimator:
             from .pipeline import BatchPipeline
 
             storage = "fp16" if self.cost_storage == "fp32" else self.cost_storage
-            self._pipeline = BatchPipeline(self, self.max_batch, storage, self.cuda_graphs)
+            self._pipeline = BatchPipeline(self, self.max_batch, storage, self.cuda_graphs, self.tuner)
         return self._pipeline
 
     # --------------------------------------------------------------------------------------

@@ -29,7 +29,8 @@ F32 = 2
 
 
 class BatchPipeline:
-    def __init__(self, estimator, max_frames: int, storage: str = "fp16", cuda_graphs: bool = True):
+    def __init__(self, estimator, max_frames: int, storage: str = "fp16", cuda_graphs: bool = True,
+                 tuner=None):
         if storage not in STORAGE:
             raise ValueError(f"storage must be one of {sorted(STORAGE)}")
         if max_frames < 1:
@@ -59,13 +60,14 @@ class BatchPipeline:
         # planes of 16-byte texel-pair entries with a zero border, (rows + 2) x (cols + 2); the
         # border is never written
         self.staged = torch.zeros(F * C * (self.rows + 2) * (self.cols + 2) * 4, **f32)
-        self.guides = [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes]
+        # guides: one 32-bit word per pixel (Y, Cb, Cr, 0)
+        self.guides = [torch.empty(F * R * r * c * 4, **u8) for r, c in self.shapes]
         # level 0 (the sweep's output) 16-bit, coarser levels float32
         self.costs = [torch.empty(F * R * self.chunks * r * c * 8, **(i16 if l == 0 else f32))
                       for l, (r, c) in enumerate(self.shapes)]
         # the distance post-filter's guide pyramid; its level 0 is the unfiltered guide itself,
         # which the batched cost filter leaves as it was
-        self.df_guides = [self.guides[0]] + [torch.empty(F * R * r * c * 3, **u8) for r, c in self.shapes[1:]]
+        self.df_guides = [self.guides[0]] + [torch.empty(F * R * r * c * 4, **u8) for r, c in self.shapes[1:]]
         self.df_costs = [torch.empty(F * R * r * c, **f32) for r, c in self.shapes[1:]]
         self.distance_raw = torch.empty(F * R * P, **f32)
         self.index = torch.empty(F * R * P, dtype=torch.int32, device=dev)
@@ -81,6 +83,10 @@ class BatchPipeline:
         self._refs = N.ints(e.references_indices)
         self._poses = N.floats([v for r in e.references_indices for v in e._poses_list[r]])
         self._graphs: dict = {}
+        # launch shapes: picked by the autotuner on first use (``tuner``: an autotune.Tuner, or
+        # None for the library's defaults)
+        self.tuner = tuner
+        self.tuned: dict[str, int] | None = None
 
     # ------------------------------------------------------------------------------------
     def _launch(self, match: torch.Tensor, stitch: torch.Tensor, frames: int, stream: int) -> None:
@@ -149,6 +155,7 @@ class BatchPipeline:
         for name, t, shape in (("images_to_match", match, (frames, self.C, self.rows, self.cols, 3)),
                                ("images_to_stitch", stitch, (frames, self.R, st.image_rows, st.image_cols, 3))):
             N.require(t, name, torch.uint8 if t.dtype == torch.uint8 else torch.float32, shape, self.device)
+        self._apply_tuning(match, stitch, frames)
         if not self.cuda_graphs:
             self._launch(match, stitch, frames, N.stream_of(match))
         else:
@@ -169,6 +176,25 @@ class BatchPipeline:
                 self._graphs[key] = graph
             graph.replay()
         return self.rgb[:frames], self.pano_distance[:frames]
+
+    TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "hole_blocks_per_sm", "merge_frames")
+
+    def _apply_tuning(self, match, stitch, frames) -> None:
+        """Sets this pipeline's launch shapes (process-wide knobs), tuning them on first use."""
+        if self.tuner is None:
+            return
+        from . import autotune
+
+        if self.tuned is None:
+            key = autotune.workload_key("batch", self.cols, self.rows, self.N, self.C, self.R, frames,
+                                        self.storage_name, self.st.pano_cols, self.st.pano_rows)
+            self.tuned = self.tuner.apply(key)
+            if self.tuned is None:
+                stream = N.stream_of(match)
+                self.tuned = self.tuner.tune(key, lambda: self._launch(match, stitch, frames, stream),
+                                             list(self.TUNED_KNOBS))
+        for name, v in self.tuned.items():
+            autotune.set_knob(name, v)
 
     def launches_per_batch(self) -> int:
         L = self.L

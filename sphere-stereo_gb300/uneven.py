@@ -26,7 +26,8 @@ STORAGE = {"fp16": 0, "unorm16": 1}
 
 
 class UnevenBatch:
-    def __init__(self, estimators, storage: str = "fp16", cuda_graphs: bool = True, input_dtype=torch.float32):
+    def __init__(self, estimators, storage: str = "fp16", cuda_graphs: bool = True, input_dtype=torch.float32,
+                 tuner=None):
         """Args:
             estimators: one RGBD_Estimator per job (rigs, resolutions and candidate counts may all
                 differ); the jobs run together on the estimators' common device
@@ -34,6 +35,8 @@ class UnevenBatch:
             cuda_graphs: replay the batch from a captured CUDA graph
             input_dtype: torch.float32 (images in [0, 255], as estimate_RGBD_panorama takes them)
                 or torch.uint8 (the 8-bit images they are made from)
+            tuner: an autotune.Tuner that picks the sweep's block shape and work-item span on
+                first use (None: the library's defaults)
         """
         if not estimators:
             raise ValueError("at least one job is required")
@@ -67,7 +70,7 @@ class UnevenBatch:
                 "match": torch.zeros(C, rows, cols, 3, dtype=input_dtype, device=dev),
                 "stitch": torch.zeros(R, st.image_rows, st.image_cols, 3, dtype=input_dtype, device=dev),
                 "staged": torch.zeros(C * (rows + 2) * (cols + 2) * 4, **f32),
-                "guide0": torch.empty(R * rows * cols * 3, **u8),
+                "guide0": torch.empty(R * rows * cols * 4, **u8),  # 32-bit guide words
                 "distance": torch.empty(R, rows, cols, **f32),
                 "rgb": torch.empty(st.pano_rows, st.pano_cols, 3, **u8),
                 "pano_distance": torch.empty(st.pano_rows, st.pano_cols, **f32),
@@ -78,11 +81,11 @@ class UnevenBatch:
             j["instances"] = []
             for slot, r in enumerate(e.references_indices):
                 P = rows * cols
-                guides = [j["guide0"][slot * P * 3:(slot + 1) * P * 3]] + \
-                    [torch.empty(rr * cc * 3, **u8) for rr, cc in shapes[1:]]
+                guides = [j["guide0"][slot * P * 4:(slot + 1) * P * 4]] + \
+                    [torch.empty(rr * cc * 4, **u8) for rr, cc in shapes[1:]]
                 costs = [torch.empty(chunks * P * 8, dtype=torch.int16, device=dev)] + \
                     [torch.empty(chunks * rr * cc * 8, **f32) for rr, cc in shapes[1:]]
-                df_guides = [guides[0]] + [torch.empty(rr * cc * 3, **u8) for rr, cc in shapes[1:]]
+                df_guides = [guides[0]] + [torch.empty(rr * cc * 4, **u8) for rr, cc in shapes[1:]]
                 df_costs = [torch.empty(rr * cc, **f32) for rr, cc in shapes[1:]]
                 raw = torch.empty(rows, cols, **f32)
                 index = torch.empty(rows, cols, dtype=torch.int32, device=dev)
@@ -138,6 +141,8 @@ class UnevenBatch:
         N.call("ssg_uneven_upload", self._handle, self._plan.data_ptr(), self._scratch.data_ptr(), stream)
         self.instance_count = len(instances)
         self._graph = None
+        self.tuner = tuner
+        self.tuned: dict[str, int] | None = None
 
     def __del__(self):
         h = getattr(self, "_handle", None)
@@ -160,6 +165,22 @@ class UnevenBatch:
                     j["images_u8"].copy_(j["stitch"])  # float -> uint8 truncation (depth_estimation.py:239)
         N.call("ssg_uneven_run", self._handle, stream)
 
+    def _apply_tuning(self, stream: int) -> None:
+        if self.tuner is None:
+            return
+        from . import autotune
+
+        if self.tuned is None:
+            shapes = [(e.matching_resolution, e.candidate_count, len(e.calibrations), len(e.references_indices))
+                      for e in self.estimators]
+            key = autotune.workload_key("uneven", self.storage, self.input_dtype, shapes)
+            self.tuned = self.tuner.apply(key)
+            if self.tuned is None:
+                self.tuned = self.tuner.tune(key, lambda: self._launch(stream),
+                                             ["sweep_variant", "uneven_span", "isb_up_blocks"], entry="ssg_uneven_run")
+        for name, v in self.tuned.items():
+            autotune.set_knob(name, v)
+
     def launches(self) -> int:
         """Kernels one batch launches."""
         per_job = 1 + (0 if self.input_dtype == torch.uint8 else 1)
@@ -181,6 +202,7 @@ class UnevenBatch:
                 N.require(t, name, self.input_dtype, tuple(m.shape), self.device)
                 m.copy_(t, non_blocking=True)
         stream = torch.cuda.current_stream(self.device)
+        self._apply_tuning(stream.cuda_stream)
         if not self.cuda_graphs:
             self._launch(stream.cuda_stream)
         else:

@@ -172,8 +172,10 @@ def test_bench_configuration_against_fp32_path(ss, native, synthetic):
         pipe = fast.pipeline()
         for lvl in range(1, pipe.L):
             r, c = pipe.shapes[lvl]
-            g16 = pipe.guides[lvl].view(pipe.max_frames, pipe.R, r, c, 3)[0, -1].cpu().numpy()
-            assert np.array_equal(g16, guides32[lvl]), f"guide level {lvl} differs from the fp32 path"
+            # 32-bit guide words (Y, Cb, Cr, 0) against the fp32 path's 3-byte pixels
+            g16 = pipe.guides[lvl].view(pipe.max_frames, pipe.R, r, c, 4)[0, -1].cpu().numpy()
+            assert not g16[..., 3].any()
+            assert np.array_equal(g16[..., :3], guides32[lvl]), f"guide level {lvl} differs from the fp32 path"
         if storage == "fp16":
             # 8-bit inputs (the images the float inputs are made from) give identical results
             idx_f = fast.batch_index_maps[0].cpu().numpy().copy()
