@@ -245,26 +245,36 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
 
 /* Image staging + guides: d_images frames x cameras x rows x cols x 3, float32 (the inputs of
  * estimate_RGBD_panorama, python/depth_estimation.py:205-227) or uint8 (the 8-bit images those
- * inputs are made from, python/utils.py:157-205) -> d_staged frames x cameras x (rows + 2) x
- * (cols + 2) 16-byte entries, entry (y + 1, x) holding texels x - 1 and x of row y as fp16 RGB
- * (exact for 8-bit values; other floats are rounded to fp16), with a border that the caller
- * zeroes once and that is never written; and d_guides frames x references x rows x cols 32-bit
- * guide words (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from
- * the float values). */
+ * inputs are made from, python/utils.py:157-205) -> d_staged frames x cameras planes of
+ * (rows + 2) x (cols + 2) 16-byte entries, entry (j, i) holding the bilinear footprint of top-left
+ * tap (i - 1, j - 1) -- texels (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1) -- as 8-bit
+ * RGB, zero outside the image (every entry is written); d_plane_flags frames x cameras int32,
+ * set to 1 for a plane with a value that is not an integer in [0, 255] (the sweep then samples
+ * that plane from the float images); and d_guides frames x references x rows x cols 32-bit guide
+ * words (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from the
+ * float values).  Zeroes d_plane_flags first (a 4 x frames x cameras byte memset). */
 SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                              const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
-                             void* stream);
+                             int32_t* d_plane_flags, void* stream);
 SSG_API int ssg_stage_images_u8(const uint8_t* d_images, int frames, int cameras, int cols, int rows,
                                 const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
-                                void* stream);
+                                int32_t* d_plane_flags, void* stream);
+
+/* float32 -> uint8 truncation of `count` values in [0, 255] (the float -> uint8 copy of the images
+ * to stitch, python/depth_estimation.py:239-240); 16-byte loads and stores where both buffers are
+ * 16-byte aligned. */
+SSG_API int ssg_convert_u8(const float* d_src, uint8_t* d_dst, int64_t count, void* stream);
 
 /* Sphere sweep + cost for every instance (python/depth_estimation.py:141-175), 16-bit output.
- * relative_poses: references x cameras x 12 floats (host); d_selected: references x pixels
- * int8; d_cost: instances x level-0 volume. */
+ * relative_poses: references x cameras x 12 floats (host); d_staged / d_plane_flags from
+ * ssg_stage_images[_u8]; d_images: the float32 images staged (read for planes whose flag is set;
+ * NULL for 8-bit inputs); d_selected: references x pixels int8; d_cost: instances x level-0
+ * volume. */
 SSG_API int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_count, const ssg_camera* cameras,
                                  int references, const int* reference_cameras, const float* relative_poses,
-                                 const float* d_staged, const int8_t* d_selected, const float* candidates,
-                                 int candidate_count, int storage, void* d_cost, void* stream);
+                                 const float* d_staged, const float* d_images, const int32_t* d_plane_flags,
+                                 const int8_t* d_selected, const float* candidates, int candidate_count, int storage,
+                                 void* d_cost, void* stream);
 
 /* ISB down / up steps (python/isb_filter.cu:44-329) on `instances` contiguous levels.  The
  * downsampling reads a level stored as `storage` and writes float32; the upsampling reads and
@@ -279,12 +289,14 @@ SSG_API int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_cost
 
 /* Last ISB level fused with distance selection (python/isb_filter.cu:132-329 +
  * python/depth_estimation.py:179-198): float32 coarse level, fine (level-0) volume stored as
- * `storage`; d_distance / d_index instances x fine pixels. */
+ * `storage`; d_distance / d_index instances x fine pixels; d_distance_copy (or NULL) receives the
+ * same distances (the post-filter's input, which it filters in place). */
 SSG_API int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
                                           uint8_t* d_guide_inout, const void* d_cost_fine, int rows_fine,
                                           int cols_fine, int candidate_count, int instances, int storage,
                                           float weight_up, float weight_down, float var_inv_i,
-                                          const float* candidates, float* d_distance, int32_t* d_index, void* stream);
+                                          const float* candidates, float* d_distance, int32_t* d_index,
+                                          float* d_distance_copy, void* stream);
 
 /* Distance selection from a level-0 volume (pyramids of fewer than two levels). */
 SSG_API int ssg_select_distance_batch(const void* d_cost, int candidate_count, int64_t pixels, int instances,
@@ -413,6 +425,8 @@ typedef struct {
     const float* candidates;      /* host, candidate_count distances */
     double sigma_i, sigma_s;      /* cost filter; the distance post-filter uses half of each */
     const float* d_staged;        /* the rig frame's planes from ssg_stage_images (camera_count planes) */
+    const float* d_images;        /* the frame's float32 images staged (or NULL for 8-bit inputs) */
+    const int32_t* d_plane_flags; /* the frame's camera_count plane flags from ssg_stage_images */
     const int8_t* d_selected;     /* rows x cols selected cameras */
     uint8_t* const* d_guides;     /* host array of level_count pointers: the guide pyramid (level 0 staged) */
     void* const* d_costs;         /* host array: level 0 16-bit chunked (written by the sweep), others float32 */

@@ -53,7 +53,8 @@ class ssg_uneven_instance(ctypes.Structure):
                 ("reference_camera", ctypes.c_int), ("candidate_count", ctypes.c_int),
                 ("cameras", ctypes.c_void_p), ("relative_poses", ctypes.c_void_p), ("candidates", ctypes.c_void_p),
                 ("sigma_i", ctypes.c_double), ("sigma_s", ctypes.c_double),
-                ("d_staged", ctypes.c_void_p), ("d_selected", ctypes.c_void_p), ("d_guides", ctypes.c_void_p),
+                ("d_staged", ctypes.c_void_p), ("d_images", ctypes.c_void_p), ("d_plane_flags", ctypes.c_void_p),
+                ("d_selected", ctypes.c_void_p), ("d_guides", ctypes.c_void_p),
                 ("d_costs", ctypes.c_void_p), ("d_df_guides", ctypes.c_void_p), ("d_df_costs", ctypes.c_void_p),
                 ("d_distance_raw", ctypes.c_void_p), ("d_distance", ctypes.c_void_p), ("d_index", ctypes.c_void_p)]
 
@@ -94,12 +95,13 @@ SIGNATURES = {
     "ssg_reproject_distance": (_I, [_P, _P, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint": (_I, [_P, _P, _P, _I, _I, _D, _I, _P]),
     "ssg_merge_panorama": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P]),
-    "ssg_stage_images": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P]),
-    "ssg_stage_images_u8": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P]),
-    "ssg_sweep_cost_batch": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "ssg_stage_images": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "ssg_stage_images_u8": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "ssg_sweep_cost_batch": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
     "ssg_isb_downsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _P]),
     "ssg_isb_upsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P]),
-    "ssg_isb_upsample_select_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P]),
+    "ssg_isb_upsample_select_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P,
+                                           _P]),
     "ssg_select_distance_batch": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, _P]),
     "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _P]),
     "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
@@ -113,6 +115,7 @@ SIGNATURES = {
     "ssg_isb_downsample_transpose": (_I, [_P, _I, _I, _I, _I, _I, _F, _P, _P, _P]),
     "ssg_sweep_cost_backward": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "ssg_convert_u8": (_I, [_P, _P, _I64, _P]),
     "ssg_tuning_set": (_I, [_I, _I]),
     "ssg_tuning_get": (_I, [_I]),
     "ssg_tuning_choices": (_I, [_I, _P, _I]),

@@ -775,7 +775,7 @@ extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const vo
                                              int rows_fine, int cols_fine, int candidate_count, int instances,
                                              int storage, float weight_up, float weight_down, float var_inv_i,
                                              const float* candidates, float* d_distance, int32_t* d_index,
-                                             void* stream)
+                                             float* d_distance_copy, void* stream)
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_inout && d_cost_fine && d_distance && candidates, "null pointer");
     if (int e = check_levels(rows_fine, cols_fine, rows_in, cols_in)) return e;
@@ -784,7 +784,8 @@ extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const vo
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
     const int chunks = chunks_of(candidate_count);
-    const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
+    SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
+    so.distance2 = d_distance_copy;
     const float* coarse = static_cast<const float*>(d_cost_in);
     void* fine = const_cast<void*>(d_cost_fine);  // read only in the selecting variant
     cudaStream_t st = as_stream(stream);

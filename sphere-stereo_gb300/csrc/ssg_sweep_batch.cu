@@ -4,8 +4,8 @@
 // A batch is `instances` independent (frame, reference camera) pairs of one rig; blockIdx.y is the
 // instance, so a whole batch is one launch.  One thread per pixel of the reference camera walks
 // the candidates in order, projects each candidate point into the pixel's selected camera,
-// samples it bilinearly from float4 texels (16-byte loads) and writes 8 candidates at a time as
-// one 16-byte cell.  Level-0 storage is __half (fp16) or unorm16 (q = round(c * 65535 / 500);
+// samples it bilinearly (one 16-byte load of the 2 x 2 footprint) and writes 8 candidates at a
+// time as one 16-byte cell.  Level-0 storage is __half (fp16) or unorm16 (q = round(c * 65535 / 500);
 // costs are clamped to [0, 500]); the arithmetic is fp32.  The fp32 kernels of ssg_sweep.cu are
 // the ones that reproduce the reference bit for bit; this sweep projects with approximate square
 // roots and reciprocal, a change far below the 16-bit rounding of its output.
@@ -18,75 +18,127 @@ namespace ssg {
 
 
 // ---------------------------------------------------------------------------------------------
-// Image staging.  The sweep reads each bilinear sample as two 16-byte loads, one per image row:
-// a staged entry holds two horizontally adjacent texels as fp16 RGB ([R0 G0 B0 R1 G1 B1 0 0],
-// texels x - 1 and x of entry x).  fp16 holds every 8-bit value exactly, so for images made from
-// 8-bit data (all of the reference's inputs before resizing) the samples are the float32 ones;
-// other float inputs are rounded to fp16 (a relative 2^-11).  Entries form planes of
-// (rows + 2) x (cols + 2) with a border of zeros, so that every tap of a sample whose top-left
-// tap lies in [-1, cols - 1] x [-1, rows - 1] is a plain load and the border supplies
-// grid_sample's zero padding; the border rows and the last column are never written (the caller
-// zeroes the buffer once).  The guide of every reference camera (rgb2yCbCr + uint8 cast) is
-// written in the same pass, from the float values, as one 32-bit word per pixel (Y, Cb, Cr, 0).
+// Image staging.  The sweep's samples are bilinear, so what it reads per sample is a 2 x 2
+// footprint of texels.  A staged entry holds one whole footprint as 8-bit RGB in 16 bytes, one
+// 32-bit word per channel: word c of entry (j, i) holds channel c of texels (x0, y0), (x0 + 1, y0),
+// (x0, y0 + 1), (x0 + 1, y0 + 1) (bytes 0..3) with (x0, y0) = (i - 1, j - 1); texels outside the
+// image are 0 (grid_sample's zero padding).  Entries form planes of (rows + 2) x (cols + 2), one
+// per (frame, camera), covering every footprint whose top-left tap lies in [-1, cols] x
+// [-1, rows]; every entry is written.  A sample is one 16-byte load (half the bytes of two rows
+// of fp16 texel pairs), and a channel's bilinear blend is two 16-bit x 8-bit dot products.
+//
+// 8 bits hold the reference's inputs exactly: images are 8-bit data (python/utils.py:157-205)
+// that estimate_RGBD_panorama receives as float32.  Float inputs are checked while staging: a
+// plane with a value that is not an integer in [0, 255] gets its flag set (plane_flags[plane] =
+// 1), and the sweep samples that plane from the float images themselves.  The guide of every
+// reference camera (rgb2yCbCr + uint8 cast) is written in the same pass, from the float values,
+// as one 32-bit word per pixel (Y, Cb, Cr, 0).
 // ---------------------------------------------------------------------------------------------
 struct StageParams {
     int cameras, references, cols, rows;
     int ref_slot[SSG_MAX_CAMERAS];  // reference slot of each camera, -1 if not a reference
 };
 
+constexpr int kStageTileX = 64, kStageTileY = 16;                         // entries per block
+constexpr int kStageTexX = kStageTileX + 1, kStageTexY = kStageTileY + 1;  // texels they cover
+
 __device__ __forceinline__ float texel_value(float v) { return v; }
 __device__ __forceinline__ float texel_value(uint8_t v) { return (float)v; }
+__device__ __forceinline__ bool is_byte(float v) { return v >= 0.0f && v <= 255.0f && v == rintf(v); }
+__device__ __forceinline__ bool is_byte(uint8_t) { return true; }
 
-__device__ __forceinline__ uint32_t half_bits(float v) { return (uint32_t)__half_as_ushort(__float2half_rn(v)); }
-
+// One block: a kStageTileX x kStageTileY tile of entries from a shared-memory tile of texels.
+// Each thread converts whole texels (three consecutive values: a warp reads 384 contiguous
+// bytes per channel load), checks them and, for the texels that are pixels of this tile, writes
+// their guide word; then each thread assembles entries from the shared tile.
+// blockIdx.y: frame * cameras + camera.
 template <typename Tin>
 __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_constant__ StageParams p,
                                                                   const Tin* __restrict__ images,
                                                                   uint4* __restrict__ staged,
-                                                                  uint8_t* __restrict__ guides)
+                                                                  uint32_t* __restrict__ guides,
+                                                                  int* __restrict__ plane_flags)
 {
-    const int64_t P = (int64_t)p.cols * p.rows;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // entry (y, e), e in [0, cols]
-    if (i >= (int64_t)p.rows * (p.cols + 1)) return;
+    __shared__ uint32_t tex[kStageTexY][kStageTexX];  // RGB bytes, byte 3 zero
+    __shared__ int not_bytes;
+    const int pitch = p.cols + 2;
+    const int64_t P = (int64_t)p.cols * p.rows, plane = (int64_t)pitch * (p.rows + 2);
+    const int tiles_x = (pitch + kStageTileX - 1) / kStageTileX;
+    const int i0 = (blockIdx.x % tiles_x) * kStageTileX, j0 = (blockIdx.x / tiles_x) * kStageTileY;
     const int inst = blockIdx.y;  // frame * cameras + camera
     const int frame = inst / p.cameras, cam = inst % p.cameras;
-    const int y = (int)(i / (p.cols + 1)), e = (int)(i % (p.cols + 1));
-    const Tin* row = images + ((int64_t)inst * P + (int64_t)y * p.cols) * 3;
-    float lo[3] = {0.0f, 0.0f, 0.0f}, hi[3] = {0.0f, 0.0f, 0.0f};
-    if (e >= 1)
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) lo[ch] = texel_value(row[3 * (e - 1) + ch]);
-    if (e < p.cols)
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) hi[ch] = texel_value(row[3 * e + ch]);
-    const int64_t plane = (int64_t)(p.cols + 2) * (p.rows + 2);
-    staged[(int64_t)inst * plane + (int64_t)(y + 1) * (p.cols + 2) + e] =
-        make_uint4(half_bits(lo[0]) | (half_bits(lo[1]) << 16), half_bits(lo[2]) | (half_bits(hi[0]) << 16),
-                   half_bits(hi[1]) | (half_bits(hi[2]) << 16), 0u);
+    const Tin* img = images + (int64_t)inst * P * 3;
     const int slot = p.ref_slot[cam];
-    if (slot >= 0 && e < p.cols) {
-        // utils.py:144-155, the arithmetic of ssg_rgb_to_guide, for pixel (e, y)
-        const float c0 = hi[0], c1 = hi[1], c2 = hi[2];
-        float yy = fadd(fadd(fadd(fmul(c0, 0.1826f), 16.0f), fmul(c1, 0.6142f)), fmul(c2, 0.062f));
-        float cb = fadd(fsub(fsub(128.0f, fmul(c0, 0.1006f)), fmul(c1, 0.3386f)), fmul(c2, 0.4392f));
-        float cr = fsub(fsub(fadd(fmul(c0, 0.4392f), 128.0f), fmul(c1, 0.3989f)), fmul(c2, 0.0403f));
-        // one 32-bit word per pixel: bytes (Y, Cb, Cr, 0)
-        const uint32_t g0 = __float2uint_rz(fminf(fmaxf(yy, 16.0f), 235.0f));
-        const uint32_t g1 = __float2uint_rz(fminf(fmaxf(cb, 16.0f), 240.0f));
-        const uint32_t g2 = __float2uint_rz(fminf(fmaxf(cr, 16.0f), 240.0f));
-        reinterpret_cast<uint32_t*>(guides)[((int64_t)frame * p.references + slot) * P + (int64_t)y * p.cols + e] =
-            g0 | (g1 << 8) | (g2 << 16);
+    uint32_t* guide = slot >= 0 ? guides + ((int64_t)frame * p.references + slot) * P : nullptr;
+    if (threadIdx.x == 0) not_bytes = 0;
+    // texel (x, y), x in [i0 - 1, i0 + kStageTileX - 1], y in [j0 - 1, j0 + kStageTileY - 1]: the
+    // entries' top-left taps and their right / lower neighbours.  The top-left taps are the
+    // pixels whose guide words this block writes.
+    bool bytes = true;
+    for (int t = threadIdx.x; t < kStageTexY * kStageTexX; t += blockDim.x) {
+        const int ly = t / kStageTexX, lx = t % kStageTexX;
+        const int x = i0 - 1 + lx, y = j0 - 1 + ly;
+        uint32_t word = 0;
+        if (x >= 0 && y >= 0 && x < p.cols && y < p.rows) {
+            const int64_t o = (int64_t)y * p.cols + x;
+            const Tin r0 = img[o * 3], r1 = img[o * 3 + 1], r2 = img[o * 3 + 2];
+            const bool ok0 = is_byte(r0), ok1 = is_byte(r1), ok2 = is_byte(r2);
+            bytes = bytes && ok0 && ok1 && ok2;
+            const float c0 = texel_value(r0), c1 = texel_value(r1), c2 = texel_value(r2);
+            word = (ok0 ? (uint32_t)c0 : 0u) | ((ok1 ? (uint32_t)c1 : 0u) << 8) | ((ok2 ? (uint32_t)c2 : 0u) << 16);
+            if (guide && lx < kStageTileX && ly < kStageTileY) {
+                // utils.py:144-155, the arithmetic of ssg_rgb_to_guide, from the input values
+                const float yy = fadd(fadd(fadd(fmul(c0, 0.1826f), 16.0f), fmul(c1, 0.6142f)), fmul(c2, 0.062f));
+                const float cb = fadd(fsub(fsub(128.0f, fmul(c0, 0.1006f)), fmul(c1, 0.3386f)), fmul(c2, 0.4392f));
+                const float cr = fsub(fsub(fadd(fmul(c0, 0.4392f), 128.0f), fmul(c1, 0.3989f)), fmul(c2, 0.0403f));
+                // one 32-bit word per pixel: bytes (Y, Cb, Cr, 0)
+                const uint32_t g0 = __float2uint_rz(fminf(fmaxf(yy, 16.0f), 235.0f));
+                const uint32_t g1 = __float2uint_rz(fminf(fmaxf(cb, 16.0f), 240.0f));
+                const uint32_t g2 = __float2uint_rz(fminf(fmaxf(cr, 16.0f), 240.0f));
+                guide[o] = g0 | (g1 << 8) | (g2 << 16);
+            }
+        }
+        tex[ly][lx] = word;
+    }
+    __syncthreads();  // not_bytes is cleared before any thread sets it
+    if (!bytes) not_bytes = 1;
+    __syncthreads();
+    if (threadIdx.x == 0 && not_bytes) atomicOr(plane_flags + inst, 1);
+    uint4* out = staged + (int64_t)inst * plane;
+    for (int e = threadIdx.x; e < kStageTileX * kStageTileY; e += blockDim.x) {
+        const int li = e % kStageTileX, lj = e / kStageTileX;
+        const int i = i0 + li, j = j0 + lj;
+        if (i >= pitch || j >= p.rows + 2) continue;
+        const uint32_t t00 = tex[lj][li], t10 = tex[lj][li + 1];
+        const uint32_t t01 = tex[lj + 1][li], t11 = tex[lj + 1][li + 1];
+        uint32_t word[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const uint32_t sel = (uint32_t)ch | ((uint32_t)(4 + ch) << 4);
+            word[ch] = __byte_perm(__byte_perm(t00, t10, sel), __byte_perm(t01, t11, sel), 0x5410);
+        }
+        out[(int64_t)j * pitch + i] = make_uint4(word[0], word[1], word[2], 0u);
     }
 }
 
-// the two texels of an entry as float RGB
-__device__ __forceinline__ void unpack_entry(uint4 q, float lo[3], float hi[3])
+// channel c (0..2) of texel k (0: nw, 1: ne, 2: sw, 3: se) of an entry
+__device__ __forceinline__ float entry_texel(const uint4& q, int c, int k)
 {
-    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
-    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
-    const float2 c = __half22float2(*reinterpret_cast<const __half2*>(&q.z));
-    lo[0] = a.x; lo[1] = a.y; lo[2] = b.x;
-    hi[0] = b.y; hi[1] = c.x; hi[2] = c.y;
+    const uint32_t w = c == 0 ? q.x : c == 1 ? q.y : q.z;
+    return (float)((w >> (8 * k)) & 0xFFu);
+}
+
+// the same footprint from the float images (a plane whose values are not all 8-bit integers)
+__device__ __forceinline__ void float_footprint(const float* __restrict__ img, int cols, int rows, int x0, int y0,
+                                                float (&t)[4][3])
+{
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = x0 + (k & 1), y = y0 + (k >> 1);
+        const bool in = x >= 0 && y >= 0 && x < cols && y < rows;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) t[k][ch] = in ? __ldg(img + ((int64_t)y * cols + x) * 3 + ch) : 0.0f;
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -120,30 +172,36 @@ __device__ __forceinline__ void project_pair(float2 x, float2 y, float2 z, const
 }
 
 // Bilinear samples with zero padding (torch grid_sample, align_corners=False, taps nw, ne, sw,
-// se) at two positions, from a bordered plane of texel pairs; `img` points at the entry of texels
-// (-1, 0), (0, 0), `pitch` = cols + 2.  The coordinates are clamped to [-1, cols] x [-1, rows]
-// (a NaN to -1): a sample whose four taps all lie outside the image then reads border zeros, or
-// has weight 0 on its in-image taps, so it is exactly 0 as grid_sample's, without a branch.  The
-// bottom tap row is clamped to the last border row for a sample at row `rows` (its weight is 0).
-__device__ __forceinline__ void sample_pair(const uint4* __restrict__ img, int pitch, float colsf, float rowsf,
-                                            int rows, float2 ix, float2 iy, float (&s)[2][3])
+// se) at two positions of one camera plane.  The coordinates are clamped to [-1, cols] x
+// [-1, rows] (a NaN to -1): a sample whose four taps all lie outside the image then reads a
+// footprint of zeros, or has weight 0 on its in-image taps, so it is exactly 0 as grid_sample's,
+// without a branch.  The tap weights of both samples are returned as (nw, ne, sw, se) = (wa, wb,
+// wc, wd), the top-left taps as x0, y0.
+__device__ __forceinline__ void bilinear_pair(int cols, int rows, float2 ix, float2 iy, float2& x0, float2& y0,
+                                              float2& wa, float2& wb, float2& wc, float2& wd)
 {
+    const float colsf = (float)cols, rowsf = (float)rows;
     ix = make_float2(fminf(fmaxf(ix.x, -1.0f), colsf), fminf(fmaxf(ix.y, -1.0f), colsf));
     iy = make_float2(fminf(fmaxf(iy.x, -1.0f), rowsf), fminf(fmaxf(iy.y, -1.0f), rowsf));
-    const float2 x0 = make_float2(floorf(ix.x), floorf(ix.y)), y0 = make_float2(floorf(iy.x), floorf(iy.y));
+    x0 = make_float2(floorf(ix.x), floorf(ix.y));
+    y0 = make_float2(floorf(iy.x), floorf(iy.y));
     const float2 fx = add2(ix, make_float2(-x0.x, -x0.y)), fy = add2(iy, make_float2(-y0.x, -y0.y));
     const float2 gx = add2(splat(1.0f), make_float2(-fx.x, -fx.y)), gy = add2(splat(1.0f), make_float2(-fy.x, -fy.y));
-    // weights of the taps of both samples: (nw, ne, sw, se)
-    const float2 wa = mul2(gx, gy), wb = mul2(fx, gy), wc = mul2(gx, fy), wd = mul2(fx, fy);
+    wa = mul2(gx, gy);
+    wb = mul2(fx, gy);
+    wc = mul2(gx, fy);
+    wd = mul2(fx, fy);
+}
+
+// Samples of a plane whose values are not all 8-bit integers, from its float image.
+__device__ __forceinline__ void sample_pair_floats(const float* __restrict__ floats, int cols, int rows, float2 ix,
+                                                   float2 iy, float (&s)[2][3])
+{
+    float2 x0, y0, wa, wb, wc, wd;
+    bilinear_pair(cols, rows, ix, iy, x0, y0, wa, wb, wc, wd);
     float t[2][4][3];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int xi = (int)(h ? x0.y : x0.x), yi = (int)(h ? y0.y : y0.x);
-        const uint4* top = img + yi * pitch + xi + 1;  // entry of texels (xi, yi), (xi + 1, yi)
-        const uint4* bot = img + min(yi + 1, rows) * pitch + xi + 1;
-        unpack_entry(__ldg(top), t[h][0], t[h][1]);
-        unpack_entry(__ldg(bot), t[h][2], t[h][3]);
-    }
+    for (int h = 0; h < 2; ++h) float_footprint(floats, cols, rows, (int)(h ? x0.y : x0.x), (int)(h ? y0.y : y0.x), t[h]);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
         float2 v = mul2(wa, make_float2(t[0][0][ch], t[1][0][ch]));
@@ -155,18 +213,126 @@ __device__ __forceinline__ void sample_pair(const uint4* __restrict__ img, int p
     }
 }
 
+// Samples of an 8-bit plane from its footprints (`entries`), in units of 1/65535: the weights
+// are 16-bit fractions of 65535 (a rounding of at most 1/131070 each: a sample moves by at most
+// 4 * 255 / 131070 < 0.008), each channel blended by two dot products of two 16-bit weights
+// with two 8-bit taps.  w * 65535 + 1.5 * 2^23 has round(w * 65535) in the low 16 bits of its
+// representation (one fused multiply-add per weight, for both samples).
+__device__ __forceinline__ void sample_pair_bytes(const uint4* __restrict__ entries, int cols, int rows, float2 ix,
+                                                  float2 iy, uint32_t (&s)[2][3])
+{
+    float2 x0, y0, wa, wb, wc, wd;
+    bilinear_pair(cols, rows, ix, iy, x0, y0, wa, wb, wc, wd);
+    const float2 scale = splat(65535.0f), magic = splat(12582912.0f);
+    const float2 qa = fma2(wa, scale, magic), qb = fma2(wb, scale, magic), qc = fma2(wc, scale, magic),
+                 qd = fma2(wd, scale, magic);
+    // entry index (y0 + 1) * pitch + x0 + 1, exact in float (below 2^24 entries a plane)
+    const float pitchf = (float)(cols + 2);
+    const float2 e = fma2(add2(y0, splat(1.0f)), splat(pitchf), add2(x0, splat(1.0f)));
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t top = __byte_perm(__float_as_uint(h ? qa.y : qa.x), __float_as_uint(h ? qb.y : qb.x), 0x5410);
+        const uint32_t bot = __byte_perm(__float_as_uint(h ? qc.y : qc.x), __float_as_uint(h ? qd.y : qd.x), 0x5410);
+        const uint4 q = __ldg(entries + __float2int_rz(h ? e.y : e.x));
+        s[h][0] = __dp2a_hi(bot, q.x, __dp2a_lo(top, q.x, 0u));
+        s[h][1] = __dp2a_hi(bot, q.y, __dp2a_lo(top, q.y, 0u));
+        s[h][2] = __dp2a_hi(bot, q.z, __dp2a_lo(top, q.z, 0u));
+    }
+}
+
+// The candidate loop of one pixel: points d (R u) + t, projected and sampled in pairs, costs
+// written 8 candidates per cell.  kFloats: the plane is sampled from its float image (the rare
+// path, kept out of line so that its registers do not weigh on the 8-bit path); otherwise the
+// cost sum_c |sample_c - ref_c| is formed in units of 1/65535 with integer absolute differences
+// (the reference texels are integers there).
+template <typename T, bool kFloats, typename V>
+__device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4* __restrict__ entries,
+                                                 const float* __restrict__ floats, int cols, int rows, float2 ax,
+                                                 float2 ay, float2 az, float2 tx, float2 ty, float2 tz,
+                                                 const FastCam& k, const float (&rp)[3], T* __restrict__ out,
+                                                 int64_t chunk_stride)
+{
+    const int chunks = view.chunks();
+    uint32_t rq[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) rq[ch] = (uint32_t)rp[ch] * 65535u;
+    for (int ch = 0; ch < chunks; ++ch) {
+        uint32_t packed[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+            const float2 d = view.cand2(ch * 8 + j);
+            float2 u, v;
+            project_pair(fma2(d, ax, tx), fma2(d, ay, ty), fma2(d, az, tz), k, u, v);
+            float c2[2];
+            if constexpr (kFloats) {
+                float s[2][3];
+                sample_pair_floats(floats, cols, rows, u, v, s);
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    c2[h] = fminf(fabsf(s[h][0] - rp[0]) + fabsf(s[h][1] - rp[1]) + fabsf(s[h][2] - rp[2]), 500.0f);
+            } else {
+                uint32_t s[2][3];
+                sample_pair_bytes(entries, cols, rows, u, v, s);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t sad = __usad(s[h][2], rq[2], __usad(s[h][1], rq[1], __usad(s[h][0], rq[0], 0u)));
+                    c2[h] = (float)min(sad, 500u * 65535u);
+                }
+                const float2 c = mul2(make_float2(c2[0], c2[1]), splat(1.0f / 65535.0f));
+                c2[0] = c.x;
+                c2[1] = c.y;
+            }
+            packed[j / 2] = Cell<T>::pack2(c2[0], c2[1]);
+        }
+        reinterpret_cast<uint4*>(out + ch * chunk_stride)[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
+}
+
+template <typename T, bool kFloats, typename V>
+__device__ __forceinline__ void sweep_candidates(const V& view, const uint4* __restrict__ entries,
+                                                 const float* __restrict__ floats, int cols, int rows, float2 ax,
+                                                 float2 ay, float2 az, float2 tx, float2 ty, float2 tz,
+                                                 const FastCam& k, const float (&rp)[3], T* __restrict__ out,
+                                                 int64_t chunk_stride)
+{
+    sweep_candidates_body<T, kFloats>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, out,
+                                      chunk_stride);
+}
+
+template <typename T, typename V>
+__device__ __noinline__ void sweep_candidates_floats(const V view, const float* __restrict__ floats, int cols,
+                                                     int rows, float2 ax, float2 ay, float2 az, float2 tx, float2 ty,
+                                                     float2 tz, const FastCam k, float r0, float r1, float r2,
+                                                     T* __restrict__ out, int64_t chunk_stride)
+{
+    const float rp[3] = {r0, r1, r2};
+    sweep_candidates_body<T, true>(view, nullptr, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, out,
+                                   chunk_stride);
+}
+
 // Sweep + cost of one reference pixel (x, y) over all candidates, into its cells (`out`, chunk
 // stride `chunk_stride`).  `V` gives the instance's constants: ref_cam(), cam(c), pose(c) (12
-// floats), cand(k) (pairs are read as float2) and cameras(), chunks().  `frame_img` points at row
-// 0, entry 0 of the frame's camera 0 plane; planes are `plane` entries apart.
+// floats), cand(k) (pairs are read as float2) and cameras(), chunks().  `frame_entries` /
+// `frame_floats` point at the frame's camera-0 plane of footprints / float image (planes `plane`
+// entries / cols x rows x 3 floats apart), `flags` at the frame's per-camera flags.
 template <typename T, typename V>
-__device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restrict__ frame_img, int plane,
-                                            int ref_camera, int cols, int rows, int x, int y, int sel,
+__device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restrict__ frame_entries,
+                                            const float* __restrict__ frame_floats, const int* __restrict__ flags,
+                                            int plane, int ref_camera, int cols, int rows, int x, int y, int sel,
                                             T* __restrict__ out, int64_t chunk_stride)
 {
     const int pitch = cols + 2;
-    float rp[3], unused[3];
-    unpack_entry(__ldg(frame_img + (int64_t)ref_camera * plane + y * pitch + x + 1), rp, unused);
+    const int64_t P = (int64_t)cols * rows;
+    float rp[3];
+    if (!__ldg(flags + ref_camera)) {
+        // the footprint of top-left tap (x, y): its nw texel is the pixel
+        const uint4 q = __ldg(frame_entries + (int64_t)ref_camera * plane + (y + 1) * pitch + x + 1);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) rp[ch] = entry_texel(q, ch, 0);
+    } else {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) rp[ch] = __ldg(frame_floats + (ref_camera * P + (int64_t)y * cols + x) * 3 + ch);
+    }
     const int chunks = view.chunks();
     if (sel < 0 || sel >= view.cameras()) {
         // no camera sees the point: grid_sample of an all-zero image (depth_estimation.py:166)
@@ -187,25 +353,14 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
     const float2 az = splat(fmaf(m[10], pu[2], fmaf(m[9], pu[1], m[8] * pu[0])));
     const float2 tx = splat(m[3]), ty = splat(m[7]), tz = splat(m[11]);
     const FastCam k = view.cam(sel);
-    const uint4* img = frame_img + (int64_t)sel * plane;
-    const float colsf = (float)cols, rowsf = (float)rows;
-    for (int ch = 0; ch < chunks; ++ch) {
-        uint32_t packed[4];
-#pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-            const float2 d = view.cand2(ch * 8 + j);
-            float2 u, v;
-            project_pair(fma2(d, ax, tx), fma2(d, ay, ty), fma2(d, az, tz), k, u, v);
-            float s[2][3];
-            sample_pair(img, pitch, colsf, rowsf, rows, u, v, s);
-            float c2[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h)
-                c2[h] = fminf(fabsf(s[h][0] - rp[0]) + fabsf(s[h][1] - rp[1]) + fabsf(s[h][2] - rp[2]), 500.0f);
-            packed[j / 2] = Cell<T>::pack2(c2[0], c2[1]);
-        }
-        reinterpret_cast<uint4*>(out + ch * chunk_stride)[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-    }
+    const uint4* entries = frame_entries + (int64_t)sel * plane;
+    const float* floats = frame_floats ? frame_floats + sel * P * 3 : nullptr;
+    if ((__ldg(flags + sel) || __ldg(flags + ref_camera)) && floats)
+        sweep_candidates_floats<T>(view, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp[0], rp[1], rp[2], out,
+                                   chunk_stride);
+    else
+        sweep_candidates<T, false>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, out,
+                                   chunk_stride);
 }
 
 // the constants of one reference slot of a uniform batch (kernel parameters)
@@ -239,10 +394,9 @@ struct SweepShape<2> {
 
 template <typename T, int V>
 __global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
-    sweep_batch_kernel(const __grid_constant__ FastSweepParams p,
-                                                                const uint4* __restrict__ staged,
-                                                                const int8_t* __restrict__ selected,
-                                                                T* __restrict__ cost)
+    sweep_batch_kernel(const __grid_constant__ FastSweepParams p, const uint4* __restrict__ staged,
+                       const float* __restrict__ floats, const int* __restrict__ plane_flags,
+                       const int8_t* __restrict__ selected, T* __restrict__ cost)
 {
     const int cols = p.cols, rows = p.rows, pitch = cols + 2;
     const int P = cols * rows;
@@ -251,10 +405,11 @@ __global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
     const int inst = blockIdx.y;  // frame * references + slot
     const int frame = inst / p.references, slot = inst % p.references;
     const int plane = pitch * (rows + 2);
-    const uint4* frame_img = staged + (int64_t)frame * p.cameras * plane + pitch;  // row 0, entry 0 of camera 0
     T* out = cost + (int64_t)inst * p.chunks * P * 8 + (int64_t)i * 8;
-    sweep_pixel<T>(UniformView{p, slot}, frame_img, plane, p.ref_index[slot], cols, rows, i % cols, i / cols,
-                   selected[(int64_t)slot * P + i], out, (int64_t)P * 8);
+    sweep_pixel<T>(UniformView{p, slot}, staged + (int64_t)frame * p.cameras * plane,
+                   floats ? floats + (int64_t)frame * p.cameras * P * 3 : nullptr, plane_flags + frame * p.cameras,
+                   plane, p.ref_index[slot], cols, rows, i % cols, i / cols, selected[(int64_t)slot * P + i], out,
+                   (int64_t)P * 8);
 }
 
 // the constants of one instance of an uneven batch (device memory)
@@ -302,8 +457,8 @@ __global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
                 const int i = (first + u - I->tile_begin) * kSweepTile + j;
                 if (i < P) {
                     T* out = static_cast<T*>(I->cost) + (int64_t)i * 8;
-                    sweep_pixel<T>(InstView{I}, I->staged, plane, I->ref_camera, cols, rows, i % cols, i / cols,
-                                   I->selected[i], out, (int64_t)P * 8);
+                    sweep_pixel<T>(InstView{I}, I->staged, I->floats, I->plane_flags, plane, I->ref_camera, cols,
+                                   rows, i % cols, i / cols, I->selected[i], out, (int64_t)P * 8);
                 }
             }
         }
@@ -346,22 +501,22 @@ int launch_sweep_uneven(const SweepInst* d_insts, int instances, int total_tiles
 }
 
 template <typename T, int V>
-static void launch_sweep_shape(const FastSweepParams& p, const uint4* staged, const int8_t* selected, T* cost,
-                               int64_t P, int instances, cudaStream_t st)
+static void launch_sweep_shape(const FastSweepParams& p, const uint4* staged, const float* floats, const int* flags,
+                               const int8_t* selected, T* cost, int64_t P, int instances, cudaStream_t st)
 {
     constexpr int threads = SweepShape<V>::threads;
     const dim3 grid(grid_1d(P, threads), instances);
-    sweep_batch_kernel<T, V><<<grid, threads, 0, st>>>(p, staged, selected, cost);
+    sweep_batch_kernel<T, V><<<grid, threads, 0, st>>>(p, staged, floats, flags, selected, cost);
 }
 
 template <typename T>
-static void launch_sweep(const FastSweepParams& p, const uint4* staged, const int8_t* selected, T* cost, int64_t P,
-                         int instances, cudaStream_t st)
+static void launch_sweep(const FastSweepParams& p, const uint4* staged, const float* floats, const int* flags,
+                         const int8_t* selected, T* cost, int64_t P, int instances, cudaStream_t st)
 {
     switch (tuning(SSG_TUNE_SWEEP_VARIANT)) {
-        case 1: launch_sweep_shape<T, 1>(p, staged, selected, cost, P, instances, st); break;
-        case 2: launch_sweep_shape<T, 2>(p, staged, selected, cost, P, instances, st); break;
-        default: launch_sweep_shape<T, 0>(p, staged, selected, cost, P, instances, st); break;
+        case 1: launch_sweep_shape<T, 1>(p, staged, floats, flags, selected, cost, P, instances, st); break;
+        case 2: launch_sweep_shape<T, 2>(p, staged, floats, flags, selected, cost, P, instances, st); break;
+        default: launch_sweep_shape<T, 0>(p, staged, floats, flags, selected, cost, P, instances, st); break;
     }
 }
 
@@ -390,9 +545,9 @@ static int staged_plane_fits(int cols, int rows)
 template <typename Tin>
 static int stage_images(const Tin* d_images, int frames, int cameras, int cols, int rows,
                         const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
-                        void* stream)
+                        int32_t* d_plane_flags, void* stream)
 {
-    SSG_REQUIRE(d_images && d_staged && d_guides && reference_cameras, "null pointer");
+    SSG_REQUIRE(d_images && d_staged && d_guides && d_plane_flags && reference_cameras, "null pointer");
     SSG_REQUIRE(frames >= 1 && frames <= 65535 / SSG_MAX_CAMERAS, "frames %d outside [1, %d]", frames,
                 65535 / SSG_MAX_CAMERAS);
     SSG_REQUIRE(cameras >= 1 && cameras <= SSG_MAX_CAMERAS && references >= 1 && references <= SSG_MAX_REFERENCES,
@@ -410,35 +565,76 @@ static int stage_images(const Tin* d_images, int frames, int cameras, int cols, 
         SSG_REQUIRE(reference_cameras[r] >= 0 && reference_cameras[r] < cameras, "reference camera out of range");
         p.ref_slot[reference_cameras[r]] = r;
     }
-    dim3 grid(grid_1d((int64_t)(cols + 1) * rows, kBatchBlock), frames * cameras);
-    stage_images_kernel<Tin><<<grid, kBatchBlock, 0, as_stream(stream)>>>(p, d_images,
-                                                                         reinterpret_cast<uint4*>(d_staged), d_guides);
+    const cudaError_t e = cudaMemsetAsync(d_plane_flags, 0, sizeof(int32_t) * frames * cameras, as_stream(stream));
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    const int64_t tiles = (int64_t)((cols + 2 + kStageTileX - 1) / kStageTileX) *
+                          ((rows + 2 + kStageTileY - 1) / kStageTileY);
+    SSG_REQUIRE(tiles < ((int64_t)1 << 31), "images of %dx%d pixels are too large", cols, rows);
+    dim3 grid((unsigned)tiles, frames * cameras);
+    stage_images_kernel<Tin><<<grid, kBatchBlock, 0, as_stream(stream)>>>(
+        p, d_images, reinterpret_cast<uint4*>(d_staged), reinterpret_cast<uint32_t*>(d_guides), d_plane_flags);
     return launch_status("stage_images_kernel");
+}
+
+// float32 -> uint8 truncation (the reference's float -> uint8 copy of the images to stitch,
+// python/depth_estimation.py:239-240): 16 values per thread, four 16-byte loads and one store
+template <bool kAligned>
+__global__ void __launch_bounds__(kBatchBlock) convert_u8_kernel(const float* __restrict__ src,
+                                                                 uint8_t* __restrict__ dst, int64_t n)
+{
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 16;
+    if (kAligned && i + 16 <= n) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(src + i) + q);
+            w[q] = __float2uint_rz(v.x) | (__float2uint_rz(v.y) << 8) | (__float2uint_rz(v.z) << 16) |
+                   (__float2uint_rz(v.w) << 24);
+        }
+        reinterpret_cast<uint4*>(dst + i)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    } else {
+        for (int64_t k = i; k < n; ++k) dst[k] = (uint8_t)__float2uint_rz(src[k]);
+    }
+}
+
+extern "C" int ssg_convert_u8(const float* d_src, uint8_t* d_dst, int64_t count, void* stream)
+{
+    SSG_REQUIRE(d_src && d_dst, "null pointer");
+    SSG_REQUIRE(count >= 0, "negative count");
+    if (count == 0) return SSG_OK;
+    const int grid = grid_1d((count + 15) / 16, kBatchBlock);
+    if (((uintptr_t)d_src & 15) == 0 && ((uintptr_t)d_dst & 15) == 0)
+        convert_u8_kernel<true><<<grid, kBatchBlock, 0, as_stream(stream)>>>(d_src, d_dst, count);
+    else
+        convert_u8_kernel<false><<<grid, kBatchBlock, 0, as_stream(stream)>>>(d_src, d_dst, count);
+    return launch_status("convert_u8_kernel");
 }
 
 extern "C" int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                                 const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
-                                void* stream)
+                                int32_t* d_plane_flags, void* stream)
 {
     return stage_images(d_images, frames, cameras, cols, rows, reference_cameras, references, d_staged, d_guides,
-                        stream);
+                        d_plane_flags, stream);
 }
 
 extern "C" int ssg_stage_images_u8(const uint8_t* d_images, int frames, int cameras, int cols, int rows,
                                    const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
-                                   void* stream)
+                                   int32_t* d_plane_flags, void* stream)
 {
     return stage_images(d_images, frames, cameras, cols, rows, reference_cameras, references, d_staged, d_guides,
-                        stream);
+                        d_plane_flags, stream);
 }
 
 extern "C" int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_count, const ssg_camera* cameras,
                                     int references, const int* reference_cameras, const float* relative_poses,
-                                    const float* d_staged, const int8_t* d_selected, const float* candidates,
-                                    int candidate_count, int storage, void* d_cost, void* stream)
+                                    const float* d_staged, const float* d_images, const int32_t* d_plane_flags,
+                                    const int8_t* d_selected, const float* candidates, int candidate_count,
+                                    int storage, void* d_cost, void* stream)
 {
     if (int e = staged_plane_fits(cols, rows)) return e;
-    SSG_REQUIRE(cameras && reference_cameras && relative_poses && d_staged && d_selected && candidates && d_cost,
+    SSG_REQUIRE(cameras && reference_cameras && relative_poses && d_staged && d_plane_flags && d_selected &&
+                    candidates && d_cost,
                 "null pointer");
     SSG_REQUIRE(camera_count >= 1 && camera_count <= SSG_MAX_CAMERAS, "camera_count out of range");
     SSG_REQUIRE(references >= 1 && references <= SSG_MAX_REFERENCES, "references out of range");
@@ -472,10 +668,10 @@ extern "C" int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_c
     const int64_t P = (int64_t)cols * rows;
     const uint4* staged = reinterpret_cast<const uint4*>(d_staged);
     if (storage == SSG_STORAGE_F16)
-        launch_sweep<__half>(p, staged, d_selected, static_cast<__half*>(d_cost), P, frames * references,
-                             as_stream(stream));
+        launch_sweep<__half>(p, staged, d_images, d_plane_flags, d_selected, static_cast<__half*>(d_cost), P,
+                             frames * references, as_stream(stream));
     else
-        launch_sweep<uint16_t>(p, staged, d_selected, static_cast<uint16_t*>(d_cost), P, frames * references,
-                               as_stream(stream));
+        launch_sweep<uint16_t>(p, staged, d_images, d_plane_flags, d_selected, static_cast<uint16_t*>(d_cost), P,
+                               frames * references, as_stream(stream));
     return launch_status("sweep_batch_kernel");
 }

@@ -65,8 +65,8 @@ static int check_instance(const ssg_uneven_instance& in, int i)
                 "instance %d: candidate_count out of range", i);
     SSG_REQUIRE(in.cameras && in.relative_poses && in.candidates, "instance %d: null host array", i);
     SSG_REQUIRE(in.sigma_i > 0 && in.sigma_s > 0, "instance %d: sigmas must be positive", i);
-    SSG_REQUIRE(in.d_staged && in.d_selected && in.d_guides && in.d_costs && in.d_df_guides && in.d_df_costs &&
-                    in.d_distance_raw && in.d_distance,
+    SSG_REQUIRE(in.d_staged && in.d_plane_flags && in.d_selected && in.d_guides && in.d_costs && in.d_df_guides &&
+                    in.d_df_costs && in.d_distance_raw && in.d_distance,
                 "instance %d: null device pointer", i);
     SSG_REQUIRE(((uintptr_t)in.d_staged & 15) == 0, "instance %d: staged planes must be 16-byte aligned", i);
     const int L = ssg_isb_level_count(in.cols, in.rows);
@@ -143,7 +143,9 @@ extern "C" int ssg_uneven_create(const ssg_uneven_instance* instances, int insta
         s.tile_begin = (int)tiles;
         tiles += s.tiles;
         s.storage = storage;
-        s.staged = reinterpret_cast<const uint4*>(in.d_staged) + (in.cols + 2);
+        s.staged = reinterpret_cast<const uint4*>(in.d_staged);
+        s.floats = in.d_images;
+        s.plane_flags = in.d_plane_flags;
         s.selected = in.d_selected;
         s.cost = in.d_costs[0];
         s.ref_cam = make_torch_cam(in.cameras[in.reference_camera]);

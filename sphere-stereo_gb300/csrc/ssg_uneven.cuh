@@ -18,7 +18,9 @@ struct SweepInst {
     int cols, rows, cameras, ncand;
     int chunks, ref_camera, tile_begin, tiles;
     int storage, pad0, pad1, pad2;
-    const uint4* staged;     // row 0, entry 0 of camera 0's bordered plane of the instance's frame
+    const uint4* staged;     // camera 0's plane of footprints of the instance's frame
+    const float* floats;     // camera 0's float image of the frame (planes with flags set), or NULL
+    const int* plane_flags;  // per camera of the frame: 1 where the plane is sampled from `floats`
     const int8_t* selected;  // rows x cols
     void* cost;              // chunks x rows x cols x 8, 16-bit
     TorchCam ref_cam;

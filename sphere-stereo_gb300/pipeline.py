@@ -4,7 +4,7 @@ volume (coarser levels float32) with fp32 arithmetic, optional CUDA-graph captur
 One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_panorama
 (python/depth_estimation.py:205-242) for all F x R (frame, reference) instances at once:
 
-    ssg_stage_images[_u8]          inputs -> fp16 texel pairs + guides of the references 1 launch
+    ssg_stage_images[_u8]          inputs -> 8-bit footprints + guides of the references 1 launch
     ssg_sweep_cost_batch           sweep + cost, 16-bit chunked volume                  1
     ssg_isb_downsample_batch       L - 1 levels                                         L - 1
     ssg_isb_upsample_batch         levels L - 2 .. 1                                    L - 2
@@ -57,9 +57,10 @@ class BatchPipeline:
         u8 = dict(dtype=torch.uint8, device=dev)
         f32 = dict(dtype=torch.float32, device=dev)
         i16 = dict(dtype=torch.int16, device=dev)
-        # planes of 16-byte texel-pair entries with a zero border, (rows + 2) x (cols + 2); the
-        # border is never written
+        # planes of 16-byte bilinear footprints (8-bit RGB), (rows + 2) x (cols + 2) per camera, and
+        # a flag per plane for the planes sampled from the float images instead
         self.staged = torch.zeros(F * C * (self.rows + 2) * (self.cols + 2) * 4, **f32)
+        self.plane_flags = torch.zeros(F * C, dtype=torch.int32, device=dev)
         # guides: one 32-bit word per pixel (Y, Cb, Cr, 0)
         self.guides = [torch.empty(F * R * r * c * 4, **u8) for r, c in self.shapes]
         # level 0 (the sweep's output) 16-bit, coarser levels float32
@@ -95,10 +96,11 @@ class BatchPipeline:
         cols, rows, P = self.cols, self.rows, self.P
         stage = "ssg_stage_images_u8" if match.dtype == torch.uint8 else "ssg_stage_images"
         N.call(stage, match.data_ptr(), frames, self.C, cols, rows, self._refs, self.R, self.staged.data_ptr(),
-               self.guides[0].data_ptr(), stream)
+               self.guides[0].data_ptr(), self.plane_flags.data_ptr(), stream)
+        floats = None if match.dtype == torch.uint8 else match.data_ptr()
         N.call("ssg_sweep_cost_batch", cols, rows, frames, self.C, e._cams, self.R, self._refs, self._poses,
-               self.staged.data_ptr(), self.selected.data_ptr(), e._candidates, self.N, self.storage,
-               self.costs[0].data_ptr(), stream)
+               self.staged.data_ptr(), floats, self.plane_flags.data_ptr(), self.selected.data_ptr(), e._candidates,
+               self.N, self.storage, self.costs[0].data_ptr(), stream)
         var_inv_i = 1 / (2 * e.sigma_i * e.sigma_i)
         L = self.L
         if L >= 2:
@@ -114,17 +116,20 @@ class BatchPipeline:
                 N.call("ssg_isb_upsample_batch", self.guides[s + 1].data_ptr(), self.costs[s + 1].data_ptr(), rc, cc,
                        self.guides[s].data_ptr(), self.costs[s].data_ptr(), rf, cf, self.N, inst, F32, wu, wd,
                        var_inv_i, stream)
+        # the selection writes the raw distance and, for the post-filter to filter in place, a copy
+        dist = self.distance.view(-1)[: inst * P]
+        if L >= 2:
             (rc, cc) = self.shapes[1]
             wu, wd = weights[0]
             N.call("ssg_isb_upsample_select_batch", self.guides[1].data_ptr(), self.costs[1].data_ptr(), rc, cc,
                    self.guides[0].data_ptr(), self.costs[0].data_ptr(), rows, cols, self.N, inst, self.storage, wu, wd,
-                   var_inv_i, e._candidates, self.distance_raw.data_ptr(), self.index.data_ptr(), stream)
+                   var_inv_i, e._candidates, self.distance_raw.data_ptr(), self.index.data_ptr(), dist.data_ptr(),
+                   stream)
         else:
             N.call("ssg_select_distance_batch", self.costs[0].data_ptr(), self.N, P, inst, self.storage,
                    e._candidates, self.distance_raw.data_ptr(), self.index.data_ptr(), stream)
+            dist.copy_(self.distance_raw[: inst * P])
         # distance post-filter on the unfiltered guide (python/depth_estimation.py:200-203)
-        dist = self.distance.view(-1)[: inst * P]
-        dist.copy_(self.distance_raw[: inst * P])
         if L >= 2:
             N.call("ssg_isb_apply_batch", N.pointers([g.data_ptr() for g in self.df_guides]),
                    N.pointers([dist.data_ptr()] + [c.data_ptr() for c in self.df_costs]), L, rows, cols, 1, inst,
@@ -134,7 +139,9 @@ class BatchPipeline:
             images_u8 = stitch
         else:
             images_u8 = self.images_u8
-            images_u8[:frames].copy_(stitch[:frames])  # float -> uint8 truncation (depth_estimation.py:239)
+            # float -> uint8 truncation (depth_estimation.py:239)
+            N.call("ssg_convert_u8", stitch.data_ptr(), images_u8.data_ptr(), frames * self.R * st.image_rows *
+                   st.image_cols * 3, stream)
         N.call("ssg_reproject_distance_batch", dist.data_ptr(), self.reprojected.data_ptr(), cols, rows, inst, self.R,
                st._intr, st._trans, 1, stream)
         N.call("ssg_inpaint_holes_batch", self.reprojected.data_ptr(), self.tables.data_ptr(), self.stamps.data_ptr(),

@@ -5,7 +5,7 @@ frame per call of estimate_RGBD_panorama, python/depth_estimation.py:205-242).
 Each job is one frame of one rig, described by an RGBD_Estimator built for that rig (camera
 selection, candidates and stitcher tables come from it).  Per batch:
 
-    ssg_stage_images[_u8]    one launch per job (inputs -> fp16 texel planes + guides)
+    ssg_stage_images[_u8]    one launch per job (inputs -> 8-bit footprint planes + guides)
     ssg_uneven_run           one persistent sweep launch over every instance, one launch per
                              cost-filter and post-filter step, the fused selection, then fill,
                              reprojection, hole lists and merge over every job
@@ -70,6 +70,7 @@ class UnevenBatch:
                 "match": torch.zeros(C, rows, cols, 3, dtype=input_dtype, device=dev),
                 "stitch": torch.zeros(R, st.image_rows, st.image_cols, 3, dtype=input_dtype, device=dev),
                 "staged": torch.zeros(C * (rows + 2) * (cols + 2) * 4, **f32),
+                "flags": torch.zeros(C, dtype=torch.int32, device=dev),
                 "guide0": torch.empty(R * rows * cols * 4, **u8),  # 32-bit guide words
                 "distance": torch.empty(R, rows, cols, **f32),
                 "rgb": torch.empty(st.pano_rows, st.pano_cols, 3, **u8),
@@ -104,7 +105,9 @@ class UnevenBatch:
                     relative_poses=ctypes.cast(arrays["poses"], ctypes.c_void_p),
                     candidates=ctypes.cast(arrays["candidates"], ctypes.c_void_p),
                     sigma_i=float(e.sigma_i), sigma_s=float(e.sigma_s),
-                    d_staged=j["staged"].data_ptr(), d_selected=e._selected[slot].data_ptr(),
+                    d_staged=j["staged"].data_ptr(),
+                    d_images=None if input_dtype == torch.uint8 else j["match"].data_ptr(),
+                    d_plane_flags=j["flags"].data_ptr(), d_selected=e._selected[slot].data_ptr(),
                     d_guides=ctypes.cast(arrays["guides"], ctypes.c_void_p),
                     d_costs=ctypes.cast(arrays["costs"], ctypes.c_void_p),
                     d_df_guides=ctypes.cast(arrays["df_guides"], ctypes.c_void_p),
@@ -159,10 +162,12 @@ class UnevenBatch:
             cols, rows = e.matching_resolution
             stage = "ssg_stage_images_u8" if self.input_dtype == torch.uint8 else "ssg_stage_images"
             N.call(stage, j["match"].data_ptr(), 1, len(e.calibrations), cols, rows, j["refs"],
-                   len(e.references_indices), j["staged"].data_ptr(), j["guide0"].data_ptr(), stream)
+                   len(e.references_indices), j["staged"].data_ptr(), j["guide0"].data_ptr(), j["flags"].data_ptr(),
+                   stream)
             if j["images_u8"] is not None:
-                with torch.cuda.stream(torch.cuda.ExternalStream(stream, device=self.device)):
-                    j["images_u8"].copy_(j["stitch"])  # float -> uint8 truncation (depth_estimation.py:239)
+                # float -> uint8 truncation (depth_estimation.py:239)
+                N.call("ssg_convert_u8", j["stitch"].data_ptr(), j["images_u8"].data_ptr(), j["stitch"].numel(),
+                       stream)
         N.call("ssg_uneven_run", self._handle, stream)
 
     def _apply_tuning(self, stream: int) -> None:

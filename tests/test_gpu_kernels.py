@@ -260,3 +260,15 @@ def test_merge_from_identical_inputs(ss, native, small_rig, golden_small):
 
     assert psnr(st.RGB_panorama.cpu().numpy(), want_rgb) >= 60
     np.testing.assert_allclose(st.distance_panorama.cpu().numpy(), want_d, rtol=1e-5)
+
+
+@pytest.mark.parametrize("offset", [0, 1])
+def test_convert_u8_matches_torch(ss, native, offset):
+    """The float -> uint8 conversion of the images to stitch truncates like torch's copy, with
+    and without 16-byte alignment and with a ragged tail."""
+    rng = np.random.default_rng(11)
+    n = 16 * 1000 + 7
+    src = torch.as_tensor(rng.uniform(0, 255.999, n + offset).astype(np.float32), device=DEV)[offset:]
+    dst = torch.empty(n + offset, dtype=torch.uint8, device=DEV)[offset:]
+    ss._native.call("ssg_convert_u8", src.data_ptr(), dst.data_ptr(), n, torch.cuda.current_stream().cuda_stream)
+    assert torch.equal(dst, src.to(torch.uint8))
