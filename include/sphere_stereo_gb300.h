@@ -469,6 +469,46 @@ SSG_API int ssg_uneven_run(const ssg_uneven_batch* batch, void* stream);
 SSG_API int ssg_uneven_launches(const ssg_uneven_batch* batch);
 SSG_API void ssg_uneven_destroy(ssg_uneven_batch* batch);
 
+/* ---------------------------------------------------------------------------------------------
+ * Input preparation: the resize of decoded images to the matching and stitching resolutions
+ * (python/utils.py:198-201), on the device.
+ * ------------------------------------------------------------------------------------------- */
+#define SSG_PIXEL_U8 0
+#define SSG_PIXEL_F32 1
+
+/* Linear resize of `images` images (contiguous) of src_cols x src_rows x channels (1..4,
+ * interleaved) to dst_cols x dst_rows: the interpolation the reference's
+ * cv2.resize(image, size, cv2.INTER_AREA) call performs (its third positional argument is `dst`,
+ * so the default INTER_LINEAR applies), restated from OpenCV's published algorithm: pixel-centre
+ * mapping, edge clamping, separately rounded float products and sums; an exact 2x reduction is a
+ * 2x2 average.  Types: uint8 -> float32 (the reference converts decoded images to float32 and
+ * resizes those), float32 -> float32, and uint8 -> uint8 with 11-bit fixed-point weights (its
+ * ground-truth resize, utils.py:221-222).  One launch. */
+SSG_API int ssg_resize_linear(const void* d_src, int src_type, int src_cols, int src_rows, int channels, void* d_dst,
+                              int dst_type, int dst_cols, int dst_rows, int images, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Evaluation against ground truth (python/utils.py:206-250, evaluate_rgbd_panorama): the
+ * reference computes these per frame on the host with scikit-image and numpy; here a batch of
+ * frames is reduced on the device.
+ * ------------------------------------------------------------------------------------------- */
+#define SSG_EVAL_MAX_THRESHOLDS 16
+#define SSG_EVAL_FIXED_METRICS 4 /* psnr, ssim, mae, rmse */
+
+/* Bytes of the scratch ssg_eval_panoramas needs (8-byte aligned); 0 for invalid arguments. */
+SSG_API size_t ssg_eval_scratch_bytes(int frames, int threshold_count);
+/* Metrics of `frames` RGB-D panoramas of cols x rows (contiguous per frame) against their ground
+ * truth: d_rgb / d_gt_rgb uint8 [rows][cols][3], d_inv_distance / d_gt_inv_distance float32
+ * [rows][cols] (inverse distances, python/main.py:114).  d_metrics (float64, device) receives per
+ * frame psnr, ssim, mae, rmse, then threshold_count bad-pixel ratios in percent (thresholds: host
+ * array), with the definitions of peak_signal_noise_ratio(gt, est), structural_similarity(gt, est,
+ * multichannel=True) on x / 255 float32 images and the reference's numpy expressions
+ * (utils.py:230-244).  Panoramas must be at least 7 x 7 (the SSIM window).  Deterministic: fixed
+ * reduction order.  Three launches. */
+SSG_API int ssg_eval_panoramas(int cols, int rows, int frames, const uint8_t* d_rgb, const uint8_t* d_gt_rgb,
+                               const float* d_inv_distance, const float* d_gt_inv_distance, const float* thresholds,
+                               int threshold_count, void* d_scratch, double* d_metrics, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

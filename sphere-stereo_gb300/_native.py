@@ -28,6 +28,10 @@ TUNE_HOLE_BLOCKS_PER_SM = 1
 TUNE_MERGE_FRAMES = 2
 TUNE_UNEVEN_SPAN = 3
 TUNE_ISB_UP_BLOCKS = 4
+PIXEL_U8 = 0
+PIXEL_F32 = 1
+SSG_EVAL_MAX_THRESHOLDS = 16
+SSG_EVAL_FIXED_METRICS = 4
 
 
 class NativeLibraryError(RuntimeError):
@@ -125,6 +129,9 @@ SIGNATURES = {
     "ssg_uneven_launches": (_I, [_P]),
     "ssg_uneven_destroy": (None, [_P]),
     "ssg_merge_panorama_batch_approx": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "ssg_resize_linear": (_I, [_P, _I, _I, _I, _I, _P, _I, _I, _I, _I, _P]),
+    "ssg_eval_scratch_bytes": (ctypes.c_size_t, [_I, _I]),
+    "ssg_eval_panoramas": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
 }
 
 _lock = threading.Lock()
@@ -222,8 +229,10 @@ def pointers(values) -> ctypes.Array:
 def kernels_launched(name: str, args) -> int:
     """Number of kernels one call of entry point ``name`` with ``args`` launches."""
     if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count", "ssg_tuning_set",
-                "ssg_tuning_get", "ssg_tuning_choices"):
+                "ssg_tuning_get", "ssg_tuning_choices", "ssg_eval_scratch_bytes"):
         return 0
+    if name == "ssg_eval_panoramas":
+        return 3
     if name in ("ssg_isb_apply", "ssg_isb_apply_batch"):
         return 2 * max(0, int(args[2]) - 1)
     if name == "ssg_reproject_distance":

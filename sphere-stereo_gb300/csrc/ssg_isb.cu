@@ -14,12 +14,72 @@
 // (ssg_isb_common.cuh), so both layouts give the same bits; the batched path differs from the
 // reference only by the 16-bit rounding of its level-0 volume.
 #include <cmath>
+#include <cstring>
+#include <mutex>
 
 #include "ssg_cells.cuh"
 #include "ssg_isb_common.cuh"
 #include "ssg_uneven.cuh"
 
 namespace ssg {
+
+// ---------------------------------------------------------------------------------------------
+// Range-weight tables: one per distinct var_inv_i, evaluated once by a kernel with the same
+// device function as the per-block tables, so the values are the same bits.
+// ---------------------------------------------------------------------------------------------
+constexpr int kRangeTableSlots = 64;
+__device__ float g_range_tables[kRangeTableSlots][kRangeLutStride];
+
+__global__ void range_table_kernel(float* __restrict__ table, float var_inv_i)
+{
+    for (int d = threadIdx.x; d < kRangeLutStride; d += blockDim.x)
+        table[d] = d < kRangeLutSize ? range_weight((float)d, var_inv_i) : 0.0f;
+}
+
+const float* range_table(float var_inv_i, cudaStream_t stream)
+{
+    struct Device {
+        uint32_t key[kRangeTableSlots];
+        int used = 0;
+        float* base = nullptr;
+    };
+    constexpr int kMaxDevices = 64;
+    static std::mutex mutex;
+    static Device devices[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    uint32_t key;
+    std::memcpy(&key, &var_inv_i, sizeof key);
+    std::lock_guard<std::mutex> lock(mutex);
+    Device& D = devices[dev];
+    for (int s = 0; s < D.used; ++s)
+        if (D.key[s] == key) return D.base + (int64_t)s * kRangeLutStride;
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &capture) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (capture != cudaStreamCaptureStatusNone || D.used == kRangeTableSlots) return nullptr;
+    if (!D.base) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_range_tables) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        D.base = static_cast<float*>(p);
+    }
+    float* table = D.base + (int64_t)D.used * kRangeLutStride;
+    range_table_kernel<<<1, kBatchBlock, 0, stream>>>(table, var_inv_i);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    D.key[D.used++] = key;
+    return table;
+}
 
 // ---------------------------------------------------------------------------------------------
 // ISB filter on the chunked layout. Guides and range weights come from the same device functions
@@ -70,10 +130,11 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __
                                                                    const Tin* __restrict__ cost_in,
                                                                    uint8_t* __restrict__ guide_out,
                                                                    float* __restrict__ cost_out, LevelGeom g,
-                                                                   int chunks, float var_inv_i)
+                                                                   int chunks, float var_inv_i,
+                                                                   const float* __restrict__ table)
 {
-    __shared__ float lut[kRangeLutSize];
-    fill_range_lut(lut, var_inv_i);
+    __shared__ __align__(16) float lut[kRangeLutStride];
+    load_range_lut(lut, table, var_inv_i);
     __syncthreads();
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -328,7 +389,7 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
 template <int W>
 struct UpShared {
     __align__(16) float tile[2][UpTile<W>::floats];
-    float lut[kRangeLutSize];
+    __align__(16) float lut[kRangeLutStride];
 };
 
 // One block of an upsampling step: coarse pixels x0 .. x0 + kUpTileX - 1 of coarse row y, their
@@ -418,10 +479,11 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint
                                                             uint8_t* __restrict__ guide_io,
                                                             Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
                                                             int ncand, float weight_up, float weight_down,
-                                                            float var_inv_i, SelectOut so)
+                                                            float var_inv_i, const float* __restrict__ table,
+                                                            SelectOut so)
 {
     __shared__ UpShared<W> sh;
-    fill_range_lut(sh.lut, var_inv_i);
+    load_range_lut(sh.lut, table, var_inv_i);
     __syncthreads();  // the range table is filled
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
     const int inst = blockIdx.z;
@@ -473,8 +535,8 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_uneven_kernel(const Leve
     const LevelGeom g = d.g;
     const int64_t pout = (int64_t)g.rows_out * g.cols_out;
     if ((int64_t)blockIdx.x * blockDim.x >= pout) return;
-    __shared__ float lut[kRangeLutSize];
-    fill_range_lut(lut, d.var_inv_i);
+    __shared__ __align__(16) float lut[kRangeLutStride];
+    load_range_lut(lut, d.lut, d.var_inv_i);
     __syncthreads();
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pout) return;
@@ -490,7 +552,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_uneven_kernel(con
     const int x0 = blockIdx.x * kUpTileX, y = blockIdx.y;
     if (x0 >= g.cols_in || y >= g.rows_in) return;
     __shared__ UpShared<W> sh;
-    fill_range_lut(sh.lut, d.var_inv_i);
+    load_range_lut(sh.lut, d.lut, d.var_inv_i);
     __syncthreads();
     isb_up_block<W, Tf, kSelect, G4>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
                                      static_cast<Tf*>(d.cost_out), g, d.chunks, d.ncand, d.weight_up, d.weight_down,
@@ -583,7 +645,8 @@ static int launch_down(const uint8_t* gi, const Tin* ci, int ri, int cl_i, uint8
 {
     const LevelGeom g{ri, cl_i, ro, cl_o};
     const dim3 grid(grid_1d((int64_t)ro * cl_o, kBatchBlock), instances);
-    isb_down_kernel<W, Tin, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, go, co, g, chunks, var_inv_i);
+    isb_down_kernel<W, Tin, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, go, co, g, chunks, var_inv_i,
+                                                              range_table(var_inv_i, st));
     return launch_status("isb_down_kernel");
 }
 
@@ -593,12 +656,13 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
                      cudaStream_t st)
 {
     const LevelGeom g{rc, cc, rf, cf_cols};
+    const float* table = range_table(var_inv_i, st);
     if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
         isb_up_kernel<W, Tf, kSelect, GL, 3><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
-            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, so);
+            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
     else
         isb_up_kernel<W, Tf, kSelect, GL><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
-            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, so);
+            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
     return launch_status(kSelect ? "isb_up_kernel<select>" : "isb_up_kernel");
 }
 

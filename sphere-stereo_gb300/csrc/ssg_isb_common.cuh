@@ -54,6 +54,7 @@ __device__ __forceinline__ void load_guide(const uint8_t* __restrict__ g, int64_
 // shared-memory table of all 766 values, filled per block with range_weight, which gives the
 // same bits as evaluating the exponential per tap.
 constexpr int kRangeLutSize = 766;
+constexpr int kRangeLutStride = 768;  // a table padded to whole 16-byte words
 
 __device__ __forceinline__ int colour_distance(const int a[3], const int b[3])
 {
@@ -113,6 +114,23 @@ __device__ __forceinline__ void fill_range_lut(float* lut, float var_inv_i)
 {
     for (int d = threadIdx.x; d < kRangeLutSize; d += blockDim.x) lut[d] = range_weight((float)d, var_inv_i);
 }
+
+// the block's table (16-byte aligned, kRangeLutStride floats): copied from the precomputed table
+// `table` (range_table()) when there is one, else evaluated; the caller synchronises the block
+__device__ __forceinline__ void load_range_lut(float* lut, const float* __restrict__ table, float var_inv_i)
+{
+    if (table) {
+        for (int q = threadIdx.x; q < kRangeLutStride / 4; q += blockDim.x)
+            reinterpret_cast<float4*>(lut)[q] = __ldg(reinterpret_cast<const float4*>(table) + q);
+    } else {
+        fill_range_lut(lut, var_inv_i);
+    }
+}
+
+// The range-weight table of var_inv_i in device memory (filled once per device and value, on
+// `stream`, which is synchronised then), or nullptr when it cannot be had now (the stream is
+// being captured, or all slots are taken): kernels then evaluate the table per block.
+const float* range_table(float var_inv_i, cudaStream_t stream);
 
 // Guide weights of one coarse pixel of guideDownsample2xKernel (isb_filter.cu:44-119): the
 // centre tap (weight 1) and its 8 neighbours in the reference's order, edge-clamped. Writes the

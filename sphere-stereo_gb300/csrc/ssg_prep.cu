@@ -1,0 +1,152 @@
+// Input preparation on the GPU: the linear resize the reference applies to every decoded image
+// before the estimator (python/utils.py:198-201, cv2.resize(image, size, cv2.INTER_AREA) -- the
+// third positional argument of cv2.resize is `dst`, so the interpolation in effect is the
+// default, INTER_LINEAR).
+//
+// The arithmetic restates OpenCV's published linear resize:
+//   - source coordinate of destination column dx: fx = float((dx + 0.5) * scale_x - 0.5) in
+//     double, scale_x = 1 / (dst_cols / src_cols); sx = floor(fx), fx -= sx; sx < 0 gives
+//     (sx, fx) = (0, 0) and sx >= src_cols - 1 gives (src_cols - 1, 0) (the second tap then has
+//     weight 0 and is not read); rows the same way, except that the row weights are kept and the
+//     rows clamped to [0, src_rows - 1];
+//   - float pixels: h = S[sx] * (1 - fx) + S[sx + 1] * fx per row, then h0 * (1 - fy) + h1 * fy,
+//     each product and sum rounded separately;
+//   - uint8 pixels to uint8 (the ground-truth resize of the evaluation): 11-bit fixed-point
+//     weights w0 = round(2048 (1 - f)) (saturated), w1 = 2048 - w0, integer sums, result
+//     (v + 2^21) >> 22;
+//   - an exact 2x reduction on both axes is an area average (OpenCV switches to INTER_AREA
+//     there): floats (a + b + c + d) * 0.25, bytes (a + b + c + d + 2) >> 2.
+// cv2 is not available here, so these statements are not pinned against OpenCV's own outputs.
+#include <cmath>
+
+#include "ssg_common.cuh"
+
+namespace ssg {
+
+struct ResizeParams {
+    int src_cols, src_rows, dst_cols, dst_rows, channels;
+    double scale_x, scale_y;
+    int area2;  // exact 2x reduction on both axes
+};
+
+struct Tap {
+    int s0, s1;
+    float f;  // weight of s1
+};
+
+__device__ __forceinline__ Tap column_tap(const ResizeParams& p, int dx)
+{
+    float fx = (float)((dx + 0.5) * p.scale_x - 0.5);
+    int sx = (int)floorf(fx);
+    fx -= (float)sx;
+    if (sx < 0) fx = 0.0f, sx = 0;
+    if (sx >= p.src_cols - 1) fx = 0.0f, sx = p.src_cols - 1;
+    return Tap{sx, min(sx + 1, p.src_cols - 1), fx};
+}
+
+__device__ __forceinline__ Tap row_tap(const ResizeParams& p, int dy)
+{
+    float fy = (float)((dy + 0.5) * p.scale_y - 0.5);
+    const int sy = (int)floorf(fy);
+    fy -= (float)sy;
+    return Tap{min(max(sy, 0), p.src_rows - 1), min(max(sy + 1, 0), p.src_rows - 1), fy};
+}
+
+__device__ __forceinline__ float in_value(const float* s, int64_t i) { return __ldg(s + i); }
+__device__ __forceinline__ float in_value(const uint8_t* s, int64_t i) { return (float)__ldg(s + i); }
+
+__device__ __forceinline__ int fixed_weight(float f)
+{
+    const float w = __fmul_rn(__fsub_rn(1.0f, f), 2048.0f);
+    return min(max(__float2int_rn(w), -32768), 32767);
+}
+
+// one thread per destination pixel (all channels); blockIdx.y: image
+template <typename Tin, typename Tout>
+__global__ void __launch_bounds__(256) resize_linear_kernel(const __grid_constant__ ResizeParams p,
+                                                            const Tin* __restrict__ src, Tout* __restrict__ dst)
+{
+    const int64_t n = (int64_t)p.dst_cols * p.dst_rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int dx = (int)(i % p.dst_cols), dy = (int)(i / p.dst_cols);
+    const int C = p.channels;
+    src += (int64_t)blockIdx.y * p.src_cols * p.src_rows * C;
+    dst += ((int64_t)blockIdx.y * n + i) * C;
+    if (p.area2) {
+        const int64_t r0 = (int64_t)(2 * dy) * p.src_cols, r1 = r0 + p.src_cols;
+        for (int c = 0; c < C; ++c) {
+            const int64_t a = (r0 + 2 * dx) * C + c, b = a + C, d0 = (r1 + 2 * dx) * C + c, d1 = d0 + C;
+            if constexpr (sizeof(Tout) == 1) {
+                const int s = (int)__ldg(src + a) + __ldg(src + b) + __ldg(src + d0) + __ldg(src + d1);
+                dst[c] = (Tout)((s + 2) >> 2);
+            } else {
+                const float s = __fadd_rn(__fadd_rn(__fadd_rn(in_value(src, a), in_value(src, b)), in_value(src, d0)),
+                                          in_value(src, d1));
+                dst[c] = __fmul_rn(s, 0.25f);
+            }
+        }
+        return;
+    }
+    const Tap tx = column_tap(p, dx), ty = row_tap(p, dy);
+    const int64_t r0 = (int64_t)ty.s0 * p.src_cols, r1 = (int64_t)ty.s1 * p.src_cols;
+    if constexpr (sizeof(Tout) == 1) {
+        const int a0 = fixed_weight(tx.f), a1 = 2048 - a0, b0 = fixed_weight(ty.f), b1 = 2048 - b0;
+        for (int c = 0; c < C; ++c) {
+            const int h0 = (int)__ldg(src + (r0 + tx.s0) * C + c) * a0 + (int)__ldg(src + (r0 + tx.s1) * C + c) * a1;
+            const int h1 = (int)__ldg(src + (r1 + tx.s0) * C + c) * a0 + (int)__ldg(src + (r1 + tx.s1) * C + c) * a1;
+            const int v = (h0 * b0 + h1 * b1 + (1 << 21)) >> 22;
+            dst[c] = (Tout)min(max(v, 0), 255);
+        }
+    } else {
+        const float a0 = __fsub_rn(1.0f, tx.f), a1 = tx.f, b0 = __fsub_rn(1.0f, ty.f), b1 = ty.f;
+        for (int c = 0; c < C; ++c) {
+            const float h0 = __fadd_rn(__fmul_rn(in_value(src, (r0 + tx.s0) * C + c), a0),
+                                       __fmul_rn(in_value(src, (r0 + tx.s1) * C + c), a1));
+            const float h1 = __fadd_rn(__fmul_rn(in_value(src, (r1 + tx.s0) * C + c), a0),
+                                       __fmul_rn(in_value(src, (r1 + tx.s1) * C + c), a1));
+            dst[c] = __fadd_rn(__fmul_rn(h0, b0), __fmul_rn(h1, b1));
+        }
+    }
+}
+
+}  // namespace ssg
+
+using namespace ssg;
+
+extern "C" int ssg_resize_linear(const void* d_src, int src_type, int src_cols, int src_rows, int channels,
+                                 void* d_dst, int dst_type, int dst_cols, int dst_rows, int images, void* stream)
+{
+    SSG_REQUIRE(d_src && d_dst, "null pointer");
+    SSG_REQUIRE(src_cols >= 1 && src_rows >= 1 && dst_cols >= 1 && dst_rows >= 1, "empty image");
+    SSG_REQUIRE(channels >= 1 && channels <= 4, "channels %d outside [1, 4]", channels);
+    SSG_REQUIRE(images >= 1 && images <= 65535, "images %d outside [1, 65535]", images);
+    SSG_REQUIRE((int64_t)src_cols * src_rows * channels < ((int64_t)1 << 40) &&
+                    (int64_t)dst_cols * dst_rows < ((int64_t)1 << 31) * 256,
+                "images too large");
+    SSG_REQUIRE((src_type == SSG_PIXEL_U8 || src_type == SSG_PIXEL_F32) &&
+                    (dst_type == SSG_PIXEL_F32 || (dst_type == SSG_PIXEL_U8 && src_type == SSG_PIXEL_U8)),
+                "unsupported pixel types %d -> %d (u8 -> f32, f32 -> f32, u8 -> u8)", src_type, dst_type);
+    ResizeParams p{};
+    p.src_cols = src_cols;
+    p.src_rows = src_rows;
+    p.dst_cols = dst_cols;
+    p.dst_rows = dst_rows;
+    p.channels = channels;
+    p.scale_x = 1.0 / ((double)dst_cols / src_cols);
+    p.scale_y = 1.0 / ((double)dst_rows / src_rows);
+    p.area2 = src_cols == 2 * dst_cols && src_rows == 2 * dst_rows;
+    const int64_t n = (int64_t)dst_cols * dst_rows;
+    const dim3 grid(grid_1d(n, 256), images);
+    cudaStream_t st = as_stream(stream);
+    if (src_type == SSG_PIXEL_F32)
+        resize_linear_kernel<float, float>
+            <<<grid, 256, 0, st>>>(p, static_cast<const float*>(d_src), static_cast<float*>(d_dst));
+    else if (dst_type == SSG_PIXEL_F32)
+        resize_linear_kernel<uint8_t, float>
+            <<<grid, 256, 0, st>>>(p, static_cast<const uint8_t*>(d_src), static_cast<float*>(d_dst));
+    else
+        resize_linear_kernel<uint8_t, uint8_t>
+            <<<grid, 256, 0, st>>>(p, static_cast<const uint8_t*>(d_src), static_cast<uint8_t*>(d_dst));
+    return launch_status("resize_linear_kernel");
+}

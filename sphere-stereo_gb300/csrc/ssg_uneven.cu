@@ -368,12 +368,13 @@ extern "C" int ssg_uneven_upload(ssg_uneven_batch* b, void* d_plan, void* d_scra
                 "plan and scratch must be 256-byte aligned");
     unsigned char* scratch = static_cast<unsigned char*>(d_scratch);
     for (StitchJob& j : b->jobs) j.reprojected = reinterpret_cast<float*>(scratch + b->maps_offset) + j.map_begin;
+    cudaStream_t st = as_stream(stream);
+    for (LevelDesc& d : b->levels) d.lut = range_table(d.var_inv_i, st);  // nullptr: evaluated per block
     std::vector<unsigned char> host(b->plan_bytes, 0);
     std::memcpy(host.data() + b->sweep_offset, b->sweep.data(), sizeof(SweepInst) * b->sweep.size());
     std::memcpy(host.data() + b->levels_offset, b->levels.data(), sizeof(LevelDesc) * b->levels.size());
     if (!b->jobs.empty())
         std::memcpy(host.data() + b->jobs_offset, b->jobs.data(), sizeof(StitchJob) * b->jobs.size());
-    cudaStream_t st = as_stream(stream);
     cudaError_t e = cudaMemcpyAsync(d_plan, host.data(), host.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemcpyAsync(plan): %s", cudaGetErrorString(e));
     // the host buffer is released below: wait for the copy (set-up, outside any capture)

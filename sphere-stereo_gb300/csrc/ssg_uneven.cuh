@@ -40,6 +40,7 @@ struct LevelDesc {
     uint8_t* guide_out;  // down: the coarse guide; up: the fine guide (read, and written if not the select)
     void* cost_out;      // down: coarse costs; up: fine costs (in place; read only by the select)
     SelectOut so;        // the selecting step
+    const float* lut;    // the range-weight table of var_inv_i (range_table()), or nullptr
 };
 
 // Stitch of one job (python/stitcher.py:166-220): `references` maps of cols x rows, contiguous

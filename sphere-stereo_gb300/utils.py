@@ -117,6 +117,82 @@ def rgb_to_guide(rgb: torch.Tensor, out: torch.Tensor | None = None) -> torch.Te
     return out
 
 
+def resize_linear(images: torch.Tensor, size, out_dtype: torch.dtype = torch.float32) -> torch.Tensor:
+    """The linear resize of the reference's input path (python/utils.py:198-201, cv2.resize with
+    the default INTER_LINEAR in effect) on the GPU: ssg_resize_linear.
+
+    Args:
+        images: [rows, cols, channels] or [images, rows, cols, channels] uint8 or float32 CUDA tensor
+            (channels 1..4)
+        size: (cols, rows) of the result
+        out_dtype: torch.float32 (uint8 inputs are converted as the reference's astype(float32)
+            does, then resized) or torch.uint8 (uint8 inputs only: OpenCV's fixed-point path)
+    """
+    single = images.dim() == 3
+    x = images.unsqueeze(0) if single else images
+    if x.dim() != 4 or not 1 <= x.shape[-1] <= 4:
+        raise ValueError(f"images must be [images,] rows, cols, channels (got {tuple(images.shape)})")
+    if x.dtype not in (torch.uint8, torch.float32):
+        raise TypeError(f"images must be uint8 or float32 (got {x.dtype})")
+    N.require(x, "images", x.dtype)
+    cols, rows = int(size[0]), int(size[1])
+    src_type = N.PIXEL_U8 if x.dtype == torch.uint8 else N.PIXEL_F32
+    dst_type = N.PIXEL_U8 if out_dtype == torch.uint8 else N.PIXEL_F32
+    out = torch.empty((x.shape[0], rows, cols, x.shape[-1]), dtype=out_dtype, device=x.device)
+    with torch.cuda.device(x.device):
+        N.call("ssg_resize_linear", x.data_ptr(), src_type, x.shape[2], x.shape[1], x.shape[3], out.data_ptr(),
+               dst_type, cols, rows, x.shape[0], N.stream_of(x))
+    return out[0] if single else out
+
+
+def read_input_images(filename, dataset_path, matching_resolution, rgb_to_stitch_resolution, calibrations,
+                      references_indices, device="cuda"):
+    """python/utils.py:157-204 with the resize on the GPU: reads <dataset_path>/cam<i>/<filename>
+    (PNG or EXR: imageio.imread), maps uint8 to float32, uint16 to float32 / 255 and float32 to
+    255 * clip(x, 0, 1) (with the reference's warnings), and resizes to the matching resolution
+    (every camera) and the stitching resolution (reference cameras).  Returns the reference's dict
+    with lists of float32 [rows, cols, 3] CUDA tensors."""
+    import os
+    import warnings
+
+    import numpy as np
+
+    from . import imageio
+
+    images_to_match, images_to_stitch = [], []
+    valid_frame = True
+    for cam_index, calibration in enumerate(calibrations):
+        file_path = os.path.join(dataset_path, "cam" + str(cam_index)) + "/" + filename
+        image = imageio.imread(file_path)
+        if image is not None:
+            res = calibration.original_resolution
+            if image.shape == (res[1], res[0], 3):
+                if image.dtype == np.uint8:
+                    t = torch.as_tensor(np.ascontiguousarray(image), device=device)  # uint8 upload
+                elif image.dtype == np.uint16:
+                    t = torch.as_tensor(image.astype(np.float32) / 255, device=device)
+                elif image.dtype == np.float32:
+                    if np.max(image) > 1:
+                        image = np.clip(image, 0, 1)
+                        warnings.warn("Image has out-of-range float values for file " + file_path
+                                      + ". Clipped for processing.")
+                    t = torch.as_tensor(np.ascontiguousarray(image * 255), device=device)
+                else:
+                    warnings.warn("Invalide image type for file " + file_path)
+                    valid_frame = False
+            else:
+                warnings.warn("Invalid image size / channels for file " + file_path)
+                valid_frame = False
+        else:
+            warnings.warn("Cannot read image for file " + file_path)
+            valid_frame = False
+        if valid_frame:
+            if cam_index in references_indices:
+                images_to_stitch.append(resize_linear(t, rgb_to_stitch_resolution))
+            images_to_match.append(resize_linear(t, matching_resolution))
+    return {"images_to_match": images_to_match, "images_to_stitch": images_to_stitch, "is_valid": valid_frame}
+
+
 # ---------------------------------------------------------------------------------------------
 # Calibration -> C ABI structs.  Small matrices are computed on the CPU in float32 with the
 # reference's own expressions, so that every device and every run sees the same values.
