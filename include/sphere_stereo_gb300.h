@@ -305,9 +305,14 @@ SSG_API int ssg_select_distance_batch(const void* d_cost, int candidate_count, i
 
 /* ISB_Filter.apply (python/isb_filter.py:72-136) on `instances` contiguous float32 pyramids:
  * level l holds instances x ceil(rows/2^l) x ceil(cols/2^l) 32-bit guide words and instances x
- * (candidate_count x ... ) costs. */
+ * (candidate_count x ... ) costs.  flags: 0, or SSG_ISB_SKIP_FINE_GUIDE when the caller wants
+ * only the filtered costs (the distance post-filter, python/depth_estimation.py:200-203, keeps
+ * the distance and drops the guide): the filtered level-0 guide is then not formed and d_guides[0]
+ * keeps its input. */
+#define SSG_ISB_SKIP_FINE_GUIDE 1
 SSG_API int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
-                                int candidate_count, int instances, double sigma_i, double sigma_s, void* stream);
+                                int candidate_count, int instances, double sigma_i, double sigma_s, int flags,
+                                void* stream);
 
 /* Reprojection (python/stitcher.cu:181-204) of `instances` distance maps; instance i uses
  * intrinsics / translation of slot i % references. */

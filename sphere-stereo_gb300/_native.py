@@ -28,6 +28,7 @@ TUNE_HOLE_BLOCKS_PER_SM = 1
 TUNE_MERGE_FRAMES = 2
 TUNE_UNEVEN_SPAN = 3
 TUNE_ISB_UP_BLOCKS = 4
+ISB_SKIP_FINE_GUIDE = 1
 PIXEL_U8 = 0
 PIXEL_F32 = 1
 SSG_EVAL_MAX_THRESHOLDS = 16
@@ -107,7 +108,7 @@ SIGNATURES = {
     "ssg_isb_upsample_select_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P,
                                            _P]),
     "ssg_select_distance_batch": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, _P]),
-    "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _P]),
+    "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _I, _P]),
     "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint_batch": (_I, [_P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
     "ssg_inpaint_holes_batch": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),

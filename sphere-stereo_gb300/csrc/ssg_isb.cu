@@ -397,7 +397,10 @@ struct UpShared {
 // sh.lut is filled with the level's range weights and the block synchronised before the call.
 // kSelect = false: coarse float32 -> fine float32 in place (and the fine guides);
 // kSelect = true: the last step, fine level-0 costs of type Tf in, the selection out.
-template <int W, typename Tf, bool kSelect, typename GL>
+// kWriteGuide: the filtered fine guide is formed and written (kGuideDefault: always except by
+// the chunked selecting step, whose guide nothing reads; the planar one writes it as the
+// reference's filter does).
+template <int W, typename Tf, bool kSelect, typename GL, bool kWriteGuide>
 __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
                                              uint8_t* __restrict__ guide_io, Tf* __restrict__ cost_fine,
                                              const LevelGeom& g, int chunks, int ncand, float weight_up,
@@ -408,9 +411,6 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     const int kind = warp >> 2;  // warp-uniform
     const int lx = (warp & 3) * 32 + lane, x = x0 + lx;
     const bool coarse_ok = x < g.cols_in;
-    // the planar selecting step writes the filtered level-0 guide as the reference's filter does;
-    // the chunked one leaves it, as nothing reads it after the selection
-    constexpr bool kWriteGuide = !kSelect || W == 1;
     const LutRange range{sh.lut};
     FinePixel pa, pb;
     {
@@ -470,10 +470,14 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     }
 }
 
+template <int W, bool kSelect>
+constexpr bool kGuideDefault = !kSelect || W == 1;
+
 // blockIdx.z: instance of contiguous levels.  kBlocks: blocks per SM the registers are bounded
 // for (3 for the single-candidate filter; 2 or 3 for the chunked volumes, SSG_TUNE_ISB_UP_BLOCKS:
 // 3 spills a few of the taps' registers for more resident warps).
-template <int W, typename Tf, bool kSelect, typename GL, int kBlocks = (W == 1 ? 3 : 2)>
+template <int W, typename Tf, bool kSelect, typename GL, int kBlocks = (W == 1 ? 3 : 2),
+          bool kWriteGuide = kGuideDefault<W, kSelect>>
 __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint8_t* __restrict__ guide_in,
                                                             const float* __restrict__ cost_in,
                                                             uint8_t* __restrict__ guide_io,
@@ -492,7 +496,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint
         if (so.distance2) so.distance2 += (int64_t)inst * pio;
         if (so.index) so.index += (int64_t)inst * pio;
     }
-    isb_up_block<W, Tf, kSelect, GL>(guide_in + (int64_t)inst * pin * GL::bytes,
+    isb_up_block<W, Tf, kSelect, GL, kWriteGuide>(guide_in + (int64_t)inst * pin * GL::bytes,
                                      cost_in + (int64_t)inst * chunks * pin * W,
                                      guide_io + (int64_t)inst * pio * GL::bytes,
                                      cost_fine + (int64_t)inst * chunks * pio * W, g, chunks, ncand, weight_up,
@@ -544,7 +548,8 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_uneven_kernel(const Leve
                                static_cast<float*>(d.cost_out), g, d.chunks, o, lut);
 }
 
-template <int W, typename Tf, bool kSelect, int kBlocks = (W == 1 ? 3 : 2)>
+template <int W, typename Tf, bool kSelect, int kBlocks = (W == 1 ? 3 : 2),
+          bool kWriteGuide = kGuideDefault<W, kSelect>>
 __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_uneven_kernel(const LevelDesc* __restrict__ descs)
 {
     const LevelDesc& d = descs[blockIdx.z];
@@ -554,7 +559,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_uneven_kernel(con
     __shared__ UpShared<W> sh;
     load_range_lut(sh.lut, d.lut, d.var_inv_i);
     __syncthreads();
-    isb_up_block<W, Tf, kSelect, G4>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
+    isb_up_block<W, Tf, kSelect, G4, kWriteGuide>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
                                      static_cast<Tf*>(d.cost_out), g, d.chunks, d.ncand, d.weight_up, d.weight_down,
                                      d.so, x0, y, sh);
 }
@@ -576,12 +581,14 @@ int launch_down_uneven(const LevelDesc* d_descs, int count, int max_rows_out, in
 }
 
 int launch_up_uneven(const LevelDesc* d_descs, int count, int max_rows_in, int max_cols_in, int width,
-                     int storage_fine, bool select, cudaStream_t st)
+                     int storage_fine, bool select, bool guide, cudaStream_t st)
 {
     SSG_REQUIRE(count >= 1 && count <= 65535 && max_rows_in <= 65535, "sizes out of range");
     const dim3 grid((unsigned)((max_cols_in + kUpTileX - 1) / kUpTileX), (unsigned)max_rows_in, (unsigned)count);
     const bool three = tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3;
-    if (width == 1)
+    if (width == 1 && !guide)
+        isb_up_uneven_kernel<1, float, false, 3, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
+    else if (width == 1)
         isb_up_uneven_kernel<1, float, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
     else if (!select)
         three ? isb_up_uneven_kernel<8, float, false, 3><<<grid, kBatchBlock, 0, st>>>(d_descs)
@@ -650,14 +657,18 @@ static int launch_down(const uint8_t* gi, const Tin* ci, int ri, int cl_i, uint8
     return launch_status("isb_down_kernel");
 }
 
+// guide = false: the single-candidate step does not form the filtered fine guide
 template <int W, typename Tf, bool kSelect, typename GL>
 static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t* gio, Tf* cf, int rf, int cf_cols,
                      int chunks, int ncand, int instances, float wu, float wd, float var_inv_i, const SelectOut& so,
-                     cudaStream_t st)
+                     cudaStream_t st, bool guide = true)
 {
     const LevelGeom g{rc, cc, rf, cf_cols};
     const float* table = range_table(var_inv_i, st);
-    if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
+    if (W == 1 && !kSelect && !guide)
+        isb_up_kernel<W, Tf, kSelect, GL, 3, false><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
+            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
+    else if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
         isb_up_kernel<W, Tf, kSelect, GL, 3><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
             gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
     else
@@ -669,7 +680,8 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
 // the whole filter on planar levels (W = 1, chunks = candidates): python/isb_filter.py:72-136
 template <typename GL>
 static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
-                        int candidate_count, int instances, double sigma_i, double sigma_s, cudaStream_t st)
+                        int candidate_count, int instances, double sigma_i, double sigma_s, cudaStream_t st,
+                        int flags = 0)
 {
     const Levels c = isb_constants(level_count, sigma_i, sigma_s);
     for (int s = 1; s < level_count; ++s) {
@@ -685,7 +697,8 @@ static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int lev
                   cf = level_rows(cols, s);
         if (int e = launch_up<1, float, false, GL>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s],
                                                    rf, cf, candidate_count, candidate_count, instances,
-                                                   c.weight_up[s], c.weight_down[s], c.var_inv_i, SelectOut{}, st))
+                                                   c.weight_up[s], c.weight_down[s], c.var_inv_i, SelectOut{}, st,
+                                                   s > 0 || !(flags & SSG_ISB_SKIP_FINE_GUIDE)))
             return e;
     }
     return SSG_OK;
@@ -753,13 +766,14 @@ extern "C" int ssg_isb_apply(uint8_t* const* d_guides, float* const* d_costs, in
 
 extern "C" int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows,
                                    int cols, int candidate_count, int instances, double sigma_i, double sigma_s,
-                                   void* stream)
+                                   int flags, void* stream)
 {
     if (int e = check_apply_args(d_guides, d_costs, level_count, rows, cols, candidate_count, sigma_i, sigma_s))
         return e;
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    SSG_REQUIRE((flags & ~SSG_ISB_SKIP_FINE_GUIDE) == 0, "unknown flags 0x%x", flags);
     return apply_planar<G4>(d_guides, d_costs, level_count, rows, cols, candidate_count, instances, sigma_i, sigma_s,
-                        as_stream(stream));
+                        as_stream(stream), flags);
 }
 
 extern "C" int ssg_select_distance(const float* d_cost, int candidate_count, int64_t pixels, const float* candidates,

@@ -343,15 +343,17 @@ struct Selector {
     float m = __builtin_huge_valf(), M = -__builtin_huge_valf(), L = 0.0f, R = 0.0f, prev = 0.0f;
     int idx = 0;
     bool need_right = false;
+    // the first strict minimum and the maximum as the reference's min / max take them; fminf and
+    // fmaxf give the same values (a NaN cost leaves both unchanged, as the comparisons do)
     __device__ __forceinline__ void push(int z, float c)
     {
         R = need_right ? c : R;
         const bool lt = c < m;
-        m = lt ? c : m;
+        m = fminf(c, m);
         idx = lt ? z : idx;
         L = lt ? prev : L;
         need_right = lt;
-        M = c > M ? c : M;
+        M = fmaxf(c, M);
         prev = c;
     }
 };

@@ -28,6 +28,7 @@ struct Step {
     size_t offset;  // byte offset of the step's LevelDesc array in the plan
     int count, rows, cols, width, storage;
     bool down, select;
+    bool guide;  // an upsampling step forms the filtered fine guide
 };
 
 constexpr size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -177,9 +178,11 @@ extern "C" int ssg_uneven_create(const ssg_uneven_instance* instances, int insta
         const int rc = level_rows(in.rows, coarse), cc = level_rows(in.cols, coarse);
         return down ? LevelGeom{rf, cf, rc, cc} : LevelGeom{rc, cc, rf, cf};
     };
-    auto add_step = [&](bool down, bool select, int width, int st, const std::vector<LevelDesc>& descs) {
+    auto add_step = [&](bool down, bool select, int width, int st, const std::vector<LevelDesc>& descs,
+                        bool guide = true) {
         if (descs.empty()) return;
         Step step{};
+        step.guide = guide;
         step.offset = b->levels.size();  // index for now, bytes after layout
         step.count = (int)descs.size();
         step.down = down;
@@ -295,7 +298,8 @@ extern "C" int ssg_uneven_create(const ssg_uneven_instance* instances, int insta
             d.cost_out = s == 0 ? static_cast<void*>(in.d_distance) : static_cast<void*>(in.d_df_costs[s - 1]);
             descs.push_back(d);
         }
-        add_step(false, false, 1, SSG_STORAGE_F32, descs);
+        // the estimator keeps the post-filtered distance only: no filtered level-0 guide
+        add_step(false, false, 1, SSG_STORAGE_F32, descs, s > 0);
     }
 
     // --- stitch jobs: maps concatenated job by job
@@ -396,7 +400,7 @@ extern "C" int ssg_uneven_run(const ssg_uneven_batch* b, void* stream)
     for (const Step& s : b->steps) {
         const LevelDesc* d = reinterpret_cast<const LevelDesc*>(b->d_plan + s.offset);
         const int e = s.down ? launch_down_uneven(d, s.count, s.rows, s.cols, s.width, s.storage, st)
-                             : launch_up_uneven(d, s.count, s.rows, s.cols, s.width, s.storage, s.select, st);
+                             : launch_up_uneven(d, s.count, s.rows, s.cols, s.width, s.storage, s.select, s.guide, st);
         if (e) return e;
     }
     if (b->jobs.empty()) return SSG_OK;

@@ -75,8 +75,9 @@ int launch_sweep_uneven(const SweepInst* d_insts, int instances, int total_tiles
                         cudaStream_t st);
 int launch_down_uneven(const LevelDesc* d_descs, int count, int max_rows_out, int max_cols_out, int width,
                        int storage_in, cudaStream_t st);
+// guide = false: the single-candidate step does not form the filtered fine guide
 int launch_up_uneven(const LevelDesc* d_descs, int count, int max_rows_in, int max_cols_in, int width,
-                     int storage_fine, bool select, cudaStream_t st);
+                     int storage_fine, bool select, bool guide, cudaStream_t st);
 // fill + reprojection + hole filling + merge of every job: maps concatenated job by job
 // (total_map_pixels), d_stamps one byte per map pixel, d_holes 3 x total_map_pixels + 4 int32
 int launch_stitch_uneven(const StitchJob* d_jobs, int jobs, float* d_maps, int64_t total_map_pixels,

@@ -133,7 +133,7 @@ class BatchPipeline:
         if L >= 2:
             N.call("ssg_isb_apply_batch", N.pointers([g.data_ptr() for g in self.df_guides]),
                    N.pointers([dist.data_ptr()] + [c.data_ptr() for c in self.df_costs]), L, rows, cols, 1, inst,
-                   float(e.sigma_i) / 2, float(e.sigma_s) / 2, stream)
+                   float(e.sigma_i) / 2, float(e.sigma_s) / 2, N.ISB_SKIP_FINE_GUIDE, stream)
         # stitch (python/stitcher.py:166-220)
         if stitch.dtype == torch.uint8:
             images_u8 = stitch

@@ -216,3 +216,37 @@ def test_non_integer_inputs_against_fp32_path(ss, native, golden_c1):
     same = (fast.batch_index_maps[0].cpu().numpy() == idx32).mean()
     print(f"\nnon-integer inputs, fp16 vs fp32 path: same index {same:.6f}")
     assert same >= 0.999
+
+
+def test_isb_apply_batch_skip_fine_guide(ss, native):
+    """SSG_ISB_SKIP_FINE_GUIDE changes nothing but the level-0 guide, which keeps its input."""
+    N = ss._native
+    rng = np.random.default_rng(21)
+    rows, cols, inst = 96, 80, 3
+    levels = native.ssg_isb_level_count(cols, rows)
+    shapes = [(-(-rows // 2 ** s), -(-cols // 2 ** s)) for s in range(levels)]
+    g0 = rng.integers(0, 256, (inst, rows, cols, 4), dtype=np.uint8)
+    g0[..., 3] = 0
+    c0 = rng.random((inst, rows, cols), dtype=np.float32) * 50
+
+    def run(flags):
+        guides = [torch.as_tensor(g0.copy(), device="cuda:0")] + [
+            torch.zeros(inst * r * c * 4, dtype=torch.uint8, device="cuda:0") for r, c in shapes[1:]]
+        costs = [torch.as_tensor(c0.copy(), device="cuda:0")] + [
+            torch.zeros(inst * r * c, dtype=torch.float32, device="cuda:0") for r, c in shapes[1:]]
+        N.call("ssg_isb_apply_batch", N.pointers([g.data_ptr() for g in guides]),
+               N.pointers([c.data_ptr() for c in costs]), levels, rows, cols, 1, inst, 5.0, 12.5, flags,
+               torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return [g.cpu().numpy() for g in guides], [c.cpu().numpy() for c in costs]
+
+    g_all, c_all = run(0)
+    g_skip, c_skip = run(N.ISB_SKIP_FINE_GUIDE)
+    for a, b in zip(c_all, c_skip):
+        assert np.array_equal(a, b)
+    for a, b in zip(g_all[1:], g_skip[1:]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(g_skip[0], g0)
+    assert not np.array_equal(g_all[0], g0)
+    with pytest.raises(ValueError):
+        run(4)
