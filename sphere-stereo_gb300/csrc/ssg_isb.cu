@@ -96,12 +96,13 @@ const float* range_table(float var_inv_i, cudaStream_t stream)
 template <int W, typename Tin, typename GL>
 __device__ __forceinline__ void isb_down_pixel(const uint8_t* __restrict__ guide_in, const Tin* __restrict__ cost_in,
                                                uint8_t* __restrict__ guide_out, float* __restrict__ cost_out,
-                                               const LevelGeom& g, int chunks, int64_t o, const float* lut)
+                                               const LevelGeom& g, int chunks, int o, const float* lut)
 {
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
     DownTapsT<int> t;
-    down_weights<int, LutRange, GL>(guide_in, g.rows_in, g.cols_in, (int)(o % g.cols_out), (int)(o / g.cols_out),
-                                    LutRange{lut}, guide_out, o, t);
+    const int y = o / g.cols_out;  // 32-bit: a level holds fewer than 2^31 pixels
+    down_weights<int, LutRange, GL>(guide_in, g.rows_in, g.cols_in, o - y * g.cols_out, y, LutRange{lut}, guide_out,
+                                    o, t);
     // the chunked (16-bit) path sums with fused multiply-adds and scales by the reciprocal; the
     // planar path keeps the reference's separate products and its division
     constexpr bool kFast = W == 8;
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_kernel(const uint8_t* __
     const int inst = blockIdx.y;
     isb_down_pixel<W, Tin, GL>(guide_in + (int64_t)inst * pin * GL::bytes, cost_in + (int64_t)inst * chunks * pin * W,
                                guide_out + (int64_t)inst * pout * GL::bytes, cost_out + (int64_t)inst * chunks * pout * W,
-                               g, chunks, o, lut);
+                               g, chunks, (int)o, lut);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -470,6 +471,86 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Single-candidate upsampling (W = 1: planar one-candidate volumes and the distance post-filter).
+// One thread per coarse pixel filters its four fine pixels: the 3x3 coarse guides and values are
+// read once (neighbouring threads share them through L1) and each fine pixel's weights are formed
+// once for its one value, with the same device functions and order as the chunked kernels.  No
+// shared tile or barrier besides the range table.  Blocks of kUp1X x kUp1Y coarse pixels.
+// ---------------------------------------------------------------------------------------------
+constexpr int kUp1X = 32, kUp1Y = 8;
+
+template <int F, typename GL, bool kWriteGuide>
+__device__ __forceinline__ void up1_fine(const typename GL::Pix (&gd)[9], const float (&cv)[9],
+                                         uint8_t* __restrict__ guide_io, float* __restrict__ cost_io,
+                                         const LevelGeom& g, int x, int y, float weight_up, float weight_down,
+                                         const LutRange& range)
+{
+    const int fx = 2 * x + (F >= 2 ? 1 : 0), fy = 2 * y + (F & 1);
+    if (fx >= g.cols_out || fy >= g.rows_out) return;  // the clamped duplicate of another pixel
+    const int index = fy * g.cols_out + fx;
+    const typename GL::Pix up = GL::load(guide_io, index);
+    float w[UpTaps<F>::n], gsum[3];
+    const float inv = fine_weights<F, LutRange, GL>(gd, up, weight_up, weight_down, range, w, gsum);
+    float acc = fmul(weight_up, __ldg(cost_io + index));
+#pragma unroll
+    for (int i = 0; i < UpTaps<F>::n; ++i) acc = fadd(acc, fmul(w[i], cv[UpTaps<F>::tap(i)]));
+    cost_io[index] = fmul(acc, inv);
+    if (kWriteGuide) {
+        uint32_t v[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) v[ch] = __float2uint_rz(fmul(gsum[ch], inv));
+        GL::store(guide_io, index, v);
+    }
+}
+
+// coarse pixel (x, y) of one instance's level pair; `lut` is the block's filled range table
+template <typename GL, bool kWriteGuide>
+__device__ __forceinline__ void isb_up1_pixel(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
+                                              uint8_t* __restrict__ guide_io, float* __restrict__ cost_io,
+                                              const LevelGeom& g, float weight_up, float weight_down, int x, int y,
+                                              const float* lut)
+{
+    int ci[9];
+    typename GL::Pix gd[9];
+    coarse_neighbourhood<int, GL>(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+    float cv[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) cv[k] = __ldg(cost_in + ci[k]);
+    const LutRange range{lut};
+    up1_fine<0, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<1, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<2, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<3, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+}
+
+// blockIdx.z: instance of contiguous levels
+template <typename GL, bool kWriteGuide>
+__global__ void __launch_bounds__(kUp1X * kUp1Y) isb_up1_kernel(const uint8_t* __restrict__ guide_in,
+                                                                const float* __restrict__ cost_in,
+                                                                uint8_t* __restrict__ guide_io,
+                                                                float* __restrict__ cost_io, LevelGeom g,
+                                                                float weight_up, float weight_down, float var_inv_i,
+                                                                const float* __restrict__ table)
+{
+    __shared__ __align__(16) float lut[kRangeLutStride];
+    load_range_lut(lut, table, var_inv_i);
+    __syncthreads();
+    const int x = blockIdx.x * kUp1X + (threadIdx.x % kUp1X), y = blockIdx.y * kUp1Y + (threadIdx.x / kUp1X);
+    if (x >= g.cols_in || y >= g.rows_in) return;
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
+    const int inst = blockIdx.z;
+    isb_up1_pixel<GL, kWriteGuide>(guide_in + inst * pin * GL::bytes, cost_in + inst * pin,
+                                   guide_io + inst * pio * GL::bytes, cost_io + inst * pio, g, weight_up, weight_down,
+                                   x, y, lut);
+}
+
+static dim3 up1_grid(int cols_in, int rows_in, int instances)
+{
+    return dim3((unsigned)((cols_in + kUp1X - 1) / kUp1X), (unsigned)((rows_in + kUp1Y - 1) / kUp1Y),
+                (unsigned)instances);
+}
+
 template <int W, bool kSelect>
 constexpr bool kGuideDefault = !kSelect || W == 1;
 
@@ -545,7 +626,7 @@ __global__ void __launch_bounds__(kBatchBlock) isb_down_uneven_kernel(const Leve
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pout) return;
     isb_down_pixel<W, Tin, G4>(d.guide_in, static_cast<const Tin*>(d.cost_in), d.guide_out,
-                               static_cast<float*>(d.cost_out), g, d.chunks, o, lut);
+                               static_cast<float*>(d.cost_out), g, d.chunks, (int)o, lut);
 }
 
 template <int W, typename Tf, bool kSelect, int kBlocks = (W == 1 ? 3 : 2),
@@ -580,17 +661,35 @@ int launch_down_uneven(const LevelDesc* d_descs, int count, int max_rows_out, in
     return launch_status("isb_down_uneven_kernel");
 }
 
+template <bool kWriteGuide>
+__global__ void __launch_bounds__(kUp1X * kUp1Y) isb_up1_uneven_kernel(const LevelDesc* __restrict__ descs)
+{
+    const LevelDesc& d = descs[blockIdx.z];
+    const LevelGeom g = d.g;
+    const int x = blockIdx.x * kUp1X + (threadIdx.x % kUp1X), y = blockIdx.y * kUp1Y + (threadIdx.x / kUp1X);
+    if ((int)(blockIdx.x * kUp1X) >= g.cols_in || (int)(blockIdx.y * kUp1Y) >= g.rows_in) return;
+    __shared__ __align__(16) float lut[kRangeLutStride];
+    load_range_lut(lut, d.lut, d.var_inv_i);
+    __syncthreads();
+    if (x >= g.cols_in || y >= g.rows_in) return;
+    isb_up1_pixel<G4, kWriteGuide>(d.guide_in, static_cast<const float*>(d.cost_in), d.guide_out,
+                                   static_cast<float*>(d.cost_out), g, d.weight_up, d.weight_down, x, y, lut);
+}
+
 int launch_up_uneven(const LevelDesc* d_descs, int count, int max_rows_in, int max_cols_in, int width,
                      int storage_fine, bool select, bool guide, cudaStream_t st)
 {
+    if (width == 1 && !select) {
+        SSG_REQUIRE(count >= 1 && count <= 65535, "sizes out of range");
+        const dim3 grid = up1_grid(max_cols_in, max_rows_in, count);
+        if (guide) isb_up1_uneven_kernel<true><<<grid, kUp1X * kUp1Y, 0, st>>>(d_descs);
+        else isb_up1_uneven_kernel<false><<<grid, kUp1X * kUp1Y, 0, st>>>(d_descs);
+        return launch_status("isb_up1_uneven_kernel");
+    }
     SSG_REQUIRE(count >= 1 && count <= 65535 && max_rows_in <= 65535, "sizes out of range");
     const dim3 grid((unsigned)((max_cols_in + kUpTileX - 1) / kUpTileX), (unsigned)max_rows_in, (unsigned)count);
     const bool three = tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3;
-    if (width == 1 && !guide)
-        isb_up_uneven_kernel<1, float, false, 3, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
-    else if (width == 1)
-        isb_up_uneven_kernel<1, float, false><<<grid, kBatchBlock, 0, st>>>(d_descs);
-    else if (!select)
+    if (!select)
         three ? isb_up_uneven_kernel<8, float, false, 3><<<grid, kBatchBlock, 0, st>>>(d_descs)
               : isb_up_uneven_kernel<8, float, false, 2><<<grid, kBatchBlock, 0, st>>>(d_descs);
     else if (storage_fine == SSG_STORAGE_F16)
@@ -665,10 +764,18 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
 {
     const LevelGeom g{rc, cc, rf, cf_cols};
     const float* table = range_table(var_inv_i, st);
-    if (W == 1 && !kSelect && !guide)
-        isb_up_kernel<W, Tf, kSelect, GL, 3, false><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
-            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
-    else if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
+    if constexpr (W == 1 && !kSelect) {
+        if (chunks == 1) {
+            if (guide)
+                isb_up1_kernel<GL, true><<<up1_grid(cc, rc, instances), kUp1X * kUp1Y, 0, st>>>(
+                    gi, ci, gio, cf, g, wu, wd, var_inv_i, table);
+            else
+                isb_up1_kernel<GL, false><<<up1_grid(cc, rc, instances), kUp1X * kUp1Y, 0, st>>>(
+                    gi, ci, gio, cf, g, wu, wd, var_inv_i, table);
+            return launch_status("isb_up1_kernel");
+        }
+    }
+    if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
         isb_up_kernel<W, Tf, kSelect, GL, 3><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
             gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
     else
