@@ -42,7 +42,7 @@ DATA = "synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast pe
 # DRAM bytes (read + write) of sweep_batch_kernel per (frame, reference) instance with fp16 storage,
 # measured by ncu on one launch of an 8-frame batch of this workload (579,591,936 B read +
 # 1,029,880,576 B written for 16 instances)
-SWEEP_DRAM_BYTES_PER_INSTANCE = (579591936 + 1029880576) // 16
+SWEEP_DRAM_BYTES_PER_INSTANCE = (577766912 + 1028907008) // 16
 
 
 def _env_int(name, default):
@@ -212,6 +212,8 @@ def run_ours(args, rank, world, device, rendered):
     tuner = None if args.no_autotune else autotune.Tuner()
     est = _estimator(ss, calibration, device, args.storage, B, True, tuner)
     pipe = est.pipeline()
+    if args.overlap_groups is not None:
+        pipe.overlap_groups = args.overlap_groups
     mw, mh = WORKLOAD["matching"]
 
     # two input batches (B frames each, assembled from the rendered frames), device resident:
@@ -241,31 +243,36 @@ def run_ours(args, rank, world, device, rendered):
         torch.cuda.synchronize()
         barrier(world)
     ms = max_over_ranks(start.elapsed_time(end) / args.steps, world, device)
-    launches = pipe.launches_per_batch() * args.steps
+    launches = pipe.launches_per_batch(B, float_stitch=True) * args.steps
 
     # end to end through the public API: pinned host inputs in, panoramas back to pinned host
-    # memory, every step; the next batch's upload (copy stream) overlaps the current batch's work
+    # memory, every step.  The next batch's upload runs on an upload stream and the previous
+    # batch's download on a download stream, both overlapping the current batch's work: the
+    # outputs (which alias the pipeline's buffers) are first copied to one of two device slots.
     pinned = [(torch.as_tensor(m).pin_memory(), torch.as_tensor(st).pin_memory()) for m, st in host_batches]
     staging = [(torch.empty_like(dev_batches[0][0]), torch.empty_like(dev_batches[0][1])) for _ in range(2)]
-    out_rgb = torch.empty(pipe.rgb.shape, dtype=torch.uint8).pin_memory()
-    out_d = torch.empty(pipe.pano_distance.shape).pin_memory()
+    out_dev = [(torch.empty_like(pipe.rgb), torch.empty_like(pipe.pano_distance)) for _ in range(2)]
+    out_host = [(torch.empty(pipe.rgb.shape, dtype=torch.uint8).pin_memory(),
+                 torch.empty(pipe.pano_distance.shape).pin_memory()) for _ in range(2)]
     h2d = sum(t.numel() * t.element_size() for t in pinned[0])
-    d2h = out_rgb.numel() + out_d.numel() * 4
-    copy = torch.cuda.Stream(device)
+    d2h = out_host[0][0].numel() + out_host[0][1].numel() * 4
+    up_stream, down_stream = torch.cuda.Stream(device), torch.cuda.Stream(device)
     compute = torch.cuda.current_stream(device)
     uploaded = [torch.cuda.Event() for _ in range(2)]
     consumed = [torch.cuda.Event() for _ in range(2)]
+    produced = [torch.cuda.Event() for _ in range(2)]
+    downloaded = [torch.cuda.Event() for _ in range(2)]
 
     def upload(i):
         slot = i % 2
-        with torch.cuda.stream(copy):
-            copy.wait_event(consumed[slot])
+        with torch.cuda.stream(up_stream):
+            up_stream.wait_event(consumed[slot])
             for d, h in zip(staging[slot], pinned[i % 2]):
                 d.copy_(h, non_blocking=True)
-            uploaded[slot].record(copy)
+            uploaded[slot].record(up_stream)
 
     def e2e(steps):
-        for ev in consumed:
+        for ev in consumed + downloaded:
             ev.record(compute)
         upload(0)
         for i in range(steps):
@@ -275,8 +282,17 @@ def run_ours(args, rank, world, device, rendered):
             compute.wait_event(uploaded[slot])
             rgb, dist = est.estimate_RGBD_panoramas(*staging[slot])
             consumed[slot].record(compute)
-            out_rgb.copy_(rgb, non_blocking=True)
-            out_d.copy_(dist, non_blocking=True)
+            compute.wait_event(downloaded[slot])
+            out_dev[slot][0].copy_(rgb, non_blocking=True)
+            out_dev[slot][1].copy_(dist, non_blocking=True)
+            produced[slot].record(compute)
+            with torch.cuda.stream(down_stream):
+                down_stream.wait_event(produced[slot])
+                out_host[slot][0].copy_(out_dev[slot][0], non_blocking=True)
+                out_host[slot][1].copy_(out_dev[slot][1], non_blocking=True)
+                downloaded[slot].record(down_stream)
+        for ev in downloaded:
+            compute.wait_event(ev)  # the timed region ends with every output on the host
 
     e2e(args.warmup)
     torch.cuda.synchronize()
@@ -345,6 +361,7 @@ def run_ours(args, rank, world, device, rendered):
                      "launches_timed": len(rec.events)},
         "e2e_u8": e2e_u8,
         "tuned": pipe.tuned,
+        "overlap_groups": pipe._group_count(B),
     }
 
 
@@ -556,6 +573,8 @@ def main():
                          "64 candidates, every camera a reference; uneven: a mixed batch of jobs")
     ap.add_argument("--jobs", type=int, default=128, help="jobs of the uneven workload")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--overlap-groups", type=int, default=None,
+                    help="frame groups whose post-filter and stitch overlap the next group's sweep (default: tuned)")
     args = ap.parse_args()
 
     world = _env_int("WORLD_SIZE", 1)
@@ -611,7 +630,7 @@ def main():
             "vs_baseline": None, "dtype": f"{args.storage} storage, f32 arithmetic", "data": DATA,
             "config": {"workload": WORKLOAD_NAME, "batch_frames": args.batch,
                        "mode": f"batched, {args.storage} cost volume, fp32 arithmetic, CUDA-graph replay",
-                       "tuned": ours["tuned"],
+                       "tuned": ours["tuned"], "overlap_groups": ours["overlap_groups"],
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"each step reads a {args.batch}-frame batch of inputs "
                              f"({args.batch} x {(4 * 1024 * 1024 + len(WORKLOAD['refs']) * 1216 * 1216) * 12 / 1e6:.0f} MB), "

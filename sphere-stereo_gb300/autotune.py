@@ -33,6 +33,12 @@ KNOBS = {
 }
 
 
+# choices made by the caller rather than the library (name -> meaning), cached with the knobs
+CHOICES = {
+    "overlap_groups": "frame groups of a batch whose post-filter and stitch overlap the next group's sweep",
+}
+
+
 def default_cache_path() -> str:
     env = os.environ.get("SSG_TUNING_CACHE")
     if env:
@@ -97,8 +103,8 @@ class Tuner:
             with open(self.cache_path) as f:
                 data = json.load(f)
             if isinstance(data, dict):
-                self.cache = {k: {n: int(v) for n, v in d.items() if n in KNOBS} for k, d in data.items()
-                              if isinstance(d, dict)}
+                self.cache = {k: {n: int(v) for n, v in d.items() if n in KNOBS or n in CHOICES}
+                              for k, d in data.items() if isinstance(d, dict)}
         except (OSError, ValueError):
             pass
 
@@ -113,13 +119,35 @@ class Tuner:
             pass  # a read-only home keeps the results in memory only
 
     def apply(self, key: str) -> dict[str, int] | None:
-        """Sets the knobs cached for ``key``; returns them, or None when the key is not cached."""
+        """Sets the knobs cached for ``key``; returns them (with the cached caller choices), or None
+        when the key is not cached."""
         values = self.cache.get(key)
         if values is None:
             return None
         for name, v in values.items():
-            set_knob(name, v)
+            if name in KNOBS:
+                set_knob(name, v)
         return dict(values)
+
+    def pick(self, key: str, name: str, runs: dict, stream: int, repeats: int = 3) -> int:
+        """Times each whole launch sequence of ``runs`` (choice -> eager launches on ``stream``)
+        with CUDA events on that stream, caches the fastest choice as ``name`` for ``key`` and
+        returns it."""
+        s = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+        timings = {}
+        for value, run in runs.items():
+            run()  # warm-up
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            for _ in range(repeats):
+                run()
+            b.record(s)
+            b.synchronize()
+            timings[value] = a.elapsed_time(b) / repeats
+        best = min(timings, key=timings.get)
+        self.cache.setdefault(key, {})[name] = int(best)
+        self._save()
+        return int(best)
 
     def tune(self, key: str, run: Callable[[], None], knobs: list[str], repeats: int = 3,
              entry: str | None = None) -> dict[str, int]:

@@ -315,9 +315,15 @@ __device__ __forceinline__ void fine_setup(const typename GL::Pix (&gd)[9], cons
     const int fx = 2 * x + (F >= 2 ? 1 : 0), fy = 2 * y + (F & 1);
     // a fine pixel outside the level is the clamped duplicate of another one and is skipped
     px.active = coarse_ok && fx < g.cols_out && fy < g.rows_out;
-    px.index = fy * g.cols_out + fx;
+    // an inactive pixel reads pixel 0 with zero weights (the selecting step filters it without a
+    // branch and drops the result)
+    px.index = px.active ? fy * g.cols_out + fx : 0;
     px.inv = 0.0f;
-    if (!px.active) return;
+    if (!px.active) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) px.w[i] = 0.0f;
+        return;
+    }
     float gsum[3];
     const typename GL::Pix up = GL::load(guide_io, px.index);
     px.inv = fine_weights_padded<F, GL>(gd, up, weight_up, weight_down, range, px.w, gsum);
@@ -381,8 +387,8 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
             }
         }
         const int k0 = c * W + part * E;
-        if (pa.active) up_part<FA, W, Tf, kSelect>(tap, pa, ra, part, k0, full, ncand, weight_up, fine_chunk, sa);
-        if (pb.active) up_part<FB, W, Tf, kSelect>(tap, pb, rb, part, k0, full, ncand, weight_up, fine_chunk, sb);
+        if (kSelect || pa.active) up_part<FA, W, Tf, kSelect>(tap, pa, ra, part, k0, full, ncand, weight_up, fine_chunk, sa);
+        if (kSelect || pb.active) up_part<FB, W, Tf, kSelect>(tap, pb, rb, part, k0, full, ncand, weight_up, fine_chunk, sb);
     }
 }
 
@@ -431,8 +437,8 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     cp_async_commit();
     // fine cells are read once, from memory: prefetched a chunk ahead of their use
     RawCell<W, Tf> ra, rb;
-    if (pa.active) ra.load(cost_fine + (int64_t)pa.index * W);
-    if (pb.active) rb.load(cost_fine + (int64_t)pb.index * W);
+    if (kSelect || pa.active) ra.load(cost_fine + (int64_t)pa.index * W);
+    if (kSelect || pb.active) rb.load(cost_fine + (int64_t)pb.index * W);
     for (int c = 0; c < chunks; ++c) {
         if (c + 1 < chunks)
             load_tile_async<W>(sh.tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in, x0,
@@ -441,8 +447,8 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
         RawCell<W, Tf> na = ra, nb = rb;
         if (c + 1 < chunks) {
             const Tf* next = cost_fine + (int64_t)(c + 1) * pio * W;
-            if (pa.active) na.load(next + (int64_t)pa.index * W);
-            if (pb.active) nb.load(next + (int64_t)pb.index * W);
+            if (kSelect || pa.active) na.load(next + (int64_t)pa.index * W);
+            if (kSelect || pb.active) nb.load(next + (int64_t)pb.index * W);
         }
         cp_async_wait_one();  // this chunk's tile has landed
         __syncthreads();

@@ -29,12 +29,21 @@ F32 = 2
 
 
 class BatchPipeline:
+    MAX_GROUPS = 8
+
     def __init__(self, estimator, max_frames: int, storage: str = "fp16", cuda_graphs: bool = True,
-                 tuner=None):
+                 tuner=None, overlap_groups: int | None = None):
+        """overlap_groups: the batch's frames are split into this many groups; the distance
+        post-filter and the stitch of a group run on a second stream while the next group's sweep
+        and cost filter run (1 = one group, no overlap; None = the tuner's pick, or 1 without a
+        tuner)."""
         if storage not in STORAGE:
             raise ValueError(f"storage must be one of {sorted(STORAGE)}")
         if max_frames < 1:
             raise ValueError("max_frames must be positive")
+        if overlap_groups is not None and not 1 <= overlap_groups <= self.MAX_GROUPS:
+            raise ValueError(f"overlap_groups must be in [1, {self.MAX_GROUPS}]")
+        self.overlap_groups = overlap_groups
         e = estimator
         self.e = e
         self.device = e.device
@@ -75,7 +84,7 @@ class BatchPipeline:
         self.distance = torch.empty(F, R, self.rows, self.cols, **f32)
         self.reprojected = torch.empty(F * R * P, **f32)
         self.stamps = torch.empty(F * R * P, **u8)
-        self.holes = torch.empty(3 * F * R * P + 4, dtype=torch.int32, device=dev)
+        self.holes = torch.empty(3 * F * R * P + 4 * self.MAX_GROUPS, dtype=torch.int32, device=dev)
         self.images_u8 = torch.empty(F, R, st.image_rows, st.image_cols, 3, **u8)
         self.rgb = torch.empty(F, st.pano_rows, st.pano_cols, 3, **u8)
         self.pano_distance = torch.empty(F, st.pano_rows, st.pano_cols, **f32)
@@ -84,72 +93,145 @@ class BatchPipeline:
         self._refs = N.ints(e.references_indices)
         self._poses = N.floats([v for r in e.references_indices for v in e._poses_list[r]])
         self._graphs: dict = {}
+        self._side = torch.cuda.Stream(dev)  # the post-filter and stitch of overlapped groups
         # launch shapes: picked by the autotuner on first use (``tuner``: an autotune.Tuner, or
         # None for the library's defaults)
         self.tuner = tuner
         self.tuned: dict[str, int] | None = None
 
     # ------------------------------------------------------------------------------------
-    def _launch(self, match: torch.Tensor, stitch: torch.Tensor, frames: int, stream: int) -> None:
-        e, st = self.e, self.st
-        inst = frames * self.R
-        cols, rows, P = self.cols, self.rows, self.P
+    def _estimate(self, match: torch.Tensor, f0: int, frames: int, stream: int) -> None:
+        """Staging, sweep, cost filter and selection of frames [f0, f0 + frames)."""
+        e = self.e
+        R, C, P = self.R, self.C, self.P
+        i0, inst = f0 * R, frames * R
+        cols, rows = self.cols, self.rows
         stage = "ssg_stage_images_u8" if match.dtype == torch.uint8 else "ssg_stage_images"
-        N.call(stage, match.data_ptr(), frames, self.C, cols, rows, self._refs, self.R, self.staged.data_ptr(),
-               self.guides[0].data_ptr(), self.plane_flags.data_ptr(), stream)
-        floats = None if match.dtype == torch.uint8 else match.data_ptr()
-        N.call("ssg_sweep_cost_batch", cols, rows, frames, self.C, e._cams, self.R, self._refs, self._poses,
-               self.staged.data_ptr(), floats, self.plane_flags.data_ptr(), self.selected.data_ptr(), e._candidates,
-               self.N, self.storage, self.costs[0].data_ptr(), stream)
+        plane = (rows + 2) * (cols + 2) * 4  # floats of one plane of footprints
+        staged = self.staged.data_ptr() + 4 * f0 * C * plane
+        flags = self.plane_flags.data_ptr() + 4 * f0 * C
+        m = match[f0:f0 + frames]
+        N.call(stage, m.data_ptr(), frames, C, cols, rows, self._refs, R, staged,
+               self.guides[0].data_ptr() + 4 * i0 * P, flags, stream)
+        floats = None if match.dtype == torch.uint8 else m.data_ptr()
+        cell0 = 2 * 8 * self.chunks  # bytes of a level-0 pixel's cells
+        N.call("ssg_sweep_cost_batch", cols, rows, frames, C, e._cams, R, self._refs, self._poses, staged, floats,
+               flags, self.selected.data_ptr(), e._candidates, self.N, self.storage,
+               self.costs[0].data_ptr() + cell0 * i0 * P, stream)
         var_inv_i = 1 / (2 * e.sigma_i * e.sigma_i)
         L = self.L
+
+        def guide(s):
+            r, c = self.shapes[s]
+            return self.guides[s].data_ptr() + 4 * i0 * r * c
+
+        def cost(s):
+            r, c = self.shapes[s]
+            return self.costs[s].data_ptr() + (cell0 if s == 0 else 4 * 8 * self.chunks) * i0 * r * c
+
         if L >= 2:
             weights = level_weights(L, e.sigma_s)
             for s in range(1, L):
                 (ri, ci), (ro, co) = self.shapes[s - 1], self.shapes[s]
-                N.call("ssg_isb_downsample_batch", self.guides[s - 1].data_ptr(), self.costs[s - 1].data_ptr(), ri, ci,
-                       self.guides[s].data_ptr(), self.costs[s].data_ptr(), ro, co, self.N, inst,
-                       self.storage if s == 1 else F32, var_inv_i, stream)
+                N.call("ssg_isb_downsample_batch", guide(s - 1), cost(s - 1), ri, ci, guide(s), cost(s), ro, co,
+                       self.N, inst, self.storage if s == 1 else F32, var_inv_i, stream)
             for s in range(L - 2, 0, -1):
                 (rc, cc), (rf, cf) = self.shapes[s + 1], self.shapes[s]
                 wu, wd = weights[s]
-                N.call("ssg_isb_upsample_batch", self.guides[s + 1].data_ptr(), self.costs[s + 1].data_ptr(), rc, cc,
-                       self.guides[s].data_ptr(), self.costs[s].data_ptr(), rf, cf, self.N, inst, F32, wu, wd,
-                       var_inv_i, stream)
+                N.call("ssg_isb_upsample_batch", guide(s + 1), cost(s + 1), rc, cc, guide(s), cost(s), rf, cf,
+                       self.N, inst, F32, wu, wd, var_inv_i, stream)
         # the selection writes the raw distance and, for the post-filter to filter in place, a copy
-        dist = self.distance.view(-1)[: inst * P]
+        dist = self.distance.view(-1)[i0 * P:(i0 + inst) * P]
+        raw = self.distance_raw.data_ptr() + 4 * i0 * P
+        index = self.index.data_ptr() + 4 * i0 * P
         if L >= 2:
             (rc, cc) = self.shapes[1]
             wu, wd = weights[0]
-            N.call("ssg_isb_upsample_select_batch", self.guides[1].data_ptr(), self.costs[1].data_ptr(), rc, cc,
-                   self.guides[0].data_ptr(), self.costs[0].data_ptr(), rows, cols, self.N, inst, self.storage, wu, wd,
-                   var_inv_i, e._candidates, self.distance_raw.data_ptr(), self.index.data_ptr(), dist.data_ptr(),
-                   stream)
+            N.call("ssg_isb_upsample_select_batch", guide(1), cost(1), rc, cc, guide(0), cost(0), rows, cols, self.N,
+                   inst, self.storage, wu, wd, var_inv_i, e._candidates, raw, index, dist.data_ptr(), stream)
         else:
-            N.call("ssg_select_distance_batch", self.costs[0].data_ptr(), self.N, P, inst, self.storage,
-                   e._candidates, self.distance_raw.data_ptr(), self.index.data_ptr(), stream)
-            dist.copy_(self.distance_raw[: inst * P])
+            N.call("ssg_select_distance_batch", cost(0), self.N, P, inst, self.storage, e._candidates, raw, index,
+                   stream)
+            with torch.cuda.stream(self._stream(stream)):
+                dist.copy_(self.distance_raw[i0 * P:(i0 + inst) * P])
+
+    def _finish(self, stitch: torch.Tensor, f0: int, frames: int, group: int, stream: int) -> None:
+        """Distance post-filter and stitch of frames [f0, f0 + frames)."""
+        e, st = self.e, self.st
+        R, P = self.R, self.P
+        i0, inst = f0 * R, frames * R
+        cols, rows = self.cols, self.rows
+        L = self.L
+        dist = self.distance.view(-1)[i0 * P:(i0 + inst) * P]
         # distance post-filter on the unfiltered guide (python/depth_estimation.py:200-203)
         if L >= 2:
-            N.call("ssg_isb_apply_batch", N.pointers([g.data_ptr() for g in self.df_guides]),
-                   N.pointers([dist.data_ptr()] + [c.data_ptr() for c in self.df_costs]), L, rows, cols, 1, inst,
+            df_guides = [self.guides[0].data_ptr() + 4 * i0 * P] + [
+                g.data_ptr() + 4 * i0 * r * c for g, (r, c) in zip(self.df_guides[1:], self.shapes[1:])]
+            df_costs = [dist.data_ptr()] + [c.data_ptr() + 4 * i0 * r * cc
+                                            for c, (r, cc) in zip(self.df_costs, self.shapes[1:])]
+            N.call("ssg_isb_apply_batch", N.pointers(df_guides), N.pointers(df_costs), L, rows, cols, 1, inst,
                    float(e.sigma_i) / 2, float(e.sigma_s) / 2, N.ISB_SKIP_FINE_GUIDE, stream)
         # stitch (python/stitcher.py:166-220)
+        s_img = stitch[f0:f0 + frames]
         if stitch.dtype == torch.uint8:
-            images_u8 = stitch
+            images_u8 = s_img
         else:
-            images_u8 = self.images_u8
+            images_u8 = self.images_u8[f0:f0 + frames]
             # float -> uint8 truncation (depth_estimation.py:239)
-            N.call("ssg_convert_u8", stitch.data_ptr(), images_u8.data_ptr(), frames * self.R * st.image_rows *
-                   st.image_cols * 3, stream)
-        N.call("ssg_reproject_distance_batch", dist.data_ptr(), self.reprojected.data_ptr(), cols, rows, inst, self.R,
-               st._intr, st._trans, 1, stream)
-        N.call("ssg_inpaint_holes_batch", self.reprojected.data_ptr(), self.tables.data_ptr(), self.stamps.data_ptr(),
-               self.holes.data_ptr(), cols, rows, inst, self.R, st.max_dist, st.inpainting_iterations, stream)
+            N.call("ssg_convert_u8", s_img.data_ptr(), images_u8.data_ptr(),
+                   frames * R * st.image_rows * st.image_cols * 3, stream)
+        reprojected = self.reprojected.data_ptr() + 4 * i0 * P
+        N.call("ssg_reproject_distance_batch", dist.data_ptr(), reprojected, cols, rows, inst, R, st._intr, st._trans,
+               1, stream)
+        holes = self.holes.data_ptr() + 4 * (3 * i0 * P + 4 * group)
+        N.call("ssg_inpaint_holes_batch", reprojected, self.tables.data_ptr(), self.stamps.data_ptr() + i0 * P, holes,
+               cols, rows, inst, R, st.max_dist, st.inpainting_iterations, stream)
         N.call("ssg_merge_panorama_batch_approx", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
-               self.reprojected.data_ptr(), dist.data_ptr(), images_u8.data_ptr(), st.image_rows, st.image_cols,
-               st._trans, st._intr, self.R, cols, rows, st.pano_cols, st.pano_rows, frames,
-               self.pano_distance.data_ptr(), self.rgb.data_ptr(), stream)
+               reprojected, dist.data_ptr(), images_u8.data_ptr(), st.image_rows, st.image_cols, st._trans, st._intr,
+               R, cols, rows, st.pano_cols, st.pano_rows, frames, self.pano_distance[f0].data_ptr(),
+               self.rgb[f0].data_ptr(), stream)
+
+    def _stream(self, handle: int) -> torch.cuda.Stream:
+        if not handle:
+            return torch.cuda.default_stream(self.device)
+        return torch.cuda.ExternalStream(handle, device=self.device)
+
+    def _groups(self, frames: int, groups: int) -> list[tuple[int, int]]:
+        groups = max(1, min(groups, frames))
+        base, extra = divmod(frames, groups)
+        out, f0 = [], 0
+        for g in range(groups):
+            n = base + (1 if g < extra else 0)
+            out.append((f0, n))
+            f0 += n
+        return out
+
+    def _group_count(self, frames: int) -> int:
+        if self.overlap_groups is not None:
+            return self.overlap_groups
+        if self.tuned is not None and "overlap_groups" in self.tuned:
+            return self.tuned["overlap_groups"]
+        return 1
+
+    def _launch(self, match: torch.Tensor, stitch: torch.Tensor, frames: int, stream: int,
+                groups: int | None = None) -> None:
+        groups = self._group_count(frames) if groups is None else groups
+        parts = self._groups(frames, groups)
+        if len(parts) == 1:
+            self._estimate(match, 0, frames, stream)
+            self._finish(stitch, 0, frames, 0, stream)
+            return
+        main = self._stream(stream)
+        side = self._side
+        for g, (f0, n) in enumerate(parts):
+            self._estimate(match, f0, n, stream)
+            ready = torch.cuda.Event()
+            ready.record(main)
+            side.wait_event(ready)
+            self._finish(stitch, f0, n, g, side.cuda_stream)
+        done = torch.cuda.Event()
+        done.record(side)
+        main.wait_event(done)
 
     def run(self, match: torch.Tensor, stitch: torch.Tensor):
         """match: [F, C, rows, cols, 3], stitch: [F, R, image_rows, image_cols, 3], each float32 or
@@ -166,7 +248,7 @@ class BatchPipeline:
         if not self.cuda_graphs:
             self._launch(match, stitch, frames, N.stream_of(match))
         else:
-            key = (match.data_ptr(), match.dtype, stitch.data_ptr(), stitch.dtype, frames)
+            key = (match.data_ptr(), match.dtype, stitch.data_ptr(), stitch.dtype, frames, self._group_count(frames))
             graph = self._graphs.get(key)
             if graph is None:
                 # one eager run (first-use set-up such as shared-memory opt-in happens outside capture)
@@ -185,9 +267,11 @@ class BatchPipeline:
         return self.rgb[:frames], self.pano_distance[:frames]
 
     TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "hole_blocks_per_sm", "merge_frames")
+    GROUP_CHOICES = (1, 2, 4)
 
     def _apply_tuning(self, match, stitch, frames) -> None:
-        """Sets this pipeline's launch shapes (process-wide knobs), tuning them on first use."""
+        """Sets this pipeline's launch shapes (process-wide knobs), tuning them on first use; then
+        picks the overlap group count (unless the caller fixed it) by timing whole batches."""
         if self.tuner is None:
             return
         from . import autotune
@@ -196,17 +280,26 @@ class BatchPipeline:
             key = autotune.workload_key("batch", self.cols, self.rows, self.N, self.C, self.R, frames,
                                         self.storage_name, self.st.pano_cols, self.st.pano_rows)
             self.tuned = self.tuner.apply(key)
-            if self.tuned is None:
-                stream = N.stream_of(match)
-                self.tuned = self.tuner.tune(key, lambda: self._launch(match, stitch, frames, stream),
+            stream = N.stream_of(match)
+            if self.tuned is None or not set(self.TUNED_KNOBS) <= set(self.tuned):
+                self.tuned = self.tuner.tune(key, lambda: self._launch(match, stitch, frames, stream, groups=1),
                                              list(self.TUNED_KNOBS))
+            if self.overlap_groups is None and "overlap_groups" not in self.tuned:
+                runs = {g: (lambda g=g: self._launch(match, stitch, frames, stream, groups=g))
+                        for g in self.GROUP_CHOICES if g <= frames}
+                self.tuned["overlap_groups"] = self.tuner.pick(key, "overlap_groups", runs, stream)
         for name, v in self.tuned.items():
-            autotune.set_knob(name, v)
+            if name in autotune.KNOBS:
+                autotune.set_knob(name, v)
 
-    def launches_per_batch(self) -> int:
+    def launches_per_batch(self, frames: int | None = None, float_stitch: bool = True) -> int:
+        """Kernels one batch of ``frames`` frames launches (float32 images to stitch add a
+        conversion per group)."""
+        frames = self.max_frames if frames is None else frames
         L = self.L
         isb = (L - 1) + (L - 2) + 1 if L >= 2 else 1
         post = 2 * (L - 1) if L >= 2 else 0
         it = self.st.inpainting_iterations
         inpaint = 0 if it == 0 else 1 + it
-        return 2 + isb + post + 2 + inpaint + 1
+        per_group = 2 + isb + post + (1 if float_stitch else 0) + 2 + inpaint + 1
+        return per_group * len(self._groups(frames, self._group_count(frames)))

@@ -101,6 +101,20 @@ def test_batch_equals_single_frames_and_graphs_equal_eager(ss, native, golden_sm
     stitch2.copy_(stitch.flip(0))
     rgb_f, _ = est.estimate_RGBD_panoramas(match2, stitch2)
     torch.testing.assert_close(rgb_f[0], rgb3[2], rtol=0, atol=0)
+    # frame groups whose post-filter and stitch run on a second stream: the same bits, with and
+    # without graphs, uint8 and float32 images to stitch
+    for groups in (2, 3):
+        for graphs in (True, False):
+            ov, _ = _estimator(ss, g, "fp16", max_batch=3, graphs=graphs)
+            ov.pipeline().overlap_groups = groups
+            for s_in in (stitch, stitch.to(torch.uint8)):
+                rgb_o, d_o = ov.estimate_RGBD_panoramas(match, s_in)
+                torch.testing.assert_close(rgb_o, rgb3, rtol=0, atol=0)
+                torch.testing.assert_close(d_o, d3, rtol=0, atol=0)
+            pipe = ov.pipeline()
+            n = pipe.launches_per_batch(3)
+            pipe.overlap_groups = 1
+            assert n == groups * pipe.launches_per_batch(3)
 
 
 def test_single_frame_api_on_16_bit_storage(ss, native, golden_small):
