@@ -110,6 +110,53 @@ __global__ void __launch_bounds__(kStitchBlock) box_filter_kernel(const float* _
     out[(int64_t)plane * P + i] = s;
 }
 
+// The same box mean from a shared-memory tile: a block stages the products v * kw of its
+// (kBoxX + 2r) x (kBoxY + 2r) input window once, then each thread sums the (2r + 1)^2 products of
+// each of its kBoxK outputs in the same row-major window order (identical bits).  Threads of a
+// warp take consecutive columns, so the tile reads are conflict-free.
+constexpr int kBoxX = 64, kBoxY = 32, kBoxThreadsX = 32, kBoxThreadsY = 8;
+
+__host__ __device__ constexpr int box_tile_floats(int radius)
+{
+    return (kBoxX + 2 * radius) * (kBoxY + 2 * radius);
+}
+
+__global__ void __launch_bounds__(kBoxThreadsX * kBoxThreadsY) box_filter_tiled_kernel(
+    const float* __restrict__ in, int rows, int cols, int radius, float pad, float kw, float* __restrict__ out)
+{
+    extern __shared__ float tile[];
+    const int64_t P = (int64_t)cols * rows;
+    const int plane = blockIdx.z;
+    const float* src = in + (int64_t)plane * P;
+    const int x0 = blockIdx.x * kBoxX, y0 = blockIdx.y * kBoxY;
+    const int tw = kBoxX + 2 * radius, th = kBoxY + 2 * radius;
+    const float pad_product = fmul(pad, kw);
+    for (int q = threadIdx.x; q < tw * th; q += blockDim.x) {
+        const int lx = q % tw, ly = q / tw;
+        const int xx = x0 - radius + lx, yy = y0 - radius + ly;
+        tile[q] = (xx >= 0 && yy >= 0 && xx < cols && yy < rows) ? fmul(__ldg(src + (int64_t)yy * cols + xx), kw)
+                                                                : pad_product;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % kBoxThreadsX, ty = threadIdx.x / kBoxThreadsX;
+    const int side = 2 * radius + 1;
+    for (int m = 0; m < kBoxY / kBoxThreadsY; ++m) {
+        const int ly = ty + m * kBoxThreadsY, y = y0 + ly;
+        if (y >= rows) break;
+#pragma unroll
+        for (int k = 0; k < kBoxX / kBoxThreadsX; ++k) {
+            const int lx = tx + k * kBoxThreadsX, x = x0 + lx;
+            if (x >= cols) continue;
+            float s = 0.0f;
+            for (int dy = 0; dy < side; ++dy) {
+                const float* row = tile + (ly + dy) * tw + lx;
+                for (int dx = 0; dx < side; ++dx) s = fadd(s, row[dx]);
+            }
+            out[(int64_t)plane * P + (int64_t)y * cols + x] = s;
+        }
+    }
+}
+
 struct LutParams {
     int cols, rows, pano_cols, pano_rows, nref;
     float dmin, dmax;
@@ -830,6 +877,14 @@ extern "C" int ssg_box_filter(const float* d_in, int planes, int rows, int cols,
     const int64_t P = (int64_t)cols * rows;
     const int side = 2 * radius + 1;
     const float kw = 1.0f / (float)(side * side);
+    const size_t smem = sizeof(float) * (size_t)box_tile_floats(radius);
+    if (radius <= 64 && smem <= 48 * 1024) {
+        const dim3 grid((unsigned)((cols + kBoxX - 1) / kBoxX), (unsigned)((rows + kBoxY - 1) / kBoxY), planes);
+        SSG_REQUIRE(grid.y <= 65535, "maps of %d rows are too tall", rows);
+        box_filter_tiled_kernel<<<grid, kBoxThreadsX * kBoxThreadsY, smem, as_stream(stream)>>>(
+            d_in, rows, cols, radius, pad_value, kw, d_out);
+        return launch_status("box_filter_tiled_kernel");
+    }
     dim3 grid(grid_1d(P, kStitchBlock), planes);
     box_filter_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(d_in, rows, cols, radius, pad_value, kw, d_out);
     return launch_status("box_filter_kernel");

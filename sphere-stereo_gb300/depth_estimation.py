@@ -111,6 +111,7 @@ class RGBD_Estimator:
         self.distance_raw_maps = torch.empty([len(self.references_indices), rows, cols], device=device)
         # per reference: the selected candidate index (torch.min's index, depth_estimation.py:180)
         self.index_maps = torch.empty([len(self.references_indices), rows, cols], dtype=torch.int32, device=device)
+        self._masks = masks  # kept for re-selection after a rig update
         self.select_camera(masks)
         self.cost_storage = cost_storage
         self.max_batch = int(max_batch)
@@ -178,6 +179,39 @@ class RGBD_Estimator:
         return self._pipeline
 
     # --------------------------------------------------------------------------------------
+    def update_extrinsics(self, rts=None, reprojection_viewpoint=None) -> None:
+        """Calibration refinement without rebuilding the estimator (no counterpart in the
+        reference, which fixes the rig in its constructor): new camera -> rig poses ``rts``
+        (one [4, 4] per camera; None keeps them) and/or a new ``reprojection_viewpoint``.
+
+        Recomputes what depends on them, on the GPU and in place: the relative poses of the
+        sweep, the camera selection (python/depth_estimation.py:83-135) and the stitcher's
+        translations, inpainting tables, blending LUT and weights (python/stitcher.py:126-164).
+        Intrinsics, resolutions, masks, buffers and tuned launch shapes stay; the batched
+        pipeline's captured graphs are dropped and recaptured on the next batch.  Results equal
+        those of an estimator constructed with the new poses.  An UnevenBatch built from this
+        estimator holds the old poses in its descriptors and must be rebuilt."""
+        if rts is not None:
+            if len(rts) != len(self.calibrations):
+                raise ValueError(f"expected {len(self.calibrations)} poses, got {len(rts)}")
+            new = []
+            for c, rt in zip(self.calibrations, rts):
+                t = torch.as_tensor(rt, dtype=torch.float32)
+                if tuple(t.shape) != (4, 4) or not bool(torch.isfinite(t).all()):
+                    raise ValueError("each pose must be a finite [4, 4] matrix")
+                new.append(t.to(c.rt.device) if isinstance(c.rt, torch.Tensor) else t)
+            for c, t in zip(self.calibrations, new):
+                c.rt = t
+            self._poses_list = {r: relative_poses(self.calibrations, r) for r in self.references_indices}
+            self._poses = {r: N.floats(v) for r, v in self._poses_list.items()}
+            self.select_camera(self._masks)
+        if reprojection_viewpoint is not None:
+            self.reprojection_viewpoint = reprojection_viewpoint
+        self.fishey_stitcher.update_extrinsics([self.calibrations[r] for r in self.references_indices],
+                                               self.reprojection_viewpoint)
+        if self._pipeline is not None:
+            self._pipeline.refresh_rig()
+
     def select_camera(self, masks):
         """Per reference pixel, the camera with the largest near-far displacement
         (python/depth_estimation.py:83-135).  Fills ``selected_cameras`` ([1, rows, cols] int64,

@@ -99,6 +99,16 @@ class BatchPipeline:
         self.tuner = tuner
         self.tuned: dict[str, int] | None = None
 
+    def refresh_rig(self) -> None:
+        """Takes the estimator's updated rig (RGBD_Estimator.update_extrinsics): camera selection
+        and inpainting tables copied in place, poses re-read, captured graphs dropped (their
+        launches hold the old poses as parameters)."""
+        e = self.e
+        self.selected.copy_(torch.stack(e._selected))
+        self.tables.copy_(torch.stack(self.st.inpainting_weights_list))
+        self._poses = N.floats([v for r in e.references_indices for v in e._poses_list[r]])
+        self._graphs.clear()
+
     # ------------------------------------------------------------------------------------
     def _estimate(self, match: torch.Tensor, f0: int, frames: int, stream: int) -> None:
         """Staging, sweep, cost filter and selection of frames [f0, f0 + frames)."""

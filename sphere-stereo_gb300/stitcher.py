@@ -75,33 +75,60 @@ class Stitcher:
         self.distance_panorama = torch.zeros([Hp, Wp], device=device)
 
         # tables (python/stitcher.py:126-164); small matrices on the CPU in float32
-        vp = torch.cat([_cpu32(reprojection_viewpoint), torch.ones(1)])
         self.intrinsics = [intrinsics_struct(c) for c in calibrations]
         self.calibration_vectors_list = [vectorize_calibration(c, device) for c in calibrations]
+        self.calibration_vectors = torch.cat(self.calibration_vectors_list).contiguous()
+        self._intr = N.intrinsics_array(self.intrinsics)
+        self.smoothing_radius = int(smoothing_radius)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        # the smoothed masks depend on the masks only: kept for rig updates
+        mask_stack = torch.stack([torch.as_tensor(m, dtype=torch.float32).reshape(H, W) for m in masks]).to(device)
+        mask_stack = mask_stack.contiguous()
+        self.smoothed_masks = torch.empty_like(mask_stack)
+        N.call("ssg_box_filter", mask_stack.data_ptr(), R, H, W, self.smoothing_radius, 1.0,
+               self.smoothed_masks.data_ptr(), stream)
+        self._raw_weights = torch.empty_like(self.blending_weights)
+        self._build_tables(calibrations, reprojection_viewpoint, stream)
+
+    def _build_tables(self, calibrations, reprojection_viewpoint, stream: int) -> None:
+        """The tables that depend on the references' poses and the viewpoint: translations,
+        inpainting tables, blending LUT and weights (python/stitcher.py:126-164)."""
+        H, W, Hp, Wp = self.rows, self.cols, self.pano_rows, self.pano_cols
+        R = self.reference_count
+        vp = torch.cat([_cpu32(reprojection_viewpoint), torch.ones(1)])
         translations = [torch.matmul(torch.inverse(_cpu32(c.rt)), vp)[:3] for c in calibrations]
         self.translations_host = torch.cat(translations).contiguous()
-        self.translations = self.translations_host.to(device)
+        if hasattr(self, "translations"):
+            self.translations.copy_(self.translations_host)
+        else:
+            self.translations = self.translations_host.to(self.device)
         self.translations_list = [self.translations[3 * i:3 * i + 3] for i in range(R)]
-        self.calibration_vectors = torch.cat(self.calibration_vectors_list).contiguous()
         rotations = torch.cat([torch.inverse(_cpu32(c.rt)[:3, :3]) for c in calibrations]).contiguous()
-        self._intr = N.intrinsics_array(self.intrinsics)
         self._trans = N.floats(self.translations_host.tolist())
-        stream = torch.cuda.current_stream(device).cuda_stream
         for r, table in enumerate(self.inpainting_weights_list):
             N.call("ssg_inpainting_table", W, H, N.intrinsics_array([self.intrinsics[r]]),
                    N.floats(translations[r].tolist()), self.min_dist, self.max_dist, table.data_ptr(), stream)
-        mask_stack = torch.stack([torch.as_tensor(m, dtype=torch.float32).reshape(H, W) for m in masks]).to(device)
-        mask_stack = mask_stack.contiguous()
-        smoothed_masks = torch.empty_like(mask_stack)
-        N.call("ssg_box_filter", mask_stack.data_ptr(), R, H, W, int(smoothing_radius), 1.0, smoothed_masks.data_ptr(),
-               stream)
-        raw_weights = torch.empty_like(self.blending_weights)
         N.call("ssg_blending_lut", W, H, Wp, Hp, R, self._intr, N.floats(rotations.reshape(-1).tolist()), self._trans,
-               smoothed_masks.data_ptr(), self.min_dist, self.max_dist, self.blending_sampling.data_ptr(),
-               raw_weights.data_ptr(), stream)
-        N.call("ssg_box_filter", raw_weights.data_ptr(), R, Hp, Wp, int(smoothing_radius), 0.0,
+               self.smoothed_masks.data_ptr(), self.min_dist, self.max_dist, self.blending_sampling.data_ptr(),
+               self._raw_weights.data_ptr(), stream)
+        N.call("ssg_box_filter", self._raw_weights.data_ptr(), R, Hp, Wp, self.smoothing_radius, 0.0,
                self.blending_weights.data_ptr(), stream)
         N.call("ssg_normalize_weights", self.blending_weights.data_ptr(), R, Hp * Wp, stream)
+
+    def update_extrinsics(self, calibrations, reprojection_viewpoint) -> None:
+        """Rebuilds the pose-dependent tables in place after the references' extrinsics (``rt``)
+        or the viewpoint changed (calibration refinement; no counterpart in the reference, which
+        builds them once in its constructor).  Intrinsics, resolutions and masks stay; buffers
+        keep their addresses.  The result equals a Stitcher constructed with the new poses."""
+        if len(calibrations) != self.reference_count:
+            raise ValueError(f"expected {self.reference_count} calibrations, got {len(calibrations)}")
+        def fields(k):
+            return tuple(getattr(k, f) for f, _ in k._fields_)
+
+        for c, k in zip(calibrations, self.intrinsics):
+            if fields(intrinsics_struct(c)) != fields(k):
+                raise ValueError("update_extrinsics keeps the intrinsics; construct a new Stitcher to change them")
+        self._build_tables(calibrations, reprojection_viewpoint, torch.cuda.current_stream(self.device).cuda_stream)
 
     def reproject_and_inpaint(self, reference: int, distance_map: torch.Tensor) -> None:
         """Reprojected, hole-filled distance map of one reference (python/stitcher.py:184-200)
