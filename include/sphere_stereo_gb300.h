@@ -72,11 +72,14 @@ typedef struct {
  * workload by the Python autotuner (sphere-stereo_gb300/autotune.py).  Process-wide; read when a
  * launch is enqueued, so a captured CUDA graph keeps the values it was captured with. */
 #define SSG_TUNE_SWEEP_VARIANT 0      /* sweep block shape: 0 = 256 threads x 4 blocks/SM (64 registers),
-                                         1 = 256 x 3 (80 registers), 2 = 128 x 8 (64 registers) */
+                                         1 = 256 x 3 (80 registers), 2 = 128 x 8 (64 registers),
+                                         3 = 128 x 7 (72 registers) */
 #define SSG_TUNE_HOLE_BLOCKS_PER_SM 1 /* blocks per SM of the hole-filling steps: 2, 4, 8 */
 #define SSG_TUNE_MERGE_FRAMES 2       /* frames one thread of the batched merge handles: 2, 4, 8 */
 #define SSG_TUNE_UNEVEN_SPAN 3        /* 256-pixel tiles per work item of the uneven sweep: 1, 2, 4 */
-#define SSG_TUNE_ISB_UP_BLOCKS 4      /* blocks per SM the chunked ISB upsampling is register-bounded for: 2, 3 */
+#define SSG_TUNE_ISB_UP_BLOCKS 4      /* blocks per SM the chunked ISB upsampling (coarse levels) is
+                                         register-bounded for: 2, 3 */
+#define SSG_TUNE_ISB_SELECT_BLOCKS 5  /* the same for the last level fused with the selection: 2, 3 */
 SSG_API int ssg_tuning_set(int knob, int value);
 /* The knob's current value (-1 for an unknown knob). */
 SSG_API int ssg_tuning_get(int knob);

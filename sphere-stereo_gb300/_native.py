@@ -28,6 +28,7 @@ TUNE_HOLE_BLOCKS_PER_SM = 1
 TUNE_MERGE_FRAMES = 2
 TUNE_UNEVEN_SPAN = 3
 TUNE_ISB_UP_BLOCKS = 4
+TUNE_ISB_SELECT_BLOCKS = 5
 ISB_SKIP_FINE_GUIDE = 1
 PIXEL_U8 = 0
 PIXEL_F32 = 1

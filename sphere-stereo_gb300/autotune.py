@@ -2,7 +2,8 @@
 
 The library exposes a few launch-shape knobs (include/sphere_stereo_gb300.h, SSG_TUNE_*): the
 sweep's block shape, the blocks per SM of the hole-filling steps, the frames one merge thread
-handles, the work-item span of the uneven sweep and the register bound of the ISB upsampling.  For a workload (a key naming the device and
+handles, the work-item span of the uneven sweep and the register bounds of the ISB upsampling
+(coarse levels and the fused selecting level).  For a workload (a key naming the device and
 the shapes), ``Tuner.tune`` runs the caller's launch sequence eagerly, times the entry point each
 knob affects with CUDA events on the stream it is enqueued on, one knob at a time over its
 choices (coordinate descent: the knobs act on different kernels), and keeps the fastest.  Results
@@ -29,7 +30,8 @@ KNOBS = {
     "hole_blocks_per_sm": (N.TUNE_HOLE_BLOCKS_PER_SM, ("ssg_inpaint_holes_batch",)),
     "merge_frames": (N.TUNE_MERGE_FRAMES, ("ssg_merge_panorama_batch_approx",)),
     "uneven_span": (N.TUNE_UNEVEN_SPAN, ("ssg_uneven_run",)),
-    "isb_up_blocks": (N.TUNE_ISB_UP_BLOCKS, ("ssg_isb_upsample_batch", "ssg_isb_upsample_select_batch")),
+    "isb_up_blocks": (N.TUNE_ISB_UP_BLOCKS, ("ssg_isb_upsample_batch",)),
+    "isb_select_blocks": (N.TUNE_ISB_SELECT_BLOCKS, ("ssg_isb_upsample_select_batch",)),
 }
 
 

@@ -62,17 +62,18 @@ struct Knob {
     int count;
     std::atomic<int> value;
 };
-constexpr int kSweepVariants[] = {0, 1, 2};
+constexpr int kSweepVariants[] = {0, 1, 2, 3};
 constexpr int kHoleBlocks[] = {2, 4, 8};
 constexpr int kMergeFramesValues[] = {2, 4, 8};
 constexpr int kUnevenSpans[] = {1, 2, 4};
 constexpr int kIsbUpBlocks[] = {2, 3};
 Knob g_knobs[] = {
-    {kSweepVariants, 3, {0}},      // SSG_TUNE_SWEEP_VARIANT
+    {kSweepVariants, 4, {0}},      // SSG_TUNE_SWEEP_VARIANT
     {kHoleBlocks, 3, {4}},         // SSG_TUNE_HOLE_BLOCKS_PER_SM
     {kMergeFramesValues, 3, {4}},  // SSG_TUNE_MERGE_FRAMES
     {kUnevenSpans, 3, {1}},        // SSG_TUNE_UNEVEN_SPAN
     {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_UP_BLOCKS
+    {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_SELECT_BLOCKS
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

@@ -561,7 +561,8 @@ template <int W, bool kSelect>
 constexpr bool kGuideDefault = !kSelect || W == 1;
 
 // blockIdx.z: instance of contiguous levels.  kBlocks: blocks per SM the registers are bounded
-// for (3 for the single-candidate filter; 2 or 3 for the chunked volumes, SSG_TUNE_ISB_UP_BLOCKS:
+// for (3 for the single-candidate filter; 2 or 3 for the chunked volumes, SSG_TUNE_ISB_UP_BLOCKS and
+// SSG_TUNE_ISB_SELECT_BLOCKS:
 // 3 spills a few of the taps' registers for more resident warps).
 template <int W, typename Tf, bool kSelect, typename GL, int kBlocks = (W == 1 ? 3 : 2),
           bool kWriteGuide = kGuideDefault<W, kSelect>>
@@ -694,7 +695,7 @@ int launch_up_uneven(const LevelDesc* d_descs, int count, int max_rows_in, int m
     }
     SSG_REQUIRE(count >= 1 && count <= 65535 && max_rows_in <= 65535, "sizes out of range");
     const dim3 grid((unsigned)((max_cols_in + kUpTileX - 1) / kUpTileX), (unsigned)max_rows_in, (unsigned)count);
-    const bool three = tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3;
+    const bool three = tuning(select ? SSG_TUNE_ISB_SELECT_BLOCKS : SSG_TUNE_ISB_UP_BLOCKS) == 3;
     if (!select)
         three ? isb_up_uneven_kernel<8, float, false, 3><<<grid, kBatchBlock, 0, st>>>(d_descs)
               : isb_up_uneven_kernel<8, float, false, 2><<<grid, kBatchBlock, 0, st>>>(d_descs);
@@ -781,7 +782,7 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
             return launch_status("isb_up1_kernel");
         }
     }
-    if (W == 8 && tuning(SSG_TUNE_ISB_UP_BLOCKS) == 3)
+    if (W == 8 && tuning(kSelect ? SSG_TUNE_ISB_SELECT_BLOCKS : SSG_TUNE_ISB_UP_BLOCKS) == 3)
         isb_up_kernel<W, Tf, kSelect, GL, 3><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
             gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
     else

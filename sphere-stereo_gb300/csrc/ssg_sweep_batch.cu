@@ -233,7 +233,7 @@ __device__ __forceinline__ void sample_pair_bytes(const uint4* __restrict__ entr
     for (int h = 0; h < 2; ++h) {
         const uint32_t top = __byte_perm(__float_as_uint(h ? qa.y : qa.x), __float_as_uint(h ? qb.y : qb.x), 0x5410);
         const uint32_t bot = __byte_perm(__float_as_uint(h ? qc.y : qc.x), __float_as_uint(h ? qd.y : qd.x), 0x5410);
-        const uint4 q = __ldg(entries + __float2int_rz(h ? e.y : e.x));
+        const uint4 q = __ldg(entries + __float2uint_rz(h ? e.y : e.x));  // e >= 0: an unsigned offset
         s[h][0] = __dp2a_hi(bot, q.x, __dp2a_lo(top, q.x, 0u));
         s[h][1] = __dp2a_hi(bot, q.y, __dp2a_lo(top, q.y, 0u));
         s[h][2] = __dp2a_hi(bot, q.z, __dp2a_lo(top, q.z, 0u));
@@ -376,7 +376,7 @@ struct UniformView {
 };
 
 // Block shapes of the sweep (SSG_TUNE_SWEEP_VARIANT): threads per block and blocks per SM, which
-// bounds the registers (64, 80, 64)
+// bounds the registers (64, 80, 64, 72)
 template <int V>
 struct SweepShape;
 template <>
@@ -390,6 +390,10 @@ struct SweepShape<1> {
 template <>
 struct SweepShape<2> {
     static constexpr int threads = 128, blocks = 8;
+};
+template <>
+struct SweepShape<3> {
+    static constexpr int threads = 128, blocks = 7;
 };
 
 template <typename T, int V>
@@ -481,6 +485,7 @@ static void launch_sweep_uneven_t(const SweepInst* d_insts, int instances, int t
     switch (tuning(SSG_TUNE_SWEEP_VARIANT)) {
         case 1: launch_sweep_uneven_shape<T, 1>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
         case 2: launch_sweep_uneven_shape<T, 2>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
+        case 3: launch_sweep_uneven_shape<T, 3>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
         default: launch_sweep_uneven_shape<T, 0>(d_insts, instances, total_tiles, span, d_counter, sms, st); break;
     }
 }
@@ -516,6 +521,7 @@ static void launch_sweep(const FastSweepParams& p, const uint4* staged, const fl
     switch (tuning(SSG_TUNE_SWEEP_VARIANT)) {
         case 1: launch_sweep_shape<T, 1>(p, staged, floats, flags, selected, cost, P, instances, st); break;
         case 2: launch_sweep_shape<T, 2>(p, staged, floats, flags, selected, cost, P, instances, st); break;
+        case 3: launch_sweep_shape<T, 3>(p, staged, floats, flags, selected, cost, P, instances, st); break;
         default: launch_sweep_shape<T, 0>(p, staged, floats, flags, selected, cost, P, instances, st); break;
     }
 }

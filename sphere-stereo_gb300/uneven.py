@@ -182,9 +182,11 @@ class UnevenBatch:
             self.tuned = self.tuner.apply(key)
             if self.tuned is None:
                 self.tuned = self.tuner.tune(key, lambda: self._launch(stream),
-                                             ["sweep_variant", "uneven_span", "isb_up_blocks"], entry="ssg_uneven_run")
+                                             ["sweep_variant", "uneven_span", "isb_up_blocks", "isb_select_blocks"],
+                                             entry="ssg_uneven_run")
         for name, v in self.tuned.items():
-            autotune.set_knob(name, v)
+            if name in autotune.KNOBS:
+                autotune.set_knob(name, v)
 
     def launches(self) -> int:
         """Kernels one batch launches."""

@@ -18,11 +18,12 @@ def tune(ss, native):
 
 
 def test_knobs_and_choices(tune):
-    assert tune.choices("sweep_variant") == [0, 1, 2]
+    assert tune.choices("sweep_variant") == [0, 1, 2, 3]
     assert tune.choices("hole_blocks_per_sm") == [2, 4, 8]
     assert tune.choices("merge_frames") == [2, 4, 8]
     assert tune.choices("uneven_span") == [1, 2, 4]
     assert tune.choices("isb_up_blocks") == [2, 3]
+    assert tune.choices("isb_select_blocks") == [2, 3]
     tune.set_knob("merge_frames", 8)
     assert tune.get("merge_frames") == 8
     with pytest.raises(ValueError):
@@ -37,11 +38,16 @@ def test_cache_round_trip_and_apply(tune, tmp_path):
     assert t.apply("missing") is None
     assert t.apply("k") == {"sweep_variant": 2, "merge_frames": 2}
     assert tune.get("sweep_variant") == 2 and tune.get("merge_frames") == 2
+    # caller choices (not library knobs) are kept in the cache and returned
+    path.write_text(json.dumps({"k": {"sweep_variant": 1, "overlap_groups": 2}}))
+    t = tune.Tuner(str(path))
+    assert t.apply("k") == {"sweep_variant": 1, "overlap_groups": 2}
+    assert tune.get("sweep_variant") == 1
 
 
 def test_tune_picks_the_fastest_choice(tune, tmp_path, monkeypatch):
     # fake timings: the entry's time depends on the knob value that is set when it runs
-    cost = {"sweep_variant": {0: 3.0, 1: 1.0, 2: 2.0}, "merge_frames": {2: 5.0, 4: 4.0, 8: 6.0}}
+    cost = {"sweep_variant": {0: 3.0, 1: 1.0, 2: 2.0, 3: 2.5}, "merge_frames": {2: 5.0, 4: 4.0, 8: 6.0}}
     runs = []
 
     class FakeTimer:
@@ -80,7 +86,7 @@ def test_tune_picks_the_fastest_choice(tune, tmp_path, monkeypatch):
     best = t.tune("w", run, ["sweep_variant", "merge_frames"], repeats=2)
     assert best == {"sweep_variant": 1, "merge_frames": 4}
     assert tune.get("sweep_variant") == 1 and tune.get("merge_frames") == 4
-    assert len(runs) == 3 * (1 + 2) * 2
+    assert len(runs) == (4 + 3) * (1 + 2)  # every choice of both knobs: one warm-up and two timed runs
     assert json.loads(path.read_text())["w"] == best
     assert tune.Tuner(str(path)).apply("w") == best
 
