@@ -215,4 +215,28 @@ inline Intr to_intr(const ssg_intrinsics& k) { return Intr{k.fx, k.fy, k.cx, k.c
 
 inline int grid_1d(int64_t n, int block) { return (int)((n + block - 1) / block); }
 
+// Division of n < 2^31 by a divisor fixed on the host, by a multiply-high and a shift
+// (T. Granlund and P. L. Montgomery, "Division by invariant integers using multiplication",
+// PLDI 1994): with s = floor(log2 d) and m = floor(2^(32+s) / d) + 1 (below 2^32 when d is not a
+// power of two), floor(n * m / 2^(32+s)) = floor(n / d) whenever n * (m - 2^(32+s) / d) * d <
+// 2^(32+s), which holds for every n < 2^31 because 2^(32+s) / d > 2^31.  Powers of two shift.
+struct FastDiv {
+    uint32_t m = 0;
+    int s = 0;
+    FastDiv() = default;
+    explicit FastDiv(uint32_t d)
+    {
+        while ((2u << s) <= d && s < 31) ++s;  // s = floor(log2 d)
+        m = (d & (d - 1)) ? (uint32_t)((((uint64_t)1) << (32 + s)) / d + 1) : 0u;
+    }
+    __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const
+    {
+#ifdef __CUDA_ARCH__
+        return m ? __umulhi(n, m) >> s : n >> s;
+#else
+        return m ? (uint32_t)(((uint64_t)n * m) >> 32) >> s : n >> s;
+#endif
+    }
+};
+
 }  // namespace ssg

@@ -243,16 +243,16 @@ struct ReprojParams {
 };
 
 // reprojectDistanceKernel, stitcher.cu:181-204, as a z-buffer on the float bits: pixel i of one
-// map (din -> dout, P pixels, `cols` wide)
-__device__ __forceinline__ void reproject_pixel(const Intr& k, const float* t, const float* __restrict__ din,
-                                                float* __restrict__ dout, int cols, int64_t P, int64_t i)
+// map (din -> dout, P pixels), whose unit ray `ray` (unproject_cu of the pixel) is given
+__device__ __forceinline__ void reproject_ray(const Intr& k, const float* t, const float (&ray)[3],
+                                              const float* __restrict__ din, float* __restrict__ dout, int cols,
+                                              int64_t P, int64_t i)
 {
-    float pt[3];
-    unproject_cu((float)(i % cols), (float)(i / cols), k, pt);
     const float d = din[i];
-    pt[0] = fsub(fmul(d, pt[0]), t[0]);
-    pt[1] = fsub(fmul(d, pt[1]), t[1]);
-    pt[2] = fsub(fmul(d, pt[2]), t[2]);
+    float pt[3];
+    pt[0] = fsub(fmul(d, ray[0]), t[0]);
+    pt[1] = fsub(fmul(d, ray[1]), t[1]);
+    pt[2] = fsub(fmul(d, ray[2]), t[2]);
     float o[2];
     project_cu(pt, k, o, nullptr);
     const float dist = norm3df(pt[0], pt[1], pt[2]);
@@ -260,6 +260,20 @@ __device__ __forceinline__ void reproject_pixel(const Intr& k, const float* t, c
     const int idx = (int)((unsigned)__float2int_rn(o[1]) * (unsigned)cols + (unsigned)__float2int_rn(o[0]));
     if (idx < 0 || (int64_t)idx >= P || !(dist >= 0.0f)) return;
     atomicMin(reinterpret_cast<int*>(dout) + idx, __float_as_int(dist));
+}
+
+__device__ __forceinline__ void pixel_ray(const Intr& k, int cols, int64_t i, float (&ray)[3])
+{
+    const int y = (int)i / cols;  // a map holds fewer than 2^31 pixels
+    unproject_cu((float)((int)i - y * cols), (float)y, k, ray);
+}
+
+__device__ __forceinline__ void reproject_pixel(const Intr& k, const float* t, const float* __restrict__ din,
+                                                float* __restrict__ dout, int cols, int64_t P, int64_t i)
+{
+    float ray[3];
+    pixel_ray(k, cols, i, ray);
+    reproject_ray(k, t, ray, din, dout, cols, P, i);
 }
 
 // blockIdx.y: instance (frame * references + reference slot) of contiguous maps.
@@ -272,6 +286,25 @@ __global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_co
     if (i >= P) return;
     const int slot = blockIdx.y % p.references;
     reproject_pixel(p.k[slot], p.t[slot], din + (int64_t)blockIdx.y * P, dout + (int64_t)blockIdx.y * P, p.cols, P, i);
+}
+
+// The batch's maps of one reference slot share each pixel's ray: a thread unprojects its pixel
+// once and reprojects it in every frame.  blockIdx.y: reference slot; instances frame * references
+// + slot.
+__global__ void __launch_bounds__(kStitchBlock) reproject_frames_kernel(const __grid_constant__ ReprojParams p,
+                                                                        int frames, const float* __restrict__ din,
+                                                                        float* __restrict__ dout)
+{
+    const int64_t P = (int64_t)p.cols * p.rows;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int slot = blockIdx.y;
+    float ray[3];
+    pixel_ray(p.k[slot], p.cols, i, ray);
+    for (int f = 0; f < frames; ++f) {
+        const int64_t inst = (int64_t)f * p.references + slot;
+        reproject_ray(p.k[slot], p.t[slot], ray, din + inst * P, dout + inst * P, p.cols, P, i);
+    }
 }
 
 // Tiled Jacobi inpainting: kTileW x kTileH outputs, a halo of kHalo >= steps pixels.
@@ -475,15 +508,24 @@ struct MapPixel {
     const uchar2* table;  // the map's inpainting table (entry of pixel (x, y): table[y * cols + x])
 };
 
-// `instances` maps of one size, tables per reference slot (the uniform batch)
+// `instances` maps of one size, tables per reference slot (the uniform batch); flat indices are
+// below 2^31 (the hole lists hold them as int32), so positions come from 32-bit divisions by
+// host-fixed divisors
 struct UniformMaps {
     int cols, rows, references;
     const uchar2* tables;
+    FastDiv by_map, by_cols, by_refs;
+    UniformMaps(int c, int r, int refs, const uchar2* t)
+        : cols(c), rows(r), references(refs), tables(t), by_map((uint32_t)c * (uint32_t)r), by_cols((uint32_t)c),
+          by_refs((uint32_t)refs)
+    {
+    }
     __device__ __forceinline__ MapPixel at(int64_t g) const
     {
-        const int64_t P = (int64_t)cols * rows;
-        const int64_t inst = g / P, j = g - inst * P;
-        return MapPixel{cols, rows, (int)(j % cols), (int)(j / cols), tables + (inst % references) * P};
+        const uint32_t P = (uint32_t)cols * (uint32_t)rows, gg = (uint32_t)g;
+        const uint32_t inst = by_map.div(gg), j = gg - inst * P;
+        const uint32_t y = by_cols.div(j), slot = inst - by_refs.div(inst) * (uint32_t)references;
+        return MapPixel{cols, rows, (int)(j - y * (uint32_t)cols), (int)y, tables + (int64_t)slot * P};
     }
 };
 
@@ -935,7 +977,7 @@ extern "C" int ssg_reproject_distance(const float* d_distance_in, float* d_dista
 {
     SSG_REQUIRE(d_distance_in && d_distance_out && translation, "null pointer");
     SSG_REQUIRE(d_distance_in != d_distance_out, "input and output maps must differ");
-    SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
+    SSG_REQUIRE(cols > 0 && rows > 0 && (int64_t)cols * rows < ((int64_t)1 << 31), "resolution out of range");
     if (int e = check_intrinsics(intrinsics, 1)) return e;
     const int64_t P = (int64_t)cols * rows;
     if (fill) {
@@ -959,7 +1001,7 @@ extern "C" int ssg_reproject_distance_batch(const float* d_distance_in, float* d
 {
     SSG_REQUIRE(d_distance_in && d_distance_out && translations, "null pointer");
     SSG_REQUIRE(d_distance_in != d_distance_out, "input and output maps must differ");
-    SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
+    SSG_REQUIRE(cols > 0 && rows > 0 && (int64_t)cols * rows < ((int64_t)1 << 31), "resolution out of range");
     SSG_REQUIRE(references >= 1 && references <= SSG_MAX_REFERENCES, "references out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535 && instances % references == 0,
                 "instances must be a positive multiple of references");
@@ -978,9 +1020,10 @@ extern "C" int ssg_reproject_distance_batch(const float* d_distance_in, float* d
         p.k[r] = to_intr(intrinsics[r]);
         std::memcpy(p.t[r], translations + 3 * r, sizeof(float) * 3);
     }
-    dim3 grid(grid_1d(P, kStitchBlock), instances);
-    reproject_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(p, d_distance_in, d_distance_out);
-    return launch_status("reproject_kernel");
+    dim3 grid(grid_1d(P, kStitchBlock), references);
+    reproject_frames_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(p, instances / references, d_distance_in,
+                                                                           d_distance_out);
+    return launch_status("reproject_frames_kernel");
 }
 
 extern "C" int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scratch, int cols, int rows,
@@ -1127,7 +1170,7 @@ extern "C" int ssg_inpaint_holes_batch(float* d_distance, const uint8_t* d_table
                 "instances must be a positive multiple of references");
     SSG_REQUIRE((int64_t)cols * rows * instances < ((int64_t)1 << 31), "%d maps of %dx%d pixels are too many",
                 instances, cols, rows);
-    const UniformMaps maps{cols, rows, references, reinterpret_cast<const uchar2*>(d_tables)};
+    const UniformMaps maps(cols, rows, references, reinterpret_cast<const uchar2*>(d_tables));
     return inpaint_lists(maps, (int64_t)cols * rows * instances, d_distance, d_stamps, d_holes, max_dist, iterations,
                          as_stream(stream));
 }

@@ -84,3 +84,22 @@ def test_cpu_devices_are_refused(ss):
         ss.RGBD_Estimator([], 0.55, 100, 32, [0], torch.zeros(3), [], (64, 64), (64, 64), (128, 64), 10, 25, "cpu")
     with pytest.raises(ValueError, match="CUDA"):
         ss.rgb_to_guide(torch.zeros(4, 4, 3))
+
+
+def test_fast_division_by_invariant_integers():
+    """The multiply-high division the hole kernels use (ssg_common.cuh FastDiv), restated:
+    floor(n * m / 2^(32 + s)) = floor(n / d) for every n < 2^31, m = floor(2^(32+s) / d) + 1 below
+    2^32, s = floor(log2 d); powers of two shift."""
+    rng = np.random.default_rng(3)
+    divisors = [1, 2, 3, 5, 7, 255, 256, 1000, 1024, 1025, 1216, 1048576, 1048575, 1048577, 3 * 1048576,
+                (1 << 30) + 1, (1 << 31) - 1] + [int(v) for v in rng.integers(1, 1 << 31, 200)]
+    for d in divisors:
+        s = d.bit_length() - 1
+        m = ((1 << (32 + s)) // d + 1) if d & (d - 1) else 0
+        assert m < (1 << 32)
+        ns = np.concatenate([rng.integers(0, 1 << 31, 2000, dtype=np.int64),
+                             np.array([0, 1, d - 1, d, d + 1, (1 << 31) - 1, (1 << 31) - d % (1 << 31)], np.int64)])
+        ns = ns[(ns >= 0) & (ns < (1 << 31))].astype(object)
+        for n in ns:
+            q = ((n * m) >> 32) >> s if m else n >> s
+            assert q == n // d, (n, d)
