@@ -839,12 +839,22 @@ __global__ void __launch_bounds__(kStitchBlock) merge_frames_kernel(const __grid
         const float vo = fadd(uv.y, (float)(r * p.rows));
         float ray[3];
         unproject_fast(uv.x, uv.y, p.k[r], ray);
+        // the bilinear taps of both maps are at the same place in every frame (interp_f_fast)
+        const float u1f = floorf(uv.x), v1f = floorf(vo);
+        const float fu = uv.x - u1f, fv = vo - v1f;
+        const int64_t tap = (int64_t)(int)v1f * p.cols + (int)u1f;
 #pragma unroll
         for (int f = 0; f < kMergeFrames; ++f) {
             if (f < nf) {
-                const float rd = interp_f_fast(reproj + f * map_frame, uv.x, vo, p.cols);
+                const float* a = reproj + f * map_frame + tap;
+                const float* b = dists + f * map_frame + tap;
+                const float a1 = __ldg(a), a3 = __ldg(a + 1), a2 = __ldg(a + p.cols), a4 = __ldg(a + p.cols + 1);
+                const float b1 = __ldg(b), b3 = __ldg(b + 1), b2 = __ldg(b + p.cols), b4 = __ldg(b + p.cols + 1);
+                const float at = fmaf(fu, a3 - a1, a1), ab = fmaf(fu, a4 - a2, a2);
+                const float bt = fmaf(fu, b3 - b1, b1), bb = fmaf(fu, b4 - b2, b2);
+                const float rd = fmaf(fv, ab - at, at);
                 inv[f] = fmaf(w, rcp_approx(rd), inv[f]);
-                const float dc = fminf(rd, interp_f_fast(dists + f * map_frame, uv.x, vo, p.cols));
+                const float dc = fminf(rd, fmaf(fv, bb - bt, bt));
                 float pt[3], o[2], c[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) pt[a] = fmaf(dc, ray[a], p.t[r][a]);
