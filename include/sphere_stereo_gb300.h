@@ -322,6 +322,12 @@ SSG_API int ssg_isb_apply_batch(uint8_t* const* d_guides, float* const* d_costs,
 SSG_API int ssg_reproject_distance_batch(const float* d_distance_in, float* d_distance_out, int cols, int rows,
                                          int instances, int references, const ssg_intrinsics* intrinsics,
                                          const float* translations, int fill, void* stream);
+/* ssg_reproject_distance_batch with fused multiply-adds and approximate square roots and
+ * reciprocal in the projection and the distance (the batched 16-bit path, checked against the
+ * fp32 path within tolerances). */
+SSG_API int ssg_reproject_distance_batch_approx(const float* d_distance_in, float* d_distance_out, int cols, int rows,
+                                                int instances, int references, const ssg_intrinsics* intrinsics,
+                                                const float* translations, int fill, void* stream);
 
 /* Inpainting (python/stitcher.cu:283-323) of `instances` maps; d_tables: references x rows x
  * cols x 2 (instance i uses table i % references); d_scratch: instances x rows x cols. */

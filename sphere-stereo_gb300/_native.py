@@ -111,6 +111,7 @@ SIGNATURES = {
     "ssg_select_distance_batch": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, _P]),
     "ssg_isb_apply_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _D, _D, _I, _P]),
     "ssg_reproject_distance_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
+    "ssg_reproject_distance_batch_approx": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P]),
     "ssg_inpaint_batch": (_I, [_P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
     "ssg_inpaint_holes_batch": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
     "ssg_inpaint_noalloc": (_I, [_P, _P, _I, _I, _D, _I, _P]),
@@ -239,7 +240,7 @@ def kernels_launched(name: str, args) -> int:
         return 2 * max(0, int(args[2]) - 1)
     if name == "ssg_reproject_distance":
         return 2 if args[6] else 1
-    if name == "ssg_reproject_distance_batch":
+    if name in ("ssg_reproject_distance_batch", "ssg_reproject_distance_batch_approx"):
         return 2 if args[8] else 1
     if name == "ssg_inpaint":
         return -(-int(args[6]) // 16)

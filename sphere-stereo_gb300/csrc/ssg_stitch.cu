@@ -288,9 +288,30 @@ __global__ void __launch_bounds__(kStitchBlock) reproject_kernel(const __grid_co
     reproject_pixel(p.k[slot], p.t[slot], din + (int64_t)blockIdx.y * P, dout + (int64_t)blockIdx.y * P, p.cols, P, i);
 }
 
+// reproject_ray with fused multiply-adds and approximate square roots and reciprocal (the
+// batched 16-bit path): the same steps, a relative error of a few 1e-7 in the position and the
+// distance
+__device__ __forceinline__ void reproject_ray_fast(const Intr& k, const float* t, const float (&ray)[3],
+                                                   const float* __restrict__ din, float* __restrict__ dout, int cols,
+                                                   int64_t P, int64_t i)
+{
+    const float d = din[i];
+    const float pt[3] = {fmaf(d, ray[0], -t[0]), fmaf(d, ray[1], -t[1]), fmaf(d, ray[2], -t[2])};
+    const float rxy = fmaf(pt[1], pt[1], pt[0] * pt[0]);
+    const float d1 = sqrt_approx(fmaf(pt[2], pt[2], rxy));
+    const float c = fmaf(k.xi, d1, pt[2]);
+    const float d2 = sqrt_approx(fmaf(c, c, rxy));
+    const float den = rcp_approx(fmaf(k.alpha, d2, (1.0f - k.alpha) * c));
+    const float ox = fmaf(k.fx * pt[0], den, k.cx), oy = fmaf(k.fy * pt[1], den, k.cy);
+    const int idx = (int)((unsigned)__float2int_rn(oy) * (unsigned)cols + (unsigned)__float2int_rn(ox));
+    if (idx < 0 || (int64_t)idx >= P || !(d1 >= 0.0f)) return;
+    atomicMin(reinterpret_cast<int*>(dout) + idx, __float_as_int(d1));
+}
+
 // The batch's maps of one reference slot share each pixel's ray: a thread unprojects its pixel
 // once and reprojects it in every frame.  blockIdx.y: reference slot; instances frame * references
-// + slot.
+// + slot.  kFast: reproject_ray_fast.
+template <bool kFast>
 __global__ void __launch_bounds__(kStitchBlock) reproject_frames_kernel(const __grid_constant__ ReprojParams p,
                                                                         int frames, const float* __restrict__ din,
                                                                         float* __restrict__ dout)
@@ -303,7 +324,8 @@ __global__ void __launch_bounds__(kStitchBlock) reproject_frames_kernel(const __
     pixel_ray(p.k[slot], p.cols, i, ray);
     for (int f = 0; f < frames; ++f) {
         const int64_t inst = (int64_t)f * p.references + slot;
-        reproject_ray(p.k[slot], p.t[slot], ray, din + inst * P, dout + inst * P, p.cols, P, i);
+        if (kFast) reproject_ray_fast(p.k[slot], p.t[slot], ray, din + inst * P, dout + inst * P, p.cols, P, i);
+        else reproject_ray(p.k[slot], p.t[slot], ray, din + inst * P, dout + inst * P, p.cols, P, i);
     }
 }
 
@@ -1005,9 +1027,9 @@ extern "C" int ssg_reproject_distance(const float* d_distance_in, float* d_dista
     return launch_status("reproject_kernel");
 }
 
-extern "C" int ssg_reproject_distance_batch(const float* d_distance_in, float* d_distance_out, int cols, int rows,
-                                            int instances, int references, const ssg_intrinsics* intrinsics,
-                                            const float* translations, int fill, void* stream)
+static int reproject_batch(const float* d_distance_in, float* d_distance_out, int cols, int rows, int instances,
+                           int references, const ssg_intrinsics* intrinsics, const float* translations, int fill,
+                           bool fast, void* stream)
 {
     SSG_REQUIRE(d_distance_in && d_distance_out && translations, "null pointer");
     SSG_REQUIRE(d_distance_in != d_distance_out, "input and output maps must differ");
@@ -1031,9 +1053,30 @@ extern "C" int ssg_reproject_distance_batch(const float* d_distance_in, float* d
         std::memcpy(p.t[r], translations + 3 * r, sizeof(float) * 3);
     }
     dim3 grid(grid_1d(P, kStitchBlock), references);
-    reproject_frames_kernel<<<grid, kStitchBlock, 0, as_stream(stream)>>>(p, instances / references, d_distance_in,
-                                                                           d_distance_out);
+    if (fast)
+        reproject_frames_kernel<true><<<grid, kStitchBlock, 0, as_stream(stream)>>>(p, instances / references,
+                                                                                   d_distance_in, d_distance_out);
+    else
+        reproject_frames_kernel<false><<<grid, kStitchBlock, 0, as_stream(stream)>>>(p, instances / references,
+                                                                                    d_distance_in, d_distance_out);
     return launch_status("reproject_frames_kernel");
+}
+
+extern "C" int ssg_reproject_distance_batch(const float* d_distance_in, float* d_distance_out, int cols, int rows,
+                                            int instances, int references, const ssg_intrinsics* intrinsics,
+                                            const float* translations, int fill, void* stream)
+{
+    return reproject_batch(d_distance_in, d_distance_out, cols, rows, instances, references, intrinsics,
+                           translations, fill, false, stream);
+}
+
+extern "C" int ssg_reproject_distance_batch_approx(const float* d_distance_in, float* d_distance_out, int cols,
+                                                   int rows, int instances, int references,
+                                                   const ssg_intrinsics* intrinsics, const float* translations,
+                                                   int fill, void* stream)
+{
+    return reproject_batch(d_distance_in, d_distance_out, cols, rows, instances, references, intrinsics,
+                           translations, fill, true, stream);
 }
 
 extern "C" int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scratch, int cols, int rows,
@@ -1109,7 +1152,10 @@ __global__ void __launch_bounds__(kStitchBlock) reproject_uneven_kernel(const St
     const int64_t P = (int64_t)J.cols * J.rows;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= J.references || i >= P) return;
-    reproject_pixel(J.k[slot], J.t[slot], J.distance + slot * P, J.reprojected + slot * P, J.cols, P, i);
+    // the uniform batch's arithmetic (reproject_frames_kernel<true>)
+    float ray[3];
+    pixel_ray(J.k[slot], J.cols, i, ray);
+    reproject_ray_fast(J.k[slot], J.t[slot], ray, J.distance + slot * P, J.reprojected + slot * P, J.cols, P, i);
 }
 
 // the approximate merge (merge_frames_kernel's arithmetic) of one job's panorama; blockIdx.y: job

@@ -10,7 +10,7 @@ One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_p
     ssg_isb_upsample_batch         levels L - 2 .. 1                                    L - 2
     ssg_isb_upsample_select_batch  last level + argmin / sub-candidate step             1
     ssg_isb_apply_batch            distance post-filter, fp32, N = 1                    2L - 2
-    ssg_reproject_distance_batch   fill + z-buffer                                      2
+    ssg_reproject_distance_batch_approx  fill + z-buffer                                2
     ssg_inpaint_holes_batch        hole filling: a scan, then 32 steps on hole lists    33
     ssg_merge_panorama_batch_approx panoramas                                           1
 
@@ -191,8 +191,8 @@ class BatchPipeline:
             N.call("ssg_convert_u8", s_img.data_ptr(), images_u8.data_ptr(),
                    frames * R * st.image_rows * st.image_cols * 3, stream)
         reprojected = self.reprojected.data_ptr() + 4 * i0 * P
-        N.call("ssg_reproject_distance_batch", dist.data_ptr(), reprojected, cols, rows, inst, R, st._intr, st._trans,
-               1, stream)
+        N.call("ssg_reproject_distance_batch_approx", dist.data_ptr(), reprojected, cols, rows, inst, R, st._intr,
+               st._trans, 1, stream)
         holes = self.holes.data_ptr() + 4 * (3 * i0 * P + 4 * group)
         N.call("ssg_inpaint_holes_batch", reprojected, self.tables.data_ptr(), self.stamps.data_ptr() + i0 * P, holes,
                cols, rows, inst, R, st.max_dist, st.inpainting_iterations, stream)

@@ -201,6 +201,37 @@ def test_reproject_and_inpaint(ss, native, small_rig, golden_small):
                                       small_rig.o.inpaint(want, small_rig.tables[r], st.max_dist, 32))
 
 
+def test_reproject_batch_exact_and_approximate(ss, native, golden_small):
+    """The batched reprojection (one ray per pixel for every frame of a reference) equals the
+    per-map call bit for bit; the approximate variant of the 16-bit path agrees on the target
+    pixels of all but a few boundary cases and on the distances to a few 1e-7."""
+    est = _estimator(ss, golden_small)
+    st = est.fishey_stitcher
+    N = ss._native
+    stream = torch.cuda.current_stream().cuda_stream
+    R = st.reference_count
+    dists = np.asarray(golden_small["ref/distance_filtered"], np.float32)
+    frames = np.stack([dists, dists * 1.07, dists[::-1].copy()])  # 3 frames x R maps
+    d = _t(frames.reshape(-1, st.rows, st.cols))
+    exact = torch.empty_like(d)
+    approx = torch.empty_like(d)
+    N.call("ssg_reproject_distance_batch", d.data_ptr(), exact.data_ptr(), st.cols, st.rows, 3 * R, R, st._intr,
+           st._trans, 1, stream)
+    N.call("ssg_reproject_distance_batch_approx", d.data_ptr(), approx.data_ptr(), st.cols, st.rows, 3 * R, R,
+           st._intr, st._trans, 1, stream)
+    for i in range(3 * R):
+        one = torch.empty_like(d[i])
+        r = i % R
+        N.call("ssg_reproject_distance", d[i].data_ptr(), one.data_ptr(), st.cols, st.rows,
+               N.intrinsics_array([st.intrinsics[r]]), N.floats(st.translations_host[3 * r:3 * r + 3].tolist()), 1,
+               stream)
+        torch.testing.assert_close(exact[i], one, rtol=0, atol=0)
+    e, a = exact.cpu().numpy(), approx.cpu().numpy()
+    assert ((e >= 1e8) == (a >= 1e8)).mean() >= 0.999
+    both = (e < 1e8) & (a < 1e8)
+    assert np.isclose(a[both], e[both], rtol=1e-5, atol=0).mean() >= 0.999
+
+
 @pytest.mark.parametrize("iterations", [0, 1, 5, 16, 17, 40])
 def test_inpaint_iteration_counts(ss, native, dev_oracle, iterations):
     """Tiled passes of up to 16 Jacobi steps equal one step per launch, at any count, on a map
