@@ -230,10 +230,21 @@ __global__ void __launch_bounds__(kStitchBlock) normalize_weights_kernel(float* 
     for (int r = 0; r < nref; ++r) w[(int64_t)r * Q + i] = fdiv(w[(int64_t)r * Q + i], s);
 }
 
+// out[0, n) = v: four values per thread with one 16-byte store where out is 16-byte aligned
 __global__ void __launch_bounds__(kStitchBlock) fill_kernel(float* __restrict__ out, int64_t n, float v)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = v;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i + 4 <= n && ((uintptr_t)out & 15) == 0) {
+        reinterpret_cast<float4*>(out + i)[0] = make_float4(v, v, v, v);
+    } else {
+        for (int64_t j = i; j < i + 4 && j < n; ++j) out[j] = v;
+    }
+}
+
+static int fill_map(float* out, int64_t n, float v, cudaStream_t st)
+{
+    fill_kernel<<<grid_1d((n + 3) / 4, kStitchBlock), kStitchBlock, 0, st>>>(out, n, v);
+    return launch_status("fill_kernel");
 }
 
 struct ReprojParams {
@@ -1013,8 +1024,7 @@ extern "C" int ssg_reproject_distance(const float* d_distance_in, float* d_dista
     if (int e = check_intrinsics(intrinsics, 1)) return e;
     const int64_t P = (int64_t)cols * rows;
     if (fill) {
-        fill_kernel<<<grid_1d(P, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(d_distance_out, P, 1e8f);
-        if (int e = launch_status("fill_kernel")) return e;
+        if (int e = fill_map(d_distance_out, P, 1e8f, as_stream(stream))) return e;
     }
     ReprojParams p{};
     p.cols = cols;
@@ -1040,9 +1050,7 @@ static int reproject_batch(const float* d_distance_in, float* d_distance_out, in
     if (int e = check_intrinsics(intrinsics, references)) return e;
     const int64_t P = (int64_t)cols * rows;
     if (fill) {
-        fill_kernel<<<grid_1d(P * instances, kStitchBlock), kStitchBlock, 0, as_stream(stream)>>>(
-            d_distance_out, P * instances, 1e8f);
-        if (int e = launch_status("fill_kernel")) return e;
+        if (int e = fill_map(d_distance_out, P * instances, 1e8f, as_stream(stream))) return e;
     }
     ReprojParams p{};
     p.cols = cols;
@@ -1200,8 +1208,7 @@ int launch_stitch_uneven(const StitchJob* d_jobs, int jobs, float* d_maps, int64
     SSG_REQUIRE(iterations >= 0 && iterations <= kMaxListIterations, "iterations %d outside [0, %d]", iterations,
                 kMaxListIterations);
     SSG_REQUIRE(total_map_pixels < ((int64_t)1 << 31), "too many map pixels");
-    fill_kernel<<<grid_1d(total_map_pixels, kStitchBlock), kStitchBlock, 0, st>>>(d_maps, total_map_pixels, 1e8f);
-    if (int e = launch_status("fill_kernel")) return e;
+    if (int e = fill_map(d_maps, total_map_pixels, 1e8f, st)) return e;
     reproject_uneven_kernel<<<dim3(grid_1d(max_map_pixels, kStitchBlock), jobs * max_references), kStitchBlock, 0,
                               st>>>(d_jobs, max_references);
     if (int e = launch_status("reproject_uneven_kernel")) return e;
