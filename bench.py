@@ -210,6 +210,9 @@ def run_ours(args, rank, world, device, rendered):
     B = args.batch
     autotune = importlib.import_module(PACKAGE + ".autotune")
     tuner = None if args.no_autotune else autotune.Tuner()
+    for kv in args.knob:
+        name, value = kv.split("=")
+        autotune.set_knob(name, int(value))
     est = _estimator(ss, calibration, device, args.storage, B, True, tuner)
     pipe = est.pipeline()
     if args.overlap_groups is not None:
@@ -360,7 +363,7 @@ def run_ours(args, rank, world, device, rendered):
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms,
                      "launches_timed": len(rec.events)},
         "e2e_u8": e2e_u8,
-        "tuned": pipe.tuned,
+        "tuned": pipe.tuned if pipe.tuned is not None else {k: autotune.get(k) for k in pipe.TUNED_KNOBS},
         "overlap_groups": pipe._group_count(B),
     }
 
@@ -614,6 +617,8 @@ def main():
                          "64 candidates, every camera a reference; uneven: a mixed batch of jobs")
     ap.add_argument("--jobs", type=int, default=128, help="jobs of the uneven workload")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--knob", action="append", default=[], metavar="NAME=VALUE",
+                    help="fix a launch-shape knob (with --no-autotune; autotune.KNOBS names)")
     ap.add_argument("--overlap-groups", type=int, default=None,
                     help="frame groups whose post-filter and stitch overlap the next group's sweep (default: tuned)")
     args = ap.parse_args()

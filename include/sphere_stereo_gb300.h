@@ -80,11 +80,17 @@ typedef struct {
 #define SSG_TUNE_ISB_UP_BLOCKS 4      /* blocks per SM the chunked ISB upsampling (coarse levels) is
                                          register-bounded for: 2, 3 */
 #define SSG_TUNE_ISB_SELECT_BLOCKS 5  /* the same for the last level fused with the selection: 2, 3 */
+#define SSG_TUNE_ISB_TILE_TMA 6       /* coarse tiles of the chunked ISB upsampling staged by TMA (1) or by
+                                         cp.async (0) */
 SSG_API int ssg_tuning_set(int knob, int value);
 /* The knob's current value (-1 for an unknown knob). */
 SSG_API int ssg_tuning_get(int knob);
 /* Writes up to `capacity` allowed values of a knob; returns how many it has (0 if unknown). */
 SSG_API int ssg_tuning_choices(int knob, int32_t* values, int capacity);
+
+/* Reads and clears the device status word of the ISB kernels: bit 0 is set when a bounded wait
+ * for a TMA tile ran out (the kernel skipped that work; results are then invalid).  Synchronous. */
+SSG_API int ssg_take_device_status(uint32_t* status);
 
 /* Message of the calling thread's last failed call ("" if none). */
 SSG_API const char* ssg_last_error(void);

@@ -29,6 +29,7 @@ TUNE_MERGE_FRAMES = 2
 TUNE_UNEVEN_SPAN = 3
 TUNE_ISB_UP_BLOCKS = 4
 TUNE_ISB_SELECT_BLOCKS = 5
+TUNE_ISB_TILE_TMA = 6
 ISB_SKIP_FINE_GUIDE = 1
 PIXEL_U8 = 0
 PIXEL_F32 = 1
@@ -126,6 +127,7 @@ SIGNATURES = {
     "ssg_tuning_set": (_I, [_I, _I]),
     "ssg_tuning_get": (_I, [_I]),
     "ssg_tuning_choices": (_I, [_I, _P, _I]),
+    "ssg_take_device_status": (_I, [_P]),
     "ssg_uneven_create": (_I, [_P, _I, _P, _I, _I, _D, _I, _P, _P, _P]),
     "ssg_uneven_upload": (_I, [_P, _P, _P, _P]),
     "ssg_uneven_run": (_I, [_P, _P]),
@@ -232,7 +234,7 @@ def pointers(values) -> ctypes.Array:
 def kernels_launched(name: str, args) -> int:
     """Number of kernels one call of entry point ``name`` with ``args`` launches."""
     if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count", "ssg_tuning_set",
-                "ssg_tuning_get", "ssg_tuning_choices", "ssg_eval_scratch_bytes"):
+                "ssg_tuning_get", "ssg_tuning_choices", "ssg_eval_scratch_bytes", "ssg_take_device_status"):
         return 0
     if name == "ssg_eval_panoramas":
         return 3

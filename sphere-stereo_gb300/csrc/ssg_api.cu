@@ -62,6 +62,7 @@ struct Knob {
     int count;
     std::atomic<int> value;
 };
+constexpr int kOnOff[] = {0, 1};
 constexpr int kSweepVariants[] = {0, 1, 2, 3};
 constexpr int kHoleBlocks[] = {2, 4, 8};
 constexpr int kMergeFramesValues[] = {2, 4, 8};
@@ -74,6 +75,7 @@ Knob g_knobs[] = {
     {kUnevenSpans, 3, {1}},        // SSG_TUNE_UNEVEN_SPAN
     {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_UP_BLOCKS
     {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_SELECT_BLOCKS
+    {kOnOff, 2, {0}},              // SSG_TUNE_ISB_TILE_TMA
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

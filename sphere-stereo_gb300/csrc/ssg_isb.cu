@@ -19,6 +19,7 @@
 
 #include "ssg_cells.cuh"
 #include "ssg_isb_common.cuh"
+#include "ssg_tma.cuh"
 #include "ssg_uneven.cuh"
 
 namespace ssg {
@@ -34,6 +35,37 @@ __global__ void range_table_kernel(float* __restrict__ table, float var_inv_i)
 {
     for (int d = threadIdx.x; d < kRangeLutStride; d += blockDim.x)
         table[d] = d < kRangeLutSize ? range_weight((float)d, var_inv_i) : 0.0f;
+}
+
+bool encode_tensor_map(CUtensorMap* map, const void* base, int rank, const uint64_t* dims, const uint64_t* strides,
+                       const uint32_t* box)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            fn = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }();
+    if (!encode || ((uintptr_t)base & 15) != 0 || rank < 1 || rank > 5) return false;
+    cuuint64_t gdim[5], gstride[4];
+    cuuint32_t bdim[5], estride[5];
+    for (int i = 0; i < rank; ++i) {
+        gdim[i] = dims[i];
+        bdim[i] = box[i];
+        estride[i] = 1;
+        if (i + 1 < rank) {
+            if (strides[i] % 16 != 0) return false;
+            gstride[i] = strides[i];
+        }
+    }
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, const_cast<void*>(base), gdim, gstride, bdim,
+                  estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 const float* range_table(float var_inv_i, cudaStream_t stream)
@@ -176,12 +208,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
 
 // A chunk's tile: [part][row 0..2][col 0..kUpTileCols-1][E floats], parts of E = 4 candidates
-// (W = 8, two parts) or of one candidate (W = 1).
+// (W = 8, two parts) or of one candidate (W = 1).  A part starts on a 128-byte boundary (the
+// alignment of a TMA destination).
 template <int W>
 struct UpTile {
     static constexpr int parts = W == 8 ? 2 : 1;
     static constexpr int E = W == 8 ? 4 : 1;
-    static constexpr int floats = parts * 3 * kUpTileCols * E;
+    static constexpr int part_floats = (3 * kUpTileCols * E + 31) / 32 * 32;
+    static constexpr int floats = parts * part_floats;
+    static constexpr uint32_t part_bytes = 3 * kUpTileCols * E * sizeof(float);  // one TMA box
 };
 
 template <int W>
@@ -194,10 +229,44 @@ __device__ __forceinline__ void load_tile_async(float* __restrict__ buf, const f
         const int row = rc / kUpTileCols, col = rc % kUpTileCols;
         const int gx = min(max(x0 - 1 + col, 0), cols_in - 1), gy = min(max(y - 1 + row, 0), rows_in - 1);
         const float* src = chunk + ((int64_t)gy * cols_in + gx) * W + part * 4;
+        float* dst = buf + part * UpTile<W>::part_floats + rc * UpTile<W>::E;
         if constexpr (W == 8)
-            cp_async16(buf + e * 4, src);
+            cp_async16(dst, src);
         else
-            cp_async4(buf + e, src);
+            cp_async4(dst, src);
+    }
+}
+
+// The TMA form of load_tile_async (W = 8): one box of 4 floats x kUpTileCols x 3 rows per part,
+// issued by thread 0 on `bar`.  The box starts at column x0 - 1 and row y - 1, possibly outside
+// the level: those cells arrive as zeros and tma_clamp_edges replaces them afterwards.
+// c3: the chunk's plane (instance * chunks + chunk) of the level's tensor map.
+__device__ __forceinline__ void load_tile_tma(float* __restrict__ buf, const CUtensorMap* map, int x0, int y, int c3,
+                                              uint64_t* bar)
+{
+    mbar_arrive_expect_tx(bar, 2 * UpTile<8>::part_bytes);
+#pragma unroll
+    for (int part = 0; part < 2; ++part) tma_load_4d(buf + part * UpTile<8>::part_floats, map, 4 * part, x0 - 1, y - 1, c3, bar);
+}
+
+// Edge clamping of a TMA tile: cells whose column or row lies outside the level take the value of
+// the clamped cell, as load_tile_async's addresses do.  Block-uniform; the caller synchronises
+// the block before and after.
+__device__ __forceinline__ void tma_clamp_edges(float* __restrict__ buf, int rows_in, int cols_in, int x0, int y)
+{
+    const bool left = x0 == 0, right = x0 - 1 + kUpTileCols > cols_in, top = y == 0, bottom = y + 1 >= rows_in;
+    if (!(left || right || top || bottom)) return;
+    constexpr int cells = 3 * kUpTileCols;
+    for (int e = threadIdx.x; e < 2 * cells; e += blockDim.x) {
+        const int part = e / cells, rc = e % cells;
+        const int row = rc / kUpTileCols, col = rc % kUpTileCols;
+        const int gx = x0 - 1 + col, gy = y - 1 + row;
+        const int cx = min(max(gx, 0), cols_in - 1), cy = min(max(gy, 0), rows_in - 1);
+        if (cx == gx && cy == gy) continue;
+        // the source is a cell inside the level (never itself a target)
+        const int src = (cy - (y - 1)) * kUpTileCols + (cx - (x0 - 1));
+        float* p = buf + part * UpTile<8>::part_floats;
+        reinterpret_cast<float4*>(p)[rc] = reinterpret_cast<const float4*>(p)[src];
     }
 }
 
@@ -374,12 +443,13 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
 #pragma unroll
         for (int t = 0; t < 9; ++t) {
             if (uses_tap<FA>(t) || uses_tap<FB>(t)) {
-                const int cell = (part * 3 + t / 3) * kUpTileCols + lx + t % 3;
+                const int cell = (t / 3) * kUpTileCols + lx + t % 3;
+                const float* pb = buf + part * UpTile<W>::part_floats;
                 if constexpr (E == 4) {
-                    const float4 q = reinterpret_cast<const float4*>(buf)[cell];
+                    const float4 q = reinterpret_cast<const float4*>(pb)[cell];
                     tap[t][0] = q.x; tap[t][1] = q.y; tap[t][2] = q.z; tap[t][3] = q.w;
                 } else {
-                    tap[t][0] = buf[cell];
+                    tap[t][0] = pb[cell];
                 }
             } else {
 #pragma unroll
@@ -395,8 +465,9 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
 // Shared memory of one upsampling block
 template <int W>
 struct UpShared {
-    __align__(16) float tile[2][UpTile<W>::floats];
+    __align__(128) float tile[2][UpTile<W>::floats];
     __align__(16) float lut[kRangeLutStride];
+    uint64_t bar[2];  // TMA completion of the two tile buffers
 };
 
 // One block of an upsampling step: coarse pixels x0 .. x0 + kUpTileX - 1 of coarse row y, their
@@ -407,12 +478,14 @@ struct UpShared {
 // kWriteGuide: the filtered fine guide is formed and written (kGuideDefault: always except by
 // the chunked selecting step, whose guide nothing reads; the planar one writes it as the
 // reference's filter does).
-template <int W, typename Tf, bool kSelect, typename GL, bool kWriteGuide>
+template <int W, typename Tf, bool kSelect, typename GL, bool kWriteGuide, bool kTma = false>
 __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
                                              uint8_t* __restrict__ guide_io, Tf* __restrict__ cost_fine,
                                              const LevelGeom& g, int chunks, int ncand, float weight_up,
-                                             float weight_down, const SelectOut& so, int x0, int y, UpShared<W>& sh)
+                                             float weight_down, const SelectOut& so, int x0, int y, UpShared<W>& sh,
+                                             const CUtensorMap* tmap = nullptr, int plane0 = 0)
 {
+    static_assert(!kTma || W == 8, "TMA tiles are for the chunked layout");
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int kind = warp >> 2;  // warp-uniform
@@ -433,30 +506,56 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
         }
     }
     Selector sa, sb;
-    load_tile_async<W>(sh.tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
-    cp_async_commit();
+    if constexpr (kTma) {
+        // the coarse tiles come by TMA (plane0 + c: the chunk's plane of the level's tensor map)
+        if (threadIdx.x == 0) {
+            mbar_init(&sh.bar[0], 1);
+            mbar_init(&sh.bar[1], 1);
+            mbar_init_fence();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) load_tile_tma(sh.tile[0], tmap, x0, y, plane0, &sh.bar[0]);
+    } else {
+        load_tile_async<W>(sh.tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
+        cp_async_commit();
+    }
     // fine cells are read once, from memory: prefetched a chunk ahead of their use
     RawCell<W, Tf> ra, rb;
     if (kSelect || pa.active) ra.load(cost_fine + (int64_t)pa.index * W);
     if (kSelect || pb.active) rb.load(cost_fine + (int64_t)pb.index * W);
     for (int c = 0; c < chunks; ++c) {
-        if (c + 1 < chunks)
-            load_tile_async<W>(sh.tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in, x0,
-                               y);
-        cp_async_commit();
+        if constexpr (kTma) {
+            if (threadIdx.x == 0 && c + 1 < chunks) {
+                load_tile_tma(sh.tile[(c + 1) & 1], tmap, x0, y, plane0 + c + 1, &sh.bar[(c + 1) & 1]);
+            }
+        } else {
+            if (c + 1 < chunks)
+                load_tile_async<W>(sh.tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in,
+                                   x0, y);
+            cp_async_commit();
+        }
         RawCell<W, Tf> na = ra, nb = rb;
         if (c + 1 < chunks) {
             const Tf* next = cost_fine + (int64_t)(c + 1) * pio * W;
             if (kSelect || pa.active) na.load(next + (int64_t)pa.index * W);
             if (kSelect || pb.active) nb.load(next + (int64_t)pb.index * W);
         }
-        cp_async_wait_one();  // this chunk's tile has landed
+        if constexpr (kTma) {
+            mbar_wait(&sh.bar[c & 1], (uint32_t)(c >> 1) & 1u);  // this chunk's tile has landed
+            tma_clamp_edges(sh.tile[c & 1], g.rows_in, g.cols_in, x0, y);
+        } else {
+            cp_async_wait_one();  // this chunk's tile has landed
+        }
         __syncthreads();
         Tf* fine_chunk = cost_fine + (int64_t)c * pio * W;
         if (kind == 0)
             up_chunk<0, 3, W, Tf, kSelect>(sh.tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
         else
             up_chunk<1, 2, W, Tf, kSelect>(sh.tile[c & 1], lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+        // the edge writes of this buffer (generic proxy) are ordered before the TMA copy that
+        // refills it two chunks on; the block's reads are, by the barrier
+        if constexpr (kTma)
+            if (x0 == 0 || x0 - 1 + kUpTileCols > g.cols_in || y == 0 || y + 1 >= g.rows_in) fence_proxy_async();
         __syncthreads();  // the tile is refilled two chunks on
         ra = na;
         rb = nb;
@@ -565,14 +664,14 @@ constexpr bool kGuideDefault = !kSelect || W == 1;
 // SSG_TUNE_ISB_SELECT_BLOCKS:
 // 3 spills a few of the taps' registers for more resident warps).
 template <int W, typename Tf, bool kSelect, typename GL, int kBlocks = (W == 1 ? 3 : 2),
-          bool kWriteGuide = kGuideDefault<W, kSelect>>
+          bool kWriteGuide = kGuideDefault<W, kSelect>, bool kTma = false>
 __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint8_t* __restrict__ guide_in,
                                                             const float* __restrict__ cost_in,
                                                             uint8_t* __restrict__ guide_io,
                                                             Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
                                                             int ncand, float weight_up, float weight_down,
                                                             float var_inv_i, const float* __restrict__ table,
-                                                            SelectOut so)
+                                                            SelectOut so, const __grid_constant__ CUtensorMap tmap)
 {
     __shared__ UpShared<W> sh;
     load_range_lut(sh.lut, table, var_inv_i);
@@ -584,11 +683,11 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint
         if (so.distance2) so.distance2 += (int64_t)inst * pio;
         if (so.index) so.index += (int64_t)inst * pio;
     }
-    isb_up_block<W, Tf, kSelect, GL, kWriteGuide>(guide_in + (int64_t)inst * pin * GL::bytes,
+    isb_up_block<W, Tf, kSelect, GL, kWriteGuide, kTma>(guide_in + (int64_t)inst * pin * GL::bytes,
                                      cost_in + (int64_t)inst * chunks * pin * W,
                                      guide_io + (int64_t)inst * pio * GL::bytes,
                                      cost_fine + (int64_t)inst * chunks * pio * W, g, chunks, ncand, weight_up,
-                                     weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh);
+                                     weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh, &tmap, inst * chunks);
 }
 
 // Selection from an unfiltered level-0 volume (pyramids of fewer than two levels, or the
@@ -782,12 +881,34 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
             return launch_status("isb_up1_kernel");
         }
     }
-    if (W == 8 && tuning(kSelect ? SSG_TUNE_ISB_SELECT_BLOCKS : SSG_TUNE_ISB_UP_BLOCKS) == 3)
-        isb_up_kernel<W, Tf, kSelect, GL, 3><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
-            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
-    else
-        isb_up_kernel<W, Tf, kSelect, GL><<<up_grid(cc, rc, instances), kBatchBlock, 0, st>>>(
-            gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so);
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    const dim3 grid = up_grid(cc, rc, instances);
+    if constexpr (W == 8) {
+        // the coarse level of every instance as one tensor [planes][rows][cols][8 floats], plane =
+        // instance * chunks + chunk, read in boxes of 4 floats x kUpTileCols x 3 rows
+        const uint64_t dims[4] = {8, (uint64_t)cc, (uint64_t)rc, (uint64_t)chunks * (uint64_t)instances};
+        const uint64_t strides[3] = {32, 32ull * cc, 32ull * cc * rc};
+        const uint32_t box[4] = {4, (uint32_t)kUpTileCols, 3, 1};
+        const bool tma = tuning(SSG_TUNE_ISB_TILE_TMA) == 1 && encode_tensor_map(&map, ci, 4, dims, strides, box);
+        const bool three = tuning(kSelect ? SSG_TUNE_ISB_SELECT_BLOCKS : SSG_TUNE_ISB_UP_BLOCKS) == 3;
+        constexpr bool kG = kGuideDefault<W, kSelect>;
+        if (tma && three)
+            isb_up_kernel<W, Tf, kSelect, GL, 3, kG, true><<<grid, kBatchBlock, 0, st>>>(
+                gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so, map);
+        else if (tma)
+            isb_up_kernel<W, Tf, kSelect, GL, 2, kG, true><<<grid, kBatchBlock, 0, st>>>(
+                gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so, map);
+        else if (three)
+            isb_up_kernel<W, Tf, kSelect, GL, 3><<<grid, kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu,
+                                                                              wd, var_inv_i, table, so, map);
+        else
+            isb_up_kernel<W, Tf, kSelect, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu, wd,
+                                                                           var_inv_i, table, so, map);
+    } else {
+        isb_up_kernel<W, Tf, kSelect, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu, wd,
+                                                                       var_inv_i, table, so, map);
+    }
     return launch_status(kSelect ? "isb_up_kernel<select>" : "isb_up_kernel");
 }
 
@@ -1018,4 +1139,14 @@ extern "C" int ssg_select_distance_batch(const void* d_cost, int candidate_count
         select_kernel<8, float><<<grid, kBatchBlock, 0, st>>>(static_cast<const float*>(d_cost), pixels, chunks,
                                                               candidate_count, so.d0, so.dl, so.q, d_distance, d_index);
     return launch_status("select_kernel");
+}
+
+extern "C" int ssg_take_device_status(uint32_t* status)
+{
+    SSG_REQUIRE(status, "null pointer");
+    uint32_t zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(status, ssg::g_tma_status, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(ssg::g_tma_status, &zero, sizeof(uint32_t));
+    if (e != cudaSuccess) return ssg::fail(SSG_ERR_CUDA, "device status: %s", cudaGetErrorString(e));
+    return SSG_OK;
 }

@@ -276,7 +276,8 @@ class BatchPipeline:
             graph.replay()
         return self.rgb[:frames], self.pano_distance[:frames]
 
-    TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "isb_select_blocks", "hole_blocks_per_sm", "merge_frames")
+    TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "isb_select_blocks", "isb_tile_tma", "hole_blocks_per_sm",
+                   "merge_frames")
     GROUP_CHOICES = (1, 2, 4)
 
     def _apply_tuning(self, match, stitch, frames) -> None:

@@ -264,3 +264,32 @@ def test_isb_apply_batch_skip_fine_guide(ss, native):
     assert not np.array_equal(g_all[0], g0)
     with pytest.raises(ValueError):
         run(4)
+
+
+def test_tma_tiles_equal_cp_async_tiles(ss, native, golden_c1):
+    """The chunked ISB upsampling stages its coarse tiles by TMA (cp.async.bulk.tensor with an
+    mbarrier) or by cp.async: the same bits either way, at every level and in the fused selection,
+    with edge clamping at all four borders; no bounded wait runs out."""
+    import ctypes
+    import importlib
+
+    tune = importlib.import_module("sphere-stereo_gb300.autotune")
+    N = ss._native
+    g = golden_c1
+    saved = tune.get("isb_tile_tma")
+    status = ctypes.c_uint32(0)
+    N.call("ssg_take_device_status", ctypes.byref(status))
+    outs = {}
+    try:
+        for tma in (0, 1):
+            tune.set_knob("isb_tile_tma", tma)
+            est, _ = _estimator(ss, g, "fp16", max_batch=2, graphs=False)
+            match, stitch = _batch(g, frames=2)
+            rgb, d = est.estimate_RGBD_panoramas(match, stitch)
+            outs[tma] = (rgb.clone(), d.clone(), est.pipeline().distance.clone())
+    finally:
+        tune.set_knob("isb_tile_tma", saved)
+    for a, b in zip(outs[0], outs[1]):
+        torch.testing.assert_close(a, b, rtol=0, atol=0)
+    N.call("ssg_take_device_status", ctypes.byref(status))
+    assert status.value == 0
