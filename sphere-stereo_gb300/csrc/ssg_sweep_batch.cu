@@ -24,13 +24,13 @@ namespace ssg {
 // (x0, y0 + 1), (x0 + 1, y0 + 1) (bytes 0..3) with (x0, y0) = (i - 1, j - 1); texels outside the
 // image are 0 (grid_sample's zero padding).  Entries form planes of (rows + 2) x (cols + 2), one
 // per (frame, camera), covering every footprint whose top-left tap lies in [-1, cols] x
-// [-1, rows]; every entry is written.  A sample is one 16-byte load (half the bytes of two rows
-// of fp16 texel pairs), and a channel's bilinear blend is two 16-bit x 8-bit dot products.
+// [-1, rows]; every entry is written.  A sample is one 16-byte load, and a channel's bilinear
+// blend is two 16-bit x 8-bit dot products.
 //
-// 8 bits hold the reference's inputs exactly: images are 8-bit data (python/utils.py:157-205)
-// that estimate_RGBD_panorama receives as float32.  Float inputs are checked while staging: a
-// plane with a value that is not an integer in [0, 255] gets its flag set (plane_flags[plane] =
-// 1), and the sweep samples that plane from the float images themselves.  The guide of every
+// 8 bits hold decoded images exactly (python/utils.py:157-205 decodes 8-bit files and converts
+// them to float32); a linear resize makes fractional values.  Float inputs are therefore checked
+// while staging: a plane with a value that is not an integer in [0, 255] gets its flag set
+// (plane_flags[plane] = 1), and the sweep samples that plane from the float images themselves.  The guide of every
 // reference camera (rgb2yCbCr + uint8 cast) is written in the same pass, from the float values,
 // as one 32-bit word per pixel (Y, Cb, Cr, 0).
 // ---------------------------------------------------------------------------------------------
