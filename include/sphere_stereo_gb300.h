@@ -254,14 +254,19 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
 
 /* Image staging + guides: d_images frames x cameras x rows x cols x 3, float32 (the inputs of
  * estimate_RGBD_panorama, python/depth_estimation.py:205-227) or uint8 (the 8-bit images those
- * inputs are made from, python/utils.py:157-205) -> d_staged frames x cameras planes of
- * (rows + 2) x (cols + 2) 16-byte entries, entry (j, i) holding the bilinear footprint of top-left
- * tap (i - 1, j - 1) -- texels (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1) -- as 8-bit
- * RGB, zero outside the image (every entry is written); d_plane_flags frames x cameras int32,
- * set to 1 for a plane with a value that is not an integer in [0, 255] (the sweep then samples
- * that plane from the float images); and d_guides frames x references x rows x cols 32-bit guide
- * words (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from the
- * float values).  Zeroes d_plane_flags first (a 4 x frames x cameras byte memset). */
+ * inputs are made from, python/utils.py:157-205) -> d_staged: per (frame, camera) two planes
+ * (high, low) of (rows + 2) x (cols + 2) 16-byte entries, entry (j, i) holding the bilinear
+ * footprint of top-left tap (i - 1, j - 1) -- texels (x0, y0), (x0 + 1, y0), (x0, y0 + 1),
+ * (x0 + 1, y0 + 1) -- one byte per texel and channel, zero outside the image (every entry is
+ * written).  Values are staged as 8.8 fixed-point codes round(256 v): the high plane holds the
+ * high bytes (the values themselves for 8-bit data) and the low plane the low bytes (float
+ * inputs only; the uint8 variant leaves it).  d_plane_flags frames x cameras int32: the largest
+ * class of a plane's values -- 0 integers in [0, 255], 1 values in [0, 65535/256] with fractions
+ * (as a linear resize makes them; the sweep then adds the low plane), 2 anything else (the sweep
+ * samples that plane from the float images).  d_guides frames x references x rows x cols 32-bit
+ * guide words (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from the
+ * float values).  Zeroes d_plane_flags first (a 4 x frames x cameras byte memset).  Planes of
+ * (rows + 2) x (cols + 2) >= 2^24 entries return SSG_ERR_UNSUPPORTED. */
 SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                              const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
                              int32_t* d_plane_flags, void* stream);
@@ -444,7 +449,7 @@ typedef struct {
     const float* relative_poses;  /* host, camera_count x 12: rows 0..2 of inverse(camera.rt) @ reference.rt */
     const float* candidates;      /* host, candidate_count distances */
     double sigma_i, sigma_s;      /* cost filter; the distance post-filter uses half of each */
-    const float* d_staged;        /* the rig frame's planes from ssg_stage_images (camera_count planes) */
+    const float* d_staged;        /* the rig frame's planes from ssg_stage_images (2 x camera_count planes) */
     const float* d_images;        /* the frame's float32 images staged (or NULL for 8-bit inputs) */
     const int32_t* d_plane_flags; /* the frame's camera_count plane flags from ssg_stage_images */
     const int8_t* d_selected;     /* rows x cols selected cameras */

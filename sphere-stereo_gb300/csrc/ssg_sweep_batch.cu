@@ -44,14 +44,44 @@ constexpr int kStageTexX = kStageTileX + 1, kStageTexY = kStageTileY + 1;  // te
 
 __device__ __forceinline__ float texel_value(float v) { return v; }
 __device__ __forceinline__ float texel_value(uint8_t v) { return (float)v; }
-__device__ __forceinline__ bool is_byte(float v) { return v >= 0.0f && v <= 255.0f && v == rintf(v); }
-__device__ __forceinline__ bool is_byte(uint8_t) { return true; }
 
-// One block: a kStageTileX x kStageTileY tile of entries from a shared-memory tile of texels.
+// How a plane's values are staged (plane_flags: the largest class over the plane):
+//   0: integers in [0, 255]: one byte per value (the high plane);
+//   1: values in [0, 65535 / 256] with fractions (a linear resize makes them): 8.8 fixed point,
+//      q = round(256 v), high byte in the high plane and low byte in the low plane (a value moves
+//      by at most 1/512);
+//   2: anything else (negative, larger, NaN): the sweep samples the float images.
+constexpr int kPlaneBytes = 0, kPlaneFixed = 1, kPlaneFloats = 2;
+constexpr float kFixedMax = 65535.0f / 256.0f;
+
+__device__ __forceinline__ int value_class(float v)
+{
+    if (v >= 0.0f && v <= 255.0f && v == rintf(v)) return kPlaneBytes;
+    return v >= 0.0f && v <= kFixedMax ? kPlaneFixed : kPlaneFloats;
+}
+__device__ __forceinline__ int value_class(uint8_t) { return kPlaneBytes; }
+
+// the 8.8 fixed-point code of a value of class 0 or 1 (0 for class 2)
+__device__ __forceinline__ uint32_t fixed_code(float v, int cls)
+{
+    return cls == kPlaneFloats ? 0u : __float2uint_rn(v * 256.0f);
+}
+__device__ __forceinline__ uint32_t fixed_code(uint8_t v, int) { return (uint32_t)v << 8; }
+
+// byte c of three codes' high (kLow = false) or low bytes, packed as one word (byte 3 zero)
+template <bool kLow>
+__device__ __forceinline__ uint32_t code_bytes(uint32_t q0, uint32_t q1, uint32_t q2)
+{
+    const int sh = kLow ? 0 : 8;
+    return ((q0 >> sh) & 255u) | (((q1 >> sh) & 255u) << 8) | (((q2 >> sh) & 255u) << 16);
+}
+
+// One block: a kStageTileX x kStageTileY tile of entries from shared-memory tiles of texels.
 // Each thread converts whole texels (three consecutive values: a warp reads 384 contiguous
-// bytes per channel load), checks them and, for the texels that are pixels of this tile, writes
-// their guide word; then each thread assembles entries from the shared tile.
-// blockIdx.y: frame * cameras + camera.
+// bytes per channel load), classifies them and, for the texels that are pixels of this tile,
+// writes their guide word; then each thread assembles entries of the high plane (and, for float
+// inputs, of the low plane) from the shared tiles.  blockIdx.y: frame * cameras + camera; its
+// planes are staged[2 * that] (high) and staged[2 * that + 1] (low).
 template <typename Tin>
 __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_constant__ StageParams p,
                                                                   const Tin* __restrict__ images,
@@ -59,8 +89,10 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
                                                                   uint32_t* __restrict__ guides,
                                                                   int* __restrict__ plane_flags)
 {
-    __shared__ uint32_t tex[kStageTexY][kStageTexX];  // RGB bytes, byte 3 zero
-    __shared__ int not_bytes;
+    constexpr bool kLowPlane = sizeof(Tin) == 4;  // 8-bit inputs have no fractions
+    __shared__ uint32_t tex[kStageTexY][kStageTexX];                      // high bytes, byte 3 zero
+    __shared__ uint32_t tex_low[kLowPlane ? kStageTexY : 1][kStageTexX];  // low bytes
+    __shared__ int block_class;
     const int pitch = p.cols + 2;
     const int64_t P = (int64_t)p.cols * p.rows, plane = (int64_t)pitch * (p.rows + 2);
     const int tiles_x = (pitch + kStageTileX - 1) / kStageTileX;
@@ -70,24 +102,26 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
     const Tin* img = images + (int64_t)inst * P * 3;
     const int slot = p.ref_slot[cam];
     uint32_t* guide = slot >= 0 ? guides + ((int64_t)frame * p.references + slot) * P : nullptr;
-    if (threadIdx.x == 0) not_bytes = 0;
+    if (threadIdx.x == 0) block_class = 0;
     // texel (x, y), x in [i0 - 1, i0 + kStageTileX - 1], y in [j0 - 1, j0 + kStageTileY - 1]: the
     // entries' top-left taps and their right / lower neighbours.  The top-left taps are the
     // pixels whose guide words this block writes.
-    bool bytes = true;
+    int cls = 0;
     for (int t = threadIdx.x; t < kStageTexY * kStageTexX; t += blockDim.x) {
         const int ly = t / kStageTexX, lx = t % kStageTexX;
         const int x = i0 - 1 + lx, y = j0 - 1 + ly;
-        uint32_t word = 0;
+        uint32_t q0 = 0, q1 = 0, q2 = 0;
         if (x >= 0 && y >= 0 && x < p.cols && y < p.rows) {
             const int64_t o = (int64_t)y * p.cols + x;
             const Tin r0 = img[o * 3], r1 = img[o * 3 + 1], r2 = img[o * 3 + 2];
-            const bool ok0 = is_byte(r0), ok1 = is_byte(r1), ok2 = is_byte(r2);
-            bytes = bytes && ok0 && ok1 && ok2;
-            const float c0 = texel_value(r0), c1 = texel_value(r1), c2 = texel_value(r2);
-            word = (ok0 ? (uint32_t)c0 : 0u) | ((ok1 ? (uint32_t)c1 : 0u) << 8) | ((ok2 ? (uint32_t)c2 : 0u) << 16);
+            const int k0 = value_class(r0), k1 = value_class(r1), k2 = value_class(r2);
+            cls = max(cls, max(k0, max(k1, k2)));
+            q0 = fixed_code(r0, k0);
+            q1 = fixed_code(r1, k1);
+            q2 = fixed_code(r2, k2);
             if (guide && lx < kStageTileX && ly < kStageTileY) {
                 // utils.py:144-155, the arithmetic of ssg_rgb_to_guide, from the input values
+                const float c0 = texel_value(r0), c1 = texel_value(r1), c2 = texel_value(r2);
                 const float yy = fadd(fadd(fadd(fmul(c0, 0.1826f), 16.0f), fmul(c1, 0.6142f)), fmul(c2, 0.062f));
                 const float cb = fadd(fsub(fsub(128.0f, fmul(c0, 0.1006f)), fmul(c1, 0.3386f)), fmul(c2, 0.4392f));
                 const float cr = fsub(fsub(fadd(fmul(c0, 0.4392f), 128.0f), fmul(c1, 0.3989f)), fmul(c2, 0.0403f));
@@ -98,26 +132,31 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
                 guide[o] = g0 | (g1 << 8) | (g2 << 16);
             }
         }
-        tex[ly][lx] = word;
+        tex[ly][lx] = code_bytes<false>(q0, q1, q2);
+        if constexpr (kLowPlane) tex_low[ly][lx] = code_bytes<true>(q0, q1, q2);
     }
-    __syncthreads();  // not_bytes is cleared before any thread sets it
-    if (!bytes) not_bytes = 1;
+    __syncthreads();  // block_class is cleared before any thread raises it
+    if (cls) atomicMax(&block_class, cls);
     __syncthreads();
-    if (threadIdx.x == 0 && not_bytes) atomicOr(plane_flags + inst, 1);
-    uint4* out = staged + (int64_t)inst * plane;
+    if (threadIdx.x == 0 && block_class) atomicMax(plane_flags + inst, block_class);
+    uint4* out = staged + (int64_t)(2 * inst) * plane;
     for (int e = threadIdx.x; e < kStageTileX * kStageTileY; e += blockDim.x) {
         const int li = e % kStageTileX, lj = e / kStageTileX;
         const int i = i0 + li, j = j0 + lj;
         if (i >= pitch || j >= p.rows + 2) continue;
-        const uint32_t t00 = tex[lj][li], t10 = tex[lj][li + 1];
-        const uint32_t t01 = tex[lj + 1][li], t11 = tex[lj + 1][li + 1];
-        uint32_t word[3];
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-            const uint32_t sel = (uint32_t)ch | ((uint32_t)(4 + ch) << 4);
-            word[ch] = __byte_perm(__byte_perm(t00, t10, sel), __byte_perm(t01, t11, sel), 0x5410);
+        for (int h = 0; h < (kLowPlane ? 2 : 1); ++h) {
+            const uint32_t(*tx)[kStageTexX] = h ? tex_low : tex;
+            const uint32_t t00 = tx[lj][li], t10 = tx[lj][li + 1];
+            const uint32_t t01 = tx[lj + 1][li], t11 = tx[lj + 1][li + 1];
+            uint32_t word[3];
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                const uint32_t sel = (uint32_t)ch | ((uint32_t)(4 + ch) << 4);
+                word[ch] = __byte_perm(__byte_perm(t00, t10, sel), __byte_perm(t01, t11, sel), 0x5410);
+            }
+            out[h * plane + (int64_t)j * pitch + i] = make_uint4(word[0], word[1], word[2], 0u);
         }
-        out[(int64_t)j * pitch + i] = make_uint4(word[0], word[1], word[2], 0u);
     }
 }
 
@@ -213,13 +252,17 @@ __device__ __forceinline__ void sample_pair_floats(const float* __restrict__ flo
     }
 }
 
-// Samples of an 8-bit plane from its footprints (`entries`), in units of 1/65535: the weights
+// Samples of a staged plane from its footprints (`entries`), in units of 1/65535: the weights
 // are 16-bit fractions of 65535 (a rounding of at most 1/131070 each: a sample moves by at most
 // 4 * 255 / 131070 < 0.008), each channel blended by two dot products of two 16-bit weights
 // with two 8-bit taps.  w * 65535 + 1.5 * 2^23 has round(w * 65535) in the low 16 bits of its
-// representation (one fused multiply-add per weight, for both samples).
-__device__ __forceinline__ void sample_pair_bytes(const uint4* __restrict__ entries, int cols, int rows, float2 ix,
-                                                  float2 iy, uint32_t (&s)[2][3])
+// representation (one fused multiply-add per weight, for both samples).  kFixed: the plane holds
+// 8.8 fixed-point codes; the low bytes' footprints follow `plane` entries on, and their blend
+// adds (blend + 128) >> 8 (the high bytes' blend is in units of 1/65535, the low bytes' in units
+// of 1/(65535 * 256)).
+template <bool kFixed>
+__device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entries, int64_t plane, int cols,
+                                                  int rows, float2 ix, float2 iy, uint32_t (&s)[2][3])
 {
     float2 x0, y0, wa, wb, wc, wd;
     bilinear_pair(cols, rows, ix, iy, x0, y0, wa, wb, wc, wd);
@@ -233,29 +276,34 @@ __device__ __forceinline__ void sample_pair_bytes(const uint4* __restrict__ entr
     for (int h = 0; h < 2; ++h) {
         const uint32_t top = __byte_perm(__float_as_uint(h ? qa.y : qa.x), __float_as_uint(h ? qb.y : qb.x), 0x5410);
         const uint32_t bot = __byte_perm(__float_as_uint(h ? qc.y : qc.x), __float_as_uint(h ? qd.y : qd.x), 0x5410);
-        const uint4 q = __ldg(entries + __float2uint_rz(h ? e.y : e.x));  // e >= 0: an unsigned offset
+        const uint32_t idx = __float2uint_rz(h ? e.y : e.x);  // e >= 0: an unsigned offset
+        const uint4 q = __ldg(entries + idx);
         s[h][0] = __dp2a_hi(bot, q.x, __dp2a_lo(top, q.x, 0u));
         s[h][1] = __dp2a_hi(bot, q.y, __dp2a_lo(top, q.y, 0u));
         s[h][2] = __dp2a_hi(bot, q.z, __dp2a_lo(top, q.z, 0u));
+        if constexpr (kFixed) {
+            const uint4 r = __ldg(entries + plane + idx);
+            s[h][0] += (__dp2a_hi(bot, r.x, __dp2a_lo(top, r.x, 0u)) + 128u) >> 8;
+            s[h][1] += (__dp2a_hi(bot, r.y, __dp2a_lo(top, r.y, 0u)) + 128u) >> 8;
+            s[h][2] += (__dp2a_hi(bot, r.z, __dp2a_lo(top, r.z, 0u)) + 128u) >> 8;
+        }
     }
 }
 
 // The candidate loop of one pixel: points d (R u) + t, projected and sampled in pairs, costs
-// written 8 candidates per cell.  kFloats: the plane is sampled from its float image (the rare
-// path, kept out of line so that its registers do not weigh on the 8-bit path); otherwise the
-// cost sum_c |sample_c - ref_c| is formed in units of 1/65535 with integer absolute differences
-// (the reference texels are integers there).
-template <typename T, bool kFloats, typename V>
+// written 8 candidates per cell.  kMode (the plane classes, kPlane*): kPlaneFloats samples the
+// float image with the reference's arithmetic against the float reference texels `rp`; otherwise
+// the cost sum_c |sample_c - ref_c| is formed in units of 1/65535 with integer absolute
+// differences against `rq` (the reference texels in those units).
+template <typename T, int kMode, typename V>
 __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4* __restrict__ entries,
-                                                 const float* __restrict__ floats, int cols, int rows, float2 ax,
-                                                 float2 ay, float2 az, float2 tx, float2 ty, float2 tz,
-                                                 const FastCam& k, const float (&rp)[3], T* __restrict__ out,
-                                                 int64_t chunk_stride)
+                                                      int64_t plane, const float* __restrict__ floats, int cols,
+                                                      int rows, float2 ax, float2 ay, float2 az, float2 tx, float2 ty,
+                                                      float2 tz, const FastCam& k, const float (&rp)[3],
+                                                      const uint32_t (&rq)[3], T* __restrict__ out,
+                                                      int64_t chunk_stride)
 {
     const int chunks = view.chunks();
-    uint32_t rq[3];
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) rq[ch] = (uint32_t)rp[ch] * 65535u;
     for (int ch = 0; ch < chunks; ++ch) {
         uint32_t packed[4];
 #pragma unroll
@@ -264,7 +312,7 @@ __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4
             float2 u, v;
             project_pair(fma2(d, ax, tx), fma2(d, ay, ty), fma2(d, az, tz), k, u, v);
             float c2[2];
-            if constexpr (kFloats) {
+            if constexpr (kMode == kPlaneFloats) {
                 float s[2][3];
                 sample_pair_floats(floats, cols, rows, u, v, s);
 #pragma unroll
@@ -272,7 +320,7 @@ __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4
                     c2[h] = fminf(fabsf(s[h][0] - rp[0]) + fabsf(s[h][1] - rp[1]) + fabsf(s[h][2] - rp[2]), 500.0f);
             } else {
                 uint32_t s[2][3];
-                sample_pair_bytes(entries, cols, rows, u, v, s);
+                sample_pair_codes<kMode == kPlaneFixed>(entries, plane, cols, rows, u, v, s);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const uint32_t sad = __usad(s[h][2], rq[2], __usad(s[h][1], rq[1], __usad(s[h][0], rq[0], 0u)));
@@ -288,33 +336,28 @@ __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4
     }
 }
 
-template <typename T, bool kFloats, typename V>
-__device__ __forceinline__ void sweep_candidates(const V& view, const uint4* __restrict__ entries,
-                                                 const float* __restrict__ floats, int cols, int rows, float2 ax,
-                                                 float2 ay, float2 az, float2 tx, float2 ty, float2 tz,
-                                                 const FastCam& k, const float (&rp)[3], T* __restrict__ out,
-                                                 int64_t chunk_stride)
-{
-    sweep_candidates_body<T, kFloats>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, out,
-                                      chunk_stride);
-}
-
-template <typename T, typename V>
-__device__ __noinline__ void sweep_candidates_floats(const V view, const float* __restrict__ floats, int cols,
-                                                     int rows, float2 ax, float2 ay, float2 az, float2 tx, float2 ty,
-                                                     float2 tz, const FastCam k, float r0, float r1, float r2,
-                                                     T* __restrict__ out, int64_t chunk_stride)
+// the rarer plane classes, kept out of line so that their registers do not weigh on the 8-bit path
+template <typename T, int kMode, typename V>
+__device__ __noinline__ void sweep_candidates_outlined(const V view, const uint4* __restrict__ entries, int64_t plane,
+                                                       const float* __restrict__ floats, int cols, int rows, float2 ax,
+                                                       float2 ay, float2 az, float2 tx, float2 ty, float2 tz,
+                                                       const FastCam k, float r0, float r1, float r2, uint32_t q0,
+                                                       uint32_t q1, uint32_t q2, T* __restrict__ out,
+                                                       int64_t chunk_stride)
 {
     const float rp[3] = {r0, r1, r2};
-    sweep_candidates_body<T, true>(view, nullptr, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, out,
-                                   chunk_stride);
+    const uint32_t rq[3] = {q0, q1, q2};
+    sweep_candidates_body<T, kMode>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, rq, out,
+                                    chunk_stride);
 }
 
 // Sweep + cost of one reference pixel (x, y) over all candidates, into its cells (`out`, chunk
 // stride `chunk_stride`).  `V` gives the instance's constants: ref_cam(), cam(c), pose(c) (12
 // floats), cand(k) (pairs are read as float2) and cameras(), chunks().  `frame_entries` /
-// `frame_floats` point at the frame's camera-0 plane of footprints / float image (planes `plane`
-// entries / cols x rows x 3 floats apart), `flags` at the frame's per-camera flags.
+// `frame_floats` point at the frame's camera-0 planes of footprints (camera c's high plane at
+// 2 c `plane` entries, its low plane `plane` entries after) / float image (cols x rows x 3 floats
+// apart), `flags` at the frame's per-camera plane classes.  The pixel takes the path of the larger
+// class of its reference and selected planes.
 template <typename T, typename V>
 __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restrict__ frame_entries,
                                             const float* __restrict__ frame_floats, const int* __restrict__ flags,
@@ -323,18 +366,37 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
 {
     const int pitch = cols + 2;
     const int64_t P = (int64_t)cols * rows;
+    const bool seen = sel >= 0 && sel < view.cameras();
+    const int mode = max(__ldg(flags + ref_camera), seen ? __ldg(flags + sel) : 0);
     float rp[3];
-    if (!__ldg(flags + ref_camera)) {
-        // the footprint of top-left tap (x, y): its nw texel is the pixel
-        const uint4 q = __ldg(frame_entries + (int64_t)ref_camera * plane + (y + 1) * pitch + x + 1);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) rp[ch] = entry_texel(q, ch, 0);
-    } else {
+    uint32_t rq[3];
+    if (mode == kPlaneFloats && frame_floats) {
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) rp[ch] = __ldg(frame_floats + (ref_camera * P + (int64_t)y * cols + x) * 3 + ch);
+    } else {
+        // the footprint of top-left tap (x, y): its nw texels (byte 0 of each word) are the pixel's
+        const int64_t at = (int64_t)(2 * ref_camera) * plane + (y + 1) * pitch + x + 1;
+        const uint4 q = __ldg(frame_entries + at);
+        const uint32_t hw[3] = {q.x, q.y, q.z};
+        if (mode == kPlaneFixed) {
+            const uint4 r = __ldg(frame_entries + at + plane);
+            const uint32_t lw[3] = {r.x, r.y, r.z};
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                const uint32_t code = (hw[ch] & 0xFFu) << 8 | (lw[ch] & 0xFFu);
+                rp[ch] = (float)code * (1.0f / 256.0f);
+                rq[ch] = (code * 65535u + 128u) >> 8;
+            }
+        } else {
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                rp[ch] = (float)(hw[ch] & 0xFFu);
+                rq[ch] = (hw[ch] & 0xFFu) * 65535u;
+            }
+        }
     }
     const int chunks = view.chunks();
-    if (sel < 0 || sel >= view.cameras()) {
+    if (!seen) {
         // no camera sees the point: grid_sample of an all-zero image (depth_estimation.py:166)
         float c = fminf(fabsf(rp[0]) + fabsf(rp[1]) + fabsf(rp[2]), 500.0f);
         float cc[8] = {c, c, c, c, c, c, c, c};
@@ -353,14 +415,17 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
     const float2 az = splat(fmaf(m[10], pu[2], fmaf(m[9], pu[1], m[8] * pu[0])));
     const float2 tx = splat(m[3]), ty = splat(m[7]), tz = splat(m[11]);
     const FastCam k = view.cam(sel);
-    const uint4* entries = frame_entries + (int64_t)sel * plane;
+    const uint4* entries = frame_entries + (int64_t)(2 * sel) * plane;
     const float* floats = frame_floats ? frame_floats + sel * P * 3 : nullptr;
-    if ((__ldg(flags + sel) || __ldg(flags + ref_camera)) && floats)
-        sweep_candidates_floats<T>(view, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp[0], rp[1], rp[2], out,
-                                   chunk_stride);
+    if (mode == kPlaneFloats && floats)
+        sweep_candidates_outlined<T, kPlaneFloats>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
+                                                   rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
+    else if (mode == kPlaneFixed)
+        sweep_candidates_outlined<T, kPlaneFixed>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
+                                                  rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
     else
-        sweep_candidates<T, false>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, out,
-                                   chunk_stride);
+        sweep_candidates_body<T, kPlaneBytes>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp,
+                                              rq, out, chunk_stride);
 }
 
 // the constants of one reference slot of a uniform batch (kernel parameters)
@@ -410,7 +475,7 @@ __global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
     const int frame = inst / p.references, slot = inst % p.references;
     const int plane = pitch * (rows + 2);
     T* out = cost + (int64_t)inst * p.chunks * P * 8 + (int64_t)i * 8;
-    sweep_pixel<T>(UniformView{p, slot}, staged + (int64_t)frame * p.cameras * plane,
+    sweep_pixel<T>(UniformView{p, slot}, staged + (int64_t)frame * p.cameras * 2 * plane,
                    floats ? floats + (int64_t)frame * p.cameras * P * 3 : nullptr, plane_flags + frame * p.cameras,
                    plane, p.ref_index[slot], cols, rows, i % cols, i / cols, selected[(int64_t)slot * P + i], out,
                    (int64_t)P * 8);
@@ -540,11 +605,13 @@ using namespace ssg;
 
 using namespace ssg;
 
+// the sweep forms entry offsets in float (exact below 2^24 entries a plane)
 static int staged_plane_fits(int cols, int rows)
 {
     SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
-    SSG_REQUIRE((int64_t)(cols + 2) * (rows + 2) < ((int64_t)1 << 31), "images of %dx%d pixels are too large", cols,
-                rows);
+    if ((int64_t)(cols + 2) * (rows + 2) >= ((int64_t)1 << 24))
+        return fail(SSG_ERR_UNSUPPORTED, "images of %dx%d pixels exceed the batched sweep's 2^24-entry planes", cols,
+                    rows);
     return SSG_OK;
 }
 

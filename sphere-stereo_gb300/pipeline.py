@@ -66,9 +66,9 @@ class BatchPipeline:
         u8 = dict(dtype=torch.uint8, device=dev)
         f32 = dict(dtype=torch.float32, device=dev)
         i16 = dict(dtype=torch.int16, device=dev)
-        # planes of 16-byte bilinear footprints (8-bit RGB), (rows + 2) x (cols + 2) per camera, and
-        # a flag per plane for the planes sampled from the float images instead
-        self.staged = torch.zeros(F * C * (self.rows + 2) * (self.cols + 2) * 4, **f32)
+        # two planes (high and low bytes of 8.8 fixed-point codes) of 16-byte bilinear footprints,
+        # (rows + 2) x (cols + 2) per camera, and a class per plane (integer / fixed / float)
+        self.staged = torch.zeros(F * C * 2 * (self.rows + 2) * (self.cols + 2) * 4, **f32)
         self.plane_flags = torch.zeros(F * C, dtype=torch.int32, device=dev)
         # guides: one 32-bit word per pixel (Y, Cb, Cr, 0)
         self.guides = [torch.empty(F * R * r * c * 4, **u8) for r, c in self.shapes]
@@ -117,8 +117,8 @@ class BatchPipeline:
         i0, inst = f0 * R, frames * R
         cols, rows = self.cols, self.rows
         stage = "ssg_stage_images_u8" if match.dtype == torch.uint8 else "ssg_stage_images"
-        plane = (rows + 2) * (cols + 2) * 4  # floats of one plane of footprints
-        staged = self.staged.data_ptr() + 4 * f0 * C * plane
+        plane = (rows + 2) * (cols + 2) * 4  # floats of one plane of footprints (two per camera)
+        staged = self.staged.data_ptr() + 4 * f0 * C * 2 * plane
         flags = self.plane_flags.data_ptr() + 4 * f0 * C
         m = match[f0:f0 + frames]
         N.call(stage, m.data_ptr(), frames, C, cols, rows, self._refs, R, staged,

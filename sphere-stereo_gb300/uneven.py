@@ -69,7 +69,7 @@ class UnevenBatch:
             j = {
                 "match": torch.zeros(C, rows, cols, 3, dtype=input_dtype, device=dev),
                 "stitch": torch.zeros(R, st.image_rows, st.image_cols, 3, dtype=input_dtype, device=dev),
-                "staged": torch.zeros(C * (rows + 2) * (cols + 2) * 4, **f32),
+                "staged": torch.zeros(C * 2 * (rows + 2) * (cols + 2) * 4, **f32),  # high and low planes
                 "flags": torch.zeros(C, dtype=torch.int32, device=dev),
                 "guide0": torch.empty(R * rows * cols * 4, **u8),  # 32-bit guide words
                 "distance": torch.empty(R, rows, cols, **f32),

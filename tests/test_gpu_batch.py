@@ -211,14 +211,21 @@ def test_bench_configuration_against_fp32_path(ss, native, synthetic):
         assert p >= 50
 
 
-def test_non_integer_inputs_against_fp32_path(ss, native, golden_c1):
+@pytest.mark.parametrize("kind", ["fractions", "out_of_range"])
+def test_non_integer_inputs_against_fp32_path(ss, native, golden_c1, kind):
     """Inputs that are not 8-bit values (the reference resizes float images, python/utils.py:198)
-    are staged as fp16: the 16-bit path still keeps the fp32 path's index on >= 99.9 % of pixels."""
+    are staged as 8.8 fixed point (fractions in [0, 255]) or sampled from the float images (values
+    outside that range): the 16-bit path still keeps the fp32 path's index on >= 99.9 % of
+    pixels."""
     g = golden_c1
     rng = np.random.default_rng(7)
-    noisy = {**g, "images_to_match": (g["images_to_match"].astype(np.float32)
-                                      + rng.uniform(0, 1, g["images_to_match"].shape).astype(np.float32)),
-             "images_to_stitch": g["images_to_stitch"].astype(np.float32)}
+    m = g["images_to_match"].astype(np.float32)
+    if kind == "fractions":
+        m = np.clip(m + rng.uniform(-0.5, 0.5, m.shape).astype(np.float32), 0, 255).astype(np.float32)
+    else:
+        m = (m * np.float32(1.2)).astype(np.float32)  # up to 306: outside the fixed-point range
+        m[:, 0, 0, 0] = 300.0  # every camera has a value beyond it
+    noisy = {**g, "images_to_match": m, "images_to_stitch": g["images_to_stitch"].astype(np.float32)}
     exact, cfg = _estimator(ss, noisy, "fp32")
     match = [torch.as_tensor(im, device=DEV) for im in noisy["images_to_match"]]
     stitch = [torch.as_tensor(im, device=DEV) for im in noisy["images_to_stitch"]]
@@ -228,8 +235,61 @@ def test_non_integer_inputs_against_fp32_path(ss, native, golden_c1):
     fast.estimate_RGBD_panoramas(torch.stack(match)[None].contiguous(), torch.stack(stitch)[None].contiguous())
     torch.cuda.synchronize()
     same = (fast.batch_index_maps[0].cpu().numpy() == idx32).mean()
-    print(f"\nnon-integer inputs, fp16 vs fp32 path: same index {same:.6f}")
+    flags = fast.pipeline().plane_flags[:len(match)].cpu().numpy()
+    assert (flags == (1 if kind == "fractions" else 2)).all()
+    print(f"\n{kind} inputs, fp16 vs fp32 path: same index {same:.6f}")
     assert same >= 0.999
+
+
+def test_stage_images_codes(ss, native):
+    """Staging: 8.8 fixed-point codes round(256 v) in the high / low planes, zero outside the
+    image, the plane classes (integers, fractions, out of range), the 8-bit variant, and the guide
+    words from the input values."""
+    N = ss._native
+    utils = __import__("importlib").import_module("sphere-stereo_gb300.utils")
+    rng = np.random.default_rng(11)
+    rows, cols, C = 37, 50, 3
+    imgs = rng.integers(0, 256, (C, rows, cols, 3)).astype(np.float32)
+    imgs[1] += rng.uniform(-0.49, 0.49, imgs[1].shape).astype(np.float32)
+    imgs[1] = np.clip(imgs[1], 0, 255)
+    imgs[2, 5, 7, 1] = -3.0
+    d_img = torch.as_tensor(imgs, device=DEV)
+    plane = (rows + 2) * (cols + 2)
+    staged = torch.zeros(C * 2 * plane * 4, dtype=torch.float32, device=DEV)
+    guides = torch.zeros(1 * rows * cols * 4, dtype=torch.uint8, device=DEV)
+    flags = torch.zeros(C, dtype=torch.int32, device=DEV)
+    stream = torch.cuda.current_stream().cuda_stream
+    N.call("ssg_stage_images", d_img.data_ptr(), 1, C, cols, rows, N.ints([1]), 1, staged.data_ptr(),
+           guides.data_ptr(), flags.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert flags.cpu().tolist() == [0, 1, 2]
+    words = staged.cpu().numpy().view(np.uint32).reshape(C, 2, rows + 2, cols + 2, 4)
+    for c in (0, 1):
+        code = np.rint(imgs[c].astype(np.float64) * 256).astype(np.int64)  # round half to even
+        padded = np.zeros((rows + 2, cols + 2, 3), np.int64)
+        padded[1:-1, 1:-1] = code  # texel (x, y) at [y + 1, x + 1]
+        for j in (0, 1, rows // 2, rows + 1):
+            for i in (0, 1, cols // 3, cols + 1):
+                for ch in range(3):
+                    taps = [padded[j + dy, i + dx, ch] if j + dy < rows + 2 and i + dx < cols + 2 else 0
+                            for dy, dx in ((0, 0), (0, 1), (1, 0), (1, 1))]
+                    hi = sum(((t >> 8) & 255) << (8 * k) for k, t in enumerate(taps))
+                    lo = sum((t & 255) << (8 * k) for k, t in enumerate(taps))
+                    assert words[c, 0, j, i, ch] == hi, (c, j, i, ch)
+                    assert words[c, 1, j, i, ch] == lo, (c, j, i, ch)
+    g = guides.cpu().numpy().view(np.uint32).reshape(rows, cols)
+    want = utils.rgb_to_guide(d_img[1]).cpu().numpy().astype(np.uint32)
+    np.testing.assert_array_equal(g, want[..., 0] | want[..., 1] << 8 | want[..., 2] << 16)
+    # the 8-bit variant: the high plane only, class 0
+    u8 = torch.as_tensor(imgs[0].astype(np.uint8)[None].repeat(C, 0), device=DEV)
+    staged8 = torch.zeros_like(staged)
+    N.call("ssg_stage_images_u8", u8.data_ptr(), 1, C, cols, rows, N.ints([1]), 1, staged8.data_ptr(),
+           guides.data_ptr(), flags.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert flags.cpu().tolist() == [0, 0, 0]
+    w8 = staged8.cpu().numpy().view(np.uint32).reshape(C, 2, rows + 2, cols + 2, 4)
+    np.testing.assert_array_equal(w8[0, 0], words[0, 0])
+    assert not w8[:, 1].any()
 
 
 def test_isb_apply_batch_skip_fine_guide(ss, native):
