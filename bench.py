@@ -34,15 +34,17 @@ PACKAGE = "sphere-stereo_gb300"
 WORKLOAD = dict(width_in=1216, matching=(1024, 1024), stitch=(1216, 1216), panorama=(2048, 1024), candidates=32,
                 refs=[2, 3], sigma_i=10.0, sigma_s=25.0, min_dist=0.55, max_dist=100.0)
 WORKLOAD_NAME = ("4 double-sphere fisheye cameras (fx=0.28W, xi=-0.2, alpha=0.6) on a 0.2 m square, "
-                 "matching 1024x1024, 32 candidates, references 2,3, rgb_to_stitch 1216x1216, "
-                 "panorama 2048x1024, sigma_i 10, sigma_s 25")
+                 "1216x1216 uint8 inputs, matching 1024x1024, 32 candidates, references 2,3, "
+                 "rgb_to_stitch 1216x1216, panorama 2048x1024, sigma_i 10, sigma_s 25")
 METRIC = "RGB-D panoramas/s @1024² match, 32 cand"
 UNIT = "panoramas/s"
-DATA = "synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast per frame (seed 2000+frame)"
+DATA = ("synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast per frame (seed 2000+frame) to "
+        "1216x1216 uint8 per camera; images to match = those resized to the matching resolution in float32 "
+        "(linear, the reference's cv2.resize), images to stitch = the 1216x1216 renders")
 # DRAM bytes (read + write) of sweep_batch_kernel per (frame, reference) instance with fp16 storage,
-# measured by ncu on one launch of an 8-frame batch of this workload (579,591,936 B read +
-# 1,029,880,576 B written for 16 instances)
-SWEEP_DRAM_BYTES_PER_INSTANCE = (577766912 + 1028907008) // 16
+# measured by ncu on one launch of an 8-frame batch of this workload (1,189,412,608 B read +
+# 1,038,806,784 B written for 16 instances)
+SWEEP_DRAM_BYTES_PER_INSTANCE = (1189412608 + 1038806784) // 16
 
 
 def _env_int(name, default):
@@ -57,15 +59,46 @@ def frames_for_rank(total: int, rank: int, world: int) -> list[int]:
     return [rank + world * i for i in range(total)]
 
 
-def render_pool(count: int, rank: int, world: int):
+def render_pool(count: int, rank: int, world: int, resize):
+    """Seeded frames of the workload: every camera ray-cast to width_in x width_in uint8 (the
+    inputs), the images to match made from them by `resize` (uint8 [cameras, rows, cols, 3],
+    (cols, rows) -> float32 [cameras, ...]: the library's GPU resize, or for the reference arm the
+    oracle's restatement of the same arithmetic), the images to stitch the renders of the
+    references (rgb_to_stitch = the input resolution).  frame.originals keeps the uint8 renders."""
     syn = importlib.import_module(PACKAGE + ".synthetic")
     cams = syn.square_rig(WORKLOAD["width_in"])
+    w = WORKLOAD["width_in"]
+    if tuple(WORKLOAD["stitch"]) != (w, w):
+        raise ValueError("the workload stitches at its input resolution")
     frames = []
     for f in frames_for_rank(max(1, count), rank, world):
         rng = np.random.Generator(np.random.PCG64(syn.frame_seed(2, f)))
         scene = syn.random_scene(rng)
-        frames.append(syn.render_frame(scene, cams, WORKLOAD["matching"], WORKLOAD["stitch"], WORKLOAD["refs"]))
+        fr = syn.render_frame(scene, cams, (w, w), (w, w), [])
+        originals = np.stack(fr.images_to_match)  # uint8 [cameras, w, w, 3]
+        match = resize(originals, WORKLOAD["matching"])
+        fr = syn.Frame(list(match), [originals[r] for r in WORKLOAD["refs"]], fr.inv_distance)
+        fr.originals = originals
+        frames.append(fr)
     return syn.basalt_calibration(cams), frames
+
+
+def gpu_resize(device):
+    ss_utils = importlib.import_module(PACKAGE + ".utils")
+
+    def resize(images, size):
+        import torch
+
+        return ss_utils.resize_linear(torch.as_tensor(images, device=device), size).cpu().numpy()
+
+    return resize
+
+
+def oracle_resize(images, size):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import prep_eval_oracle
+
+    return np.stack([prep_eval_oracle.resize_linear(im, size) for im in images])
 
 
 class ClockSampler:
@@ -177,12 +210,13 @@ class LaunchRecorder:
 
 
 def sweep_bytes_per_launch(cols: int, rows: int, cameras: int, candidates: int, cost_bytes: int,
-                           staged: bool = False) -> int:
+                           staged_planes: int = 0) -> int:
     """Algorithmic bytes of the sweep for one (frame, reference) instance: the reference image
     and the camera-selection map read once, each source image read at most once (upper bound),
-    the cost volume written once.  Staged images are 16-byte RGBx texels."""
+    the cost volume written once.  Staged images are read as 16-byte footprints per plane (one
+    plane for 8-bit inputs, two for 8.8 fixed point); float images as 12-byte texels."""
     P = cols * rows
-    texel = 16 if staged else 12
+    texel = 16 * staged_planes if staged_planes else 12
     return texel * P + texel * P * (cameras - 1) + P + cost_bytes * candidates * P
 
 
@@ -320,34 +354,78 @@ def run_ours(args, rank, world, device, rendered):
         rec.active = False
     peak, peak_kind = measured_peaks()
     sweep_ms = rec.mean_ms()
-    sweep_bytes = B * len(WORKLOAD["refs"]) * sweep_bytes_per_launch(mw, mh, 4, WORKLOAD["candidates"], 2, staged=True)
+    # the images to match are resized, fractional: two staged planes (8.8 fixed point) per camera
+    sweep_bytes = B * len(WORKLOAD["refs"]) * sweep_bytes_per_launch(mw, mh, 4, WORKLOAD["candidates"], 2,
+                                                                      staged_planes=2)
     achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9 if sweep_ms else None
     instances = B * len(WORKLOAD["refs"])
     traffic = (SWEEP_DRAM_BYTES_PER_INSTANCE * instances
                if SWEEP_DRAM_BYTES_PER_INSTANCE is not None and args.storage == "fp16" and args.workload == "prototype"
                else None)
 
-    # the same batches through the 8-bit inputs the float images are made from (a quarter of the
-    # upload): end to end, uploads overlapped as above
+    # the same batches from the 8-bit renders themselves: their upload, the resize to the matching
+    # resolution on the GPU (ssg_resize_linear, input preparation) and the references' renders
+    # passed as 8-bit images to stitch; uploads and downloads overlapped as above
     e2e_u8 = None
     if not args.no_u8:
-        pinned = [(torch.as_tensor(m.astype(np.uint8)).pin_memory(), torch.as_tensor(st.astype(np.uint8)).pin_memory())
-                  for m, st in host_batches]
-        staging = [(torch.empty_like(pinned[0][0], device=device), torch.empty_like(pinned[0][1], device=device))
-                   for _ in range(2)]
-        h2d_u8 = sum(t.numel() * t.element_size() for t in pinned[0])
-        e2e(args.warmup)
+        N = native
+        refs = torch.as_tensor(WORKLOAD["refs"], device=device)
+        originals = [np.stack([frames[(k + j) % len(frames)].originals for j in range(B)]) for k in range(2)]
+        pinned_u8 = [torch.as_tensor(o).pin_memory() for o in originals]
+        slots_u8 = [torch.empty_like(pinned_u8[0], device=device) for _ in range(2)]
+        C, win = pinned_u8[0].shape[1], pinned_u8[0].shape[2]
+        match_buf = torch.empty((B, C, mh, mw, 3), dtype=torch.float32, device=device)
+        stitch_buf = torch.empty((B, len(WORKLOAD["refs"]), win, win, 3), dtype=torch.uint8, device=device)
+        h2d_u8 = pinned_u8[0].numel()
+
+        def upload_u8(i):
+            slot = i % 2
+            with torch.cuda.stream(up_stream):
+                up_stream.wait_event(consumed[slot])
+                slots_u8[slot].copy_(pinned_u8[i % 2], non_blocking=True)
+                uploaded[slot].record(up_stream)
+
+        def e2e_u8_steps(steps):
+            for ev in consumed + downloaded:
+                ev.record(compute)
+            upload_u8(0)
+            for i in range(steps):
+                if i + 1 < steps:
+                    upload_u8(i + 1)
+                slot = i % 2
+                compute.wait_event(uploaded[slot])
+                src = slots_u8[slot]
+                N.call("ssg_resize_linear", src.data_ptr(), N.PIXEL_U8, win, win, 3, match_buf.data_ptr(),
+                       N.PIXEL_F32, mw, mh, B * C, compute.cuda_stream)
+                torch.index_select(src, 1, refs, out=stitch_buf)
+                consumed[slot].record(compute)
+                rgb, dist = est.estimate_RGBD_panoramas(match_buf, stitch_buf)
+                compute.wait_event(downloaded[slot])
+                out_dev[slot][0].copy_(rgb, non_blocking=True)
+                out_dev[slot][1].copy_(dist, non_blocking=True)
+                produced[slot].record(compute)
+                with torch.cuda.stream(down_stream):
+                    down_stream.wait_event(produced[slot])
+                    out_host[slot][0].copy_(out_dev[slot][0], non_blocking=True)
+                    out_host[slot][1].copy_(out_dev[slot][1], non_blocking=True)
+                    downloaded[slot].record(down_stream)
+            for ev in downloaded:
+                compute.wait_event(ev)
+
+        e2e_u8_steps(args.warmup)
         torch.cuda.synchronize()
         barrier(world)
         s3, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s3.record()
-        e2e(args.steps)
+        e2e_u8_steps(args.steps)
         e3.record()
         torch.cuda.synchronize()
         u8_ms = max_over_ranks(s3.elapsed_time(e3) / args.steps, world, device)
         e2e_u8 = {"value": world * B * 1000.0 / u8_ms, "unit": UNIT, "h2d_bytes_per_step": h2d_u8,
                   "d2h_bytes_per_step": d2h, "ms_per_step": u8_ms,
-                  "inputs": "uint8 images (the 8-bit data the float32 inputs hold)"}
+                  "inputs": "the 1216x1216 uint8 renders of every camera, resized to the matching resolution on the "
+                            "GPU inside the timed region (ssg_resize_linear); the references' renders stitched as "
+                            "uint8"}
     return {
         "value": world * B * 1000.0 / ms,
         "ms_per_step": ms,
@@ -630,7 +708,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        data = render_pool(1, 0, 1)
+        data = render_pool(1, 0, 1, oracle_resize)
         for _ in range(args.warmup):
             cpu_baseline(data, 1)
         base = cpu_baseline(data, max(1, args.steps))
@@ -659,7 +737,7 @@ def main():
         return
     if args.workload == "stream":
         use_stream_workload(args)
-    rendered = render_pool(args.unique_frames, rank, world)
+    rendered = render_pool(args.unique_frames, rank, world, gpu_resize(device))
     ours = run_ours(args, rank, world, device, rendered)
     if rank != 0:
         if world > 1:
@@ -678,6 +756,8 @@ def main():
                        "mode": f"batched, {args.storage} cost volume, fp32 arithmetic, CUDA-graph replay",
                        "tuned": ours["tuned"], "overlap_groups": ours["overlap_groups"],
                        "parallelism": "replicas" if world > 1 else "single GPU",
+                       "inputs": "images to match: 1216x1216 uint8 renders resized to 1024x1024 float32 (fractional "
+                                 "values: staged as 8.8 fixed point); images to stitch: the 1216x1216 renders",
                        "l2": f"each step reads a {args.batch}-frame batch of inputs "
                              f"({args.batch} x {(4 * 1024 * 1024 + len(WORKLOAD['refs']) * 1216 * 1216) * 12 / 1e6:.0f} MB), "
                              "alternating between two batches; both far exceed the 126 MB L2"},

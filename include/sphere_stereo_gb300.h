@@ -254,13 +254,14 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
 
 /* Image staging + guides: d_images frames x cameras x rows x cols x 3, float32 (the inputs of
  * estimate_RGBD_panorama, python/depth_estimation.py:205-227) or uint8 (the 8-bit images those
- * inputs are made from, python/utils.py:157-205) -> d_staged: per (frame, camera) two planes
- * (high, low) of (rows + 2) x (cols + 2) 16-byte entries, entry (j, i) holding the bilinear
- * footprint of top-left tap (i - 1, j - 1) -- texels (x0, y0), (x0 + 1, y0), (x0, y0 + 1),
- * (x0 + 1, y0 + 1) -- one byte per texel and channel, zero outside the image (every entry is
- * written).  Values are staged as 8.8 fixed-point codes round(256 v): the high plane holds the
- * high bytes (the values themselves for 8-bit data) and the low plane the low bytes (float
- * inputs only; the uint8 variant leaves it).  d_plane_flags frames x cameras int32: the largest
+ * inputs are made from, python/utils.py:157-205) -> d_staged: per (frame, camera) a region of
+ * 32 x (rows + 2) x (cols + 2) bytes of entries, entry (j, i) holding the bilinear footprint of
+ * top-left tap (i - 1, j - 1) -- texels (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1) --
+ * one byte per texel in a 32-bit word per channel, zero outside the image (every entry is
+ * written).  Values are staged as 8.8 fixed-point codes round(256 v): float inputs get 32-byte
+ * entries (the high-byte words of channels 0, 1, 2, the low-byte word of channel 0, then the
+ * low-byte words of channels 1, 2, zero padding); the uint8 variant writes 16-byte entries of
+ * high-byte words in the first half of the region.  d_plane_flags frames x cameras int32: the largest
  * class of a plane's values -- 0 integers in [0, 255], 1 values in [0, 65535/256] with fractions
  * (as a linear resize makes them; the sweep then adds the low plane), 2 anything else (the sweep
  * samples that plane from the float images).  d_guides frames x references x rows x cols 32-bit
@@ -281,9 +282,9 @@ SSG_API int ssg_convert_u8(const float* d_src, uint8_t* d_dst, int64_t count, vo
 
 /* Sphere sweep + cost for every instance (python/depth_estimation.py:141-175), 16-bit output.
  * relative_poses: references x cameras x 12 floats (host); d_staged / d_plane_flags from
- * ssg_stage_images[_u8]; d_images: the float32 images staged (read for planes whose flag is set;
- * NULL for 8-bit inputs); d_selected: references x pixels int8; d_cost: instances x level-0
- * volume. */
+ * ssg_stage_images[_u8]; d_images: the float32 images staged by ssg_stage_images (read for planes
+ * of class 2; it also selects the 32-byte entries), NULL after ssg_stage_images_u8; d_selected:
+ * references x pixels int8; d_cost: instances x level-0 volume. */
 SSG_API int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_count, const ssg_camera* cameras,
                                  int references, const int* reference_cameras, const float* relative_poses,
                                  const float* d_staged, const float* d_images, const int32_t* d_plane_flags,

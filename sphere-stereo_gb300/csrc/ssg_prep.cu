@@ -61,18 +61,30 @@ __device__ __forceinline__ int fixed_weight(float f)
     return min(max(__float2int_rn(w), -32768), 32767);
 }
 
-// one thread per destination pixel (all channels); blockIdx.y: image
+// One block per kTileX x kTileY destination pixels of one image (blockIdx.z): the tile's column
+// and row taps are formed once (in double, as OpenCV forms its tables) into shared memory, then
+// one thread per destination pixel (all channels) blends.
+constexpr int kTileX = 32, kTileY = 8;
+
 template <typename Tin, typename Tout>
-__global__ void __launch_bounds__(256) resize_linear_kernel(const __grid_constant__ ResizeParams p,
-                                                            const Tin* __restrict__ src, Tout* __restrict__ dst)
+__global__ void __launch_bounds__(kTileX * kTileY) resize_linear_kernel(const __grid_constant__ ResizeParams p,
+                                                                        const Tin* __restrict__ src,
+                                                                        Tout* __restrict__ dst)
 {
-    const int64_t n = (int64_t)p.dst_cols * p.dst_rows;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int dx = (int)(i % p.dst_cols), dy = (int)(i / p.dst_cols);
+    __shared__ Tap cols_tap[kTileX], rows_tap[kTileY];
+    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY;
     const int C = p.channels;
-    src += (int64_t)blockIdx.y * p.src_cols * p.src_rows * C;
-    dst += ((int64_t)blockIdx.y * n + i) * C;
+    src += (int64_t)blockIdx.z * p.src_cols * p.src_rows * C;
+    dst += (int64_t)blockIdx.z * p.dst_cols * p.dst_rows * C;
+    if (!p.area2) {
+        if (threadIdx.x < kTileX) cols_tap[threadIdx.x] = column_tap(p, min(x0 + (int)threadIdx.x, p.dst_cols - 1));
+        else if (threadIdx.x < kTileX + kTileY)
+            rows_tap[threadIdx.x - kTileX] = row_tap(p, min(y0 + (int)threadIdx.x - kTileX, p.dst_rows - 1));
+        __syncthreads();
+    }
+    const int dx = x0 + (int)(threadIdx.x % kTileX), dy = y0 + (int)(threadIdx.x / kTileX);
+    if (dx >= p.dst_cols || dy >= p.dst_rows) return;
+    dst += ((int64_t)dy * p.dst_cols + dx) * C;
     if (p.area2) {
         const int64_t r0 = (int64_t)(2 * dy) * p.src_cols, r1 = r0 + p.src_cols;
         for (int c = 0; c < C; ++c) {
@@ -88,7 +100,7 @@ __global__ void __launch_bounds__(256) resize_linear_kernel(const __grid_constan
         }
         return;
     }
-    const Tap tx = column_tap(p, dx), ty = row_tap(p, dy);
+    const Tap tx = cols_tap[threadIdx.x % kTileX], ty = rows_tap[threadIdx.x / kTileX];
     const int64_t r0 = (int64_t)ty.s0 * p.src_cols, r1 = (int64_t)ty.s1 * p.src_cols;
     if constexpr (sizeof(Tout) == 1) {
         const int a0 = fixed_weight(tx.f), a1 = 2048 - a0, b0 = fixed_weight(ty.f), b1 = 2048 - b0;
@@ -136,17 +148,19 @@ extern "C" int ssg_resize_linear(const void* d_src, int src_type, int src_cols, 
     p.scale_x = 1.0 / ((double)dst_cols / src_cols);
     p.scale_y = 1.0 / ((double)dst_rows / src_rows);
     p.area2 = src_cols == 2 * dst_cols && src_rows == 2 * dst_rows;
-    const int64_t n = (int64_t)dst_cols * dst_rows;
-    const dim3 grid(grid_1d(n, 256), images);
+    const dim3 grid((unsigned)((dst_cols + kTileX - 1) / kTileX), (unsigned)((dst_rows + kTileY - 1) / kTileY),
+                    (unsigned)images);
+    SSG_REQUIRE(grid.y <= 65535, "destination of %d rows is too tall", dst_rows);
     cudaStream_t st = as_stream(stream);
+    constexpr int kThreads = kTileX * kTileY;
     if (src_type == SSG_PIXEL_F32)
         resize_linear_kernel<float, float>
-            <<<grid, 256, 0, st>>>(p, static_cast<const float*>(d_src), static_cast<float*>(d_dst));
+            <<<grid, kThreads, 0, st>>>(p, static_cast<const float*>(d_src), static_cast<float*>(d_dst));
     else if (dst_type == SSG_PIXEL_F32)
         resize_linear_kernel<uint8_t, float>
-            <<<grid, 256, 0, st>>>(p, static_cast<const uint8_t*>(d_src), static_cast<float*>(d_dst));
+            <<<grid, kThreads, 0, st>>>(p, static_cast<const uint8_t*>(d_src), static_cast<float*>(d_dst));
     else
         resize_linear_kernel<uint8_t, uint8_t>
-            <<<grid, 256, 0, st>>>(p, static_cast<const uint8_t*>(d_src), static_cast<uint8_t*>(d_dst));
+            <<<grid, kThreads, 0, st>>>(p, static_cast<const uint8_t*>(d_src), static_cast<uint8_t*>(d_dst));
     return launch_status("resize_linear_kernel");
 }

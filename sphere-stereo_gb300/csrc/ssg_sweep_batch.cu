@@ -79,9 +79,10 @@ __device__ __forceinline__ uint32_t code_bytes(uint32_t q0, uint32_t q1, uint32_
 // One block: a kStageTileX x kStageTileY tile of entries from shared-memory tiles of texels.
 // Each thread converts whole texels (three consecutive values: a warp reads 384 contiguous
 // bytes per channel load), classifies them and, for the texels that are pixels of this tile,
-// writes their guide word; then each thread assembles entries of the high plane (and, for float
-// inputs, of the low plane) from the shared tiles.  blockIdx.y: frame * cameras + camera; its
-// planes are staged[2 * that] (high) and staged[2 * that + 1] (low).
+// writes their guide word; then each thread assembles entries from the shared tiles.  blockIdx.y:
+// frame * cameras + camera; its entries start at staged[2 * that * plane]: 16-byte entries of
+// high bytes for 8-bit inputs, 32-byte entries (high words x, y, z and low word x, then low
+// words y, z) for float inputs.
 template <typename Tin>
 __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_constant__ StageParams p,
                                                                   const Tin* __restrict__ images,
@@ -144,18 +145,25 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
         const int li = e % kStageTileX, lj = e / kStageTileX;
         const int i = i0 + li, j = j0 + lj;
         if (i >= pitch || j >= p.rows + 2) continue;
+        uint32_t word[2][3];
 #pragma unroll
         for (int h = 0; h < (kLowPlane ? 2 : 1); ++h) {
             const uint32_t(*tx)[kStageTexX] = h ? tex_low : tex;
             const uint32_t t00 = tx[lj][li], t10 = tx[lj][li + 1];
             const uint32_t t01 = tx[lj + 1][li], t11 = tx[lj + 1][li + 1];
-            uint32_t word[3];
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
                 const uint32_t sel = (uint32_t)ch | ((uint32_t)(4 + ch) << 4);
-                word[ch] = __byte_perm(__byte_perm(t00, t10, sel), __byte_perm(t01, t11, sel), 0x5410);
+                word[h][ch] = __byte_perm(__byte_perm(t00, t10, sel), __byte_perm(t01, t11, sel), 0x5410);
             }
-            out[h * plane + (int64_t)j * pitch + i] = make_uint4(word[0], word[1], word[2], 0u);
+        }
+        const int64_t at = (int64_t)j * pitch + i;
+        if constexpr (kLowPlane) {
+            // a 32-byte entry: high words x, y, z, low word x | low words y, z
+            out[2 * at] = make_uint4(word[0][0], word[0][1], word[0][2], word[1][0]);
+            out[2 * at + 1] = make_uint4(word[1][1], word[1][2], 0u, 0u);
+        } else {
+            out[at] = make_uint4(word[0][0], word[0][1], word[0][2], 0u);
         }
     }
 }
@@ -256,13 +264,13 @@ __device__ __forceinline__ void sample_pair_floats(const float* __restrict__ flo
 // are 16-bit fractions of 65535 (a rounding of at most 1/131070 each: a sample moves by at most
 // 4 * 255 / 131070 < 0.008), each channel blended by two dot products of two 16-bit weights
 // with two 8-bit taps.  w * 65535 + 1.5 * 2^23 has round(w * 65535) in the low 16 bits of its
-// representation (one fused multiply-add per weight, for both samples).  kFixed: the plane holds
-// 8.8 fixed-point codes; the low bytes' footprints follow `plane` entries on, and their blend
-// adds (blend + 128) >> 8 (the high bytes' blend is in units of 1/65535, the low bytes' in units
-// of 1/(65535 * 256)).
-template <bool kFixed>
-__device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entries, int64_t plane, int cols,
-                                                  int rows, float2 ix, float2 iy, uint32_t (&s)[2][3])
+// representation (one fused multiply-add per weight, for both samples).  Entries are kStride
+// 16-byte words apart (2: the 32-byte entries of float inputs).  kFixed: the entries hold 8.8
+// fixed-point codes, low bytes in word 3 and the second half; their blend adds (blend + 128) >> 8
+// (the high bytes' blend is in units of 1/65535, the low bytes' in units of 1/(65535 * 256)).
+template <bool kFixed, int kStride>
+__device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entries, int cols, int rows, float2 ix,
+                                                  float2 iy, uint32_t (&s)[2][3])
 {
     float2 x0, y0, wa, wb, wc, wd;
     bilinear_pair(cols, rows, ix, iy, x0, y0, wa, wb, wc, wd);
@@ -277,15 +285,15 @@ __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entr
         const uint32_t top = __byte_perm(__float_as_uint(h ? qa.y : qa.x), __float_as_uint(h ? qb.y : qb.x), 0x5410);
         const uint32_t bot = __byte_perm(__float_as_uint(h ? qc.y : qc.x), __float_as_uint(h ? qd.y : qd.x), 0x5410);
         const uint32_t idx = __float2uint_rz(h ? e.y : e.x);  // e >= 0: an unsigned offset
-        const uint4 q = __ldg(entries + idx);
+        const uint4 q = __ldg(entries + kStride * idx);
         s[h][0] = __dp2a_hi(bot, q.x, __dp2a_lo(top, q.x, 0u));
         s[h][1] = __dp2a_hi(bot, q.y, __dp2a_lo(top, q.y, 0u));
         s[h][2] = __dp2a_hi(bot, q.z, __dp2a_lo(top, q.z, 0u));
         if constexpr (kFixed) {
-            const uint4 r = __ldg(entries + plane + idx);
-            s[h][0] += (__dp2a_hi(bot, r.x, __dp2a_lo(top, r.x, 0u)) + 128u) >> 8;
-            s[h][1] += (__dp2a_hi(bot, r.y, __dp2a_lo(top, r.y, 0u)) + 128u) >> 8;
-            s[h][2] += (__dp2a_hi(bot, r.z, __dp2a_lo(top, r.z, 0u)) + 128u) >> 8;
+            const uint4 r = __ldg(entries + kStride * idx + 1);  // the entry's second half
+            s[h][0] += (__dp2a_hi(bot, q.w, __dp2a_lo(top, q.w, 0u)) + 128u) >> 8;
+            s[h][1] += (__dp2a_hi(bot, r.x, __dp2a_lo(top, r.x, 0u)) + 128u) >> 8;
+            s[h][2] += (__dp2a_hi(bot, r.y, __dp2a_lo(top, r.y, 0u)) + 128u) >> 8;
         }
     }
 }
@@ -295,9 +303,9 @@ __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entr
 // float image with the reference's arithmetic against the float reference texels `rp`; otherwise
 // the cost sum_c |sample_c - ref_c| is formed in units of 1/65535 with integer absolute
 // differences against `rq` (the reference texels in those units).
-template <typename T, int kMode, typename V>
+template <typename T, int kMode, int kStride, typename V>
 __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4* __restrict__ entries,
-                                                      int64_t plane, const float* __restrict__ floats, int cols,
+                                                      const float* __restrict__ floats, int cols,
                                                       int rows, float2 ax, float2 ay, float2 az, float2 tx, float2 ty,
                                                       float2 tz, const FastCam& k, const float (&rp)[3],
                                                       const uint32_t (&rq)[3], T* __restrict__ out,
@@ -320,7 +328,7 @@ __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4
                     c2[h] = fminf(fabsf(s[h][0] - rp[0]) + fabsf(s[h][1] - rp[1]) + fabsf(s[h][2] - rp[2]), 500.0f);
             } else {
                 uint32_t s[2][3];
-                sample_pair_codes<kMode == kPlaneFixed>(entries, plane, cols, rows, u, v, s);
+                sample_pair_codes<kMode == kPlaneFixed, kStride>(entries, cols, rows, u, v, s);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const uint32_t sad = __usad(s[h][2], rq[2], __usad(s[h][1], rq[1], __usad(s[h][0], rq[0], 0u)));
@@ -337,8 +345,8 @@ __device__ __forceinline__ void sweep_candidates_body(const V& view, const uint4
 }
 
 // the rarer plane classes, kept out of line so that their registers do not weigh on the 8-bit path
-template <typename T, int kMode, typename V>
-__device__ __noinline__ void sweep_candidates_outlined(const V view, const uint4* __restrict__ entries, int64_t plane,
+template <typename T, int kMode, int kStride, typename V>
+__device__ __noinline__ void sweep_candidates_outlined(const V view, const uint4* __restrict__ entries,
                                                        const float* __restrict__ floats, int cols, int rows, float2 ax,
                                                        float2 ay, float2 az, float2 tx, float2 ty, float2 tz,
                                                        const FastCam k, float r0, float r1, float r2, uint32_t q0,
@@ -347,17 +355,17 @@ __device__ __noinline__ void sweep_candidates_outlined(const V view, const uint4
 {
     const float rp[3] = {r0, r1, r2};
     const uint32_t rq[3] = {q0, q1, q2};
-    sweep_candidates_body<T, kMode>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, rq, out,
-                                    chunk_stride);
+    sweep_candidates_body<T, kMode, kStride>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, rq, out,
+                                             chunk_stride);
 }
 
 // Sweep + cost of one reference pixel (x, y) over all candidates, into its cells (`out`, chunk
 // stride `chunk_stride`).  `V` gives the instance's constants: ref_cam(), cam(c), pose(c) (12
 // floats), cand(k) (pairs are read as float2) and cameras(), chunks().  `frame_entries` /
-// `frame_floats` point at the frame's camera-0 planes of footprints (camera c's high plane at
-// 2 c `plane` entries, its low plane `plane` entries after) / float image (cols x rows x 3 floats
-// apart), `flags` at the frame's per-camera plane classes.  The pixel takes the path of the larger
-// class of its reference and selected planes.
+// `frame_floats` point at the frame's camera-0 footprints (camera c's at 2 c `plane` 16-byte
+// words: 16-byte entries for 8-bit inputs, 32-byte ones when frame_floats is set) / float image
+// (cols x rows x 3 floats apart), `flags` at the frame's per-camera plane classes.  The pixel takes
+// the path of the larger class of its reference and selected planes.
 template <typename T, typename V>
 __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restrict__ frame_entries,
                                             const float* __restrict__ frame_floats, const int* __restrict__ flags,
@@ -368,6 +376,7 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
     const int64_t P = (int64_t)cols * rows;
     const bool seen = sel >= 0 && sel < view.cameras();
     const int mode = max(__ldg(flags + ref_camera), seen ? __ldg(flags + sel) : 0);
+    const int stride = frame_floats ? 2 : 1;  // 16-byte words per entry: 32-byte entries for float inputs
     float rp[3];
     uint32_t rq[3];
     if (mode == kPlaneFloats && frame_floats) {
@@ -375,12 +384,12 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
         for (int ch = 0; ch < 3; ++ch) rp[ch] = __ldg(frame_floats + (ref_camera * P + (int64_t)y * cols + x) * 3 + ch);
     } else {
         // the footprint of top-left tap (x, y): its nw texels (byte 0 of each word) are the pixel's
-        const int64_t at = (int64_t)(2 * ref_camera) * plane + (y + 1) * pitch + x + 1;
+        const int64_t at = (int64_t)(2 * ref_camera) * plane + (int64_t)stride * ((y + 1) * pitch + x + 1);
         const uint4 q = __ldg(frame_entries + at);
         const uint32_t hw[3] = {q.x, q.y, q.z};
         if (mode == kPlaneFixed) {
-            const uint4 r = __ldg(frame_entries + at + plane);
-            const uint32_t lw[3] = {r.x, r.y, r.z};
+            const uint4 r = __ldg(frame_entries + at + 1);
+            const uint32_t lw[3] = {q.w, r.x, r.y};
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
                 const uint32_t code = (hw[ch] & 0xFFu) << 8 | (lw[ch] & 0xFFu);
@@ -418,14 +427,17 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
     const uint4* entries = frame_entries + (int64_t)(2 * sel) * plane;
     const float* floats = frame_floats ? frame_floats + sel * P * 3 : nullptr;
     if (mode == kPlaneFloats && floats)
-        sweep_candidates_outlined<T, kPlaneFloats>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
-                                                   rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
+        sweep_candidates_outlined<T, kPlaneFloats, 2>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
+                                                      rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
     else if (mode == kPlaneFixed)
-        sweep_candidates_outlined<T, kPlaneFixed>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
-                                                  rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
+        sweep_candidates_outlined<T, kPlaneFixed, 2>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
+                                                     rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
+    else if (stride == 2)
+        sweep_candidates_outlined<T, kPlaneBytes, 2>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k,
+                                                     rp[0], rp[1], rp[2], rq[0], rq[1], rq[2], out, chunk_stride);
     else
-        sweep_candidates_body<T, kPlaneBytes>(view, entries, plane, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp,
-                                              rq, out, chunk_stride);
+        sweep_candidates_body<T, kPlaneBytes, 1>(view, entries, floats, cols, rows, ax, ay, az, tx, ty, tz, k, rp, rq,
+                                                 out, chunk_stride);
 }
 
 // the constants of one reference slot of a uniform batch (kernel parameters)

@@ -242,9 +242,9 @@ def test_non_integer_inputs_against_fp32_path(ss, native, golden_c1, kind):
 
 
 def test_stage_images_codes(ss, native):
-    """Staging: 8.8 fixed-point codes round(256 v) in the high / low planes, zero outside the
-    image, the plane classes (integers, fractions, out of range), the 8-bit variant, and the guide
-    words from the input values."""
+    """Staging: 8.8 fixed-point codes round(256 v) as high and low bytes of the footprints, zero
+    outside the image, the plane classes (integers, fractions, out of range), the 8-bit variant,
+    and the guide words from the input values."""
     N = ss._native
     utils = __import__("importlib").import_module("sphere-stereo_gb300.utils")
     rng = np.random.default_rng(11)
@@ -263,7 +263,8 @@ def test_stage_images_codes(ss, native):
            guides.data_ptr(), flags.data_ptr(), stream)
     torch.cuda.synchronize()
     assert flags.cpu().tolist() == [0, 1, 2]
-    words = staged.cpu().numpy().view(np.uint32).reshape(C, 2, rows + 2, cols + 2, 4)
+    # float inputs: 32-byte entries, high words x, y, z then low words x, y, z
+    words = staged.cpu().numpy().view(np.uint32).reshape(C, rows + 2, cols + 2, 8)
     for c in (0, 1):
         code = np.rint(imgs[c].astype(np.float64) * 256).astype(np.int64)  # round half to even
         padded = np.zeros((rows + 2, cols + 2, 3), np.int64)
@@ -275,8 +276,8 @@ def test_stage_images_codes(ss, native):
                             for dy, dx in ((0, 0), (0, 1), (1, 0), (1, 1))]
                     hi = sum(((t >> 8) & 255) << (8 * k) for k, t in enumerate(taps))
                     lo = sum((t & 255) << (8 * k) for k, t in enumerate(taps))
-                    assert words[c, 0, j, i, ch] == hi, (c, j, i, ch)
-                    assert words[c, 1, j, i, ch] == lo, (c, j, i, ch)
+                    assert words[c, j, i, ch] == hi, (c, j, i, ch)
+                    assert words[c, j, i, 3 + ch] == lo, (c, j, i, ch)
     g = guides.cpu().numpy().view(np.uint32).reshape(rows, cols)
     want = utils.rgb_to_guide(d_img[1]).cpu().numpy().astype(np.uint32)
     np.testing.assert_array_equal(g, want[..., 0] | want[..., 1] << 8 | want[..., 2] << 16)
@@ -287,9 +288,10 @@ def test_stage_images_codes(ss, native):
            guides.data_ptr(), flags.data_ptr(), stream)
     torch.cuda.synchronize()
     assert flags.cpu().tolist() == [0, 0, 0]
+    # 8-bit inputs: 16-byte entries of high words in the first half of each camera's region
     w8 = staged8.cpu().numpy().view(np.uint32).reshape(C, 2, rows + 2, cols + 2, 4)
-    np.testing.assert_array_equal(w8[0, 0], words[0, 0])
-    assert not w8[:, 1].any()
+    np.testing.assert_array_equal(w8[0, 0, ..., :3], words[0, ..., :3])
+    assert not w8[:, 0, ..., 3].any() and not w8[:, 1].any()
 
 
 def test_isb_apply_batch_skip_fine_guide(ss, native):
