@@ -470,6 +470,80 @@ def run_plain_fp32(args, device, rendered, frames_timed: int):
             "mode": "fp32 cost volume, one frame per estimate_RGBD_panorama call, eager launches"}
 
 
+def run_reference_as_written_gpu(args, device, rendered, frames_timed: int):
+    """The reference's per-frame algorithm as it is written (python/depth_estimation.py:137-242),
+    on the same GPU: torch sweep over materialised [N, H, W, 3] point volumes and a 5-D
+    grid_sample per camera, torch selection (min / max / gather / parabola), the ISB filter and the
+    stitcher through the package's fp32 entry points (the reference's CUDA kernels' arithmetic).
+    The reference itself cannot run here (it needs CuPy); this restates its torch part."""
+    import torch
+
+    ss = importlib.import_module(PACKAGE)
+    utils = importlib.import_module(PACKAGE + ".utils")
+    calibration, frames = rendered
+    W = WORKLOAD
+    est = _estimator(ss, calibration, device, "fp32", 1, False)
+    cols, rows = W["matching"]
+    N = W["candidates"]
+    calibs = est.calibrations
+    yy, xx = torch.meshgrid(torch.arange(rows, device=device), torch.arange(cols, device=device), indexing="ij")
+    pixels = torch.stack([xx, yy], dim=-1).unsqueeze(0)
+    cands = 1 / torch.linspace(1 / W["min_dist"], 1 / W["max_dist"], N, device=device)
+    size = torch.tensor([cols, rows], device=device)
+
+    def distance_of(ref, selected, images_p, image_list):
+        pt_unit, _ = utils.unproject(pixels, calibs[ref])
+        points = cands.view(N, 1, 1, 1) * pt_unit.view(1, rows, cols, 3)
+        volume = torch.zeros([1, 3, N, rows, cols], device=device)
+        for c, cal in enumerate(calibs):
+            rt = torch.matmul(torch.inverse(cal.rt), calibs[ref].rt)
+            in_cam = torch.matmul(torch.cat([points, torch.ones_like(points[..., :1])], dim=-1), rt.T)
+            uv, _ = utils.project(in_cam[..., :3], cal)
+            uv = ((uv + 0.5) / size) * 2 - 1
+            uv = torch.cat([uv.unsqueeze(0), torch.zeros_like(uv[..., :1]).unsqueeze(0)], dim=-1)
+            sampled = torch.nn.functional.grid_sample(images_p[c], uv, align_corners=False)
+            mask = (selected == c).repeat(1, 3, N, 1, 1)
+            volume[mask] = sampled[mask]
+        cost = torch.clamp(torch.sum(torch.abs(volume - images_p[ref]), dim=1).squeeze(0), max=500)
+        guide = utils.rgb2yCbCr(image_list[ref]).type(torch.uint8)
+        cost, _ = est.cost_filter.apply(guide.clone(), cost.clone(), W["sigma_i"], W["sigma_s"])
+        m, idx = torch.min(cost, dim=0, keepdim=True)
+        M, _ = torch.max(cost, dim=0, keepdim=True)
+        left = torch.gather(cost, 0, torch.clamp(idx - 1, 0, N - 1))
+        right = torch.gather(cost, 0, torch.clamp(idx + 1, 0, N - 1))
+        var = torch.clamp(0.5 * (left - right) / ((left + right) - 2.0 * m + 1e-8), -0.5, 0.5)
+        var[idx == N - 1] = 0
+        var[idx == 0] = 0
+        sel = idx.float() + var
+        sel[M == m] = N - 1
+        dist = cands[0] / ((cands[0] / cands[-1] - 1) * sel / (N - 1) + 1)
+        dist[torch.abs(M - m) < 1e-8] = cands[-1]
+        filtered, _ = est.distance_filter.apply(guide.clone(), dist.clone(), W["sigma_i"] / 2, W["sigma_s"] / 2)
+        return filtered[0]
+
+    def frame(match, stitch):
+        images_p = [im.unsqueeze(0).permute(0, 3, 1, 2).unsqueeze(2) for im in match]
+        maps = [distance_of(r, est.selected_cameras[k], images_p, match) for k, r in enumerate(W["refs"])]
+        return est.fishey_stitcher.stitch([im.type(torch.uint8) for im in stitch], maps)
+
+    inputs = [([torch.as_tensor(im.astype(np.float32), device=device) for im in f.images_to_match],
+               [torch.as_tensor(im.astype(np.float32), device=device) for im in f.images_to_stitch]) for f in frames]
+    with torch.no_grad():
+        for i in range(max(1, args.warmup)):
+            frame(*inputs[i % len(inputs)])
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for i in range(frames_timed):
+            frame(*inputs[i % len(inputs)])
+        end.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / frames_timed
+    return {"value": 1000.0 / ms, "unit": UNIT, "ms_per_frame": ms, "frames": frames_timed,
+            "mode": "the reference's torch sweep and selection (materialised volumes, grid_sample) with its ISB "
+                    "and stitcher kernels' arithmetic, one frame per call, fp32"}
+
+
 def cpu_baseline(frames_calib, sample_frames: int):
     """The oracle (C restatement of the reference, OpenMP over all cores) on full frames."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -695,6 +769,8 @@ def main():
                          "64 candidates, every camera a reference; uneven: a mixed batch of jobs")
     ap.add_argument("--jobs", type=int, default=128, help="jobs of the uneven workload")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the leg that runs the reference's torch algorithm as written on the GPU")
     ap.add_argument("--knob", action="append", default=[], metavar="NAME=VALUE",
                     help="fix a launch-shape knob (with --no-autotune; autotune.KNOBS names)")
     ap.add_argument("--overlap-groups", type=int, default=None,
@@ -746,6 +822,10 @@ def main():
     plain = run_plain_fp32(args, device, rendered, args.plain_frames) if args.plain_frames > 0 else None
     if plain is not None:
         plain["batched_over_plain"] = ours["value"] / (world * plain["value"])
+    written = None
+    if args.plain_frames > 0 and not args.no_reference_gpu:
+        written = run_reference_as_written_gpu(args, device, rendered, max(2, args.plain_frames // 4))
+        written["batched_over_it"] = ours["value"] / (world * written["value"])
     base = None
     if not args.no_cpu_baseline:
         base = cpu_baseline((rendered[0], rendered[1][:1]), args.cpu_frames)
@@ -762,6 +842,7 @@ def main():
                              f"({args.batch} x {(4 * 1024 * 1024 + len(WORKLOAD['refs']) * 1216 * 1216) * 12 / 1e6:.0f} MB), "
                              "alternating between two batches; both far exceed the 126 MB L2"},
             "e2e": ours["e2e"], "e2e_u8": ours["e2e_u8"], "plain_fp32_gpu": plain,
+            "reference_algorithm_gpu": written,
             "gpu_launches": ours["gpu_launches"], "clocks": ours["clocks"],
             "roofline": ours["roofline"], "cpu_baseline": base}
     print(json.dumps(line))
