@@ -266,8 +266,11 @@ __device__ __forceinline__ void sample_pair_floats(const float* __restrict__ flo
 // with two 8-bit taps.  w * 65535 + 1.5 * 2^23 has round(w * 65535) in the low 16 bits of its
 // representation (one fused multiply-add per weight, for both samples).  Entries are kStride
 // 16-byte words apart (2: the 32-byte entries of float inputs).  kFixed: the entries hold 8.8
-// fixed-point codes, low bytes in word 3 and the second half; their blend adds (blend + 128) >> 8
-// (the high bytes' blend is in units of 1/65535, the low bytes' in units of 1/(65535 * 256)).
+// fixed-point codes, low bytes in word 3 and the second half.  A low byte weighs 1/256 of a high
+// one, so the low bytes are blended by one 4-way byte dot product with the high bytes of the
+// 16-bit weights (floor(w * 65535 / 256), within 1 of w * 65535 / 256): the result is again in
+// units of 1/65535, below the exact low-byte blend by less than 4 * 255 units (0.016 of a grey
+// level), on top of the high bytes' rounding above.
 template <bool kFixed, int kStride>
 __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entries, int cols, int rows, float2 ix,
                                                   float2 iy, uint32_t (&s)[2][3])
@@ -291,9 +294,10 @@ __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entr
         s[h][2] = __dp2a_hi(bot, q.z, __dp2a_lo(top, q.z, 0u));
         if constexpr (kFixed) {
             const uint4 r = __ldg(entries + kStride * idx + 1);  // the entry's second half
-            s[h][0] += (__dp2a_hi(bot, q.w, __dp2a_lo(top, q.w, 0u)) + 128u) >> 8;
-            s[h][1] += (__dp2a_hi(bot, r.x, __dp2a_lo(top, r.x, 0u)) + 128u) >> 8;
-            s[h][2] += (__dp2a_hi(bot, r.y, __dp2a_lo(top, r.y, 0u)) + 128u) >> 8;
+            const uint32_t w8 = __byte_perm(top, bot, 0x7531);   // high bytes of the weights nw, ne, sw, se
+            s[h][0] = __dp4a(w8, q.w, s[h][0]);
+            s[h][1] = __dp4a(w8, r.x, s[h][1]);
+            s[h][2] = __dp4a(w8, r.y, s[h][2]);
         }
     }
 }
