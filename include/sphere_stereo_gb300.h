@@ -284,7 +284,8 @@ SSG_API int ssg_convert_u8(const float* d_src, uint8_t* d_dst, int64_t count, vo
  * relative_poses: references x cameras x 12 floats (host); d_staged / d_plane_flags from
  * ssg_stage_images[_u8]; d_images: the float32 images staged by ssg_stage_images (read for planes
  * of class 2; it also selects the 32-byte entries), NULL after ssg_stage_images_u8; d_selected:
- * references x pixels int8; d_cost: instances x level-0 volume. */
+ * references x pixels int8; d_cost: instances x level-0 volume.  d_staged and d_cost are 16-byte
+ * aligned, d_staged 32-byte aligned when d_images is given (one 256-bit load per entry). */
 SSG_API int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_count, const ssg_camera* cameras,
                                  int references, const int* reference_cameras, const float* relative_poses,
                                  const float* d_staged, const float* d_images, const int32_t* d_plane_flags,

@@ -271,10 +271,21 @@ __device__ __forceinline__ void sample_pair_floats(const float* __restrict__ flo
 // 16-bit weights (floor(w * 65535 / 256), within 1 of w * 65535 / 256): the result is again in
 // units of 1/65535, below the exact low-byte blend by less than 4 * 255 units (0.016 of a grey
 // level), on top of the high bytes' rounding above.
+// One 32-byte footprint entry in one 256-bit load (sm_100 and later; `p` 32-byte aligned, which
+// the entry points check for the staged planes of float inputs)
+__device__ __forceinline__ void load_entry32(const uint4* p, uint4& q, uint4& r)
+{
+    unsigned long long a, b, c, d;
+    asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+    q = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
+    r = make_uint4((uint32_t)c, (uint32_t)(c >> 32), (uint32_t)d, (uint32_t)(d >> 32));
+}
+
 template <bool kFixed, int kStride>
 __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entries, int cols, int rows, float2 ix,
                                                   float2 iy, uint32_t (&s)[2][3])
 {
+    static_assert(!kFixed || kStride == 2, "fixed-point codes are staged in 32-byte entries");
     float2 x0, y0, wa, wb, wc, wd;
     bilinear_pair(cols, rows, ix, iy, x0, y0, wa, wb, wc, wd);
     const float2 scale = splat(65535.0f), magic = splat(12582912.0f);
@@ -288,13 +299,14 @@ __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entr
         const uint32_t top = __byte_perm(__float_as_uint(h ? qa.y : qa.x), __float_as_uint(h ? qb.y : qb.x), 0x5410);
         const uint32_t bot = __byte_perm(__float_as_uint(h ? qc.y : qc.x), __float_as_uint(h ? qd.y : qd.x), 0x5410);
         const uint32_t idx = __float2uint_rz(h ? e.y : e.x);  // e >= 0: an unsigned offset
-        const uint4 q = __ldg(entries + kStride * idx);
+        uint4 q, r;
+        if constexpr (kFixed) load_entry32(entries + kStride * idx, q, r);  // both halves of the entry
+        else q = __ldg(entries + kStride * idx);
         s[h][0] = __dp2a_hi(bot, q.x, __dp2a_lo(top, q.x, 0u));
         s[h][1] = __dp2a_hi(bot, q.y, __dp2a_lo(top, q.y, 0u));
         s[h][2] = __dp2a_hi(bot, q.z, __dp2a_lo(top, q.z, 0u));
         if constexpr (kFixed) {
-            const uint4 r = __ldg(entries + kStride * idx + 1);  // the entry's second half
-            const uint32_t w8 = __byte_perm(top, bot, 0x7531);   // high bytes of the weights nw, ne, sw, se
+            const uint32_t w8 = __byte_perm(top, bot, 0x7531);  // high bytes of the weights nw, ne, sw, se
             s[h][0] = __dp4a(w8, q.w, s[h][0]);
             s[h][1] = __dp4a(w8, r.x, s[h][1]);
             s[h][2] = __dp4a(w8, r.y, s[h][2]);
@@ -731,6 +743,8 @@ extern "C" int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_c
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count %d outside [1, %d]",
                 candidate_count, SSG_MAX_CANDIDATES);
     SSG_REQUIRE(((uintptr_t)d_staged & 15) == 0 && ((uintptr_t)d_cost & 15) == 0, "buffers must be 16-byte aligned");
+    SSG_REQUIRE(!d_images || ((uintptr_t)d_staged & 31) == 0,
+                "the staged planes of float images (32-byte entries) must be 32-byte aligned");
     if (int e = check_storage(storage)) return e;
     FastSweepParams p{};
     p.cols = cols;

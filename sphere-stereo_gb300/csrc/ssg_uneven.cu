@@ -70,6 +70,8 @@ static int check_instance(const ssg_uneven_instance& in, int i)
                     in.d_df_costs && in.d_distance_raw && in.d_distance,
                 "instance %d: null device pointer", i);
     SSG_REQUIRE(((uintptr_t)in.d_staged & 15) == 0, "instance %d: staged planes must be 16-byte aligned", i);
+    SSG_REQUIRE(!in.d_images || ((uintptr_t)in.d_staged & 31) == 0,
+                "instance %d: the staged planes of float images (32-byte entries) must be 32-byte aligned", i);
     const int L = ssg_isb_level_count(in.cols, in.rows);
     SSG_REQUIRE(L >= 2 && L <= SSG_MAX_LEVELS, "instance %d: a %dx%d image has %d filter levels (2 or more needed)",
                 i, in.cols, in.rows, L);
