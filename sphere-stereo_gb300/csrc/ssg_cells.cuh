@@ -85,6 +85,31 @@ struct Cell<float> {};
 
 __device__ __forceinline__ uint4 ldg16(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
 
+// A float32 cell (32 bytes) in one 256-bit access (sm_100 and later).  The address is 32-byte
+// aligned: every entry point that passes float32 chunked levels checks their base pointers, and
+// cells lie at multiples of 32 bytes from them.
+__device__ __forceinline__ void ldg256(const float* p, float v[8])
+{
+    unsigned long long a, b, c, d;
+    asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+    const unsigned long long w[4] = {a, b, c, d};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v[2 * i] = __uint_as_float((uint32_t)w[i]);
+        v[2 * i + 1] = __uint_as_float((uint32_t)(w[i] >> 32));
+    }
+}
+__device__ __forceinline__ void stg256(float* p, const float v[8])
+{
+    unsigned long long w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        w[i] = (unsigned long long)__float_as_uint(v[2 * i]) |
+               ((unsigned long long)__float_as_uint(v[2 * i + 1]) << 32);
+    asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(w[0]), "l"(w[1]), "l"(w[2]), "l"(w[3])
+                 : "memory");
+}
+
 // 8 consecutive candidates of one cell, any storage type
 template <typename T>
 __device__ __forceinline__ void load8(const T* __restrict__ p, float v[8])
@@ -94,9 +119,7 @@ __device__ __forceinline__ void load8(const T* __restrict__ p, float v[8])
 template <>
 __device__ __forceinline__ void load8<float>(const float* __restrict__ p, float v[8])
 {
-    const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    ldg256(p, v);
 }
 template <typename T>
 __device__ __forceinline__ void store8(T* p, const float v[8])
@@ -106,8 +129,7 @@ __device__ __forceinline__ void store8(T* p, const float v[8])
 template <>
 __device__ __forceinline__ void store8<float>(float* p, const float v[8])
 {
-    reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
-    reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+    stg256(p, v);
 }
 
 // Cells of W candidates: W = 8 for the chunked layout [chunks][pixels][8] of the batched path,

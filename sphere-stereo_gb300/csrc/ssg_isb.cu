@@ -301,16 +301,14 @@ struct RawCell<8, uint16_t> {
 };
 template <>
 struct RawCell<8, float> {
-    float4 a, b;
-    __device__ __forceinline__ void load(const float* cell)
-    {
-        a = __ldg(reinterpret_cast<const float4*>(cell));
-        b = __ldg(reinterpret_cast<const float4*>(cell) + 1);
-    }
+    float c[8];
+    __device__ __forceinline__ void load(const float* cell) { ldg256(cell, c); }
     __device__ __forceinline__ void part(int p, float v[4]) const
     {
-        const float4 q = p == 0 ? a : b;
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+        v[0] = p == 0 ? c[0] : c[4];
+        v[1] = p == 0 ? c[1] : c[5];
+        v[2] = p == 0 ? c[2] : c[6];
+        v[3] = p == 0 ? c[3] : c[7];
     }
 };
 template <>
@@ -839,6 +837,18 @@ SelectOut select_constants(const float* candidates, int ncand, float* distance, 
     return SelectOut{d0, dl, d0 / dl - 1.0f, distance, index, nullptr};
 }
 
+// chunked cost levels are read and written in whole cells: 16-byte cells of 16-bit levels,
+// 32-byte cells (one 256-bit access) of float32 levels
+static int check_aligned(const void* p, int bytes, const char* what)
+{
+    SSG_REQUIRE(((uintptr_t)p & (uintptr_t)(bytes - 1)) == 0, "%s must be %d-byte aligned", what, bytes);
+    return SSG_OK;
+}
+static int check_cells(const void* p, int storage, const char* what)
+{
+    return check_aligned(p, storage == SSG_STORAGE_F32 ? 32 : 16, what);
+}
+
 static int check_levels(int rows_in, int cols_in, int rows_out, int cols_out)
 {
     SSG_REQUIRE(rows_in > 0 && cols_in > 0 && rows_out > 0 && cols_out > 0, "sizes must be positive");
@@ -1053,6 +1063,8 @@ extern "C" int ssg_isb_downsample_batch(const uint8_t* d_guide_in, const void* d
                 "unknown input storage %d", storage);
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    if (int e = check_cells(d_cost_in, storage, "d_cost_in")) return e;
+    if (int e = check_cells(d_cost_out, SSG_STORAGE_F32, "d_cost_out")) return e;
     const int chunks = chunks_of(candidate_count);
     float* out = static_cast<float*>(d_cost_out);
     cudaStream_t st = as_stream(stream);
@@ -1076,6 +1088,8 @@ extern "C" int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_c
     SSG_REQUIRE(storage == SSG_STORAGE_F32, "coarse levels are float32 (storage must be SSG_STORAGE_F32)");
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    if (int e = check_aligned(d_cost_in, 16, "d_cost_in")) return e;  // staged by 16-byte copies
+    if (int e = check_cells(d_cost_inout, SSG_STORAGE_F32, "d_cost_inout")) return e;
     const int chunks = chunks_of(candidate_count);
     return launch_up<8, float, false, G4>(d_guide_in, static_cast<const float*>(d_cost_in), rows_in, cols_in,
                                       d_guide_inout, static_cast<float*>(d_cost_inout), rows_inout, cols_inout, chunks,
@@ -1096,6 +1110,8 @@ extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const vo
                 "unknown fine-level storage %d", storage);
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    if (int e = check_aligned(d_cost_in, 16, "d_cost_in")) return e;  // staged by 16-byte copies
+    if (int e = check_cells(d_cost_fine, storage, "d_cost_fine")) return e;
     const int chunks = chunks_of(candidate_count);
     SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
     so.distance2 = d_distance_copy;
@@ -1124,6 +1140,7 @@ extern "C" int ssg_select_distance_batch(const void* d_cost, int candidate_count
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
     SSG_REQUIRE(storage == SSG_STORAGE_F16 || storage == SSG_STORAGE_UNORM16 || storage == SSG_STORAGE_F32,
                 "unknown storage %d", storage);
+    if (int e = check_cells(d_cost, storage, "d_cost")) return e;
     const SelectOut so = select_constants(candidates, candidate_count, d_distance, d_index);
     const dim3 grid(grid_1d(pixels, kBatchBlock), instances);
     const int chunks = chunks_of(candidate_count);

@@ -75,8 +75,13 @@ static int check_instance(const ssg_uneven_instance& in, int i)
     const int L = ssg_isb_level_count(in.cols, in.rows);
     SSG_REQUIRE(L >= 2 && L <= SSG_MAX_LEVELS, "instance %d: a %dx%d image has %d filter levels (2 or more needed)",
                 i, in.cols, in.rows, L);
-    for (int l = 0; l < L; ++l)
+    for (int l = 0; l < L; ++l) {
         SSG_REQUIRE(in.d_guides[l] && in.d_costs[l] && in.d_df_guides[l], "instance %d: level %d is NULL", i, l);
+        // whole cells: 16 bytes of the 16-bit level 0, 32 bytes (one 256-bit access) of float32 levels
+        const uintptr_t mask = l == 0 ? 15 : 31;
+        SSG_REQUIRE(((uintptr_t)in.d_costs[l] & mask) == 0, "instance %d: cost level %d must be %d-byte aligned", i, l,
+                    (int)mask + 1);
+    }
     for (int l = 1; l < L; ++l) SSG_REQUIRE(in.d_df_costs[l - 1], "instance %d: post-filter level %d is NULL", i, l);
     for (int c = 0; c < in.camera_count; ++c) {
         const ssg_camera& k = in.cameras[c];
