@@ -267,7 +267,8 @@ SSG_API int ssg_merge_panorama(const float* d_lut, const float* d_weights, const
  * samples that plane from the float images).  d_guides frames x references x rows x cols 32-bit
  * guide words (rgb2yCbCr + uint8 cast of each reference camera, python/utils.py:144-155, from the
  * float values).  Zeroes d_plane_flags first (a 4 x frames x cameras byte memset).  Planes of
- * (rows + 2) x (cols + 2) >= 2^24 entries return SSG_ERR_UNSUPPORTED. */
+ * (rows + 2) x (cols + 2) >= 2^24 entries return SSG_ERR_UNSUPPORTED.  d_staged is 16-byte aligned,
+ * 32-byte aligned for float inputs (one 256-bit store per entry); d_guides 4-byte aligned. */
 SSG_API int ssg_stage_images(const float* d_images, int frames, int cameras, int cols, int rows,
                              const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
                              int32_t* d_plane_flags, void* stream);

@@ -406,7 +406,7 @@ __device__ __forceinline__ void fine_setup(const typename GL::Pix (&gd)[9], cons
 template <int F, int W, typename Tf, bool kSelect>
 __device__ __forceinline__ void up_part(const float (&tap)[9][UpTile<W>::E], const FinePixel& px,
                                         const RawCell<W, Tf>& raw, int part, int k0, bool full, int ncand,
-                                        float weight_up, Tf* __restrict__ fine_chunk, Selector& s)
+                                        float weight_up, Tf* __restrict__ fine_chunk, Selector& s, float* kept)
 {
     constexpr int E = UpTile<W>::E;
     float acc[E];
@@ -421,6 +421,10 @@ __device__ __forceinline__ void up_part(const float (&tap)[9][UpTile<W>::E], con
             for (int e = 0; e < E; ++e)
                 if (k0 + e < ncand) s.push(k0 + e, acc[e]);
         }
+    } else if constexpr (W == 8) {
+        // kept for the store of the whole cell after both parts
+#pragma unroll
+        for (int e = 0; e < E; ++e) kept[part * E + e] = acc[e];
     } else {
         store_part<E>(reinterpret_cast<float*>(fine_chunk + (int64_t)px.index * W), part, acc);
     }
@@ -435,6 +439,7 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
 {
     constexpr int E = UpTile<W>::E;
     const bool full = (c + 1) * W <= ncand;
+    float kept_a[W], kept_b[W];  // the non-selecting chunked step's filtered cells
 #pragma unroll
     for (int part = 0; part < UpTile<W>::parts; ++part) {
         float tap[9][E];
@@ -455,8 +460,15 @@ __device__ __forceinline__ void up_chunk(const float* __restrict__ buf, int lx, 
             }
         }
         const int k0 = c * W + part * E;
-        if (kSelect || pa.active) up_part<FA, W, Tf, kSelect>(tap, pa, ra, part, k0, full, ncand, weight_up, fine_chunk, sa);
-        if (kSelect || pb.active) up_part<FB, W, Tf, kSelect>(tap, pb, rb, part, k0, full, ncand, weight_up, fine_chunk, sb);
+        if (kSelect || pa.active)
+            up_part<FA, W, Tf, kSelect>(tap, pa, ra, part, k0, full, ncand, weight_up, fine_chunk, sa, kept_a);
+        if (kSelect || pb.active)
+            up_part<FB, W, Tf, kSelect>(tap, pb, rb, part, k0, full, ncand, weight_up, fine_chunk, sb, kept_b);
+    }
+    if constexpr (!kSelect && W == 8) {
+        // one 256-bit store per fine cell (float32 levels, 32-byte aligned)
+        if (pa.active) stg256(reinterpret_cast<float*>(fine_chunk + (int64_t)pa.index * W), kept_a);
+        if (pb.active) stg256(reinterpret_cast<float*>(fine_chunk + (int64_t)pb.index * W), kept_b);
     }
 }
 

@@ -159,9 +159,13 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
         }
         const int64_t at = (int64_t)j * pitch + i;
         if constexpr (kLowPlane) {
-            // a 32-byte entry: high words x, y, z, low word x | low words y, z
-            out[2 * at] = make_uint4(word[0][0], word[0][1], word[0][2], word[1][0]);
-            out[2 * at + 1] = make_uint4(word[1][1], word[1][2], 0u, 0u);
+            // a 32-byte entry, one 256-bit store: high words x, y, z, low word x | low words y, z
+            const unsigned long long w0 = word[0][0] | (unsigned long long)word[0][1] << 32,
+                                     w1 = word[0][2] | (unsigned long long)word[1][0] << 32,
+                                     w2 = word[1][1] | (unsigned long long)word[1][2] << 32;
+            asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(out + 2 * at), "l"(w0), "l"(w1), "l"(w2),
+                         "l"(0ull)
+                         : "memory");
         } else {
             out[at] = make_uint4(word[0][0], word[0][1], word[0][2], 0u);
         }
@@ -656,6 +660,8 @@ static int stage_images(const Tin* d_images, int frames, int cameras, int cols, 
     if (int e = staged_plane_fits(cols, rows)) return e;
     SSG_REQUIRE(((uintptr_t)d_staged & 15) == 0 && ((uintptr_t)d_guides & 3) == 0,
                 "staged images must be 16-byte and guides 4-byte aligned");
+    SSG_REQUIRE(sizeof(Tin) == 1 || ((uintptr_t)d_staged & 31) == 0,
+                "the staged planes of float images (32-byte entries) must be 32-byte aligned");
     StageParams p{};
     p.cameras = cameras;
     p.references = references;
