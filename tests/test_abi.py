@@ -74,3 +74,41 @@ def test_invalid_arguments_rejected_without_a_device(native, ss):
     assert "alpha" in N.last_error()
     with pytest.raises(ValueError):
         N.call("ssg_rgb_to_guide", None, 10, None, None)
+
+
+def test_misaligned_cells_and_entries_rejected_without_a_device(native, ss):
+    """32-byte units (float32 cost cells, the fixed-point footprint entries of float inputs) move
+    as single 256-bit accesses: every entry point refuses a buffer that is not 32-byte aligned
+    (16 bytes for 16-bit cells) before anything is launched."""
+    N = ss._native
+    A, M = 0x100000, 0x100010  # 32-byte aligned / 16-byte but not 32-byte aligned
+    F16, F32 = 0, 2
+    # downsampling: float32 input cells, then float32 output cells
+    assert native.ssg_isb_downsample_batch(A, M, 64, 64, A, A, 32, 32, 32, 1, F32, 0.1, None) == \
+        N.SSG_ERR_INVALID_ARGUMENT
+    assert "d_cost_in must be 32-byte aligned" in N.last_error()
+    assert native.ssg_isb_downsample_batch(A, M, 64, 64, A, M, 32, 32, 32, 1, F16, 0.1, None) == \
+        N.SSG_ERR_INVALID_ARGUMENT
+    assert "d_cost_out must be 32-byte aligned" in N.last_error()
+    assert native.ssg_isb_downsample_batch(A, A + 8, 64, 64, A, A, 32, 32, 32, 1, F16, 0.1, None) == \
+        N.SSG_ERR_INVALID_ARGUMENT
+    assert "16-byte aligned" in N.last_error()
+    # coarse upsampling: the fine float32 cells are read and written whole
+    assert native.ssg_isb_upsample_batch(A, A, 32, 32, A, M, 64, 64, 32, 1, F32, 0.5, 0.5, 0.1, None) == \
+        N.SSG_ERR_INVALID_ARGUMENT
+    assert "d_cost_inout must be 32-byte aligned" in N.last_error()
+    cand = N.floats([1.0 + k for k in range(32)])
+    assert native.ssg_isb_upsample_select_batch(A, A, 32, 32, A, M, 64, 64, 32, 1, F32, 0.5, 0.5, 0.1, cand, A, A,
+                                                None, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "d_cost_fine must be 32-byte aligned" in N.last_error()
+    assert native.ssg_select_distance_batch(M, 32, 64 * 64, 1, F32, cand, A, A, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "d_cost must be 32-byte aligned" in N.last_error()
+    # staging and sweep of float images: 32-byte footprint entries
+    refs = N.ints([0])
+    assert native.ssg_stage_images(A, 1, 2, 64, 64, refs, 1, M, A, A, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "32-byte aligned" in N.last_error()
+    cams = N.cameras_array([N.ssg_camera(100, 100, 32, 32, -0.2, 0.6)] * 2)
+    poses = N.floats([0.0] * 24)
+    assert native.ssg_sweep_cost_batch(64, 64, 1, 2, cams, 1, refs, poses, M, A, A, A, cand, 32, F16, A, None) == \
+        N.SSG_ERR_INVALID_ARGUMENT
+    assert "32-byte aligned" in N.last_error()
