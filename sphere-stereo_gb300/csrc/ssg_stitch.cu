@@ -706,6 +706,7 @@ static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t*
 struct MergeParams {
     int cols, rows, pano_cols, pano_rows, nref, image_rows, image_cols;
     float ratio_x, ratio_y;
+    int word_rows;  // the images start and end on 4-byte boundaries: texel pairs read as words
     Intr k[SSG_MAX_REFERENCES];
     float t[SSG_MAX_REFERENCES][3];
 };
@@ -739,14 +740,44 @@ __device__ __forceinline__ float interp_f_fast(const float* __restrict__ s, floa
     return fmaf(fv, bot - top, top);
 }
 
+// The six bytes of two horizontally adjacent RGB texels from the aligned 32-bit words that hold
+// them (two words, three when the pair starts at byte 3 of a word): lo = bytes 0..3 of the pair,
+// hi = bytes 4, 5.  Only words holding one of the six bytes are read, so a buffer that starts
+// and ends on 4-byte boundaries is never read outside.
+__device__ __forceinline__ void texel_pair_words(const uint8_t* p, uint32_t& lo, uint32_t& hi)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+    const uint32_t s = (uint32_t)(a & 3) * 8;
+    const uint32_t w0 = __ldg(w), w1 = __ldg(w + 1);
+    const uint32_t w2 = s == 24 ? __ldg(w + 2) : 0u;
+    lo = __funnelshift_r(w0, w1, s);
+    hi = __funnelshift_r(w1, w2, s);
+}
+
+// words: the texel pairs are read with texel_pair_words (same values, fewer loads)
 __device__ __forceinline__ void interp_rgb_fast(const uint8_t* __restrict__ img, float u, float v, int cols,
-                                                float out[3])
+                                                float out[3], bool words = false)
 {
     const float u1f = floorf(u), v1f = floorf(v);
     const int u1 = (int)u1f, v1 = (int)v1f;
     const float fu = u - u1f, fv = v - v1f;
     const uint8_t* p1 = img + 3 * ((int64_t)v1 * cols + u1);
     const uint8_t* p2 = p1 + 3 * (int64_t)cols;
+    if (words) {
+        uint32_t t0, t1, b0, b1;
+        texel_pair_words(p1, t0, t1);
+        texel_pair_words(p2, b0, b1);
+        const uint32_t tr = __byte_perm(t0, t1, 0x0543), br = __byte_perm(b0, b1, 0x0543);  // right texels
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const float a = (float)((t0 >> (8 * ch)) & 0xFFu), b = (float)((tr >> (8 * ch)) & 0xFFu);
+            const float c = (float)((b0 >> (8 * ch)) & 0xFFu), d = (float)((br >> (8 * ch)) & 0xFFu);
+            const float top = fmaf(fu, b - a, a), bot = fmaf(fu, d - c, c);
+            out[ch] = fmaf(fv, bot - top, top);
+        }
+        return;
+    }
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
         const float a = p1[ch], b = p1[3 + ch], c = p2[ch], d = p2[3 + ch];
@@ -894,7 +925,7 @@ __global__ void __launch_bounds__(kStitchBlock) merge_frames_kernel(const __grid
                 project_fast(pt, p.k[r], o);
                 o[0] = fminf(fmaxf(fmul(o[0], p.ratio_x), 0.1f), colsm);
                 o[1] = fadd(fminf(fmaxf(fmul(o[1], p.ratio_y), 0.1f), rowsm), (float)(r * p.image_rows));
-                interp_rgb_fast(images + f * image_frame, o[0], o[1], p.image_cols, c);
+                interp_rgb_fast(images + f * image_frame, o[0], o[1], p.image_cols, c, p.word_rows != 0);
 #pragma unroll
                 for (int ch = 0; ch < 3; ++ch) rgb[f][ch] = fmaf(c[ch], w, rgb[f][ch]);
             }
@@ -1281,6 +1312,8 @@ static int merge_batch(const float* d_lut, const float* d_weights, const float* 
     }
     const int64_t Q = (int64_t)pano_cols * pano_rows;
     dim3 grid(grid_1d(Q, kStitchBlock), frames);
+    const int64_t image_bytes = (int64_t)frames * reference_count * image_rows * image_cols * 3;
+    p.word_rows = ((uintptr_t)d_images & 3) == 0 && (image_bytes & 3) == 0;
     if constexpr (kFast) {
         const int group = tuning(SSG_TUNE_MERGE_FRAMES);
         const dim3 fgrid(grid_1d(Q, kStitchBlock), (frames + group - 1) / group);
