@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(kStitchBlock) merge_uneven_kernel(const Stitch
         project_fast(pt, J.k[r], o);
         o[0] = fminf(fmaxf(fmul(o[0], J.ratio_x), 0.1f), colsm);
         o[1] = fadd(fminf(fmaxf(fmul(o[1], J.ratio_y), 0.1f), rowsm), (float)(r * J.image_rows));
-        interp_rgb_fast(J.images, o[0], o[1], J.image_cols, c);
+        interp_rgb_fast(J.images, o[0], o[1], J.image_cols, c, J.word_rows != 0);
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) rgb[ch] = fmaf(c[ch], w, rgb[ch]);
     }

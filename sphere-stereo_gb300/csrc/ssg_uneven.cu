@@ -329,6 +329,8 @@ extern "C" int ssg_uneven_create(const ssg_uneven_instance* instances, int insta
         s.lut = reinterpret_cast<const float2*>(in.d_lut);
         s.weights = in.d_weights;
         s.images = in.d_images;
+        s.word_rows = ((uintptr_t)in.d_images & 3) == 0 &&
+                      (((int64_t)in.references * in.image_rows * in.image_cols * 3) & 3) == 0;
         s.pano_distance = in.d_pano_distance;
         s.rgb = in.d_rgb;
         for (int r = 0; r < in.references; ++r) {

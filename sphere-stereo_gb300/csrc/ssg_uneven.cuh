@@ -48,7 +48,8 @@ struct StitchJob {
     int cols, rows, references, pano_cols, pano_rows, image_cols, image_rows;
     int map_begin;        // flat index of the job's first map pixel in the concatenated maps
     float ratio_x, ratio_y;
-    float pad0, pad1;
+    int word_rows;  // `images` starts and ends on 4-byte boundaries: texel pairs read as words
+    int pad1;
     const float* distance;      // references x rows x cols, filtered distance maps
     float* reprojected;         // references x rows x cols, in the concatenated maps
     const uint8_t* tables;      // references x rows x cols x 2 inpainting tables
