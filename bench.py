@@ -37,6 +37,9 @@ WORKLOAD_NAME = ("4 double-sphere fisheye cameras (fx=0.28W, xi=-0.2, alpha=0.6)
                  "1216x1216 uint8 inputs, matching 1024x1024, 32 candidates, references 2,3, "
                  "rgb_to_stitch 1216x1216, panorama 2048x1024, sigma_i 10, sigma_s 25")
 METRIC = "RGB-D panoramas/s @1024² match, 32 cand"
+DTYPE = {storage: (f"{storage} level-0 cost storage, f32 coarse levels and arithmetic; the sweep samples the "
+                   "resized images in 8.8 fixed point with 16-bit bilinear weights (integer dot products)")
+         for storage in ("fp16", "unorm16")}
 UNIT = "panoramas/s"
 DATA = ("synthetic: seeded 6x5x3 m box room + 20 value-noise spheres, ray-cast per frame (seed 2000+frame) to "
         "1216x1216 uint8 per camera; images to match = those resized to the matching resolution in float32 "
@@ -70,17 +73,36 @@ def render_pool(count: int, rank: int, world: int, resize):
     w = WORKLOAD["width_in"]
     if tuple(WORKLOAD["stitch"]) != (w, w):
         raise ValueError("the workload stitches at its input resolution")
+    ids = frames_for_rank(max(1, count), rank, world)
+    # the ray casting is numpy on the host: frames render in parallel worker processes (spawned,
+    # so that no CUDA state is inherited)
+    import concurrent.futures
+    import multiprocessing
+
+    workers = max(1, min(len(ids), (os.cpu_count() or 1) // 2))
+    if workers > 1:
+        with concurrent.futures.ProcessPoolExecutor(workers, mp_context=multiprocessing.get_context("spawn")) as pool:
+            renders = list(pool.map(render_frame, ids))
+    else:
+        renders = [render_frame(f) for f in ids]
     frames = []
-    for f in frames_for_rank(max(1, count), rank, world):
-        rng = np.random.Generator(np.random.PCG64(syn.frame_seed(2, f)))
-        scene = syn.random_scene(rng)
-        fr = syn.render_frame(scene, cams, (w, w), (w, w), [])
-        originals = np.stack(fr.images_to_match)  # uint8 [cameras, w, w, 3]
+    for originals, inv in renders:
         match = resize(originals, WORKLOAD["matching"])
-        fr = syn.Frame(list(match), [originals[r] for r in WORKLOAD["refs"]], fr.inv_distance)
+        fr = syn.Frame(list(match), [originals[r] for r in WORKLOAD["refs"]], inv)
         fr.originals = originals
         frames.append(fr)
     return syn.basalt_calibration(cams), frames
+
+
+def render_frame(f: int):
+    """Frame f of the workload: every camera ray-cast to width_in x width_in uint8 (seed
+    synthetic.frame_seed(2, f)); returns (uint8 [cameras, w, w, 3], ground-truth inverse distances)."""
+    syn = importlib.import_module(PACKAGE + ".synthetic")
+    w = WORKLOAD["width_in"]
+    cams = syn.square_rig(w)
+    rng = np.random.Generator(np.random.PCG64(syn.frame_seed(2, f)))
+    fr = syn.render_frame(syn.random_scene(rng), cams, (w, w), (w, w), [])
+    return np.stack(fr.images_to_match), fr.inv_distance
 
 
 def gpu_resize(device):
@@ -116,7 +138,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -209,15 +231,42 @@ class LaunchRecorder:
         return sum(a.elapsed_time(b) for a, b in self.events) / len(self.events)
 
 
-def sweep_bytes_per_launch(cols: int, rows: int, cameras: int, candidates: int, cost_bytes: int,
-                           staged_planes: int = 0) -> int:
-    """Algorithmic bytes of the sweep for one (frame, reference) instance: the reference image
-    and the camera-selection map read once, each source image read at most once (upper bound),
-    the cost volume written once.  Staged images are read as 16-byte footprints per plane (one
-    plane for 8-bit inputs, two for 8.8 fixed point); float images as 12-byte texels."""
+def level_pixels(cols: int, rows: int) -> list[int]:
+    """Pixels of each ISB level (python/isb_filter.py:59-69): L = int(min(log2 cols, log2 rows) - 1)
+    levels of ceil(rows / 2^l) x ceil(cols / 2^l)."""
+    import math
+
+    L = int(min(math.log2(cols), math.log2(rows)) - 1)
+    return [-(-rows // 2 ** l) * -(-cols // 2 ** l) for l in range(L)]
+
+
+def sweep_bytes_per_instance(cols: int, rows: int, cameras: int, references: int, candidates: int,
+                             cost_bytes: int) -> int:
+    """Algorithmic bytes of the sweep for one (frame, reference) instance, by the byte model of the
+    hot path: each float32 image to match read once per frame (12 B per pixel and camera, shared
+    by the frame's references), the camera-selection map (1 B per pixel) and the cost volume
+    written once (cost_bytes x candidates per pixel).  89 B per pixel at 1024^2, 4 cameras, 2
+    references, 32 fp16 candidates."""
     P = cols * rows
-    texel = 16 * staged_planes if staged_planes else 12
-    return texel * P + texel * P * (cameras - 1) + P + cost_bytes * candidates * P
+    return (12 * cameras * P) // references + P + cost_bytes * candidates * P
+
+
+def frame_bytes(cols: int, rows: int, cameras: int, references: int, candidates: int, cost_bytes: int,
+                stitch_pixels: int, panorama_pixels: int) -> int:
+    """Algorithmic bytes of one RGB-D panorama, by the same model: float32 inputs read once; per
+    reference the cost volume (sweep write, level-0 read by the downsampling, the last upsampling
+    read fused with the selection: 3 P; coarse levels written, read and read-modify-written:
+    4 sum(P_l)), two guide pyramids of 3 bytes per pixel, the distance post-filter's float32
+    pyramid, the distance map; the stitch (16 B per matching pixel and reference, float32 blend
+    weights per panorama pixel and reference, 7 B of outputs per panorama pixel).  781 P at
+    1024^2 / 32 fp16 candidates / 1216^2 stitch / 2048 x 1024 panorama."""
+    levels = level_pixels(cols, rows)
+    P, coarse = levels[0], sum(levels[1:])
+    b_in = 12 * cameras * P + 12 * references * stitch_pixels
+    per_ref = (cost_bytes * candidates * (3 * P + 4 * coarse) + 2 * 3 * (2 * P + 4 * coarse) +
+               4 * (3 * P + 4 * coarse) + 4 * P)
+    b_stitch = 16 * P * references + 4 * references * panorama_pixels + 7 * panorama_pixels
+    return b_in + references * per_ref + b_stitch
 
 
 def _estimator(ss, calibration, device, storage, batch, graphs, tuner=None):
@@ -354,14 +403,17 @@ def run_ours(args, rank, world, device, rendered):
         rec.active = False
     peak, peak_kind = measured_peaks()
     sweep_ms = rec.mean_ms()
-    # the images to match are resized, fractional: two staged planes (8.8 fixed point) per camera
-    sweep_bytes = B * len(WORKLOAD["refs"]) * sweep_bytes_per_launch(mw, mh, 4, WORKLOAD["candidates"], 2,
-                                                                      staged_planes=2)
+    R = len(WORKLOAD["refs"])
+    cost_bytes = 2 if args.storage in ("fp16", "unorm16") else 4
+    instances = B * R
+    sweep_bytes = instances * sweep_bytes_per_instance(mw, mh, 4, R, WORKLOAD["candidates"], cost_bytes)
     achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9 if sweep_ms else None
-    instances = B * len(WORKLOAD["refs"])
     traffic = (SWEEP_DRAM_BYTES_PER_INSTANCE * instances
-               if SWEEP_DRAM_BYTES_PER_INSTANCE is not None and args.storage == "fp16" and args.workload == "prototype"
-               else None)
+               if SWEEP_DRAM_BYTES_PER_INSTANCE is not None and args.storage == "fp16" else None)
+    sw, sh = WORKLOAD["stitch"]
+    pw, ph = WORKLOAD["panorama"]
+    per_frame = frame_bytes(mw, mh, 4, R, WORKLOAD["candidates"], cost_bytes, sw * sh, pw * ph)
+    frame_gbs = per_frame * B / (ms * 1e-3) / 1e9
 
     # the same batches from the 8-bit renders themselves: their upload, the resize to the matching
     # resolution on the GPU (ssg_resize_linear, input preparation) and the references' renders
@@ -438,8 +490,18 @@ def run_ours(args, rank, world, device, rendered):
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
                                        "batch, profiles/sweep_batch_kernel_1024_n32.md",
-                     "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms,
-                     "launches_timed": len(rec.events)},
+                     "algorithmic_bytes_per_launch": sweep_bytes,
+                     "algorithmic_bytes_model": "per instance: 12 B x cameras / references (float32 images to "
+                                                "match, once per frame) + 1 B selection + cost_bytes x candidates "
+                                                "per pixel",
+                     "traffic_over_algorithmic": (traffic / sweep_bytes) if traffic else None,
+                     "dram_gbs": (traffic / (sweep_ms * 1e-3) / 1e9) if traffic and sweep_ms else None,
+                     "mean_launch_ms": sweep_ms, "launches_timed": len(rec.events),
+                     "frame": {"algorithmic_bytes_per_frame": per_frame, "achieved": frame_gbs,
+                               "frac": frame_gbs / peak, "unit": "GB/s",
+                               "model": "float32 inputs once, per reference the cost pyramid (3 P + 4 sum P_l "
+                                        "cells), two guide pyramids, the distance post-filter and map, the "
+                                        "stitch tables and outputs"}},
         "e2e_u8": e2e_u8,
         "tuned": pipe.tuned if pipe.tuned is not None else {k: autotune.get(k) for k in pipe.TUNED_KNOBS},
         "overlap_groups": pipe._group_count(B),
@@ -470,12 +532,12 @@ def run_plain_fp32(args, device, rendered, frames_timed: int):
             "mode": "fp32 cost volume, one frame per estimate_RGBD_panorama call, eager launches"}
 
 
-def run_reference_as_written_gpu(args, device, rendered, frames_timed: int):
-    """The reference's per-frame algorithm as it is written (python/depth_estimation.py:137-242),
-    on the same GPU: torch sweep over materialised [N, H, W, 3] point volumes and a 5-D
-    grid_sample per camera, torch selection (min / max / gather / parabola), the ISB filter and the
-    stitcher through the package's fp32 entry points (the reference's CUDA kernels' arithmetic).
-    The reference itself cannot run here (it needs CuPy); this restates its torch part."""
+def run_torch_sweep_gpu(args, device, rendered, frames_timed: int):
+    """The reference's torch part restated on the same GPU (python/depth_estimation.py:137-242):
+    the sweep over materialised [N, H, W, 3] point volumes with a 5-D grid_sample per camera and
+    the torch selection (min / max / gather / parabola); the ISB filter and the stitcher are this
+    library's fp32 kernels (the reference's kernels need CuPy, which is not on the GPU host).  An
+    informational leg: the target ratio is against the plain fp32 path."""
     import torch
 
     ss = importlib.import_module(PACKAGE)
@@ -540,8 +602,8 @@ def run_reference_as_written_gpu(args, device, rendered, frames_timed: int):
         torch.cuda.synchronize()
     ms = start.elapsed_time(end) / frames_timed
     return {"value": 1000.0 / ms, "unit": UNIT, "ms_per_frame": ms, "frames": frames_timed,
-            "mode": "the reference's torch sweep and selection (materialised volumes, grid_sample) with its ISB "
-                    "and stitcher kernels' arithmetic, one frame per call, fp32"}
+            "mode": "the reference's torch sweep and selection restated (materialised volumes, grid_sample), "
+                    "this library's fp32 ISB filter and stitcher kernels, one frame per call"}
 
 
 def cpu_baseline(frames_calib, sample_frames: int):
@@ -759,7 +821,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--batch", type=int, default=8, help="frames per step (one batch)")
     ap.add_argument("--storage", choices=["fp16", "unorm16"], default="fp16")
-    ap.add_argument("--unique-frames", type=int, default=2, help="distinct rendered frames batches are built from")
+    ap.add_argument("--unique-frames", type=int, default=8, help="distinct rendered frames batches are built from")
     ap.add_argument("--cpu-frames", type=int, default=8, help="frames timed for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-u8", action="store_true", help="skip the uint8-input end-to-end leg")
@@ -770,7 +832,7 @@ def main():
     ap.add_argument("--jobs", type=int, default=128, help="jobs of the uneven workload")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
     ap.add_argument("--no-reference-gpu", action="store_true",
-                    help="skip the leg that runs the reference's torch algorithm as written on the GPU")
+                    help="skip the leg that runs the reference's torch sweep, restated, on the GPU")
     ap.add_argument("--knob", action="append", default=[], metavar="NAME=VALUE",
                     help="fix a launch-shape knob (with --no-autotune; autotune.KNOBS names)")
     ap.add_argument("--overlap-groups", type=int, default=None,
@@ -824,14 +886,14 @@ def main():
         plain["batched_over_plain"] = ours["value"] / (world * plain["value"])
     written = None
     if args.plain_frames > 0 and not args.no_reference_gpu:
-        written = run_reference_as_written_gpu(args, device, rendered, max(2, args.plain_frames // 4))
+        written = run_torch_sweep_gpu(args, device, rendered, max(2, args.plain_frames // 4))
         written["batched_over_it"] = ours["value"] / (world * written["value"])
     base = None
     if not args.no_cpu_baseline:
         base = cpu_baseline((rendered[0], rendered[1][:1]), args.cpu_frames)
     line = {"metric": METRIC, "value": ours["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ours["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": f"{args.storage} storage, f32 arithmetic", "data": DATA,
+            "vs_baseline": None, "dtype": DTYPE[args.storage], "data": DATA,
             "config": {"workload": WORKLOAD_NAME, "batch_frames": args.batch,
                        "mode": f"batched, {args.storage} cost volume, fp32 arithmetic, CUDA-graph replay",
                        "tuned": ours["tuned"], "overlap_groups": ours["overlap_groups"],
@@ -842,7 +904,7 @@ def main():
                              f"({args.batch} x {(4 * 1024 * 1024 + len(WORKLOAD['refs']) * 1216 * 1216) * 12 / 1e6:.0f} MB), "
                              "alternating between two batches; both far exceed the 126 MB L2"},
             "e2e": ours["e2e"], "e2e_u8": ours["e2e_u8"], "plain_fp32_gpu": plain,
-            "reference_algorithm_gpu": written,
+            "torch_sweep_gpu": written,
             "gpu_launches": ours["gpu_launches"], "clocks": ours["clocks"],
             "roofline": ours["roofline"], "cpu_baseline": base}
     print(json.dumps(line))

@@ -82,14 +82,21 @@ typedef struct {
 #define SSG_TUNE_ISB_SELECT_BLOCKS 5  /* the same for the last level fused with the selection: 2, 3 */
 #define SSG_TUNE_ISB_TILE_TMA 6       /* coarse tiles of the chunked ISB upsampling staged by TMA (1) or by
                                          cp.async (0) */
+#define SSG_TUNE_TMA_WITHHOLD 7       /* tests of the bounded TMA wait: 1 = the TMA-staged upsampling arms
+                                         its tile barriers but issues no copy, so every block's first
+                                         wait runs out (after a short limit), it writes nothing and
+                                         ssg_take_device_status reports SSG_STATUS_TMA_TIMEOUT; 0 = off */
 SSG_API int ssg_tuning_set(int knob, int value);
 /* The knob's current value (-1 for an unknown knob). */
 SSG_API int ssg_tuning_get(int knob);
 /* Writes up to `capacity` allowed values of a knob; returns how many it has (0 if unknown). */
 SSG_API int ssg_tuning_choices(int knob, int32_t* values, int capacity);
 
-/* Reads and clears the device status word of the ISB kernels: bit 0 is set when a bounded wait
- * for a TMA tile ran out (the kernel skipped that work; results are then invalid).  Synchronous. */
+/* Reads and clears the device status word of the ISB kernels: SSG_STATUS_TMA_TIMEOUT is set when
+ * a bounded wait for a TMA tile ran out.  The block that waited then wrote nothing more (no later
+ * chunk, no selection), so the outputs of that launch are incomplete.  The word stays set until
+ * this call clears it.  Synchronous. */
+#define SSG_STATUS_TMA_TIMEOUT 1u
 SSG_API int ssg_take_device_status(uint32_t* status);
 
 /* Message of the calling thread's last failed call ("" if none). */

@@ -51,7 +51,13 @@ def _fixed(f: np.ndarray) -> np.ndarray:
 
 
 def resize_linear(img: np.ndarray, size, out_dtype=np.float32) -> np.ndarray:
-    """img: [rows, cols, channels] uint8 or float32; size (cols, rows)."""
+    """img: [rows, cols, channels] uint8 or float32; size (cols, rows).  The result is C-contiguous
+    (row-major, like cv2.resize's): the fancy indexing below yields a transposed layout, which
+    torch.tensor would keep, and the reference hands its tensors' raw memory to its kernels."""
+    return np.ascontiguousarray(_resize_linear(img, size, out_dtype))
+
+
+def _resize_linear(img: np.ndarray, size, out_dtype=np.float32) -> np.ndarray:
     src = np.asarray(img)
     rows_in, cols_in = src.shape[:2]
     cols, rows = int(size[0]), int(size[1])

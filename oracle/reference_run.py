@@ -25,7 +25,15 @@ import types
 import numpy as np
 import torch
 
-DEFAULT_REFERENCE = "/root/reference"
+REFERENCE_ENV = "SPHERE_STEREO_REFERENCE"
+
+
+def reference_root() -> str:
+    """The reference checkout named by $SPHERE_STEREO_REFERENCE (a directory holding python/)."""
+    root = os.environ.get(REFERENCE_ENV)
+    if not root or not os.path.isdir(os.path.join(root, "python")):
+        raise RuntimeError(f"set {REFERENCE_ENV} to a checkout of the reference (a directory with python/*.py)")
+    return root
 
 
 @contextlib.contextmanager
@@ -38,7 +46,7 @@ def _cwd(path):
         os.chdir(old)
 
 
-def import_reference(reference_root: str = DEFAULT_REFERENCE):
+def import_reference(reference_root: str):
     """Import the reference modules; returns a namespace with utils, isb_filter, stitcher,
     depth_estimation.  The kernel sources are read relative to the reference root."""
     here = os.path.dirname(os.path.abspath(__file__))
@@ -142,7 +150,7 @@ def run_pipeline(ref, calibration: dict, images_to_match, images_to_stitch, mask
     return out
 
 
-def build_reference_libraries(reference_root: str = DEFAULT_REFERENCE, candidate_counts=(1, 3, 8, 32)) -> None:
+def build_reference_libraries(reference_root: str, candidate_counts=(1, 3, 8, 32)) -> None:
     """Compile the reference's kernels for the host into oracle/_ref (cached by content hash):
     the ISB module for each candidate count of the golden vectors, and the stitcher module of
     the small golden configuration.  The reference's own classes assemble the sources

@@ -30,6 +30,8 @@ TUNE_UNEVEN_SPAN = 3
 TUNE_ISB_UP_BLOCKS = 4
 TUNE_ISB_SELECT_BLOCKS = 5
 TUNE_ISB_TILE_TMA = 6
+TUNE_TMA_WITHHOLD = 7
+STATUS_TMA_TIMEOUT = 1
 ISB_SKIP_FINE_GUIDE = 1
 PIXEL_U8 = 0
 PIXEL_F32 = 1

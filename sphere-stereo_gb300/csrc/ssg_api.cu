@@ -76,6 +76,7 @@ Knob g_knobs[] = {
     {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_UP_BLOCKS
     {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_SELECT_BLOCKS
     {kOnOff, 2, {0}},              // SSG_TUNE_ISB_TILE_TMA
+    {kOnOff, 2, {0}},              // SSG_TUNE_TMA_WITHHOLD
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

@@ -37,6 +37,14 @@ __global__ void range_table_kernel(float* __restrict__ table, float var_inv_i)
         table[d] = d < kRangeLutSize ? range_weight((float)d, var_inv_i) : 0.0f;
 }
 
+cudaError_t clear_tma_abort(cudaStream_t st)
+{
+    void* word = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&word, g_tma_abort);
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync(word, 0, sizeof(uint32_t), st);
+}
+
 bool encode_tensor_map(CUtensorMap* map, const void* base, int rank, const uint64_t* dims, const uint64_t* strides,
                        const uint32_t* box)
 {
@@ -241,12 +249,26 @@ __device__ __forceinline__ void load_tile_async(float* __restrict__ buf, const f
 // issued by thread 0 on `bar`.  The box starts at column x0 - 1 and row y - 1, possibly outside
 // the level: those cells arrive as zeros and tma_clamp_edges replaces them afterwards.
 // c3: the chunk's plane (instance * chunks + chunk) of the level's tensor map.
-__device__ __forceinline__ void load_tile_tma(float* __restrict__ buf, const CUtensorMap* map, int x0, int y, int c3,
-                                              uint64_t* bar)
+// withhold: the barrier is armed but no copy is issued, so that its wait runs out (the tests of
+// the timeout path; SSG_TUNE_TMA_WITHHOLD).  Returns whether copies were issued.
+__device__ __forceinline__ bool load_tile_tma(float* __restrict__ buf, const CUtensorMap* map, int x0, int y, int c3,
+                                              uint64_t* bar, bool withhold = false)
 {
     mbar_arrive_expect_tx(bar, 2 * UpTile<8>::part_bytes);
+    if (withhold) return false;
 #pragma unroll
     for (int part = 0; part < 2; ++part) tma_load_4d(buf + part * UpTile<8>::part_floats, map, 4 * part, x0 - 1, y - 1, c3, bar);
+    return true;
+}
+
+// A block whose tile wait ran out: thread 0 waits (bounded, without the early-out) for the copies
+// it issued that have not been seen to land, for chunk c (buffer c & 1) and chunk c + 1, so that
+// no copy writes the block's shared memory after it exits.
+__device__ __forceinline__ void tma_drain(uint64_t* bar, uint32_t in_flight, int c)
+{
+#pragma unroll
+    for (int k = c; k <= c + 1; ++k)
+        if (in_flight & (1u << (k & 1))) mbar_wait(&bar[k & 1], (uint32_t)(k >> 1) & 1u, kTmaMaxPolls, false);
 }
 
 // Edge clamping of a TMA tile: cells whose column or row lies outside the level take the value of
@@ -493,7 +515,7 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
                                              uint8_t* __restrict__ guide_io, Tf* __restrict__ cost_fine,
                                              const LevelGeom& g, int chunks, int ncand, float weight_up,
                                              float weight_down, const SelectOut& so, int x0, int y, UpShared<W>& sh,
-                                             const CUtensorMap* tmap = nullptr, int plane0 = 0)
+                                             const CUtensorMap* tmap = nullptr, int plane0 = 0, bool withhold = false)
 {
     static_assert(!kTma || W == 8, "TMA tiles are for the chunked layout");
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
@@ -516,6 +538,7 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
         }
     }
     Selector sa, sb;
+    uint32_t in_flight = 0;  // thread 0, TMA: bit b set while a copy into sh.tile[b] has not been seen to land
     if constexpr (kTma) {
         // the coarse tiles come by TMA (plane0 + c: the chunk's plane of the level's tensor map)
         if (threadIdx.x == 0) {
@@ -524,7 +547,7 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
             mbar_init_fence();
         }
         __syncthreads();
-        if (threadIdx.x == 0) load_tile_tma(sh.tile[0], tmap, x0, y, plane0, &sh.bar[0]);
+        if (threadIdx.x == 0 && load_tile_tma(sh.tile[0], tmap, x0, y, plane0, &sh.bar[0], withhold)) in_flight = 1u;
     } else {
         load_tile_async<W>(sh.tile[0], cost_in, g.rows_in, g.cols_in, x0, y);
         cp_async_commit();
@@ -535,9 +558,9 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
     if (kSelect || pb.active) rb.load(cost_fine + (int64_t)pb.index * W);
     for (int c = 0; c < chunks; ++c) {
         if constexpr (kTma) {
-            if (threadIdx.x == 0 && c + 1 < chunks) {
-                load_tile_tma(sh.tile[(c + 1) & 1], tmap, x0, y, plane0 + c + 1, &sh.bar[(c + 1) & 1]);
-            }
+            if (threadIdx.x == 0 && c + 1 < chunks &&
+                load_tile_tma(sh.tile[(c + 1) & 1], tmap, x0, y, plane0 + c + 1, &sh.bar[(c + 1) & 1], withhold))
+                in_flight |= 1u << ((c + 1) & 1);
         } else {
             if (c + 1 < chunks)
                 load_tile_async<W>(sh.tile[(c + 1) & 1], cost_in + (int64_t)(c + 1) * pin * W, g.rows_in, g.cols_in,
@@ -551,7 +574,15 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
             if (kSelect || pb.active) nb.load(next + (int64_t)pb.index * W);
         }
         if constexpr (kTma) {
-            mbar_wait(&sh.bar[c & 1], (uint32_t)(c >> 1) & 1u);  // this chunk's tile has landed
+            // this chunk's tile has landed, for every thread of the block; else the block stops
+            // here and writes nothing more (the chunks before it are written, the selection not)
+            const bool landed =
+                mbar_wait(&sh.bar[c & 1], (uint32_t)(c >> 1) & 1u, withhold ? kTmaShortPolls : kTmaMaxPolls);
+            if (!__syncthreads_and(landed)) {
+                if (threadIdx.x == 0) tma_drain(sh.bar, in_flight, c);
+                return;
+            }
+            if (threadIdx.x == 0) in_flight &= ~(1u << (c & 1));
             tma_clamp_edges(sh.tile[c & 1], g.rows_in, g.cols_in, x0, y);
         } else {
             cp_async_wait_one();  // this chunk's tile has landed
@@ -681,7 +712,8 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint
                                                             Tf* __restrict__ cost_fine, LevelGeom g, int chunks,
                                                             int ncand, float weight_up, float weight_down,
                                                             float var_inv_i, const float* __restrict__ table,
-                                                            SelectOut so, const __grid_constant__ CUtensorMap tmap)
+                                                            SelectOut so, const __grid_constant__ CUtensorMap tmap,
+                                                            bool withhold)
 {
     __shared__ UpShared<W> sh;
     load_range_lut(sh.lut, table, var_inv_i);
@@ -697,7 +729,8 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_kernel(const uint
                                      cost_in + (int64_t)inst * chunks * pin * W,
                                      guide_io + (int64_t)inst * pio * GL::bytes,
                                      cost_fine + (int64_t)inst * chunks * pio * W, g, chunks, ncand, weight_up,
-                                     weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh, &tmap, inst * chunks);
+                                     weight_down, so, blockIdx.x * kUpTileX, blockIdx.y, sh, &tmap, inst * chunks,
+                                     withhold);
 }
 
 // Selection from an unfiltered level-0 volume (pyramids of fewer than two levels, or the
@@ -914,22 +947,27 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
         const uint32_t box[4] = {4, (uint32_t)kUpTileCols, 3, 1};
         const bool tma = tuning(SSG_TUNE_ISB_TILE_TMA) == 1 && encode_tensor_map(&map, ci, 4, dims, strides, box);
         const bool three = tuning(kSelect ? SSG_TUNE_ISB_SELECT_BLOCKS : SSG_TUNE_ISB_UP_BLOCKS) == 3;
+        const bool withhold = tma && tuning(SSG_TUNE_TMA_WITHHOLD) == 1;
         constexpr bool kG = kGuideDefault<W, kSelect>;
+        if (tma) {
+            const cudaError_t e = clear_tma_abort(st);
+            if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "clearing the TMA abort word: %s", cudaGetErrorString(e));
+        }
         if (tma && three)
             isb_up_kernel<W, Tf, kSelect, GL, 3, kG, true><<<grid, kBatchBlock, 0, st>>>(
-                gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so, map);
+                gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so, map, withhold);
         else if (tma)
             isb_up_kernel<W, Tf, kSelect, GL, 2, kG, true><<<grid, kBatchBlock, 0, st>>>(
-                gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so, map);
+                gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so, map, withhold);
         else if (three)
             isb_up_kernel<W, Tf, kSelect, GL, 3><<<grid, kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu,
-                                                                              wd, var_inv_i, table, so, map);
+                                                                              wd, var_inv_i, table, so, map, false);
         else
             isb_up_kernel<W, Tf, kSelect, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu, wd,
-                                                                           var_inv_i, table, so, map);
+                                                                           var_inv_i, table, so, map, false);
     } else {
         isb_up_kernel<W, Tf, kSelect, GL><<<grid, kBatchBlock, 0, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu, wd,
-                                                                       var_inv_i, table, so, map);
+                                                                       var_inv_i, table, so, map, false);
     }
     return launch_status(kSelect ? "isb_up_kernel<select>" : "isb_up_kernel");
 }

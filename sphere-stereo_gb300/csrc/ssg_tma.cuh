@@ -5,8 +5,11 @@
 // the runtime (no link against the driver library).  Device: one elected thread arms an mbarrier
 // with the expected byte count and issues the copies; every thread waits on the barrier's phase
 // with a bounded number of polls.  A wait that runs out records kTmaTimeout in the translation
-// unit's status word (g_tma_status; ssg_take_device_status reads the ISB kernels' word) and the
-// kernel skips the tile's work.
+// unit's status word (g_tma_status, sticky until ssg_take_device_status reads and clears it) and
+// raises the launch's abort word (g_tma_abort, cleared by the host before every launch that
+// waits on TMA tiles, so it only shortens the waits of the launch that failed).  The block then
+// writes nothing more: it stops issuing copies, waits (again bounded) for the copies it has in
+// flight so that none lands in shared memory after it exits, and returns.
 #pragma once
 
 #include <cuda.h>
@@ -16,10 +19,12 @@
 
 namespace ssg {
 
-constexpr uint32_t kTmaTimeout = 1u;
-constexpr int kTmaMaxPolls = 1 << 20;  // each poll may suspend the thread for a short while
+constexpr uint32_t kTmaTimeout = SSG_STATUS_TMA_TIMEOUT;
+constexpr int kTmaMaxPolls = 1 << 20;   // each poll may suspend the thread for a short while
+constexpr int kTmaShortPolls = 4096;    // the limit while a copy is withheld on purpose (tests)
 
-static __device__ uint32_t g_tma_status;
+static __device__ uint32_t g_tma_status;  // sticky: kTmaTimeout once any wait ran out
+static __device__ uint32_t g_tma_abort;   // nonzero once a wait of the current launch ran out
 
 // Encodes a map of a float32 tensor of `rank` dims (dims[0] innermost, strides in bytes for dims
 // 1..rank-1) read in boxes of `box`; returns false when the driver refuses it.
@@ -61,14 +66,17 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// waits for the barrier phase of parity `parity`; false when the polls ran out (recorded), or at
-// once when an earlier wait of the launch's kernels ran out, so that a broken copy costs one
-// bounded wait per resident block rather than one per tile
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Waits for the barrier phase of parity `parity`, at most `max_polls` polls; false when the polls
+// ran out (recorded in g_tma_status and g_tma_abort).  `early_out`: also false at once when
+// another wait of this launch has run out, so that a broken copy costs one bounded wait per
+// resident block rather than one per tile.  Waits for copies already issued (the drain before a
+// failed block exits) pass early_out = false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_polls = kTmaMaxPolls,
+                                          bool early_out = true)
 {
     const uint32_t a = smem_address(bar);
-    for (int i = 0; i < kTmaMaxPolls; ++i) {
-        if ((i & 1023) == 0 && *reinterpret_cast<volatile uint32_t*>(&g_tma_status) != 0) return false;
+    for (int i = 0; i < max_polls; ++i) {
+        if (early_out && (i & 1023) == 0 && *reinterpret_cast<volatile uint32_t*>(&g_tma_abort) != 0) return false;
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -78,7 +86,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
         if (done) return true;
     }
     atomicOr(&g_tma_status, kTmaTimeout);
+    atomicExch(&g_tma_abort, 1u);
     return false;
 }
+
+// Clears the abort word before a launch that waits on TMA tiles (enqueued on its stream, so a
+// captured graph clears it on every replay).  Launches on other streams share the word: a clear
+// can only lengthen another launch's failed waits, never hide a failure, which g_tma_status keeps.
+cudaError_t clear_tma_abort(cudaStream_t st);
 
 }  // namespace ssg

@@ -19,6 +19,9 @@ the largest batch; outputs alias them, as the reference's outputs alias its stit
 """
 from __future__ import annotations
 
+import ctypes
+import warnings
+
 import torch
 
 from . import _native as N
@@ -255,6 +258,27 @@ class BatchPipeline:
                                ("images_to_stitch", stitch, (frames, self.R, st.image_rows, st.image_cols, 3))):
             N.require(t, name, torch.uint8 if t.dtype == torch.uint8 else torch.float32, shape, self.device)
         self._apply_tuning(match, stitch, frames)
+        tma = N.library().ssg_tuning_get(N.TUNE_ISB_TILE_TMA) == 1
+        self._run(match, stitch, frames)
+        if tma and self._tma_wait_ran_out():
+            # a tile never landed: the launch's outputs are incomplete; stage by cp.async from now on
+            warnings.warn("a bounded wait for a TMA tile of the ISB upsampling ran out; the batch is run again "
+                          "with cp.async staging (SSG_TUNE_ISB_TILE_TMA = 0)", RuntimeWarning, stacklevel=2)
+            N.call("ssg_tuning_set", N.TUNE_ISB_TILE_TMA, 0)
+            if self.tuned is not None:
+                self.tuned["isb_tile_tma"] = 0
+            self._graphs.clear()
+            self._run(match, stitch, frames)
+        return self.rgb[:frames], self.pano_distance[:frames]
+
+    @staticmethod
+    def _tma_wait_ran_out() -> bool:
+        """Reads (and clears) the library's device status word; synchronises the device."""
+        status = ctypes.c_uint32(0)
+        N.call("ssg_take_device_status", ctypes.byref(status))
+        return bool(status.value & N.STATUS_TMA_TIMEOUT)
+
+    def _run(self, match: torch.Tensor, stitch: torch.Tensor, frames: int) -> None:
         if not self.cuda_graphs:
             self._launch(match, stitch, frames, N.stream_of(match))
         else:
@@ -274,7 +298,6 @@ class BatchPipeline:
                     self._graphs.pop(next(iter(self._graphs)))
                 self._graphs[key] = graph
             graph.replay()
-        return self.rgb[:frames], self.pano_distance[:frames]
 
     TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "isb_select_blocks", "isb_tile_tma", "hole_blocks_per_sm",
                    "merge_frames")

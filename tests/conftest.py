@@ -73,6 +73,19 @@ def golden_c1():
 
 
 @pytest.fixture(scope="session")
+def golden_c2():
+    g = load_golden("pipeline_c2.npz")
+    g["inputs"] = json.loads(str(g["inputs"]))
+    return g
+
+
+def sample_lattice(cols: int, rows: int, stride: int) -> np.ndarray:
+    """The pixel sample of the c2 fixture: flat indices of (x, y) with (x + 3 y) mod stride == 0."""
+    y, x = np.divmod(np.arange(cols * rows, dtype=np.int64), cols)
+    return np.nonzero((x + 3 * y) % stride == 0)[0]
+
+
+@pytest.fixture(scope="session")
 def golden_isb():
     return load_golden("isb_cases.npz")
 

@@ -106,3 +106,51 @@ def test_c1_against_reference(oracle_mod, golden_c1):
     assert inverse_distance_mae(d, dref) <= 1e-6 * inv_range
     assert psnr(out["rgb_panorama"], g["ref/rgb_panorama"]) >= 50
     assert inverse_distance_mae(out["distance_panorama"], g["ref/distance_panorama"]) <= 1e-4 * inv_range
+
+
+def test_c2_against_reference(oracle_mod, golden_c2, synthetic):
+    """The benchmarked configuration (1024^2 matching on resized, fractional inputs, 32
+    candidates, sigma_s 25, 1216^2 stitch, 2048 x 1024 panorama): inputs rebuilt from the
+    fixture's seed with the oracle's restatement of the linear resize and checked against its
+    digests; camera selection, candidate indices, distances and panorama against the reference's."""
+    import hashlib
+
+    import prep_eval_oracle
+    from conftest import sample_lattice
+
+    g = golden_c2
+    cfg, inputs = g["config"], g["inputs"]
+    w = inputs["width_in"]
+    cams = synthetic.square_rig(w)
+    rng = np.random.Generator(np.random.PCG64(inputs["seed"]))
+    renders = np.stack(synthetic.render_frame(synthetic.random_scene(rng), cams, (w, w), (w, w), []).images_to_match)
+    assert hashlib.sha256(renders.tobytes()).hexdigest() == inputs["renders_sha256"]
+    match = np.stack([prep_eval_oracle.resize_linear(im, cfg["matching_resolution"]) for im in renders])
+    assert hashlib.sha256(match.tobytes()).hexdigest() == inputs["images_to_match_sha256"]
+    cols, rows = cfg["matching_resolution"]
+    rig = oracle_mod.OracleRig(g["calibration"], masks=[np.ones((rows, cols), np.float32)] * 4, **cfg)
+    # torch's CPU square root (not correctly rounded) flips a handful of near-ties between two
+    # cameras' distances to their image borders: 6 of 2^21 pixels here
+    agree = (np.stack([rig.selected[r] for r in rig.refs]) == g["ref/selected_cameras"]).mean()
+    assert agree >= 0.99999, agree
+    np.testing.assert_array_equal(rig.candidates, g["ref/candidates"])
+    # from here on the reference's own selection and poses, so that the per-frame path is compared
+    rig.set_rig_tables(list(g["ref/selected_cameras"]), list(g["ref/relative_poses"]))
+    out = rig.estimate(list(match), [renders[r].astype(np.float32) for r in cfg["references_indices"]],
+                       keep_intermediates=True)
+    assert (out["index"] == g["ref/index"]).mean() >= 0.9999
+    inv_range = 1 / cfg["min_dist"] - 1 / cfg["max_dist"]
+    stride = int(g["sample_stride"])
+    pix = sample_lattice(cols, rows, stride)
+    pw, ph = cfg["panorama_resolution"]
+    pano = sample_lattice(pw, ph, stride)
+    for key in ("distance_raw", "distance_filtered"):
+        d, dref = out[key].reshape(2, -1)[:, pix], g[f"ref/{key}@sample"]
+        # the sub-candidate parabola divides by a cost curvature that can be small: a one-ulp cost
+        # difference (torch's sqrt) moves a rare pixel by a little more than 1e-5 relative
+        assert (np.abs(d.astype(np.float64) / dref - 1) <= 1e-5).mean() >= 0.9999, key
+        np.testing.assert_allclose(d, dref, rtol=1e-4)
+        assert inverse_distance_mae(d, dref) <= 1e-6 * inv_range
+    assert psnr(out["rgb_panorama"].reshape(-1, 3)[pano], g["ref/rgb_panorama@sample"]) >= 50
+    assert inverse_distance_mae(out["distance_panorama"].reshape(-1)[pano],
+                                g["ref/distance_panorama@sample"]) <= 1e-4 * inv_range
