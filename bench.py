@@ -475,14 +475,19 @@ def run_ours(args, rank, world, device, rendered):
         u8_ms = max_over_ranks(s3.elapsed_time(e3) / args.steps, world, device)
         e2e_u8 = {"value": world * B * 1000.0 / u8_ms, "unit": UNIT, "h2d_bytes_per_step": h2d_u8,
                   "d2h_bytes_per_step": d2h, "ms_per_step": u8_ms,
-                  "inputs": "the 1216x1216 uint8 renders of every camera, resized to the matching resolution on the "
-                            "GPU inside the timed region (ssg_resize_linear); the references' renders stitched as "
-                            "uint8"}
+                  "inputs": "the decoded 1216x1216 uint8 images of every camera (the reference's per-frame input, "
+                            "python/main.py:73-81), resized to the matching resolution on the GPU inside the timed "
+                            "region (utils.resize_linear); the references' images stitched as uint8"}
+    e2e_f32 = {"value": world * B * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+               "inputs": "the float32 images estimate_RGBD_panorama takes (already resized on the host)"}
     return {
         "value": world * B * 1000.0 / ms,
         "ms_per_step": ms,
-        "e2e": {"value": world * B * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        # the headline end-to-end number starts where the reference's frame loop starts: decoded
+        # 8-bit images on the host
+        "e2e": e2e_u8 if e2e_u8 is not None else e2e_f32,
+        "e2e_f32": e2e_f32,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "roofline": {"bound": "hbm", "kernel": "sweep_batch_kernel", "achieved": achieved, "peak": peak,
@@ -502,7 +507,6 @@ def run_ours(args, rank, world, device, rendered):
                                "model": "float32 inputs once, per reference the cost pyramid (3 P + 4 sum P_l "
                                         "cells), two guide pyramids, the distance post-filter and map, the "
                                         "stitch tables and outputs"}},
-        "e2e_u8": e2e_u8,
         "tuned": pipe.tuned if pipe.tuned is not None else {k: autotune.get(k) for k in pipe.TUNED_KNOBS},
         "overlap_groups": pipe._group_count(B),
     }
@@ -903,7 +907,7 @@ def main():
                        "l2": f"each step reads a {args.batch}-frame batch of inputs "
                              f"({args.batch} x {(4 * 1024 * 1024 + len(WORKLOAD['refs']) * 1216 * 1216) * 12 / 1e6:.0f} MB), "
                              "alternating between two batches; both far exceed the 126 MB L2"},
-            "e2e": ours["e2e"], "e2e_u8": ours["e2e_u8"], "plain_fp32_gpu": plain,
+            "e2e": ours["e2e"], "e2e_f32": ours["e2e_f32"], "plain_fp32_gpu": plain,
             "torch_sweep_gpu": written,
             "gpu_launches": ours["gpu_launches"], "clocks": ours["clocks"],
             "roofline": ours["roofline"], "cpu_baseline": base}

@@ -37,12 +37,14 @@ __global__ void range_table_kernel(float* __restrict__ table, float var_inv_i)
         table[d] = d < kRangeLutSize ? range_weight((float)d, var_inv_i) : 0.0f;
 }
 
+// a one-thread launch rather than a memset of the symbol: no host-side symbol lookup, which is
+// not allowed while the stream is being captured into a graph
+__global__ void clear_tma_abort_kernel() { g_tma_abort = 0u; }
+
 cudaError_t clear_tma_abort(cudaStream_t st)
 {
-    void* word = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&word, g_tma_abort);
-    if (e != cudaSuccess) return e;
-    return cudaMemsetAsync(word, 0, sizeof(uint32_t), st);
+    clear_tma_abort_kernel<<<1, 1, 0, st>>>();
+    return cudaGetLastError();
 }
 
 bool encode_tensor_map(CUtensorMap* map, const void* base, int rank, const uint64_t* dims, const uint64_t* strides,

@@ -90,8 +90,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int ma
     return false;
 }
 
-// Clears the abort word before a launch that waits on TMA tiles (enqueued on its stream, so a
-// captured graph clears it on every replay).  Launches on other streams share the word: a clear
+// Clears the abort word before a launch that waits on TMA tiles (a one-thread kernel enqueued on
+// its stream, so a captured graph clears it on every replay).  Launches on other streams share the word: a clear
 // can only lengthen another launch's failed waits, never hide a failure, which g_tma_status keeps.
 cudaError_t clear_tma_abort(cudaStream_t st);
 

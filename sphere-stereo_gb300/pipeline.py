@@ -20,6 +20,7 @@ the largest batch; outputs alias them, as the reference's outputs alias its stit
 from __future__ import annotations
 
 import ctypes
+import gc
 import warnings
 
 import torch
@@ -287,6 +288,9 @@ class BatchPipeline:
             if graph is None:
                 # one eager run (first-use set-up such as shared-memory opt-in happens outside capture)
                 self._launch(match, stitch, frames, N.stream_of(match))
+                # objects that are already garbage (an earlier graph, say) are freed now: a graph
+                # destroyed while this capture runs would invalidate it
+                gc.collect()
                 graph = torch.cuda.CUDAGraph()
                 side = torch.cuda.Stream(self.device)
                 side.wait_stream(torch.cuda.current_stream(self.device))

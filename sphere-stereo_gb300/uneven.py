@@ -16,6 +16,7 @@ through ``run``), so the whole sequence is captured once in a CUDA graph and rep
 from __future__ import annotations
 
 import ctypes
+import gc
 
 import torch
 
@@ -215,6 +216,9 @@ class UnevenBatch:
         else:
             if self._graph is None:
                 self._launch(stream.cuda_stream)  # first use outside the capture
+                # objects that are already garbage (an earlier graph, say) are freed now: a graph
+                # destroyed while this capture runs would invalidate it
+                gc.collect()
                 graph = torch.cuda.CUDAGraph()
                 side = torch.cuda.Stream(self.device)
                 side.wait_stream(stream)

@@ -23,6 +23,23 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU and the built sm_103a library")
 
 
+@pytest.fixture(autouse=True)
+def _restore_tuning_knobs(request):
+    """The library's launch-shape knobs are process-wide: a GPU test that tunes or sets them must
+    not change the launches of the tests after it."""
+    if "gpu" not in request.keywords:
+        yield
+        return
+    tune = importlib.import_module(PACKAGE + ".autotune")
+    try:
+        saved = {k: tune.get(k) for k in tune.KNOBS}
+    except Exception:  # library not loadable: the test itself reports that
+        saved = {}
+    yield
+    for k, v in saved.items():
+        tune.set_knob(k, v)
+
+
 @pytest.fixture(scope="session")
 def ss():
     return importlib.import_module(PACKAGE)
