@@ -82,6 +82,9 @@ typedef struct {
 #define SSG_TUNE_ISB_SELECT_BLOCKS 5  /* the same for the last level fused with the selection: 2, 3 */
 #define SSG_TUNE_ISB_TILE_TMA 6       /* coarse tiles of the chunked ISB upsampling staged by TMA (1) or by
                                          cp.async (0) */
+#define SSG_TUNE_HOLE_PERSISTENT 8    /* hole filling: 1 = the steps after the first in one cooperative
+                                         launch, separated by grid-wide barriers; 0 = a launch per
+                                         step (default) */
 #define SSG_TUNE_TMA_WITHHOLD 7       /* tests of the bounded TMA wait: 1 = the TMA-staged upsampling arms
                                          its tile barriers but issues no copy, so every block's first
                                          wait runs out (after a short limit), it writes nothing and
@@ -92,11 +95,15 @@ SSG_API int ssg_tuning_get(int knob);
 /* Writes up to `capacity` allowed values of a knob; returns how many it has (0 if unknown). */
 SSG_API int ssg_tuning_choices(int knob, int32_t* values, int capacity);
 
-/* Reads and clears the device status word of the ISB kernels: SSG_STATUS_TMA_TIMEOUT is set when
- * a bounded wait for a TMA tile ran out.  The block that waited then wrote nothing more (no later
+/* Reads and clears the library's device status words: SSG_STATUS_TMA_TIMEOUT is set when
+ * a bounded wait for a TMA tile ran out, SSG_STATUS_BARRIER_TIMEOUT when a grid-wide barrier of the
+ * hole filling did.  The block that waited then wrote nothing more (no later
  * chunk, no selection), so the outputs of that launch are incomplete.  The word stays set until
  * this call clears it.  Synchronous. */
 #define SSG_STATUS_TMA_TIMEOUT 1u
+/* Set when a grid-wide barrier of the cooperative hole filling (SSG_TUNE_HOLE_PERSISTENT) ran
+ * out of polls: the launch left its maps partly filled. */
+#define SSG_STATUS_BARRIER_TIMEOUT 2u
 SSG_API int ssg_take_device_status(uint32_t* status);
 
 /* Message of the calling thread's last failed call ("" if none). */
@@ -360,9 +367,12 @@ SSG_API int ssg_inpaint_batch(float* d_distance, const uint8_t* d_tables, float*
  * scan stamps every pixel (d_stamps, instances x rows x cols bytes: 0 not a hole, 255 an open
  * hole, s filled at step s); step 1 visits every fillable hole, and step s > 1 only the open holes
  * that read a pixel filled at step s - 1.
- * d_holes: caller-owned int32 scratch of 3 x instances x rows x cols + 4 entries (3 rotating
- * counts, two lists, a claim word per pixel); instances x rows x cols < 2^31; iterations <= 254.
- * Launches 1 + iterations kernels after a 16-byte memset. */
+ * d_holes: caller-owned int32 scratch of 3 x instances x rows x cols + SSG_HOLE_SCRATCH_HEADER
+ * entries (3 rotating counts, the barrier words of the cooperative launch, two lists, a claim word
+ * per pixel); instances x rows x cols < 2^31; iterations <= 254.  After a 32-byte memset,
+ * launches the scan and step 1, then a kernel per later step, or one cooperative kernel for all of
+ * them (SSG_TUNE_HOLE_PERSISTENT = 1, where the device supports cooperative launches). */
+#define SSG_HOLE_SCRATCH_HEADER 8
 SSG_API int ssg_inpaint_holes_batch(float* d_distance, const uint8_t* d_tables, uint8_t* d_stamps, int32_t* d_holes,
                                     int cols, int rows, int instances, int references, double max_dist,
                                     int iterations, void* stream);

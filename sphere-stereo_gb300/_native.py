@@ -31,7 +31,10 @@ TUNE_ISB_UP_BLOCKS = 4
 TUNE_ISB_SELECT_BLOCKS = 5
 TUNE_ISB_TILE_TMA = 6
 TUNE_TMA_WITHHOLD = 7
+TUNE_HOLE_PERSISTENT = 8
 STATUS_TMA_TIMEOUT = 1
+STATUS_BARRIER_TIMEOUT = 2
+HOLE_SCRATCH_HEADER = 8
 ISB_SKIP_FINE_GUIDE = 1
 PIXEL_U8 = 0
 PIXEL_F32 = 1
@@ -233,6 +236,14 @@ def pointers(values) -> ctypes.Array:
     return (ctypes.c_void_p * len(values))(*[int(v) for v in values])
 
 
+def hole_filling_launches(iterations: int) -> int:
+    """Kernels one batched hole filling launches: the scan and step 1, then one cooperative launch
+    for the other steps or one launch per step (SSG_TUNE_HOLE_PERSISTENT)."""
+    if iterations <= 1:
+        return 2 * iterations
+    return 3 if library().ssg_tuning_get(TUNE_HOLE_PERSISTENT) == 1 else 1 + iterations
+
+
 def kernels_launched(name: str, args) -> int:
     """Number of kernels one call of entry point ``name`` with ``args`` launches."""
     if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count", "ssg_tuning_set",
@@ -249,8 +260,7 @@ def kernels_launched(name: str, args) -> int:
     if name == "ssg_inpaint":
         return -(-int(args[6]) // 16)
     if name == "ssg_inpaint_holes_batch":
-        it = int(args[9])
-        return 0 if it == 0 else 1 + it
+        return hole_filling_launches(int(args[9]))
     if name == "ssg_inpaint_batch":
         return -(-int(args[8]) // 16)
     if name == "ssg_inpaint_noalloc":

@@ -33,6 +33,7 @@ KNOBS = {
     "isb_up_blocks": (N.TUNE_ISB_UP_BLOCKS, ("ssg_isb_upsample_batch",)),
     "isb_select_blocks": (N.TUNE_ISB_SELECT_BLOCKS, ("ssg_isb_upsample_select_batch",)),
     "isb_tile_tma": (N.TUNE_ISB_TILE_TMA, ("ssg_isb_upsample_batch", "ssg_isb_upsample_select_batch")),
+    "hole_persistent": (N.TUNE_HOLE_PERSISTENT, ("ssg_inpaint_holes_batch",)),
 }
 
 

@@ -77,6 +77,7 @@ Knob g_knobs[] = {
     {kIsbUpBlocks, 2, {2}},        // SSG_TUNE_ISB_SELECT_BLOCKS
     {kOnOff, 2, {0}},              // SSG_TUNE_ISB_TILE_TMA
     {kOnOff, 2, {0}},              // SSG_TUNE_TMA_WITHHOLD
+    {kOnOff, 2, {0}},              // SSG_TUNE_HOLE_PERSISTENT
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

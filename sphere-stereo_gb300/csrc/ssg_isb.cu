@@ -1210,12 +1210,17 @@ extern "C" int ssg_select_distance_batch(const void* d_cost, int candidate_count
     return launch_status("select_kernel");
 }
 
+namespace ssg {
+uint32_t take_stitch_status(cudaError_t* err);  // ssg_stitch.cu
+}
+
 extern "C" int ssg_take_device_status(uint32_t* status)
 {
     SSG_REQUIRE(status, "null pointer");
     uint32_t zero = 0;
     cudaError_t e = cudaMemcpyFromSymbol(status, ssg::g_tma_status, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(ssg::g_tma_status, &zero, sizeof(uint32_t));
+    if (e == cudaSuccess) *status |= ssg::take_stitch_status(&e);
     if (e != cudaSuccess) return ssg::fail(SSG_ERR_CUDA, "device status: %s", cudaGetErrorString(e));
     return SSG_OK;
 }

@@ -486,20 +486,31 @@ __device__ __forceinline__ bool fillable(uchar2 t)
     return h.w0 > 0.0f || h.w1 > 0.0f;
 }
 
+// Loads of the data the hole steps change (map, stamps, lists, counts).  kL2: through L2 only
+// (ld.global.cg), for the persistent launch whose phases read what other SMs wrote in an earlier
+// phase of the same launch; otherwise ordinary loads (a launch boundary separates the steps).
+template <bool kL2, typename T>
+__device__ __forceinline__ T load_mutable(const T* p)
+{
+    if constexpr (kL2) return __ldcg(p);
+    else return *p;
+}
+
 // Jacobi step `step` of hole g: fills it (value and stamp) when a usable neighbour exists
+template <bool kL2 = false>
 __device__ __forceinline__ bool fill_hole(float* __restrict__ map, uint8_t* __restrict__ stamp, int64_t g,
                                          const HoleOffsets& h, int step, float valid_at_most)
 {
     float val = 0.0f, ws = 0.0f;
-    if (h.w0 > 0.0f && stamp[h.n0] < step) {
-        const float sd = map[h.n0];
+    if (h.w0 > 0.0f && load_mutable<kL2>(stamp + h.n0) < step) {
+        const float sd = load_mutable<kL2>(map + h.n0);
         if (sd <= valid_at_most) {
             val = fadd(val, fmul(h.w0, sd));
             ws = fadd(ws, h.w0);
         }
     }
-    if (h.w1 > 0.0f && stamp[h.n1] < step) {
-        const float sd = map[h.n1];
+    if (h.w1 > 0.0f && load_mutable<kL2>(stamp + h.n1) < step) {
+        const float sd = load_mutable<kL2>(map + h.n1);
         if (sd <= valid_at_most) {
             val = fadd(val, fmul(h.w1, sd));
             ws = fadd(ws, h.w1);
@@ -562,44 +573,100 @@ struct UniformMaps {
     }
 };
 
-// Scan: stamps map pixels [begin, end) of the flat index space, clears their claims and lists
-// the fillable holes in `list` (counted by *count).
-template <typename Maps>
-__global__ void __launch_bounds__(kStitchBlock) hole_scan_kernel(const Maps maps, int64_t total,
-                                                                 const float* __restrict__ map,
-                                                                 uint8_t* __restrict__ stamp,
-                                                                 int32_t* __restrict__ claim, float hole_at_least,
-                                                                 int32_t* __restrict__ count,
-                                                                 int32_t* __restrict__ list)
+// Appends up to 32 items per thread (bit i of `take`: item first + i) to the list counted by
+// *count, with one atomic per block; every thread of the block calls it (blockDim.x == kStitchBlock).
+__device__ __forceinline__ void block_append_bits(uint32_t take, int64_t first, int32_t* count, int32_t* list)
 {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool take = false;
-    if (g < total) {
-        const bool hole = map[g] >= hole_at_least;  // stitcher.cu:287
-        stamp[g] = hole ? kUnfilled : 0;
-        claim[g] = 0;
-        if (hole) {
-            const MapPixel m = maps.at(g);
-            // interior test of stitcher.cu:291
-            take = m.x >= 1 && m.y >= 1 && m.x < m.cols - 1 && m.y < m.rows - 1 &&
-                   fillable(m.table[(int64_t)m.y * m.cols + m.x]);
-        }
+    __shared__ int warp_base[kStitchBlock / 32];
+    __shared__ int block_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = __popc(take);
+    int incl = n;  // inclusive prefix over the warp's lanes
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += t;
     }
-    block_append(take, (int32_t)g, count, list);
+    if (lane == 31) warp_base[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int w = 0; w < kStitchBlock / 32; ++w) {
+            const int c = warp_base[w];
+            warp_base[w] = total;
+            total += c;
+        }
+        block_base = total ? atomicAdd(count, total) : 0;
+    }
+    __syncthreads();
+    int at = block_base + warp_base[warp] + incl - n;
+    while (take) {
+        const int i = __ffs(take) - 1;
+        take &= take - 1;
+        list[at++] = (int32_t)(first + i);
+    }
+}
+
+// Scan: stamps the map pixels of the flat index space, clears the claims of the holes (nothing
+// reads the claim of a pixel that is not a hole) and lists the fillable holes in `list` (counted
+// by *count).  kScanPixels consecutive pixels per thread: vector loads of the map and one vector
+// store of their stamps when `vec` (map 16-byte and stamps 8-byte aligned, total a multiple of
+// kScanPixels).
+constexpr int kScanPixels = 8;
+
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_scan_wide_kernel(const Maps maps, int64_t total,
+                                                                      const float* __restrict__ map,
+                                                                      uint8_t* __restrict__ stamp,
+                                                                      int32_t* __restrict__ claim,
+                                                                      float hole_at_least, bool vec,
+                                                                      int32_t* __restrict__ count,
+                                                                      int32_t* __restrict__ list)
+{
+    const int64_t g0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kScanPixels;
+    uint32_t take = 0;
+    if (g0 < total) {
+        float v[kScanPixels];
+        if (vec) {
+            const float4 a = __ldg(reinterpret_cast<const float4*>(map + g0));
+            const float4 b = __ldg(reinterpret_cast<const float4*>(map + g0) + 1);
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+            v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < kScanPixels; ++i) v[i] = g0 + i < total ? map[g0 + i] : 0.0f;
+        }
+        uint32_t st[2] = {0u, 0u};
+#pragma unroll
+        for (int i = 0; i < kScanPixels; ++i) {
+            const int64_t g = g0 + i;
+            const bool hole = g < total && v[i] >= hole_at_least;  // stitcher.cu:287
+            if (hole) {
+                st[i / 4] |= (uint32_t)kUnfilled << (8 * (i % 4));
+                claim[g] = 0;
+                const MapPixel m = maps.at(g);
+                // interior test of stitcher.cu:291
+                if (m.x >= 1 && m.y >= 1 && m.x < m.cols - 1 && m.y < m.rows - 1 &&
+                    fillable(m.table[(int64_t)m.y * m.cols + m.x]))
+                    take |= 1u << i;
+            }
+            if (!vec && g < total) stamp[g] = hole ? kUnfilled : 0;
+        }
+        if (vec) reinterpret_cast<uint2*>(stamp + g0)[0] = make_uint2(st[0], st[1]);
+    }
+    block_append_bits(take, g0, count, list);
 }
 
 // Step 1 on every listed hole; lists the holes it fills.  counts[3] rotate: counts[(s - 1) % 3]
 // counts step s's input list, counts[s % 3] its output (zeroed by step s - 1 or the set-up), and
 // step s zeroes counts[(s + 1) % 3].
-template <typename Maps>
-__global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Maps maps, float* __restrict__ map,
-                                                                       uint8_t* __restrict__ stamp,
-                                                                       int32_t* __restrict__ counts,
-                                                                       const int32_t* __restrict__ list_in,
-                                                                       int32_t* __restrict__ list_out,
-                                                                       float valid_at_most)
+template <bool kL2, typename Maps>
+__device__ __forceinline__ void hole_first_step(const Maps& maps, float* __restrict__ map,
+                                                uint8_t* __restrict__ stamp, int32_t* __restrict__ counts,
+                                                const int32_t* __restrict__ list_in, int32_t* __restrict__ list_out,
+                                                float valid_at_most)
 {
-    const int n = counts[0];
+    const int n = load_mutable<kL2>(counts);
     if (blockIdx.x == 0 && threadIdx.x == 0) counts[2] = 0;
     const int stride = gridDim.x * blockDim.x;
     // whole blocks iterate together (block_append is block-collective)
@@ -608,10 +675,10 @@ __global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Map
         bool filled = false;
         int32_t g = 0;
         if (h < n) {
-            g = list_in[h];
+            g = load_mutable<kL2>(list_in + h);
             const MapPixel m = maps.at(g);
             const uchar2 t = m.table[(int64_t)m.y * m.cols + m.x];
-            filled = fill_hole(map, stamp, g, hole_offsets(t, g, m.cols), 1, valid_at_most);
+            filled = fill_hole<kL2>(map, stamp, g, hole_offsets(t, g, m.cols), 1, valid_at_most);
         }
         block_append(filled, g, counts + 1, list_out);
     }
@@ -620,17 +687,15 @@ __global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Map
 // Step `step` >= 2: visits the open holes next to the pixels filled at step - 1 (list_in) that read
 // one of them, fills those it can and lists them.  One thread per (filled pixel, neighbour): the
 // frontier is short after the first steps, and a thread's work is a chain of dependent loads, so
-// spreading the 8 neighbours over threads keeps a step's time near one chain's latency.
-template <typename Maps>
-__global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const Maps maps, float* __restrict__ map,
-                                                                          uint8_t* __restrict__ stamp,
-                                                                          int32_t* __restrict__ claim, int step,
-                                                                          int32_t* __restrict__ counts,
-                                                                          const int32_t* __restrict__ list_in,
-                                                                          int32_t* __restrict__ list_out,
-                                                                          float valid_at_most)
+// spreading the 8 neighbours over threads keeps a step's time near one chain's latency.  Returns
+// the number of pixels filled at step - 1.
+template <bool kL2, typename Maps>
+__device__ __forceinline__ int hole_frontier_step(const Maps& maps, float* __restrict__ map,
+                                                  uint8_t* __restrict__ stamp, int32_t* __restrict__ claim, int step,
+                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ list_in,
+                                                  int32_t* __restrict__ list_out, float valid_at_most)
 {
-    const int n = counts[(step - 1) % 3];
+    const int n = load_mutable<kL2>(counts + (step - 1) % 3);
     if (blockIdx.x == 0 && threadIdx.x == 0) counts[(step + 1) % 3] = 0;
     const int64_t work = (int64_t)n * 8;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -640,7 +705,7 @@ __global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const 
         bool filled = false;
         int64_t q = 0;
         if (h < work) {
-            const int64_t p = list_in[h >> 3];
+            const int64_t p = load_mutable<kL2>(list_in + (h >> 3));
             const int k = (int)(h & 7);
             const int dx = k < 3 ? k - 1 : k == 3 ? -1 : k == 4 ? 1 : k - 6;  // the 8 neighbours
             const int dy = k < 3 ? -1 : k < 5 ? 0 : 1;
@@ -648,16 +713,119 @@ __global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const 
             const int qx = m.x + dx, qy = m.y + dy;
             if (qx >= 1 && qy >= 1 && qx < m.cols - 1 && qy < m.rows - 1) {
                 q = p + (int64_t)dy * m.cols + dx;
-                if (stamp[q] == kUnfilled) {
+                if (load_mutable<kL2>(stamp + q) == kUnfilled) {
                     const HoleOffsets o = hole_offsets(m.table[(int64_t)qy * m.cols + qx], q, m.cols);
                     // q reads p, and no other thread has queued q for this step
                     filled = ((o.w0 > 0.0f && o.n0 == p) || (o.w1 > 0.0f && o.n1 == p)) &&
-                             atomicMax(claim + q, step) < step && fill_hole(map, stamp, q, o, step, valid_at_most);
+                             atomicMax(claim + q, step) < step &&
+                             fill_hole<kL2>(map, stamp, q, o, step, valid_at_most);
                 }
             }
         }
         block_append(filled, (int32_t)q, counts + step % 3, list_out);
     }
+    return n;
+}
+
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Maps maps, float* __restrict__ map,
+                                                                       uint8_t* __restrict__ stamp,
+                                                                       int32_t* __restrict__ counts,
+                                                                       const int32_t* __restrict__ list_in,
+                                                                       int32_t* __restrict__ list_out,
+                                                                       float valid_at_most)
+{
+    hole_first_step<false>(maps, map, stamp, counts, list_in, list_out, valid_at_most);
+}
+
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_frontier_step_kernel(const Maps maps, float* __restrict__ map,
+                                                                          uint8_t* __restrict__ stamp,
+                                                                          int32_t* __restrict__ claim, int step,
+                                                                          int32_t* __restrict__ counts,
+                                                                          const int32_t* __restrict__ list_in,
+                                                                          int32_t* __restrict__ list_out,
+                                                                          float valid_at_most)
+{
+    hole_frontier_step<false>(maps, map, stamp, claim, step, counts, list_in, list_out, valid_at_most);
+}
+
+// ---------------------------------------------------------------------------------------------
+// The hole-filling steps after the first in one cooperative launch: steps 2 .. iterations run as
+// phases of a grid whose blocks are all resident (cudaLaunchCooperativeKernel guarantees it or
+// refuses the launch), separated by grid-wide barriers.  After step 2 a step's frontier is
+// a few hundred holes per map, so a launch per step costs more in launch gaps than in work; here
+// a step costs one barrier.  Phases read what other SMs wrote in earlier phases through L2.
+// Every barrier wait is bounded: a wait that runs out raises the launch's abort word (the other
+// blocks then leave at their next barrier) and SSG_STATUS_BARRIER_TIMEOUT in the status word,
+// and the maps are left partly filled.
+// ---------------------------------------------------------------------------------------------
+constexpr int kBarrierMaxPolls = 1 << 22;  // each poll sleeps ~0.1 us: a wait gives up after ~0.5 s
+
+static __device__ uint32_t g_stitch_status;
+
+// the launch's barrier words: the arrivals, the generation (advanced by the last arrival), abort
+struct GridSync {
+    uint32_t* count;
+    uint32_t* generation;
+    uint32_t* abort;
+};
+
+// true when every block of the grid arrived; false when the wait ran out or another block gave up
+__device__ __forceinline__ bool grid_barrier(const GridSync& b)
+{
+    __shared__ int passed;
+    __syncthreads();  // the block's writes of this phase precede its arrival
+    if (threadIdx.x == 0) {
+        const uint32_t gen = *reinterpret_cast<volatile uint32_t*>(b.generation);
+        bool ok = true;
+        __threadfence();
+        if (atomicAdd(b.count, 1u) == gridDim.x - 1) {
+            atomicExch(b.count, 0u);
+            __threadfence();
+            atomicAdd(b.generation, 1u);
+        } else {
+            for (int polls = 0; *reinterpret_cast<volatile uint32_t*>(b.generation) == gen; ++polls) {
+                if (*reinterpret_cast<volatile uint32_t*>(b.abort) != 0u || polls >= kBarrierMaxPolls) {
+                    ok = false;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        if (!ok) {
+            atomicExch(b.abort, 1u);
+            atomicOr(&g_stitch_status, SSG_STATUS_BARRIER_TIMEOUT);
+        }
+        __threadfence();
+        passed = ok;
+    }
+    __syncthreads();
+    return passed != 0;
+}
+
+template <typename Maps>
+__global__ void __launch_bounds__(kStitchBlock) hole_fill_persistent_kernel(
+    const Maps maps, float* __restrict__ map, uint8_t* __restrict__ stamp, int32_t* __restrict__ claim,
+    float valid_at_most, int iterations, int32_t* __restrict__ counts, int32_t* __restrict__ list0,
+    int32_t* __restrict__ list1, const GridSync sync)
+{
+    for (int s = 2; s <= iterations; ++s) {
+        if (s > 2 && !grid_barrier(sync)) return;
+        int32_t* in = (s & 1) ? list0 : list1;  // step s reads lists[(s - 1) % 2], writes lists[s % 2]
+        int32_t* out = (s & 1) ? list1 : list0;
+        // every block reads the same count after the barrier: an empty frontier ends all of them
+        if (hole_frontier_step<true>(maps, map, stamp, claim, s, counts, in, out, valid_at_most) == 0)
+            return;
+    }
+}
+
+uint32_t take_stitch_status(cudaError_t* err)
+{
+    uint32_t v = 0, zero = 0;
+    *err = cudaMemcpyFromSymbol(&v, g_stitch_status, sizeof(uint32_t));
+    if (*err == cudaSuccess) *err = cudaMemcpyToSymbol(g_stitch_status, &zero, sizeof(uint32_t));
+    return v;
 }
 
 // blocks of a grid-stride launch: a few per SM
@@ -676,6 +844,27 @@ static int resident_grid(int per_sm)
 
 // The hole filling of `total` flat map pixels (see above): d_holes holds 3 rotating counts (+ 1),
 // two lists and a claim word per pixel
+// Blocks per SM of the cooperative hole filling on the current device (0: no cooperative launch)
+template <typename Maps>
+static int persistent_blocks_per_sm()
+{
+    static std::atomic<int> cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    int n = cached[dev].load();
+    if (n == 0) {
+        int coop = 0, per_sm = 0;
+        if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hole_fill_persistent_kernel<Maps>, kStitchBlock,
+                                                          0) != cudaSuccess)
+            per_sm = 0;
+        cudaGetLastError();
+        n = per_sm > 0 ? per_sm : -1;
+        cached[dev].store(n);
+    }
+    return n > 0 ? n : 0;
+}
+
 template <typename Maps>
 static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t* d_stamps, int32_t* d_holes,
                          double max_dist, int iterations, cudaStream_t st)
@@ -683,18 +872,35 @@ static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t*
     if (iterations == 0) return SSG_OK;
     const float hole = float_at_least(max_dist + 0.1);
     const float ok = float_at_most(max_dist + (double)0.1f);
+    // header: 3 rotating counts and a spare, then the barrier words (arrivals, generation, abort)
     int32_t* counts = d_holes;
-    int32_t* lists[2] = {d_holes + 4, d_holes + 4 + total};
-    int32_t* claims = d_holes + 4 + 2 * total;
-    const cudaError_t e = cudaMemsetAsync(counts, 0, 4 * sizeof(int32_t), st);
+    int32_t* lists[2] = {d_holes + SSG_HOLE_SCRATCH_HEADER, d_holes + SSG_HOLE_SCRATCH_HEADER + total};
+    int32_t* claims = d_holes + SSG_HOLE_SCRATCH_HEADER + 2 * total;
+    const cudaError_t e = cudaMemsetAsync(counts, 0, SSG_HOLE_SCRATCH_HEADER * sizeof(int32_t), st);
     if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
-    hole_scan_kernel<Maps><<<grid_1d(total, kStitchBlock), kStitchBlock, 0, st>>>(maps, total, d_map, d_stamps,
-                                                                                  claims, hole, counts, lists[0]);
-    if (int err = launch_status("hole_scan_kernel")) return err;
+    const bool vec = ((uintptr_t)d_map & 15) == 0 && ((uintptr_t)d_stamps & 7) == 0 && total % kScanPixels == 0;
+    hole_scan_wide_kernel<Maps><<<grid_1d((total + kScanPixels - 1) / kScanPixels, kStitchBlock), kStitchBlock, 0,
+                                  st>>>(maps, total, d_map, d_stamps, claims, hole, vec, counts, lists[0]);
+    if (int err = launch_status("hole_scan_wide_kernel")) return err;
     const int grid = resident_grid(tuning(SSG_TUNE_HOLE_BLOCKS_PER_SM));
     hole_first_step_kernel<Maps><<<grid, kStitchBlock, 0, st>>>(maps, d_map, d_stamps, counts, lists[0], lists[1],
                                                                 ok);
     if (int err = launch_status("hole_first_step_kernel")) return err;
+    if (iterations == 1) return SSG_OK;
+    const int per_sm = tuning(SSG_TUNE_HOLE_PERSISTENT) == 1 ? persistent_blocks_per_sm<Maps>() : 0;
+    if (per_sm > 0) {
+        // one block per SM: the barrier's arrivals are one atomic per block, and a step after the
+        // first has a few thousand holes to visit
+        const int pgrid = resident_grid(1);
+        uint32_t* words = reinterpret_cast<uint32_t*>(d_holes + 4);
+        const GridSync sync{words, words + 1, words + 2};
+        void* args[] = {(void*)&maps, (void*)&d_map, (void*)&d_stamps, (void*)&claims, (void*)&ok, (void*)&iterations,
+                        (void*)&counts, (void*)&lists[0], (void*)&lists[1], (void*)&sync};
+        const cudaError_t le = cudaLaunchCooperativeKernel((const void*)hole_fill_persistent_kernel<Maps>,
+                                                           dim3(pgrid), dim3(kStitchBlock), args, 0, st);
+        if (le != cudaSuccess) return fail(SSG_ERR_CUDA, "hole_fill_persistent_kernel: %s", cudaGetErrorString(le));
+        return SSG_OK;
+    }
     for (int s = 2; s <= iterations; ++s) {
         hole_frontier_step_kernel<Maps><<<grid, kStitchBlock, 0, st>>>(maps, d_map, d_stamps, claims, s, counts,
                                                                        lists[(s - 1) % 2], lists[s % 2], ok);

@@ -366,7 +366,7 @@ extern "C" int ssg_uneven_create(const ssg_uneven_instance* instances, int insta
     b->stamps_offset = so;
     so = align_up(so + (size_t)maps, 256);
     b->holes_offset = so;
-    so = align_up(so + sizeof(int32_t) * (3 * (size_t)maps + 4), 256);
+    so = align_up(so + sizeof(int32_t) * (3 * (size_t)maps + SSG_HOLE_SCRATCH_HEADER), 256);
     b->scratch_bytes = so;
     *plan_bytes = b->plan_bytes;
     *scratch_bytes = b->scratch_bytes;

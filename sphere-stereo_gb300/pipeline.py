@@ -11,7 +11,7 @@ One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_p
     ssg_isb_upsample_select_batch  last level + argmin / sub-candidate step             1
     ssg_isb_apply_batch            distance post-filter, fp32, N = 1                    2L - 2
     ssg_reproject_distance_batch_approx  fill + z-buffer                                2
-    ssg_inpaint_holes_batch        hole filling: a scan, then 32 steps on hole lists    33
+    ssg_inpaint_holes_batch        hole filling: a scan, then 32 steps on hole lists    33 (or 3)
     ssg_merge_panorama_batch_approx panoramas                                           1
 
 so the launch count does not grow with F (about 70 at 1024^2).  Buffers are allocated once for
@@ -88,7 +88,8 @@ class BatchPipeline:
         self.distance = torch.empty(F, R, self.rows, self.cols, **f32)
         self.reprojected = torch.empty(F * R * P, **f32)
         self.stamps = torch.empty(F * R * P, **u8)
-        self.holes = torch.empty(3 * F * R * P + 4 * self.MAX_GROUPS, dtype=torch.int32, device=dev)
+        self.holes = torch.empty(3 * F * R * P + N.HOLE_SCRATCH_HEADER * self.MAX_GROUPS, dtype=torch.int32,
+                                 device=dev)
         self.images_u8 = torch.empty(F, R, st.image_rows, st.image_cols, 3, **u8)
         self.rgb = torch.empty(F, st.pano_rows, st.pano_cols, 3, **u8)
         self.pano_distance = torch.empty(F, st.pano_rows, st.pano_cols, **f32)
@@ -197,7 +198,7 @@ class BatchPipeline:
         reprojected = self.reprojected.data_ptr() + 4 * i0 * P
         N.call("ssg_reproject_distance_batch_approx", dist.data_ptr(), reprojected, cols, rows, inst, R, st._intr,
                st._trans, 1, stream)
-        holes = self.holes.data_ptr() + 4 * (3 * i0 * P + 4 * group)
+        holes = self.holes.data_ptr() + 4 * (3 * i0 * P + N.HOLE_SCRATCH_HEADER * group)
         N.call("ssg_inpaint_holes_batch", reprojected, self.tables.data_ptr(), self.stamps.data_ptr() + i0 * P, holes,
                cols, rows, inst, R, st.max_dist, st.inpainting_iterations, stream)
         N.call("ssg_merge_panorama_batch_approx", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
@@ -304,7 +305,7 @@ class BatchPipeline:
             graph.replay()
 
     TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "isb_select_blocks", "isb_tile_tma", "hole_blocks_per_sm",
-                   "merge_frames")
+                   "hole_persistent", "merge_frames")
     GROUP_CHOICES = (1, 2, 4)
 
     def _apply_tuning(self, match, stitch, frames) -> None:
@@ -337,7 +338,6 @@ class BatchPipeline:
         L = self.L
         isb = (L - 1) + (L - 2) + 1 if L >= 2 else 1
         post = 2 * (L - 1) if L >= 2 else 0
-        it = self.st.inpainting_iterations
-        inpaint = 0 if it == 0 else 1 + it
+        inpaint = N.hole_filling_launches(self.st.inpainting_iterations)
         per_group = 2 + isb + post + (1 if float_stitch else 0) + 2 + inpaint + 1
         return per_group * len(self._groups(frames, self._group_count(frames)))

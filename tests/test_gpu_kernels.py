@@ -250,11 +250,14 @@ def test_inpaint_iteration_counts(ss, native, dev_oracle, iterations):
     np.testing.assert_array_equal(src.cpu().numpy(), dev_oracle.inpaint(d, table, 100.0, iterations))
 
 
+@pytest.mark.parametrize("persistent", [1, 0])
 @pytest.mark.parametrize("iterations", [0, 1, 2, 5, 32, 33, 254])
-def test_inpaint_hole_list_batch(ss, native, dev_oracle, iterations):
+def test_inpaint_hole_list_batch(ss, native, dev_oracle, iterations, persistent):
     """The hole lists (one scan, a first step over every fillable hole, then steps over the holes
     next to the last step's fills) equal one Jacobi step per launch on every map of the batch;
-    tables are per reference slot."""
+    tables are per reference slot.  Both forms: one cooperative launch whose steps are separated
+    by grid-wide barriers, and a launch per step."""
+    ss._native.call("ssg_tuning_set", ss._native.TUNE_HOLE_PERSISTENT, persistent)
     rng = np.random.default_rng(100 + iterations)
     H, W, refs, frames = 61, 97, 2, 3
     inst = refs * frames
@@ -264,10 +267,15 @@ def test_inpaint_hole_list_batch(ss, native, dev_oracle, iterations):
     tables = rng.integers(0, 256, (refs, H, W, 2)).astype(np.uint8)
     src = _t(d)
     stamps = torch.empty(inst * H * W, dtype=torch.uint8, device=DEV)
-    holes = torch.empty(3 * inst * H * W + 4, dtype=torch.int32, device=DEV)
+    holes = torch.empty(3 * inst * H * W + ss._native.HOLE_SCRATCH_HEADER, dtype=torch.int32, device=DEV)
     ss._native.call("ssg_inpaint_holes_batch", src.data_ptr(), _t(tables).data_ptr(), stamps.data_ptr(),
                     holes.data_ptr(), W, H, inst, refs, 100.0, iterations, torch.cuda.current_stream().cuda_stream)
     got = src.cpu().numpy()
+    import ctypes
+
+    status = ctypes.c_uint32(0)
+    ss._native.call("ssg_take_device_status", ctypes.byref(status))
+    assert status.value == 0
     for i in range(inst):
         np.testing.assert_array_equal(got[i], dev_oracle.inpaint(d[i], tables[i % refs], 100.0, iterations))
 
