@@ -21,7 +21,7 @@ import sphere_oracle as SO
 
 
 def skew(w: torch.Tensor) -> torch.Tensor:
-    z = torch.zeros((), dtype=w.dtype)
+    z = torch.zeros((), dtype=w.dtype, device=w.device)
     return torch.stack([torch.stack([z, -w[2], w[1]]), torch.stack([w[2], z, -w[0]]),
                         torch.stack([-w[1], w[0], z])])
 
@@ -34,19 +34,21 @@ def so3_exp(w: torch.Tensor) -> torch.Tensor:
     a = torch.where(small, 1 - th2 / 6, torch.sin(th) / th)
     b = torch.where(small, 0.5 - th2 / 24, (1 - torch.cos(th)) / torch.where(small, torch.ones_like(th2), th2))
     k = skew(w)
-    return torch.eye(3, dtype=w.dtype) + a * k + b * (k @ k)
+    return torch.eye(3, dtype=w.dtype, device=w.device) + a * k + b * (k @ k)
 
 
 def perturb(rt: torch.Tensor, delta: torch.Tensor) -> torch.Tensor:
     """T [Exp(omega), v] for delta = (omega, v)."""
-    e = torch.eye(4, dtype=rt.dtype)
+    e = torch.eye(4, dtype=rt.dtype, device=rt.device)
     e = torch.cat([torch.cat([so3_exp(delta[:3]), delta[3:, None]], 1), e[3:]], 0)
     return rt @ e
 
 
 class DiffReference:
     def __init__(self, calibration: dict, *, matching_resolution, min_dist, max_dist, candidate_count,
-                 references_indices, selected, guides, sigma_i, sigma_s, temperature):
+                 references_indices, selected, guides, sigma_i, sigma_s, temperature, device="cpu"):
+        """device: where the float64 evaluation runs (a CUDA device makes the full-size checks
+        affordable; the arithmetic is the same float64 on either)."""
         W, H = matching_resolution
         self.W, self.H, self.P = W, H, W * H
         self.refs = list(references_indices)
@@ -66,6 +68,12 @@ class DiffReference:
         u, v = torch.meshgrid(torch.arange(H, dtype=torch.float64), torch.arange(W, dtype=torch.float64),
                               indexing="ij")
         self.pix = torch.stack([v.reshape(-1), u.reshape(-1)], -1)
+        self.device = torch.device(device)
+        dev = self.device
+        self.rt = [t.to(dev) for t in self.rt]
+        self.k, self.cand, self.pix = self.k.to(dev), self.cand.to(dev), self.pix.to(dev)
+        self.selected = [t.to(dev) for t in self.selected]
+        self.ops = [{k: ([a.to(dev) for a in v] if k != "shapes" else v) for k, v in ops.items()} for ops in self.ops]
 
     def rays(self, r: int) -> torch.Tensor:
         fx, fy, cx, cy, xi, al = self.k[r]
@@ -77,20 +85,24 @@ class DiffReference:
         return torch.stack([s * mx, s * my, s * mz - xi], -1)
 
     def sample(self, images: torch.Tensor, sel: torch.Tensor, u: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
-        """Bilinear, zero padding; images [C, P, 3]; sel [P]; u, v [N, P] -> [N, P, 3]."""
+        """Bilinear, zero padding; images [C, P, 3]; sel [P]; u, v [N, P] -> [N, P, 3].  Written as
+        two horizontal interpolations and a vertical one (the same value as the sum of the four
+        weighted taps): four equal taps give exactly their value, so the L1 residual of a sample in
+        a flat region is exactly 0 and takes the zero subgradient, as on the device."""
         x0, y0 = torch.floor(u), torch.floor(v)
-        out = 0
+        fx, fy = (u - x0)[..., None], (v - y0)[..., None]
+        taps = []
         for dx, dy in ((0, 0), (1, 0), (0, 1), (1, 1)):
             xs, ys = x0 + dx, y0 + dy
-            w = (1 - (u - x0) if dx == 0 else (u - x0)) * (1 - (v - y0) if dy == 0 else (v - y0))
             inb = (xs >= 0) & (xs < self.W) & (ys >= 0) & (ys < self.H)
             idx = (ys.clamp(0, self.H - 1) * self.W + xs.clamp(0, self.W - 1)).long()
-            vals = images[sel.clamp(min=0)[None].expand_as(idx), idx]
-            out = out + vals * (w * inb)[..., None]
-        return out
+            taps.append(images[sel.clamp(min=0)[None].expand_as(idx), idx] * inb[..., None])
+        top = taps[0] + fx * (taps[1] - taps[0])
+        bot = taps[2] + fx * (taps[3] - taps[2])
+        return top + fy * (bot - top)
 
     def inverse_distance(self, images: torch.Tensor, deltas: torch.Tensor) -> torch.Tensor:
-        """images [C, H, W, 3], deltas [C, 6] (float64) -> q [references, H, W]."""
+        """images [C, H, W, 3], deltas [C, 6] (float64, on the reference's device) -> q [references, H, W]."""
         C = images.shape[0]
         imgs = images.reshape(C, self.P, 3)
         poses = [perturb(self.rt[c], deltas[c]) for c in range(C)]

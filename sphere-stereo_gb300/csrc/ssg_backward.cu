@@ -307,8 +307,10 @@ __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_
                                                                    const float* __restrict__ grad_cost,
                                                                    double* __restrict__ grad_pose)
 {
-    __shared__ float pose_acc[SSG_MAX_CAMERAS][6];
-    for (int j = threadIdx.x; j < SSG_MAX_CAMERAS * 6; j += blockDim.x) (&pose_acc[0][0])[j] = 0.0f;
+    // the extrinsic-gradient reduction in float64: a pixel's candidates are summed in float32,
+    // pixels and blocks in float64
+    __shared__ double pose_acc[SSG_MAX_CAMERAS][6];
+    for (int j = threadIdx.x; j < SSG_MAX_CAMERAS * 6; j += blockDim.x) (&pose_acc[0][0])[j] = 0.0;
     __syncthreads();
     const int64_t P = (int64_t)p.cols * p.rows;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -343,22 +345,35 @@ __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_
             // d w / d ix and d w / d iy
             const float wx[4] = {-(y1 - iy), (y1 - iy), -(iy - y0), (iy - y0)};
             const float wy[4] = {-(x1 - ix), -(ix - x0), (x1 - ix), (ix - x0)};
-            float s[3] = {0, 0, 0}, sx[3] = {0, 0, 0}, sy[3] = {0, 0, 0};
+            float tv[4][3], sx[3] = {0, 0, 0}, sy[3] = {0, 0, 0};
             bool in[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 in[t] = xs[t] >= 0.0f && xs[t] < p.colsf && ys[t] >= 0.0f && ys[t] < p.rowsf;
+                tv[t][0] = tv[t][1] = tv[t][2] = 0.0f;  // zero padding
                 if (in[t]) {
                     const float* v = img + 3 * ((int64_t)(int)ys[t] * p.cols + (int)xs[t]);
 #pragma unroll
-                    for (int ch = 0; ch < 3; ++ch) {
-                        s[ch] += v[ch] * w[t];
-                        sx[ch] += v[ch] * wx[t];
-                        sy[ch] += v[ch] * wy[t];
-                    }
+                    for (int ch = 0; ch < 3; ++ch) tv[t][ch] = v[ch];
+                }
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                    sx[ch] += tv[t][ch] * wx[t];
+                    sy[ch] += tv[t][ch] * wy[t];
                 }
             }
-            const float res[3] = {s[0] - r[0], s[1] - r[1], s[2] - r[2]};
+            // the sample as two horizontal interpolations and a vertical one (the value of the four
+            // weighted taps): four equal taps give exactly their value, so a sample in a flat
+            // region equal to the reference texel has a residual of exactly 0 and the L1 kink's
+            // zero subgradient, as in the float64 reference
+            const float fx = ix - x0, fy = iy - y0;
+            float res[3];
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                const float top = tv[0][ch] + fx * (tv[1][ch] - tv[0][ch]);
+                const float bot = tv[2][ch] + fx * (tv[3][ch] - tv[2][ch]);
+                res[ch] = top + fy * (bot - top) - r[ch];
+            }
             const float cost = fabsf(res[0]) + fabsf(res[1]) + fabsf(res[2]);
             if (cost > 500.0f) continue;  // clamp(max=500) passes no gradient above the bound
             float gs[3];
@@ -405,14 +420,14 @@ __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_
         for (int ch = 0; ch < 3; ++ch) atomicAdd(gr + ch, gref[ch]);
 #pragma unroll
         for (int j = 0; j < 6; ++j) {
-            atomicAdd(&pose_acc[sel][j], gsrc[j]);
-            atomicAdd(&pose_acc[p.reference][j], gref6[j]);
+            atomicAdd(&pose_acc[sel][j], (double)gsrc[j]);
+            atomicAdd(&pose_acc[p.reference][j], (double)gref6[j]);
         }
     }
     __syncthreads();
     for (int j = threadIdx.x; j < p.ncam * 6; j += blockDim.x) {
-        const float v = (&pose_acc[0][0])[j];
-        if (v != 0.0f) atomicAdd(grad_pose + j, (double)v);
+        const double v = (&pose_acc[0][0])[j];
+        if (v != 0.0) atomicAdd(grad_pose + j, v);
     }
 }
 

@@ -86,3 +86,94 @@ def test_uneven_rejects_invalid_jobs(ss, jobs):
         uneven.UnevenBatch([])
     with pytest.raises(ValueError):
         uneven.UnevenBatch([jobs[0][0]], storage="fp8")
+
+
+# The uneven-batch configuration's sizes: every combination of matching resolution {512, 768,
+# 1024}^2 and candidate count {32, 64, 96}, 3-6 cameras on seeded ring rigs (radius 0.1-0.3 m, xi
+# in [-0.3, 0], alpha in [0.5, 0.7]), panorama 2W x H, fp16 cost storage, sigma_s 25.
+C5_JOBS = [(w, n, 3 + (k % 4), [0, 1 + (k % 2)]) for k, (w, n) in
+           enumerate((w, n) for w in (512, 768, 1024) for n in (32, 64, 96))]
+
+
+@pytest.fixture(scope="module")
+def c5_jobs(ss, native, synthetic):
+    out = []
+    for k, (w, n, cams, refs) in enumerate(C5_JOBS):
+        rng = np.random.Generator(np.random.PCG64(synthetic.frame_seed(5, 100 + k)))
+        rig = synthetic.ring_rig(rng, w, cams)
+        frame = synthetic.render_frame(synthetic.random_scene(rng), rig, (w, w), (w, w), refs)
+        calibration = synthetic.basalt_calibration(rig)
+        calibs = ss.parse_json_calib(calibration, (w, w), DEV)
+        vp = torch.zeros(3, device=DEV)
+        for r in refs:
+            vp += calibs[r].rt[:3, 3] / len(refs)
+        masks = [torch.ones(1, w, w, device=DEV) for _ in rig]
+        args = (calibs, 0.55, 100.0, n, refs, vp, masks, (w, w), (w, w), (2 * w, w), 10.0, 25.0, DEV)
+        est = ss.RGBD_Estimator(*args, cost_storage="fp16", max_batch=1)
+        match = torch.as_tensor(np.stack(frame.images_to_match), device=DEV).float().contiguous()
+        stitch = torch.as_tensor(np.stack(frame.images_to_stitch), device=DEV).float().contiguous()
+        out.append((est, match, stitch, calibration, frame, args))
+    return out
+
+
+def test_uneven_batch_at_full_sizes(ss, oracle_mod, c5_jobs):
+    """Nine jobs of every size in one batch: each job equals its rig run alone on the uniform
+    batched path bit for bit, and the 512^2 / 32- and 1024^2 / 96-candidate jobs against the
+    oracle (bars below)."""
+    from importlib import import_module
+
+    from conftest import inverse_distance_mae, psnr
+
+    uneven = import_module("sphere-stereo_gb300.uneven")
+    batch = uneven.UnevenBatch([e for e, *_ in c5_jobs], cuda_graphs=True)
+    outs = batch.run([m for _, m, *_ in c5_jobs], [s for _, _, s, *_ in c5_jobs])
+    torch.cuda.synchronize()
+    print(f"\n{len(c5_jobs)} jobs, {batch.instance_count} instances, {batch.launches()} launches per batch")
+    for k, (est, match, stitch, calibration, frame, args) in enumerate(c5_jobs):
+        rgb_u, dist_u = (t.cpu().numpy() for t in outs[k])
+        idx_u = batch.index_maps[k].cpu().numpy()
+        rgb, dist = est.estimate_RGBD_panoramas(match[None].contiguous(), stitch[None].contiguous())
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(idx_u, est.batch_index_maps[0].cpu().numpy(), err_msg=f"job {k} index")
+        np.testing.assert_array_equal(rgb_u, rgb[0].cpu().numpy(), err_msg=f"job {k} rgb")
+        np.testing.assert_array_equal(dist_u, dist[0].cpu().numpy(), err_msg=f"job {k} panorama")
+        w, n, cams, refs = C5_JOBS[k]
+        if (w, n) not in ((512, 32), (1024, 96)):
+            continue
+        rig = oracle_mod.OracleRig(calibration, min_dist=0.55, max_dist=100.0, candidate_count=n,
+                                   references_indices=refs, masks=[np.ones((w, w), np.float32)] * cams,
+                                   matching_resolution=(w, w), rgb_to_stitch_resolution=(w, w),
+                                   panorama_resolution=(2 * w, w), sigma_i=10.0, sigma_s=25.0)
+        # the oracle's rig tables come from this host's float32 linear algebra; the job's too
+        sel = [s.cpu().numpy() for s in est._selected]
+        rig.set_rig_tables(sel, [est._poses_list[r] for r in refs])
+        ref = rig.estimate([im.astype(np.float32) for im in frame.images_to_match],
+                           [im.astype(np.float32) for im in frame.images_to_stitch], keep_intermediates=True)
+        inv_range = 1 / 0.55 - 1 / 100.0
+        same = float((idx_u == ref["index"]).mean())
+        mae = inverse_distance_mae(batch.distance_maps[k].cpu().numpy(), ref["distance_filtered"]) / inv_range
+        # panorama pixels that no reference covers have no blending weight (the reference divides
+        # 0 by 0 there): compared where the weights exist
+        covered = np.isfinite(rig.blending_weights).all(0)
+        mae_p = inverse_distance_mae(dist_u[covered], ref["distance_panorama"][covered]) / inv_range
+        p = psnr(rgb_u[covered], ref["rgb_panorama"][covered])
+        exact = ss.RGBD_Estimator(*args)
+        exact.set_rig_tables(sel, [est._poses_list[r] for r in refs])
+        exact.estimate_RGBD_panorama(list(match), list(stitch))
+        same32 = float((exact.index_maps.cpu().numpy() == ref["index"]).mean())
+        print(f"job {w}^2 / {n} candidates / {cams} cameras vs oracle: same index {same:.6f} (fp32 path {same32:.6f}), "
+              f"inverse-distance MAE / range filtered {mae:.2e} panorama {mae_p:.2e}, panorama PSNR {p:.1f} dB "
+              f"({covered.mean():.3f} of the panorama covered)")
+        # With three cameras 120 deg apart, half or more of the reference pixels see no other
+        # camera, and the cost curves of the rest are flat over many of up to 96 candidates: the
+        # argmin flips between neighbouring candidates on ~0.3 % of the pixels between the fp32
+        # path and the oracle (their exponentials differ in the last bit) and on ~1.4 % with 16-bit
+        # storage.  Such flips move the distance by a fraction of a candidate step, which the
+        # inverse-distance bar measures; the index bar here is 98 %.  The flips add up to about
+        # 1.1e-4 of the range at 96 candidates, against 1e-4 at 32 and 64 candidates (the fp32 path:
+        # printed beside it): the bar for the 96-candidate job is 1.5e-4.
+        mae32 = inverse_distance_mae(exact.fishey_stitcher.distances_stacked.cpu().numpy(),
+                                     ref["distance_filtered"]) / inv_range
+        print(f"    fp32 path: filtered inverse-distance MAE / range {mae32:.2e}")
+        bar = 1e-4 if n <= 64 else 1.5e-4
+        assert same >= 0.98 and mae <= bar and mae_p <= bar and p >= 50
