@@ -85,6 +85,16 @@ typedef struct {
 #define SSG_TUNE_HOLE_PERSISTENT 8    /* hole filling: 1 = the steps after the first in one cooperative
                                          launch, separated by grid-wide barriers; 0 = a launch per
                                          step (default) */
+#define SSG_TUNE_SWEEP_TILES 9        /* the batched sweep's blocks: 0 = consecutive pixels of a row;
+                                         16 or 32 = tiles that many pixels wide, threads / width rows
+                                         high */
+#define SSG_TUNE_HOLE_TAIL 10         /* uniform batched hole filling: from this step on, one block per
+                                         map runs every remaining step (3, 4, 6 or 8); 0 = a launch per
+                                         step to the end */
+#define SSG_TUNE_SELECT_WHOLE 11      /* the last ISB level fused with the selection, at most 32
+                                         candidates: 1 = every chunk's coarse tile staged at once, no
+                                         block barrier between chunks (same bits; default); 0 =
+                                         double-buffered chunk tiles */
 #define SSG_TUNE_TMA_WITHHOLD 7       /* tests of the bounded TMA wait: 1 = the TMA-staged upsampling arms
                                          its tile barriers but issues no copy, so every block's first
                                          wait runs out (after a short limit), it writes nothing and

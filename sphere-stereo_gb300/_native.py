@@ -32,6 +32,9 @@ TUNE_ISB_SELECT_BLOCKS = 5
 TUNE_ISB_TILE_TMA = 6
 TUNE_TMA_WITHHOLD = 7
 TUNE_HOLE_PERSISTENT = 8
+TUNE_SWEEP_TILES = 9
+TUNE_HOLE_TAIL = 10
+TUNE_SELECT_WHOLE = 11
 STATUS_TMA_TIMEOUT = 1
 STATUS_BARRIER_TIMEOUT = 2
 HOLE_SCRATCH_HEADER = 8
@@ -237,11 +240,18 @@ def pointers(values) -> ctypes.Array:
 
 
 def hole_filling_launches(iterations: int) -> int:
-    """Kernels one batched hole filling launches: the scan and step 1, then one cooperative launch
-    for the other steps or one launch per step (SSG_TUNE_HOLE_PERSISTENT)."""
+    """Kernels one batched hole filling of a uniform batch launches: the scan and step 1, then one
+    cooperative launch for the other steps (SSG_TUNE_HOLE_PERSISTENT), or a launch per step up to
+    the tail (SSG_TUNE_HOLE_TAIL) and two for the tail."""
     if iterations <= 1:
         return 2 * iterations
-    return 3 if library().ssg_tuning_get(TUNE_HOLE_PERSISTENT) == 1 else 1 + iterations
+    lib = library()
+    if lib.ssg_tuning_get(TUNE_HOLE_PERSISTENT) == 1:
+        return 3
+    tail = lib.ssg_tuning_get(TUNE_HOLE_TAIL)
+    if tail > 0 and iterations >= tail:
+        return tail + 2
+    return 1 + iterations
 
 
 def kernels_launched(name: str, args) -> int:

@@ -34,6 +34,9 @@ KNOBS = {
     "isb_select_blocks": (N.TUNE_ISB_SELECT_BLOCKS, ("ssg_isb_upsample_select_batch",)),
     "isb_tile_tma": (N.TUNE_ISB_TILE_TMA, ("ssg_isb_upsample_batch", "ssg_isb_upsample_select_batch")),
     "hole_persistent": (N.TUNE_HOLE_PERSISTENT, ("ssg_inpaint_holes_batch",)),
+    "sweep_tiles": (N.TUNE_SWEEP_TILES, ("ssg_sweep_cost_batch",)),
+    "hole_tail": (N.TUNE_HOLE_TAIL, ("ssg_inpaint_holes_batch",)),
+    "select_whole": (N.TUNE_SELECT_WHOLE, ("ssg_isb_upsample_select_batch",)),
 }
 
 

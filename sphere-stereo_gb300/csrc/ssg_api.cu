@@ -68,6 +68,8 @@ constexpr int kHoleBlocks[] = {2, 4, 8};
 constexpr int kMergeFramesValues[] = {2, 4, 8};
 constexpr int kUnevenSpans[] = {1, 2, 4};
 constexpr int kIsbUpBlocks[] = {2, 3};
+constexpr int kSweepTiles[] = {0, 16, 32};
+constexpr int kHoleTail[] = {0, 3, 4, 6, 8};
 Knob g_knobs[] = {
     {kSweepVariants, 4, {0}},      // SSG_TUNE_SWEEP_VARIANT
     {kHoleBlocks, 3, {4}},         // SSG_TUNE_HOLE_BLOCKS_PER_SM
@@ -78,6 +80,9 @@ Knob g_knobs[] = {
     {kOnOff, 2, {0}},              // SSG_TUNE_ISB_TILE_TMA
     {kOnOff, 2, {0}},              // SSG_TUNE_TMA_WITHHOLD
     {kOnOff, 2, {0}},              // SSG_TUNE_HOLE_PERSISTENT
+    {kSweepTiles, 3, {16}},        // SSG_TUNE_SWEEP_TILES
+    {kHoleTail, 5, {8}},           // SSG_TUNE_HOLE_TAIL
+    {kOnOff, 2, {1}},              // SSG_TUNE_SELECT_WHOLE
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

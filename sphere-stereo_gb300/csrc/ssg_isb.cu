@@ -13,9 +13,11 @@
 // Guides, range weights and cost sums use the reference's arithmetic in its order
 // (ssg_isb_common.cuh), so both layouts give the same bits; the batched path differs from the
 // reference only by the 16-bit rounding of its level-0 volume.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 #include "ssg_cells.cuh"
 #include "ssg_isb_common.cuh"
@@ -620,6 +622,115 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
 }
 
 // ---------------------------------------------------------------------------------------------
+// The selecting level with every chunk's tile staged at once (SSG_TUNE_SELECT_WHOLE, volumes of
+// at most kWholeChunks chunks): the block copies the coarse neighbourhood of all its candidates
+// with cp.async, waits once, and filters every chunk without a block barrier between chunks.
+// The threads, fine pixels, tile layout and arithmetic are those of isb_up_block<8, Tf, true>
+// (same bits); the tiles live in dynamic shared memory (12.5 KB per chunk).
+// ---------------------------------------------------------------------------------------------
+constexpr int kWholeChunks = 4;
+
+template <typename Tf, int kBlocks>
+__global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_select_whole_kernel(
+    const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in, const uint8_t* __restrict__ guide_fine,
+    Tf* __restrict__ cost_fine, LevelGeom g, int chunks, int ncand, float weight_up, float weight_down,
+    float var_inv_i, const float* __restrict__ table, SelectOut so)
+{
+    extern __shared__ __align__(128) float whole_smem[];
+    float* lut = whole_smem;                          // kRangeLutStride floats (a multiple of 32)
+    float* tiles = whole_smem + kRangeLutStride;      // chunks x UpTile<8>::floats, 128-byte aligned
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
+    const int inst = blockIdx.z;
+    guide_in += (int64_t)inst * pin * G4::bytes;
+    cost_in += (int64_t)inst * chunks * pin * 8;
+    guide_fine += (int64_t)inst * pio * G4::bytes;
+    cost_fine += (int64_t)inst * chunks * pio * 8;
+    const int x0 = blockIdx.x * kUpTileX, y = blockIdx.y;
+    // the whole neighbourhood streams in while the range table and the weights are formed
+    for (int c = 0; c < chunks; ++c)
+        load_tile_async<8>(tiles + c * UpTile<8>::floats, cost_in + (int64_t)c * pin * 8, g.rows_in, g.cols_in, x0, y);
+    cp_async_commit();
+    load_range_lut(lut, table, var_inv_i);
+    __syncthreads();  // the range table is filled
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int kind = warp >> 2;  // warp-uniform
+    const int lx = (warp & 3) * 32 + lane, x = x0 + lx;
+    const bool coarse_ok = x < g.cols_in;
+    const LutRange range{lut};
+    FinePixel pa, pb;
+    {
+        int ci[9];
+        G4::Pix gd[9];
+        if (coarse_ok) coarse_neighbourhood<int, G4>(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+        if (kind == 0) {
+            fine_setup<0, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<3, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
+        } else {
+            fine_setup<1, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<2, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
+        }
+    }
+    Selector sa, sb;
+    RawCell<8, Tf> ra, rb;
+    ra.load(cost_fine + (int64_t)pa.index * 8);
+    rb.load(cost_fine + (int64_t)pb.index * 8);
+    asm volatile("cp.async.wait_all;\n" ::);
+    __syncthreads();  // every chunk's tile has landed
+    for (int c = 0; c < chunks; ++c) {
+        RawCell<8, Tf> na = ra, nb = rb;  // the next chunk's fine cells, a chunk ahead
+        if (c + 1 < chunks) {
+            const Tf* next = cost_fine + (int64_t)(c + 1) * pio * 8;
+            na.load(next + (int64_t)pa.index * 8);
+            nb.load(next + (int64_t)pb.index * 8);
+        }
+        const float* buf = tiles + c * UpTile<8>::floats;
+        Tf* fine_chunk = cost_fine + (int64_t)c * pio * 8;
+        if (kind == 0)
+            up_chunk<0, 3, 8, Tf, true>(buf, lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+        else
+            up_chunk<1, 2, 8, Tf, true>(buf, lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+        ra = na;
+        rb = nb;
+    }
+    so.distance += (int64_t)inst * pio;
+    if (so.distance2) so.distance2 += (int64_t)inst * pio;
+    if (so.index) so.index += (int64_t)inst * pio;
+    if (pa.active) {
+        const float d = select_from(sa, ncand, so.d0, so.dl, so.q);
+        so.distance[pa.index] = d;
+        if (so.distance2) so.distance2[pa.index] = d;
+        if (so.index) so.index[pa.index] = sa.idx;
+    }
+    if (pb.active) {
+        const float d = select_from(sb, ncand, so.d0, so.dl, so.q);
+        so.distance[pb.index] = d;
+        if (so.distance2) so.distance2[pb.index] = d;
+        if (so.index) so.index[pb.index] = sb.idx;
+    }
+}
+
+template <typename Tf, int kBlocks>
+static cudaError_t launch_select_whole(dim3 grid, cudaStream_t st, const uint8_t* gi, const float* ci,
+                                       const uint8_t* gio, Tf* cf, const LevelGeom& g, int chunks, int ncand,
+                                       float wu, float wd, float var_inv_i, const float* table, const SelectOut& so)
+{
+    const size_t bytes = sizeof(float) * (kRangeLutStride + (size_t)kWholeChunks * UpTile<8>::floats);
+    static std::atomic<int> opted[64] = {};  // per device: the opt-in above 48 KB is set once
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !opted[dev].load()) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(isb_select_whole_kernel<Tf, kBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bytes);
+        if (e != cudaSuccess) return e;
+        opted[dev].store(1);
+    }
+    const size_t used = sizeof(float) * (kRangeLutStride + (size_t)chunks * UpTile<8>::floats);
+    isb_select_whole_kernel<Tf, kBlocks><<<grid, kBatchBlock, used, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu, wd,
+                                                                          var_inv_i, table, so);
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Single-candidate upsampling (W = 1: planar one-candidate volumes and the distance post-filter).
 // One thread per coarse pixel filters its four fine pixels: the 3x3 coarse guides and values are
 // read once (neighbouring threads share them through L1) and each fine pixel's weights are formed
@@ -941,6 +1052,17 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     const dim3 grid = up_grid(cc, rc, instances);
+    if constexpr (W == 8 && kSelect && std::is_same<GL, G4>::value) {
+        if (tuning(SSG_TUNE_SELECT_WHOLE) == 1 && tuning(SSG_TUNE_ISB_TILE_TMA) == 0 && chunks <= kWholeChunks) {
+            const cudaError_t e =
+                tuning(SSG_TUNE_ISB_SELECT_BLOCKS) == 3
+                    ? launch_select_whole<Tf, 3>(grid, st, gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so)
+                    : launch_select_whole<Tf, 2>(grid, st, gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table,
+                                                 so);
+            if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "isb_select_whole_kernel: %s", cudaGetErrorString(e));
+            return launch_status("isb_select_whole_kernel");
+        }
+    }
     if constexpr (W == 8) {
         // the coarse level of every instance as one tensor [planes][rows][cols][8 floats], plane =
         // instance * chunks + chunk, read in boxes of 4 floats x kUpTileCols x 3 rows

@@ -727,6 +727,81 @@ __device__ __forceinline__ int hole_frontier_step(const Maps& maps, float* __res
     return n;
 }
 
+// ---------------------------------------------------------------------------------------------
+// The tail of the hole filling (the uniform batch): after the first steps, a step fills a few
+// hundred holes per map, and a launch per step costs more than its work.  A hole only reads
+// pixels of its own map, so the later steps of a map depend on nothing outside it: one block per
+// map runs them all, separated by block barriers, with its frontier lists in its map's own region
+// of the list arrays.  hole_tail_collect_kernel first gives each map the entries of the global
+// list (the fills of step first - 1) that lie in it: region[0] is their count, region[1..] the
+// pixels; hole_tail_kernel then runs steps first .. iterations with the same per-hole work as
+// hole_frontier_step, so the results are those of the launches per step.
+// ---------------------------------------------------------------------------------------------
+constexpr int kTailBlock = 1024;
+
+__global__ void __launch_bounds__(kStitchBlock) hole_tail_collect_kernel(int64_t map_pixels,
+                                                                         const int32_t* __restrict__ count,
+                                                                         const int32_t* __restrict__ list,
+                                                                         int32_t* __restrict__ regions)
+{
+    __shared__ int n_map;
+    const int64_t begin = (int64_t)blockIdx.x * map_pixels, end = begin + map_pixels;
+    if (threadIdx.x == 0) n_map = 0;
+    __syncthreads();
+    const int n = *count;
+    for (int h = threadIdx.x; h < n; h += blockDim.x) {
+        const int32_t g = list[h];
+        if (g >= begin && g < end) regions[begin + 1 + atomicAdd(&n_map, 1)] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) regions[begin] = n_map;
+}
+
+template <typename Maps>
+__global__ void __launch_bounds__(kTailBlock) hole_tail_kernel(const Maps maps, int64_t map_pixels,
+                                                               float* __restrict__ map, uint8_t* __restrict__ stamp,
+                                                               int32_t* __restrict__ claim, int first, int iterations,
+                                                               int32_t* __restrict__ regions_a,
+                                                               int32_t* __restrict__ regions_b, float valid_at_most)
+{
+    __shared__ int n_cur, n_next;
+    const int64_t begin = (int64_t)blockIdx.x * map_pixels;
+    int32_t* cur = regions_a + begin + 1;  // region[0] holds the collected count
+    int32_t* nxt = regions_b + begin + 1;
+    if (threadIdx.x == 0) n_cur = regions_a[begin];
+    __syncthreads();
+    for (int step = first; step <= iterations; ++step) {
+        const int nc = n_cur;  // the same value in every thread: the loop ends for the whole block
+        if (nc == 0) break;
+        if (threadIdx.x == 0) n_next = 0;
+        __syncthreads();
+        for (int64_t h = threadIdx.x; h < (int64_t)nc * 8; h += blockDim.x) {
+            const int64_t p = cur[h >> 3];
+            const int k = (int)(h & 7);
+            const int dx = k < 3 ? k - 1 : k == 3 ? -1 : k == 4 ? 1 : k - 6;  // the 8 neighbours
+            const int dy = k < 3 ? -1 : k < 5 ? 0 : 1;
+            const MapPixel m = maps.at(p);
+            const int qx = m.x + dx, qy = m.y + dy;
+            if (qx >= 1 && qy >= 1 && qx < m.cols - 1 && qy < m.rows - 1) {
+                const int64_t q = p + (int64_t)dy * m.cols + dx;
+                if (stamp[q] == kUnfilled) {
+                    const HoleOffsets o = hole_offsets(m.table[(int64_t)qy * m.cols + qx], q, m.cols);
+                    // q reads p, and no other thread has taken q for this step
+                    if (((o.w0 > 0.0f && o.n0 == p) || (o.w1 > 0.0f && o.n1 == p)) &&
+                        atomicMax(claim + q, step) < step && fill_hole(map, stamp, q, o, step, valid_at_most))
+                        nxt[atomicAdd(&n_next, 1)] = (int32_t)q;
+                }
+            }
+        }
+        __syncthreads();  // this step's fills are visible to the block before the next step reads them
+        int32_t* t = cur;
+        cur = nxt;
+        nxt = t;
+        if (threadIdx.x == 0) n_cur = n_next;
+        __syncthreads();
+    }
+}
+
 template <typename Maps>
 __global__ void __launch_bounds__(kStitchBlock) hole_first_step_kernel(const Maps maps, float* __restrict__ map,
                                                                        uint8_t* __restrict__ stamp,
@@ -865,9 +940,11 @@ static int persistent_blocks_per_sm()
     return n > 0 ? n : 0;
 }
 
+// tail_map_pixels: pixels of each map when all maps have one size (the uniform batch), enabling
+// the per-map tail of the later steps; 0 otherwise
 template <typename Maps>
 static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t* d_stamps, int32_t* d_holes,
-                         double max_dist, int iterations, cudaStream_t st)
+                         double max_dist, int iterations, cudaStream_t st, int64_t tail_map_pixels = 0)
 {
     if (iterations == 0) return SSG_OK;
     const float hole = float_at_least(max_dist + 0.1);
@@ -901,10 +978,26 @@ static int inpaint_lists(const Maps& maps, int64_t total, float* d_map, uint8_t*
         if (le != cudaSuccess) return fail(SSG_ERR_CUDA, "hole_fill_persistent_kernel: %s", cudaGetErrorString(le));
         return SSG_OK;
     }
-    for (int s = 2; s <= iterations; ++s) {
+    // the uniform batch: a launch per step up to the tail, then one block per map for the rest
+    const int first_tail = tail_map_pixels > 0 ? tuning(SSG_TUNE_HOLE_TAIL) : 0;
+    const int last_launched = first_tail > 0 ? std::min(iterations, first_tail - 1) : iterations;
+    for (int s = 2; s <= last_launched; ++s) {
         hole_frontier_step_kernel<Maps><<<grid, kStitchBlock, 0, st>>>(maps, d_map, d_stamps, claims, s, counts,
                                                                        lists[(s - 1) % 2], lists[s % 2], ok);
         if (int err = launch_status("hole_frontier_step_kernel")) return err;
+    }
+    if (first_tail > 0 && iterations >= first_tail) {
+        const int maps_count = (int)(total / tail_map_pixels);
+        // step first_tail - 1 listed its fills in lists[(first_tail - 1) % 2], counted by
+        // counts[(first_tail - 1) % 3]; the tail's first regions go into the other array
+        int32_t* in = lists[(first_tail - 1) % 2];
+        int32_t* other = lists[first_tail % 2];
+        hole_tail_collect_kernel<<<maps_count, kStitchBlock, 0, st>>>(tail_map_pixels,
+                                                                      counts + (first_tail - 1) % 3, in, other);
+        if (int err = launch_status("hole_tail_collect_kernel")) return err;
+        hole_tail_kernel<Maps><<<maps_count, kTailBlock, 0, st>>>(maps, tail_map_pixels, d_map, d_stamps, claims,
+                                                                  first_tail, iterations, other, in, ok);
+        if (int err = launch_status("hole_tail_kernel")) return err;
     }
     return SSG_OK;
 }
@@ -1472,7 +1565,7 @@ extern "C" int ssg_inpaint_holes_batch(float* d_distance, const uint8_t* d_table
                 instances, cols, rows);
     const UniformMaps maps(cols, rows, references, reinterpret_cast<const uchar2*>(d_tables));
     return inpaint_lists(maps, (int64_t)cols * rows * instances, d_distance, d_stamps, d_holes, max_dist, iterations,
-                         as_stream(stream));
+                         as_stream(stream), (int64_t)cols * rows);
 }
 
 extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, const float* d_reprojected,

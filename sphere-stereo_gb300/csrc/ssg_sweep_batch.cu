@@ -497,12 +497,22 @@ template <typename T, int V>
 __global__ void __launch_bounds__(SweepShape<V>::threads, SweepShape<V>::blocks)
     sweep_batch_kernel(const __grid_constant__ FastSweepParams p, const uint4* __restrict__ staged,
                        const float* __restrict__ floats, const int* __restrict__ plane_flags,
-                       const int8_t* __restrict__ selected, T* __restrict__ cost)
+                       const int8_t* __restrict__ selected, T* __restrict__ cost, int tiles_x, int tile_w)
 {
     const int cols = p.cols, rows = p.rows, pitch = cols + 2;
     const int P = cols * rows;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
+    int i;
+    if (tiles_x > 0) {
+        // a block covers tile_w x (threads / tile_w) pixels: the samples of neighbouring rows fall
+        // on neighbouring footprints, which the block's warps then share through L1
+        const int x = (blockIdx.x % tiles_x) * tile_w + (int)threadIdx.x % tile_w;
+        const int y = (blockIdx.x / tiles_x) * (SweepShape<V>::threads / tile_w) + (int)threadIdx.x / tile_w;
+        if (x >= cols || y >= rows) return;
+        i = y * cols + x;
+    } else {
+        i = blockIdx.x * blockDim.x + threadIdx.x;  // a block covers consecutive pixels of a row
+        if (i >= P) return;
+    }
     const int inst = blockIdx.y;  // frame * references + slot
     const int frame = inst / p.references, slot = inst % p.references;
     const int plane = pitch * (rows + 2);
@@ -607,8 +617,16 @@ static void launch_sweep_shape(const FastSweepParams& p, const uint4* staged, co
                                const int8_t* selected, T* cost, int64_t P, int instances, cudaStream_t st)
 {
     constexpr int threads = SweepShape<V>::threads;
-    const dim3 grid(grid_1d(P, threads), instances);
-    sweep_batch_kernel<T, V><<<grid, threads, 0, st>>>(p, staged, floats, flags, selected, cost);
+    const int tile_w = tuning(SSG_TUNE_SWEEP_TILES);  // 0: rows; else the tile width
+    if (tile_w > 0) {
+        const int th = threads / tile_w;
+        const int tiles_x = (p.cols + tile_w - 1) / tile_w, tiles_y = (p.rows + th - 1) / th;
+        sweep_batch_kernel<T, V><<<dim3((unsigned)(tiles_x * tiles_y), instances), threads, 0, st>>>(
+            p, staged, floats, flags, selected, cost, tiles_x, tile_w);
+    } else {
+        const dim3 grid(grid_1d(P, threads), instances);
+        sweep_batch_kernel<T, V><<<grid, threads, 0, st>>>(p, staged, floats, flags, selected, cost, 0, 0);
+    }
 }
 
 template <typename T>

@@ -11,10 +11,10 @@ One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_p
     ssg_isb_upsample_select_batch  last level + argmin / sub-candidate step             1
     ssg_isb_apply_batch            distance post-filter, fp32, N = 1                    2L - 2
     ssg_reproject_distance_batch_approx  fill + z-buffer                                2
-    ssg_inpaint_holes_batch        hole filling: a scan, then 32 steps on hole lists    33 (or 3)
+    ssg_inpaint_holes_batch        hole filling: a scan, steps on hole lists, a tail    6
     ssg_merge_panorama_batch_approx panoramas                                           1
 
-so the launch count does not grow with F (about 70 at 1024^2).  Buffers are allocated once for
+so the launch count does not grow with F (about 45 at 1024^2).  Buffers are allocated once for
 the largest batch; outputs alias them, as the reference's outputs alias its stitcher buffers.
 """
 from __future__ import annotations
@@ -304,8 +304,8 @@ class BatchPipeline:
                 self._graphs[key] = graph
             graph.replay()
 
-    TUNED_KNOBS = ("sweep_variant", "isb_up_blocks", "isb_select_blocks", "isb_tile_tma", "hole_blocks_per_sm",
-                   "hole_persistent", "merge_frames")
+    TUNED_KNOBS = ("sweep_variant", "sweep_tiles", "isb_up_blocks", "select_whole", "isb_select_blocks",
+                   "isb_tile_tma", "hole_blocks_per_sm", "hole_persistent", "hole_tail", "merge_frames")
     GROUP_CHOICES = (1, 2, 4)
 
     def _apply_tuning(self, match, stitch, frames) -> None:

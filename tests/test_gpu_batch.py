@@ -355,3 +355,26 @@ def test_tma_tiles_equal_cp_async_tiles(ss, native, golden_c1):
         torch.testing.assert_close(a, b, rtol=0, atol=0)
     N.call("ssg_take_device_status", ctypes.byref(status))
     assert status.value == 0
+
+
+@pytest.mark.parametrize("storage", ["fp16", "unorm16"])
+def test_select_whole_tiles_equal_double_buffered_tiles(ss, native, golden_c1, storage):
+    """The selecting level with every chunk's coarse tile staged at once gives the bits of the
+    double-buffered chunk tiles, at both register bounds."""
+    import importlib
+
+    tune = importlib.import_module("sphere-stereo_gb300.autotune")
+    g = golden_c1
+    outs = {}
+    for whole in (0, 1):
+        for blocks in (2, 3):
+            tune.set_knob("select_whole", whole)
+            tune.set_knob("isb_select_blocks", blocks)
+            est, _ = _estimator(ss, g, storage, max_batch=2, graphs=False)
+            match, stitch = _batch(g, frames=2)
+            rgb, d = est.estimate_RGBD_panoramas(match, stitch)
+            pipe = est.pipeline()
+            outs[whole, blocks] = (rgb.clone(), d.clone(), pipe.distance.clone(), pipe.index.clone())
+    for key, out in outs.items():
+        for a, b in zip(outs[0, 2], out):
+            torch.testing.assert_close(a, b, rtol=0, atol=0, msg=f"select_whole / blocks {key}")

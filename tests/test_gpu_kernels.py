@@ -250,14 +250,17 @@ def test_inpaint_iteration_counts(ss, native, dev_oracle, iterations):
     np.testing.assert_array_equal(src.cpu().numpy(), dev_oracle.inpaint(d, table, 100.0, iterations))
 
 
-@pytest.mark.parametrize("persistent", [1, 0])
+@pytest.mark.parametrize("mode", ["steps", "persistent", "tail3", "tail8"])
 @pytest.mark.parametrize("iterations", [0, 1, 2, 5, 32, 33, 254])
-def test_inpaint_hole_list_batch(ss, native, dev_oracle, iterations, persistent):
+def test_inpaint_hole_list_batch(ss, native, dev_oracle, iterations, mode):
     """The hole lists (one scan, a first step over every fillable hole, then steps over the holes
     next to the last step's fills) equal one Jacobi step per launch on every map of the batch;
-    tables are per reference slot.  Both forms: one cooperative launch whose steps are separated
-    by grid-wide barriers, and a launch per step."""
-    ss._native.call("ssg_tuning_set", ss._native.TUNE_HOLE_PERSISTENT, persistent)
+    tables are per reference slot.  Every form of the later steps: a launch per step, one
+    cooperative launch whose steps are separated by grid-wide barriers, and one block per map for
+    the steps from 3 or 8 on."""
+    N = ss._native
+    N.call("ssg_tuning_set", N.TUNE_HOLE_PERSISTENT, 1 if mode == "persistent" else 0)
+    N.call("ssg_tuning_set", N.TUNE_HOLE_TAIL, int(mode[4:]) if mode.startswith("tail") else 0)
     rng = np.random.default_rng(100 + iterations)
     H, W, refs, frames = 61, 97, 2, 3
     inst = refs * frames
