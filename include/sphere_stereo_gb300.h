@@ -95,6 +95,7 @@ typedef struct {
                                          candidates: 1 = every chunk's coarse tile staged at once, no
                                          block barrier between chunks (same bits; default); 0 =
                                          double-buffered chunk tiles */
+#define SSG_TUNE_UP_WHOLE 12          /* the same for the chunked coarse upsampling steps (default 0) */
 #define SSG_TUNE_TMA_WITHHOLD 7       /* tests of the bounded TMA wait: 1 = the TMA-staged upsampling arms
                                          its tile barriers but issues no copy, so every block's first
                                          wait runs out (after a short limit), it writes nothing and

@@ -35,6 +35,7 @@ TUNE_HOLE_PERSISTENT = 8
 TUNE_SWEEP_TILES = 9
 TUNE_HOLE_TAIL = 10
 TUNE_SELECT_WHOLE = 11
+TUNE_UP_WHOLE = 12
 STATUS_TMA_TIMEOUT = 1
 STATUS_BARRIER_TIMEOUT = 2
 HOLE_SCRATCH_HEADER = 8

@@ -37,6 +37,7 @@ KNOBS = {
     "sweep_tiles": (N.TUNE_SWEEP_TILES, ("ssg_sweep_cost_batch",)),
     "hole_tail": (N.TUNE_HOLE_TAIL, ("ssg_inpaint_holes_batch",)),
     "select_whole": (N.TUNE_SELECT_WHOLE, ("ssg_isb_upsample_select_batch",)),
+    "up_whole": (N.TUNE_UP_WHOLE, ("ssg_isb_upsample_batch",)),
 }
 
 

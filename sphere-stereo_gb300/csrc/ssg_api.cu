@@ -83,6 +83,7 @@ Knob g_knobs[] = {
     {kSweepTiles, 3, {16}},        // SSG_TUNE_SWEEP_TILES
     {kHoleTail, 5, {8}},           // SSG_TUNE_HOLE_TAIL
     {kOnOff, 2, {1}},              // SSG_TUNE_SELECT_WHOLE
+    {kOnOff, 2, {0}},              // SSG_TUNE_UP_WHOLE
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

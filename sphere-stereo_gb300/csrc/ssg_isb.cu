@@ -622,17 +622,18 @@ __device__ __forceinline__ void isb_up_block(const uint8_t* __restrict__ guide_i
 }
 
 // ---------------------------------------------------------------------------------------------
-// The selecting level with every chunk's tile staged at once (SSG_TUNE_SELECT_WHOLE, volumes of
-// at most kWholeChunks chunks): the block copies the coarse neighbourhood of all its candidates
-// with cp.async, waits once, and filters every chunk without a block barrier between chunks.
-// The threads, fine pixels, tile layout and arithmetic are those of isb_up_block<8, Tf, true>
+// Chunked upsampling with every chunk's tile staged at once (SSG_TUNE_SELECT_WHOLE for the level
+// fused with the selection, SSG_TUNE_UP_WHOLE for the coarse levels; volumes of at most
+// kWholeChunks chunks): the block copies the coarse neighbourhood of all its candidates with
+// cp.async, waits once, and filters every chunk without a block barrier between chunks.  The
+// threads, fine pixels, tile layout and arithmetic are those of isb_up_block<8, Tf, kSelect>
 // (same bits); the tiles live in dynamic shared memory (12.5 KB per chunk).
 // ---------------------------------------------------------------------------------------------
 constexpr int kWholeChunks = 4;
 
-template <typename Tf, int kBlocks>
-__global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_select_whole_kernel(
-    const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in, const uint8_t* __restrict__ guide_fine,
+template <typename Tf, bool kSelect, int kBlocks>
+__global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_up_whole_kernel(
+    const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in, uint8_t* __restrict__ guide_fine,
     Tf* __restrict__ cost_fine, LevelGeom g, int chunks, int ncand, float weight_up, float weight_down,
     float var_inv_i, const float* __restrict__ table, SelectOut so)
 {
@@ -662,36 +663,39 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_select_whole_kernel(
         int ci[9];
         G4::Pix gd[9];
         if (coarse_ok) coarse_neighbourhood<int, G4>(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+        // the coarse levels form the filtered fine guide; the selecting level's is never read
+        constexpr bool kG = !kSelect;
         if (kind == 0) {
-            fine_setup<0, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
-            fine_setup<3, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
+            fine_setup<0, kG, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<3, kG, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
         } else {
-            fine_setup<1, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
-            fine_setup<2, false, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
+            fine_setup<1, kG, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pa);
+            fine_setup<2, kG, G4>(gd, guide_fine, g, x, y, coarse_ok, weight_up, weight_down, range, pb);
         }
     }
     Selector sa, sb;
     RawCell<8, Tf> ra, rb;
-    ra.load(cost_fine + (int64_t)pa.index * 8);
-    rb.load(cost_fine + (int64_t)pb.index * 8);
+    if (kSelect || pa.active) ra.load(cost_fine + (int64_t)pa.index * 8);
+    if (kSelect || pb.active) rb.load(cost_fine + (int64_t)pb.index * 8);
     asm volatile("cp.async.wait_all;\n" ::);
     __syncthreads();  // every chunk's tile has landed
     for (int c = 0; c < chunks; ++c) {
         RawCell<8, Tf> na = ra, nb = rb;  // the next chunk's fine cells, a chunk ahead
         if (c + 1 < chunks) {
             const Tf* next = cost_fine + (int64_t)(c + 1) * pio * 8;
-            na.load(next + (int64_t)pa.index * 8);
-            nb.load(next + (int64_t)pb.index * 8);
+            if (kSelect || pa.active) na.load(next + (int64_t)pa.index * 8);
+            if (kSelect || pb.active) nb.load(next + (int64_t)pb.index * 8);
         }
         const float* buf = tiles + c * UpTile<8>::floats;
         Tf* fine_chunk = cost_fine + (int64_t)c * pio * 8;
         if (kind == 0)
-            up_chunk<0, 3, 8, Tf, true>(buf, lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+            up_chunk<0, 3, 8, Tf, kSelect>(buf, lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
         else
-            up_chunk<1, 2, 8, Tf, true>(buf, lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
+            up_chunk<1, 2, 8, Tf, kSelect>(buf, lx, fine_chunk, c, ncand, weight_up, pa, pb, ra, rb, sa, sb);
         ra = na;
         rb = nb;
     }
+    if constexpr (!kSelect) return;
     so.distance += (int64_t)inst * pio;
     if (so.distance2) so.distance2 += (int64_t)inst * pio;
     if (so.index) so.index += (int64_t)inst * pio;
@@ -709,24 +713,23 @@ __global__ void __launch_bounds__(kBatchBlock, kBlocks) isb_select_whole_kernel(
     }
 }
 
-template <typename Tf, int kBlocks>
-static cudaError_t launch_select_whole(dim3 grid, cudaStream_t st, const uint8_t* gi, const float* ci,
-                                       const uint8_t* gio, Tf* cf, const LevelGeom& g, int chunks, int ncand,
-                                       float wu, float wd, float var_inv_i, const float* table, const SelectOut& so)
+template <typename Tf, bool kSelect, int kBlocks>
+static cudaError_t launch_up_whole(dim3 grid, cudaStream_t st, const uint8_t* gi, const float* ci, uint8_t* gio, Tf* cf,
+                                   const LevelGeom& g, int chunks, int ncand, float wu, float wd, float var_inv_i,
+                                   const float* table, const SelectOut& so)
 {
     const size_t bytes = sizeof(float) * (kRangeLutStride + (size_t)kWholeChunks * UpTile<8>::floats);
     static std::atomic<int> opted[64] = {};  // per device: the opt-in above 48 KB is set once
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !opted[dev].load()) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(isb_select_whole_kernel<Tf, kBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bytes);
+        const cudaError_t e = cudaFuncSetAttribute(isb_up_whole_kernel<Tf, kSelect, kBlocks>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         if (e != cudaSuccess) return e;
         opted[dev].store(1);
     }
     const size_t used = sizeof(float) * (kRangeLutStride + (size_t)chunks * UpTile<8>::floats);
-    isb_select_whole_kernel<Tf, kBlocks><<<grid, kBatchBlock, used, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu, wd,
-                                                                          var_inv_i, table, so);
+    isb_up_whole_kernel<Tf, kSelect, kBlocks><<<grid, kBatchBlock, used, st>>>(gi, ci, gio, cf, g, chunks, ncand, wu,
+                                                                               wd, var_inv_i, table, so);
     return cudaSuccess;
 }
 
@@ -1052,15 +1055,17 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     const dim3 grid = up_grid(cc, rc, instances);
-    if constexpr (W == 8 && kSelect && std::is_same<GL, G4>::value) {
-        if (tuning(SSG_TUNE_SELECT_WHOLE) == 1 && tuning(SSG_TUNE_ISB_TILE_TMA) == 0 && chunks <= kWholeChunks) {
+    if constexpr (W == 8 && std::is_same<GL, G4>::value) {
+        if (tuning(kSelect ? SSG_TUNE_SELECT_WHOLE : SSG_TUNE_UP_WHOLE) == 1 && tuning(SSG_TUNE_ISB_TILE_TMA) == 0 &&
+            chunks <= kWholeChunks) {
+            const bool three = tuning(kSelect ? SSG_TUNE_ISB_SELECT_BLOCKS : SSG_TUNE_ISB_UP_BLOCKS) == 3;
             const cudaError_t e =
-                tuning(SSG_TUNE_ISB_SELECT_BLOCKS) == 3
-                    ? launch_select_whole<Tf, 3>(grid, st, gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table, so)
-                    : launch_select_whole<Tf, 2>(grid, st, gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i, table,
-                                                 so);
-            if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "isb_select_whole_kernel: %s", cudaGetErrorString(e));
-            return launch_status("isb_select_whole_kernel");
+                three ? launch_up_whole<Tf, kSelect, 3>(grid, st, gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i,
+                                                        table, so)
+                      : launch_up_whole<Tf, kSelect, 2>(grid, st, gi, ci, gio, cf, g, chunks, ncand, wu, wd, var_inv_i,
+                                                        table, so);
+            if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "isb_up_whole_kernel: %s", cudaGetErrorString(e));
+            return launch_status(kSelect ? "isb_up_whole_kernel<select>" : "isb_up_whole_kernel");
         }
     }
     if constexpr (W == 8) {

@@ -29,6 +29,7 @@ def test_knobs_and_choices(tune):
     assert tune.choices("sweep_tiles") == [0, 16, 32]
     assert tune.choices("hole_tail") == [0, 3, 4, 6, 8]
     assert tune.choices("select_whole") == [0, 1]
+    assert tune.choices("up_whole") == [0, 1]
     tune.set_knob("merge_frames", 8)
     assert tune.get("merge_frames") == 8
     with pytest.raises(ValueError):

@@ -359,8 +359,9 @@ def test_tma_tiles_equal_cp_async_tiles(ss, native, golden_c1):
 
 @pytest.mark.parametrize("storage", ["fp16", "unorm16"])
 def test_select_whole_tiles_equal_double_buffered_tiles(ss, native, golden_c1, storage):
-    """The selecting level with every chunk's coarse tile staged at once gives the bits of the
-    double-buffered chunk tiles, at both register bounds."""
+    """The chunked upsampling steps (coarse levels and the selecting level) with every chunk's
+    coarse tile staged at once give the bits of the double-buffered chunk tiles, at both register
+    bounds."""
     import importlib
 
     tune = importlib.import_module("sphere-stereo_gb300.autotune")
@@ -369,7 +370,9 @@ def test_select_whole_tiles_equal_double_buffered_tiles(ss, native, golden_c1, s
     for whole in (0, 1):
         for blocks in (2, 3):
             tune.set_knob("select_whole", whole)
+            tune.set_knob("up_whole", whole)
             tune.set_knob("isb_select_blocks", blocks)
+            tune.set_knob("isb_up_blocks", blocks)
             est, _ = _estimator(ss, g, storage, max_batch=2, graphs=False)
             match, stitch = _batch(g, frames=2)
             rgb, d = est.estimate_RGBD_panoramas(match, stitch)
