@@ -245,6 +245,9 @@ SSG_API int ssg_inpaint(float* d_distance, const uint8_t* d_table, float* d_scra
  *     SSG_ERR_UNSUPPORTED without launching anything.
  *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
  *     and enables the kernel's shared memory; make that first call before any stream capture.
+ *     The address is kept for the life of the process: do not reset a device (cudaDeviceReset)
+ *     after calling this on it, since the reset reloads the library's module and the kept address
+ *     would no longer be the array's.
  *   - Every call on a device shares the array: calls that overlap on the GPU (different streams
  *     without ordering) race.  Each pass overwrites the whole scratch map it uses, so nothing a
  *     previous call left there is read.

@@ -1674,7 +1674,9 @@ constexpr int64_t kNoAllocMaxPixels = int64_t(1) << 20;  // 4 MiB of float32, e.
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocMaxPixels];
 
 // Device address of g_noalloc_scratch on the current device, looked up once per device (host
-// code only sees a host-side stand-in for the symbol, never its device address).
+// code only sees a host-side stand-in for the symbol, never its device address).  Kept for the
+// life of the process: a cudaDeviceReset after the first call would leave it stale (documented
+// as unsupported at the entry point).
 static int noalloc_scratch_address(float** out)
 {
     static std::atomic<float*> cached[64] = {};

@@ -304,7 +304,9 @@ class BatchPipeline:
                 self._graphs[key] = graph
             graph.replay()
 
-    TUNED_KNOBS = ("sweep_variant", "sweep_tiles", "up_whole", "isb_up_blocks", "select_whole", "isb_select_blocks",
+    # in tuning order: a register bound before the staging it pairs with (a staging choice is timed
+    # at the bound already picked)
+    TUNED_KNOBS = ("sweep_variant", "sweep_tiles", "isb_up_blocks", "up_whole", "isb_select_blocks", "select_whole",
                    "isb_tile_tma", "hole_blocks_per_sm", "hole_persistent", "hole_tail", "merge_frames")
     GROUP_CHOICES = (1, 2, 4)
 

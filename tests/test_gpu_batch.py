@@ -381,3 +381,33 @@ def test_select_whole_tiles_equal_double_buffered_tiles(ss, native, golden_c1, s
     for key, out in outs.items():
         for a, b in zip(outs[0, 2], out):
             torch.testing.assert_close(a, b, rtol=0, atol=0, msg=f"select_whole / blocks {key}")
+
+
+def test_merge_word_and_byte_texel_reads_agree(ss, native, golden_c1):
+    """The batched merge reads RGB texel pairs as aligned 32-bit words when the images start and
+    end on 4-byte boundaries, and byte by byte otherwise: the same panoramas either way (the images
+    copied to a buffer offset by one byte take the byte path)."""
+    N = ss._native
+    g = golden_c1
+    est, _ = _estimator(ss, g, "fp16", max_batch=2, graphs=False)
+    match, stitch = _batch(g, frames=2)
+    est.estimate_RGBD_panoramas(match, stitch)
+    torch.cuda.synchronize()
+    pipe, st = est.pipeline(), est.fishey_stitcher
+    images = pipe.images_u8[:2].contiguous()
+    n = images.numel()
+    shifted = torch.empty(n + 1, dtype=torch.uint8, device=DEV)[1:]
+    shifted.copy_(images.view(-1))
+    assert shifted.data_ptr() % 4 == 1
+    outs = []
+    for imgs in (images, shifted):
+        dist = torch.empty_like(pipe.pano_distance[:2])
+        rgb = torch.empty_like(pipe.rgb[:2])
+        N.call("ssg_merge_panorama_batch_approx", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
+               pipe.reprojected.data_ptr(), pipe.distance.data_ptr(), imgs.data_ptr(), st.image_rows, st.image_cols,
+               st._trans, st._intr, pipe.R, pipe.cols, pipe.rows, st.pano_cols, st.pano_rows, 2, dist.data_ptr(),
+               rgb.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        outs.append((rgb, dist))
+    torch.testing.assert_close(outs[0][0], outs[1][0], rtol=0, atol=0)
+    torch.testing.assert_close(outs[0][1], outs[1][1], rtol=0, atol=0)
