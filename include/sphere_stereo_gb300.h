@@ -304,6 +304,20 @@ SSG_API int ssg_stage_images_u8(const uint8_t* d_images, int frames, int cameras
                                 const int* reference_cameras, int references, float* d_staged, uint8_t* d_guides,
                                 int32_t* d_plane_flags, void* stream);
 
+/* Resize and staging in one pass, from the decoded 8-bit images (python/utils.py:198-201 resizes
+ * each decoded image to the matching resolution before the estimator; python/main.py:73-81):
+ * d_images holds frames x cameras images of src_rows x src_cols x 3 bytes, resized to cols x rows
+ * with ssg_resize_linear's u8 -> float32 arithmetic and staged as ssg_stage_images stages those
+ * float32 images -- the same entries, guides and plane flags bit for bit, without the float32
+ * images in memory.  The entries are 32 bytes (sweep with ssg_sweep_cost_batch_entries,
+ * entry_bytes 32, d_images NULL: resized 8-bit values never need the float path).  d_staged
+ * 32-byte aligned.  SSG_ERR_UNSUPPORTED (resize with ssg_resize_linear and stage the result
+ * instead) when d_images is not 4-byte aligned, src_cols x src_rows is not a multiple of 4, or a
+ * tile's source window exceeds 160 KB of shared memory (reductions beyond about 2.5x). */
+SSG_API int ssg_stage_images_resized(const uint8_t* d_images, int src_cols, int src_rows, int frames, int cameras,
+                                     int cols, int rows, const int* reference_cameras, int references,
+                                     float* d_staged, uint8_t* d_guides, int32_t* d_plane_flags, void* stream);
+
 /* float32 -> uint8 truncation of `count` values in [0, 255] (the float -> uint8 copy of the images
  * to stitch, python/depth_estimation.py:239-240); 16-byte loads and stores where both buffers are
  * 16-byte aligned. */
@@ -320,6 +334,15 @@ SSG_API int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_coun
                                  const float* d_staged, const float* d_images, const int32_t* d_plane_flags,
                                  const int8_t* d_selected, const float* candidates, int candidate_count, int storage,
                                  void* d_cost, void* stream);
+/* The same with the entry size given: entry_bytes 16 (ssg_stage_images_u8) or 32
+ * (ssg_stage_images, with d_images; ssg_stage_images_resized, d_images NULL).
+ * ssg_sweep_cost_batch is this with entry_bytes = d_images ? 32 : 16. */
+SSG_API int ssg_sweep_cost_batch_entries(int cols, int rows, int frames, int camera_count,
+                                         const ssg_camera* cameras, int references, const int* reference_cameras,
+                                         const float* relative_poses, const float* d_staged, int entry_bytes,
+                                         const float* d_images, const int32_t* d_plane_flags,
+                                         const int8_t* d_selected, const float* candidates, int candidate_count,
+                                         int storage, void* d_cost, void* stream);
 
 /* ISB down / up steps (python/isb_filter.cu:44-329) on `instances` contiguous levels.  The
  * downsampling reads a level stored as `storage` and writes float32; the upsampling reads and

@@ -51,7 +51,11 @@ class NativeLibraryError(RuntimeError):
 
 
 class SSGError(RuntimeError):
-    """A library call failed on the device side."""
+    """A library call failed on the device side (``code``: the SSG_ERR_* status)."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 class ssg_camera(ctypes.Structure):
@@ -114,6 +118,9 @@ SIGNATURES = {
     "ssg_stage_images": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ssg_stage_images_u8": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ssg_sweep_cost_batch": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "ssg_stage_images_resized": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
+    "ssg_sweep_cost_batch_entries": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _I, _P, _P, _P, _P, _I, _I, _P,
+                                          _P]),
     "ssg_isb_downsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _P]),
     "ssg_isb_upsample_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P]),
     "ssg_isb_upsample_select_batch": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P,
@@ -184,7 +191,7 @@ def check(code: int, what: str) -> None:
     msg = f"{what}: {last_error()}"
     if code == SSG_ERR_INVALID_ARGUMENT:
         raise ValueError(msg)
-    raise SSGError(msg)
+    raise SSGError(msg, code)
 
 
 def call(name: str, *args) -> None:

@@ -26,7 +26,7 @@ from . import _native as N
 
 # knob name -> (SSG_TUNE_* id, the entry points whose kernels it shapes)
 KNOBS = {
-    "sweep_variant": (N.TUNE_SWEEP_VARIANT, ("ssg_sweep_cost_batch",)),
+    "sweep_variant": (N.TUNE_SWEEP_VARIANT, ("ssg_sweep_cost_batch", "ssg_sweep_cost_batch_entries")),
     "hole_blocks_per_sm": (N.TUNE_HOLE_BLOCKS_PER_SM, ("ssg_inpaint_holes_batch",)),
     "merge_frames": (N.TUNE_MERGE_FRAMES, ("ssg_merge_panorama_batch_approx",)),
     "uneven_span": (N.TUNE_UNEVEN_SPAN, ("ssg_uneven_run",)),
@@ -34,7 +34,7 @@ KNOBS = {
     "isb_select_blocks": (N.TUNE_ISB_SELECT_BLOCKS, ("ssg_isb_upsample_select_batch",)),
     "isb_tile_tma": (N.TUNE_ISB_TILE_TMA, ("ssg_isb_upsample_batch", "ssg_isb_upsample_select_batch")),
     "hole_persistent": (N.TUNE_HOLE_PERSISTENT, ("ssg_inpaint_holes_batch",)),
-    "sweep_tiles": (N.TUNE_SWEEP_TILES, ("ssg_sweep_cost_batch",)),
+    "sweep_tiles": (N.TUNE_SWEEP_TILES, ("ssg_sweep_cost_batch", "ssg_sweep_cost_batch_entries")),
     "hole_tail": (N.TUNE_HOLE_TAIL, ("ssg_inpaint_holes_batch",)),
     "select_whole": (N.TUNE_SELECT_WHOLE, ("ssg_isb_upsample_select_batch",)),
     "up_whole": (N.TUNE_UP_WHOLE, ("ssg_isb_upsample_batch",)),
@@ -165,6 +165,7 @@ class Tuner:
         best: dict[str, int] = {}
         for name in knobs:
             entries = (entry,) if entry else KNOBS[name][1]
+            before = get(name)
             timings = {}
             for value in choices(name):
                 set_knob(name, value)
@@ -177,6 +178,8 @@ class Tuner:
             if timings:
                 best[name] = min(timings, key=timings.get)
                 set_knob(name, best[name])
+            else:  # the sequence never called the knob's entry points: leave it as it was
+                set_knob(name, before)
         self.cache[key] = best
         self._save()
         return best

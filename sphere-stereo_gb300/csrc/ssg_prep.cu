@@ -3,12 +3,7 @@
 // third positional argument of cv2.resize is `dst`, so the interpolation in effect is the
 // default, INTER_LINEAR).
 //
-// The arithmetic restates OpenCV's published linear resize:
-//   - source coordinate of destination column dx: fx = float((dx + 0.5) * scale_x - 0.5) in
-//     double, scale_x = 1 / (dst_cols / src_cols); sx = floor(fx), fx -= sx; sx < 0 gives
-//     (sx, fx) = (0, 0) and sx >= src_cols - 1 gives (src_cols - 1, 0) (the second tap then has
-//     weight 0 and is not read); rows the same way, except that the row weights are kept and the
-//     rows clamped to [0, src_rows - 1];
+// The taps are ssg_resize.cuh's.  Arithmetic:
 //   - float pixels: h = S[sx] * (1 - fx) + S[sx + 1] * fx per row, then h0 * (1 - fy) + h1 * fy,
 //     each product and sum rounded separately;
 //   - uint8 pixels to uint8 (the ground-truth resize of the evaluation): 11-bit fixed-point
@@ -20,37 +15,9 @@
 #include <cmath>
 
 #include "ssg_common.cuh"
+#include "ssg_resize.cuh"
 
 namespace ssg {
-
-struct ResizeParams {
-    int src_cols, src_rows, dst_cols, dst_rows, channels;
-    double scale_x, scale_y;
-    int area2;  // exact 2x reduction on both axes
-};
-
-struct Tap {
-    int s0, s1;
-    float f;  // weight of s1
-};
-
-__device__ __forceinline__ Tap column_tap(const ResizeParams& p, int dx)
-{
-    float fx = (float)((dx + 0.5) * p.scale_x - 0.5);
-    int sx = (int)floorf(fx);
-    fx -= (float)sx;
-    if (sx < 0) fx = 0.0f, sx = 0;
-    if (sx >= p.src_cols - 1) fx = 0.0f, sx = p.src_cols - 1;
-    return Tap{sx, min(sx + 1, p.src_cols - 1), fx};
-}
-
-__device__ __forceinline__ Tap row_tap(const ResizeParams& p, int dy)
-{
-    float fy = (float)((dy + 0.5) * p.scale_y - 0.5);
-    const int sy = (int)floorf(fy);
-    fy -= (float)sy;
-    return Tap{min(max(sy, 0), p.src_rows - 1), min(max(sy + 1, 0), p.src_rows - 1), fy};
-}
 
 __device__ __forceinline__ float in_value(const float* s, int64_t i) { return __ldg(s + i); }
 __device__ __forceinline__ float in_value(const uint8_t* s, int64_t i) { return (float)__ldg(s + i); }
@@ -139,15 +106,7 @@ extern "C" int ssg_resize_linear(const void* d_src, int src_type, int src_cols, 
     SSG_REQUIRE((src_type == SSG_PIXEL_U8 || src_type == SSG_PIXEL_F32) &&
                     (dst_type == SSG_PIXEL_F32 || (dst_type == SSG_PIXEL_U8 && src_type == SSG_PIXEL_U8)),
                 "unsupported pixel types %d -> %d (u8 -> f32, f32 -> f32, u8 -> u8)", src_type, dst_type);
-    ResizeParams p{};
-    p.src_cols = src_cols;
-    p.src_rows = src_rows;
-    p.dst_cols = dst_cols;
-    p.dst_rows = dst_rows;
-    p.channels = channels;
-    p.scale_x = 1.0 / ((double)dst_cols / src_cols);
-    p.scale_y = 1.0 / ((double)dst_rows / src_rows);
-    p.area2 = src_cols == 2 * dst_cols && src_rows == 2 * dst_rows;
+    const ResizeParams p = make_resize_params(src_cols, src_rows, dst_cols, dst_rows, channels);
     const dim3 grid((unsigned)((dst_cols + kTileX - 1) / kTileX), (unsigned)((dst_rows + kTileY - 1) / kTileY),
                     (unsigned)images);
     SSG_REQUIRE(grid.y <= 65535, "destination of %d rows is too tall", dst_rows);

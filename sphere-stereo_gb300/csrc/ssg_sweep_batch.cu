@@ -9,9 +9,12 @@
 // costs are clamped to [0, 500]); the arithmetic is fp32.  The fp32 kernels of ssg_sweep.cu are
 // the ones that reproduce the reference bit for bit; this sweep projects with approximate square
 // roots and reciprocal, a change far below the 16-bit rounding of its output.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "ssg_cells.cuh"
+#include "ssg_resize.cuh"
 #include "ssg_uneven.cuh"
 
 namespace ssg {
@@ -76,19 +79,68 @@ __device__ __forceinline__ uint32_t code_bytes(uint32_t q0, uint32_t q1, uint32_
     return ((q0 >> sh) & 255u) | (((q1 >> sh) & 255u) << 8) | (((q2 >> sh) & 255u) << 16);
 }
 
-// One block: a kStageTileX x kStageTileY tile of entries from shared-memory tiles of texels.
-// Each thread converts whole texels (three consecutive values: a warp reads 384 contiguous
-// bytes per channel load), classifies them and, for the texels that are pixels of this tile,
-// writes their guide word; then each thread assembles entries from the shared tiles.  blockIdx.y:
-// frame * cameras + camera; its entries start at staged[2 * that * plane]: 16-byte entries of
-// high bytes for 8-bit inputs, 32-byte entries (high words x, y, z and low word x, then low
-// words y, z) for float inputs.
+// The texels of a tile, read from images at the matching resolution: texel (x, y) of the image
+// is three consecutive values (a warp reads 384 contiguous bytes per channel load).
 template <typename Tin>
-__global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_constant__ StageParams p,
-                                                                  const Tin* __restrict__ images,
-                                                                  uint4* __restrict__ staged,
-                                                                  uint32_t* __restrict__ guides,
-                                                                  int* __restrict__ plane_flags)
+struct ImageTexels {
+    const Tin* img;
+    int cols;
+    __device__ __forceinline__ void get(int x, int y, int, int, Tin (&v)[3]) const
+    {
+        const int64_t o = ((int64_t)y * cols + x) * 3;
+        v[0] = img[o];
+        v[1] = img[o + 1];
+        v[2] = img[o + 2];
+    }
+};
+
+// The texels of a tile resized from 8-bit source images (the linear resize of ssg_prep.cu, u8 ->
+// float32, with its taps and its separately rounded products and sums).  `win` holds the tile's
+// source window as floats (one per byte); for each texel column, `cw` gives the window offsets of
+// its two source texels' first bytes and their weights (1 - f, f), and for each texel row, `rw`
+// the window offsets of its two source rows and their weights: four floats, one 16-byte shared
+// load each.  An exact 2x reduction averages the four taps instead.
+struct TapOffsets {
+    int o0, o1;
+    float w0, w1;
+};
+
+struct ResizedTexels {
+    const float* win;
+    const TapOffsets* cw;
+    const TapOffsets* rw;
+    int area2;
+    __device__ __forceinline__ void get(int, int, int lx, int ly, float (&v)[3]) const
+    {
+        const TapOffsets tx = cw[lx], ty = rw[ly];
+        const float* r0 = win + ty.o0;
+        const float* r1 = win + ty.o1;
+        const int a = tx.o0, b = tx.o1;
+        if (area2) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                v[c] = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(r0[a + c], r0[b + c]), r1[a + c]), r1[b + c]), 0.25f);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float h0 = __fadd_rn(__fmul_rn(r0[a + c], tx.w0), __fmul_rn(r0[b + c], tx.w1));
+                const float h1 = __fadd_rn(__fmul_rn(r1[a + c], tx.w0), __fmul_rn(r1[b + c], tx.w1));
+                v[c] = __fadd_rn(__fmul_rn(h0, ty.w0), __fmul_rn(h1, ty.w1));
+            }
+        }
+    }
+};
+
+// One block: a kStageTileX x kStageTileY tile of entries from shared-memory tiles of texels.
+// Each thread converts whole texels (from `src`), classifies them and, for the texels that are
+// pixels of this tile, writes their guide word; then each thread assembles entries from the
+// shared tiles.  inst: frame * cameras + camera; its entries start at staged[2 * inst * plane]:
+// 16-byte entries of high bytes for 8-bit inputs, 32-byte entries (high words x, y, z and low
+// word x, then low words y, z) for float inputs.
+template <typename Tin, typename Src>
+__device__ __forceinline__ void stage_tile(const StageParams& p, const Src& src, int inst, int i0, int j0,
+                                           uint4* __restrict__ staged, uint32_t* __restrict__ guides,
+                                           int* __restrict__ plane_flags)
 {
     constexpr bool kLowPlane = sizeof(Tin) == 4;  // 8-bit inputs have no fractions
     __shared__ uint32_t tex[kStageTexY][kStageTexX];                      // high bytes, byte 3 zero
@@ -96,11 +148,7 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
     __shared__ int block_class;
     const int pitch = p.cols + 2;
     const int64_t P = (int64_t)p.cols * p.rows, plane = (int64_t)pitch * (p.rows + 2);
-    const int tiles_x = (pitch + kStageTileX - 1) / kStageTileX;
-    const int i0 = (blockIdx.x % tiles_x) * kStageTileX, j0 = (blockIdx.x / tiles_x) * kStageTileY;
-    const int inst = blockIdx.y;  // frame * cameras + camera
     const int frame = inst / p.cameras, cam = inst % p.cameras;
-    const Tin* img = images + (int64_t)inst * P * 3;
     const int slot = p.ref_slot[cam];
     uint32_t* guide = slot >= 0 ? guides + ((int64_t)frame * p.references + slot) * P : nullptr;
     if (threadIdx.x == 0) block_class = 0;
@@ -114,15 +162,16 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
         uint32_t q0 = 0, q1 = 0, q2 = 0;
         if (x >= 0 && y >= 0 && x < p.cols && y < p.rows) {
             const int64_t o = (int64_t)y * p.cols + x;
-            const Tin r0 = img[o * 3], r1 = img[o * 3 + 1], r2 = img[o * 3 + 2];
-            const int k0 = value_class(r0), k1 = value_class(r1), k2 = value_class(r2);
+            Tin r[3];
+            src.get(x, y, lx, ly, r);
+            const int k0 = value_class(r[0]), k1 = value_class(r[1]), k2 = value_class(r[2]);
             cls = max(cls, max(k0, max(k1, k2)));
-            q0 = fixed_code(r0, k0);
-            q1 = fixed_code(r1, k1);
-            q2 = fixed_code(r2, k2);
+            q0 = fixed_code(r[0], k0);
+            q1 = fixed_code(r[1], k1);
+            q2 = fixed_code(r[2], k2);
             if (guide && lx < kStageTileX && ly < kStageTileY) {
                 // utils.py:144-155, the arithmetic of ssg_rgb_to_guide, from the input values
-                const float c0 = texel_value(r0), c1 = texel_value(r1), c2 = texel_value(r2);
+                const float c0 = texel_value(r[0]), c1 = texel_value(r[1]), c2 = texel_value(r[2]);
                 const float yy = fadd(fadd(fadd(fmul(c0, 0.1826f), 16.0f), fmul(c1, 0.6142f)), fmul(c2, 0.062f));
                 const float cb = fadd(fsub(fsub(128.0f, fmul(c0, 0.1006f)), fmul(c1, 0.3386f)), fmul(c2, 0.4392f));
                 const float cr = fsub(fsub(fadd(fmul(c0, 0.4392f), 128.0f), fmul(c1, 0.3989f)), fmul(c2, 0.0403f));
@@ -172,6 +221,90 @@ __global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_
     }
 }
 
+// the tile of entries of block blockIdx.x, for images of cols x rows pixels
+__device__ __forceinline__ void stage_tile_origin(const StageParams& p, int& i0, int& j0)
+{
+    const int tiles_x = (p.cols + 2 + kStageTileX - 1) / kStageTileX;
+    i0 = (blockIdx.x % tiles_x) * kStageTileX;
+    j0 = (blockIdx.x / tiles_x) * kStageTileY;
+}
+
+// blockIdx.y: frame * cameras + camera, images at the matching resolution
+template <typename Tin>
+__global__ void __launch_bounds__(kBatchBlock) stage_images_kernel(const __grid_constant__ StageParams p,
+                                                                  const Tin* __restrict__ images,
+                                                                  uint4* __restrict__ staged,
+                                                                  uint32_t* __restrict__ guides,
+                                                                  int* __restrict__ plane_flags)
+{
+    int i0, j0;
+    stage_tile_origin(p, i0, j0);
+    const int inst = blockIdx.y;
+    const ImageTexels<Tin> src{images + (int64_t)inst * p.cols * p.rows * 3, p.cols};
+    stage_tile<Tin>(p, src, inst, i0, j0, staged, guides, plane_flags);
+}
+
+// The same staging from 8-bit source images of any size, resized to the matching resolution on
+// the way (ssg_stage_images_resized).  The block first forms its texel columns' and rows' taps,
+// then copies the source window they cover (rows rtap[0].s0 .. rtap[last].s1, columns
+// ctap[0].s0 .. ctap[last].s1; `win_rows` x `row_floats` floats of dynamic shared memory, sized on
+// the host for the largest window of any tile) with aligned 32-bit loads, one float per byte.
+// Each image's bytes start 4-byte aligned and end on a word boundary (checked on the host), so
+// every word read lies inside its image.
+__global__ void __launch_bounds__(kBatchBlock) stage_resized_kernel(const __grid_constant__ StageParams p,
+                                                                    const __grid_constant__ ResizeParams rp,
+                                                                    const uint8_t* __restrict__ images,
+                                                                    int row_floats, uint4* __restrict__ staged,
+                                                                    uint32_t* __restrict__ guides,
+                                                                    int* __restrict__ plane_flags)
+{
+    extern __shared__ __align__(16) float win[];
+    __shared__ Tap ctap[kStageTexX], rtap[kStageTexY];
+    __shared__ __align__(16) TapOffsets cw[kStageTexX], rw[kStageTexY];
+    int i0, j0;
+    stage_tile_origin(p, i0, j0);
+    const int inst = blockIdx.y;
+    const int t = threadIdx.x;
+    if (t < kStageTexX) ctap[t] = column_tap(rp, min(max(i0 - 1 + t, 0), p.cols - 1));
+    else if (t < kStageTexX + kStageTexY)
+        rtap[t - kStageTexX] = row_tap(rp, min(max(j0 - 1 + t - kStageTexX, 0), p.rows - 1));
+    __syncthreads();
+    const int r_min = rtap[0].s0, r_max = rtap[kStageTexY - 1].s1;
+    const int c_min = ctap[0].s0, c_max = ctap[kStageTexX - 1].s1;
+    // byte offset of source byte 3 (r src_cols + c) within its 32-bit word; only the low two bits
+    // of the (wrapping) 32-bit product matter
+    const uint32_t row_bytes = 3u * (uint32_t)rp.src_cols;
+    if (t < kStageTexX) {
+        const Tap tx = ctap[t];
+        cw[t] = TapOffsets{3 * (tx.s0 - c_min), 3 * (tx.s1 - c_min), __fsub_rn(1.0f, tx.f), tx.f};
+    } else if (t < kStageTexX + kStageTexY) {
+        const Tap ty = rtap[t - kStageTexX];
+        const uint32_t lead = 3u * (uint32_t)c_min;
+        const int o0 = (ty.s0 - r_min) * row_floats + (int)(((uint32_t)ty.s0 * row_bytes + lead) & 3u);
+        const int o1 = (ty.s1 - r_min) * row_floats + (int)(((uint32_t)ty.s1 * row_bytes + lead) & 3u);
+        rw[t - kStageTexX] = TapOffsets{o0, o1, __fsub_rn(1.0f, ty.f), ty.f};
+    }
+    // the window: rows r_min..r_max, each from the word holding byte 3 c_min to the one holding
+    // byte 3 c_max + 2, one float per byte
+    const int64_t image_bytes = (int64_t)rp.src_cols * rp.src_rows * 3;
+    const uint32_t* words = reinterpret_cast<const uint32_t*>(images + (int64_t)inst * image_bytes);
+    const int row_words = row_floats / 4;
+    for (int k = t; k < (r_max - r_min + 1) * row_words; k += blockDim.x) {
+        const int wr = k / row_words, q = k % row_words;
+        const int64_t b0 = ((int64_t)(r_min + wr) * rp.src_cols + c_min) * 3;
+        const int64_t b1 = b0 + 3 * (int64_t)(c_max - c_min + 1);
+        const int64_t w = (b0 >> 2) + q;
+        if (w < (b1 + 3) >> 2) {
+            const uint32_t v = __ldg(words + w);
+            reinterpret_cast<float4*>(win + wr * row_floats)[q] =
+                make_float4((float)(v & 255u), (float)((v >> 8) & 255u), (float)((v >> 16) & 255u), (float)(v >> 24));
+        }
+    }
+    __syncthreads();
+    const ResizedTexels src{win, cw, rw, rp.area2};
+    stage_tile<float>(p, src, inst, i0, j0, staged, guides, plane_flags);
+}
+
 // channel c (0..2) of texel k (0: nw, 1: ne, 2: sw, 3: se) of an entry
 __device__ __forceinline__ float entry_texel(const uint4& q, int c, int k)
 {
@@ -198,6 +331,7 @@ __device__ __forceinline__ void float_footprint(const float* __restrict__ img, i
 
 struct FastSweepParams {
     int cols, rows, cameras, references, ncand, chunks;
+    int entry_words;  // 16-byte words per staged entry: 1 (8-bit inputs) or 2 (8.8 fixed point)
     TorchCam ref_cam[SSG_MAX_REFERENCES];
     int ref_index[SSG_MAX_REFERENCES];
     FastCam cam[SSG_MAX_CAMERAS];
@@ -381,11 +515,12 @@ __device__ __noinline__ void sweep_candidates_outlined(const V view, const uint4
 
 // Sweep + cost of one reference pixel (x, y) over all candidates, into its cells (`out`, chunk
 // stride `chunk_stride`).  `V` gives the instance's constants: ref_cam(), cam(c), pose(c) (12
-// floats), cand(k) (pairs are read as float2) and cameras(), chunks().  `frame_entries` /
-// `frame_floats` point at the frame's camera-0 footprints (camera c's at 2 c `plane` 16-byte
-// words: 16-byte entries for 8-bit inputs, 32-byte ones when frame_floats is set) / float image
-// (cols x rows x 3 floats apart), `flags` at the frame's per-camera plane classes.  The pixel takes
-// the path of the larger class of its reference and selected planes.
+// floats), cand(k) (pairs are read as float2), cameras(), chunks() and entry_words() (16-byte
+// words per entry: 1 for 8-bit inputs, 2 for the 32-byte entries of float or resized inputs).
+// `frame_entries` / `frame_floats` point at the frame's camera-0 footprints (camera c's at 2 c
+// `plane` 16-byte words) / float image (cols x rows x 3 floats apart; NULL when the frame was
+// staged from 8-bit images, resized or not), `flags` at the frame's per-camera plane classes.  The
+// pixel takes the path of the larger class of its reference and selected planes.
 template <typename T, typename V>
 __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restrict__ frame_entries,
                                             const float* __restrict__ frame_floats, const int* __restrict__ flags,
@@ -395,8 +530,9 @@ __device__ __forceinline__ void sweep_pixel(const V& view, const uint4* __restri
     const int pitch = cols + 2;
     const int64_t P = (int64_t)cols * rows;
     const bool seen = sel >= 0 && sel < view.cameras();
-    const int mode = max(__ldg(flags + ref_camera), seen ? __ldg(flags + sel) : 0);
-    const int stride = frame_floats ? 2 : 1;  // 16-byte words per entry: 32-byte entries for float inputs
+    const int stride = view.entry_words();  // 16-byte words per entry: 2 for 32-byte entries
+    // 16-byte entries hold 8-bit texels only (a plane flagged otherwise was not staged in them)
+    const int mode = stride == 1 ? kPlaneBytes : max(__ldg(flags + ref_camera), seen ? __ldg(flags + sel) : 0);
     float rp[3];
     uint32_t rq[3];
     if (mode == kPlaneFloats && frame_floats) {
@@ -466,6 +602,7 @@ struct UniformView {
     int slot;
     __device__ __forceinline__ int chunks() const { return p.chunks; }
     __device__ __forceinline__ int cameras() const { return p.cameras; }
+    __device__ __forceinline__ int entry_words() const { return p.entry_words; }
     __device__ __forceinline__ const TorchCam& ref_cam() const { return p.ref_cam[slot]; }
     __device__ __forceinline__ float pose(int c, int j) const { return p.pose[slot][c][j]; }
     __device__ __forceinline__ FastCam cam(int c) const { return p.cam[c]; }
@@ -528,6 +665,7 @@ struct InstView {
     const SweepInst* I;
     __device__ __forceinline__ int chunks() const { return I->chunks; }
     __device__ __forceinline__ int cameras() const { return I->cameras; }
+    __device__ __forceinline__ int entry_words() const { return I->floats ? 2 : 1; }
     __device__ __forceinline__ const TorchCam& ref_cam() const { return I->ref_cam; }
     __device__ __forceinline__ float pose(int c, int j) const { return __ldg(&I->pose[c][j]); }
     __device__ __forceinline__ FastCam cam(int c) const { return I->cam[c]; }
@@ -751,13 +889,101 @@ extern "C" int ssg_stage_images_u8(const uint8_t* d_images, int frames, int came
                         d_plane_flags, stream);
 }
 
+extern "C" int ssg_stage_images_resized(const uint8_t* d_images, int src_cols, int src_rows, int frames,
+                                        int cameras, int cols, int rows, const int* reference_cameras,
+                                        int references, float* d_staged, uint8_t* d_guides, int32_t* d_plane_flags,
+                                        void* stream)
+{
+    SSG_REQUIRE(d_images && d_staged && d_guides && d_plane_flags && reference_cameras, "null pointer");
+    SSG_REQUIRE(src_cols >= 1 && src_rows >= 1, "empty source images");
+    SSG_REQUIRE(frames >= 1 && frames <= 65535 / SSG_MAX_CAMERAS, "frames %d outside [1, %d]", frames,
+                65535 / SSG_MAX_CAMERAS);
+    SSG_REQUIRE(cameras >= 1 && cameras <= SSG_MAX_CAMERAS && references >= 1 && references <= SSG_MAX_REFERENCES,
+                "camera or reference count out of range");
+    if (int e = staged_plane_fits(cols, rows)) return e;
+    SSG_REQUIRE(((uintptr_t)d_staged & 31) == 0 && ((uintptr_t)d_guides & 3) == 0,
+                "staged planes must be 32-byte and guides 4-byte aligned");
+    if (((uintptr_t)d_images & 3) != 0 || ((int64_t)src_cols * src_rows) % 4 != 0)
+        return fail(SSG_ERR_UNSUPPORTED,
+                    "source images must start on 4-byte boundaries with a pixel count divisible by 4 (%dx%d): "
+                    "resize with ssg_resize_linear and stage the result",
+                    src_cols, src_rows);
+    SSG_REQUIRE((int64_t)src_cols * src_rows * 3 < ((int64_t)1 << 40), "source images too large");
+    const ResizeParams rp = make_resize_params(src_cols, src_rows, cols, rows, 3);
+    // the largest source window of any tile: texel columns [i0 - 1, i0 + kStageTileX - 1] and
+    // rows [j0 - 1, j0 + kStageTileY - 1] clamped into the image, taps as the kernel forms them
+    int win_cols = 0, win_rows = 0;
+    for (int i0 = 0; i0 < cols + 2; i0 += kStageTileX) {
+        const int a = std::min(std::max(i0 - 1, 0), cols - 1), b = std::min(i0 + kStageTileX - 1, cols - 1);
+        win_cols = std::max(win_cols, column_tap(rp, b).s1 - column_tap(rp, a).s0 + 1);
+    }
+    for (int j0 = 0; j0 < rows + 2; j0 += kStageTileY) {
+        const int a = std::min(std::max(j0 - 1, 0), rows - 1), b = std::min(j0 + kStageTileY - 1, rows - 1);
+        win_rows = std::max(win_rows, row_tap(rp, b).s1 - row_tap(rp, a).s0 + 1);
+    }
+    // a window row starts at byte offset 0..3 of its first word: ceil((3 + 3 cols) / 4) words
+    const int row_floats = 4 * ((3 * win_cols + 6) / 4 + 1);
+    const int64_t smem = (int64_t)win_rows * row_floats * (int64_t)sizeof(float);
+    constexpr int64_t kMaxWindow = 160 * 1024;
+    if (smem > kMaxWindow)
+        return fail(SSG_ERR_UNSUPPORTED,
+                    "a tile's source window (%d x %d texels) exceeds %lld bytes of shared memory: resize with "
+                    "ssg_resize_linear and stage the result",
+                    win_cols, win_rows, (long long)kMaxWindow);
+    if (smem > 48 * 1024) {
+        // above the default limit the kernel opts in, once per device and size
+        static std::atomic<int64_t> opted[64];
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SSG_ERR_CUDA, "cudaGetDevice");
+        if (opted[dev].load() < smem) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(stage_resized_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+            opted[dev].store(smem);
+        }
+    }
+    StageParams p{};
+    p.cameras = cameras;
+    p.references = references;
+    p.cols = cols;
+    p.rows = rows;
+    for (int c = 0; c < SSG_MAX_CAMERAS; ++c) p.ref_slot[c] = -1;
+    for (int r = 0; r < references; ++r) {
+        SSG_REQUIRE(reference_cameras[r] >= 0 && reference_cameras[r] < cameras, "reference camera out of range");
+        p.ref_slot[reference_cameras[r]] = r;
+    }
+    const cudaError_t e = cudaMemsetAsync(d_plane_flags, 0, sizeof(int32_t) * frames * cameras, as_stream(stream));
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    const int64_t tiles = (int64_t)((cols + 2 + kStageTileX - 1) / kStageTileX) *
+                          ((rows + 2 + kStageTileY - 1) / kStageTileY);
+    SSG_REQUIRE(tiles < ((int64_t)1 << 31), "images of %dx%d pixels are too large", cols, rows);
+    stage_resized_kernel<<<dim3((unsigned)tiles, frames * cameras), kBatchBlock, (size_t)smem, as_stream(stream)>>>(
+        p, rp, d_images, row_floats, reinterpret_cast<uint4*>(d_staged), reinterpret_cast<uint32_t*>(d_guides),
+        d_plane_flags);
+    return launch_status("stage_resized_kernel");
+}
+
 extern "C" int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_count, const ssg_camera* cameras,
                                     int references, const int* reference_cameras, const float* relative_poses,
                                     const float* d_staged, const float* d_images, const int32_t* d_plane_flags,
                                     const int8_t* d_selected, const float* candidates, int candidate_count,
                                     int storage, void* d_cost, void* stream)
 {
+    return ssg_sweep_cost_batch_entries(cols, rows, frames, camera_count, cameras, references, reference_cameras,
+                                        relative_poses, d_staged, d_images ? 32 : 16, d_images, d_plane_flags,
+                                        d_selected, candidates, candidate_count, storage, d_cost, stream);
+}
+
+extern "C" int ssg_sweep_cost_batch_entries(int cols, int rows, int frames, int camera_count,
+                                            const ssg_camera* cameras, int references, const int* reference_cameras,
+                                            const float* relative_poses, const float* d_staged, int entry_bytes,
+                                            const float* d_images, const int32_t* d_plane_flags,
+                                            const int8_t* d_selected, const float* candidates, int candidate_count,
+                                            int storage, void* d_cost, void* stream)
+{
     if (int e = staged_plane_fits(cols, rows)) return e;
+    SSG_REQUIRE(entry_bytes == 16 || entry_bytes == 32, "entry_bytes %d is neither 16 nor 32", entry_bytes);
+    SSG_REQUIRE(!d_images || entry_bytes == 32, "float images are staged in 32-byte entries");
     SSG_REQUIRE(cameras && reference_cameras && relative_poses && d_staged && d_plane_flags && d_selected &&
                     candidates && d_cost,
                 "null pointer");
@@ -767,12 +993,13 @@ extern "C" int ssg_sweep_cost_batch(int cols, int rows, int frames, int camera_c
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count %d outside [1, %d]",
                 candidate_count, SSG_MAX_CANDIDATES);
     SSG_REQUIRE(((uintptr_t)d_staged & 15) == 0 && ((uintptr_t)d_cost & 15) == 0, "buffers must be 16-byte aligned");
-    SSG_REQUIRE(!d_images || ((uintptr_t)d_staged & 31) == 0,
-                "the staged planes of float images (32-byte entries) must be 32-byte aligned");
+    SSG_REQUIRE(entry_bytes == 16 || ((uintptr_t)d_staged & 31) == 0,
+                "staged planes of 32-byte entries must be 32-byte aligned");
     if (int e = check_storage(storage)) return e;
     FastSweepParams p{};
     p.cols = cols;
     p.rows = rows;
+    p.entry_words = entry_bytes / 16;
     p.cameras = camera_count;
     p.references = references;
     p.ncand = candidate_count;

@@ -4,7 +4,8 @@ volume (coarser levels float32) with fp32 arithmetic, optional CUDA-graph captur
 One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_panorama
 (python/depth_estimation.py:205-242) for all F x R (frame, reference) instances at once:
 
-    ssg_stage_images[_u8]          inputs -> 8-bit footprints + guides of the references 1 launch
+    ssg_stage_images[_u8|_resized] inputs -> footprints + guides of the references      1 launch
+                                   (_resized: decoded 8-bit images of any size, resized on the way)
     ssg_sweep_cost_batch           sweep + cost, 16-bit chunked volume                  1
     ssg_isb_downsample_batch       L - 1 levels                                         L - 1
     ssg_isb_upsample_batch         levels L - 2 .. 1                                    L - 2
@@ -99,6 +100,11 @@ class BatchPipeline:
         self._poses = N.floats([v for r in e.references_indices for v in e._poses_list[r]])
         self._graphs: dict = {}
         self._side = torch.cuda.Stream(dev)  # the post-filter and stitch of overlapped groups
+        # decoded 8-bit images of another size than the matching resolution: resized while staging
+        # (ssg_stage_images_resized), or, where that kernel declines the shape, resized into this
+        # float32 buffer first and staged from it
+        self._fused_resize: dict[tuple[int, int, int], bool] = {}
+        self._resized: torch.Tensor | None = None
         # launch shapes: picked by the autotuner on first use (``tuner``: an autotune.Tuner, or
         # None for the library's defaults)
         self.tuner = tuner
@@ -121,17 +127,49 @@ class BatchPipeline:
         R, C, P = self.R, self.C, self.P
         i0, inst = f0 * R, frames * R
         cols, rows = self.cols, self.rows
-        stage = "ssg_stage_images_u8" if match.dtype == torch.uint8 else "ssg_stage_images"
         plane = (rows + 2) * (cols + 2) * 4  # floats of one plane of footprints (two per camera)
         staged = self.staged.data_ptr() + 4 * f0 * C * 2 * plane
         flags = self.plane_flags.data_ptr() + 4 * f0 * C
+        guide0 = self.guides[0].data_ptr() + 4 * i0 * P
         m = match[f0:f0 + frames]
-        N.call(stage, m.data_ptr(), frames, C, cols, rows, self._refs, R, staged,
-               self.guides[0].data_ptr() + 4 * i0 * P, flags, stream)
-        floats = None if match.dtype == torch.uint8 else m.data_ptr()
+        floats = None
+        if match.dtype != torch.uint8:
+            # float32 images at the matching resolution: 32-byte entries, class-2 planes sampled from them
+            N.call("ssg_stage_images", m.data_ptr(), frames, C, cols, rows, self._refs, R, staged, guide0, flags,
+                   stream)
+            floats, entry_bytes = m.data_ptr(), 32
+        elif m.shape[2:4] == (rows, cols):
+            # 8-bit images at the matching resolution: 16-byte entries of bytes
+            N.call("ssg_stage_images_u8", m.data_ptr(), frames, C, cols, rows, self._refs, R, staged, guide0, flags,
+                   stream)
+            entry_bytes = 16
+        else:
+            # decoded 8-bit images of their own size: resized to the matching resolution (the
+            # reference's input preparation, python/utils.py:198-201) while staging
+            src_rows, src_cols = m.shape[2], m.shape[3]
+            key = (src_cols, src_rows, m.data_ptr() % 4)
+            entry_bytes = 32
+            if self._fused_resize.get(key, True):
+                try:
+                    N.call("ssg_stage_images_resized", m.data_ptr(), src_cols, src_rows, frames, C, cols, rows,
+                           self._refs, R, staged, guide0, flags, stream)
+                    self._fused_resize[key] = True
+                except N.SSGError as err:  # declined before any launch: resize first
+                    if err.code != N.SSG_ERR_UNSUPPORTED:
+                        raise
+                    self._fused_resize[key] = False
+            if not self._fused_resize[key]:
+                if self._resized is None:
+                    self._resized = torch.empty(self.max_frames * C * P * 3, dtype=torch.float32, device=self.device)
+                resized = self._resized.data_ptr() + 4 * f0 * C * P * 3
+                N.call("ssg_resize_linear", m.data_ptr(), N.PIXEL_U8, src_cols, src_rows, 3, resized, N.PIXEL_F32,
+                       cols, rows, frames * C, stream)
+                N.call("ssg_stage_images", resized, frames, C, cols, rows, self._refs, R, staged, guide0, flags,
+                       stream)
+                floats = resized
         cell0 = 2 * 8 * self.chunks  # bytes of a level-0 pixel's cells
-        N.call("ssg_sweep_cost_batch", cols, rows, frames, C, e._cams, R, self._refs, self._poses, staged, floats,
-               flags, self.selected.data_ptr(), e._candidates, self.N, self.storage,
+        N.call("ssg_sweep_cost_batch_entries", cols, rows, frames, C, e._cams, R, self._refs, self._poses, staged,
+               entry_bytes, floats, flags, self.selected.data_ptr(), e._candidates, self.N, self.storage,
                self.costs[0].data_ptr() + cell0 * i0 * P, stream)
         var_inv_i = 1 / (2 * e.sigma_i * e.sigma_i)
         L = self.L
@@ -251,12 +289,18 @@ class BatchPipeline:
     def run(self, match: torch.Tensor, stitch: torch.Tensor):
         """match: [F, C, rows, cols, 3], stitch: [F, R, image_rows, image_cols, 3], each float32 or
         uint8 (8-bit images: a quarter of the upload, no conversion pass), contiguous on the
-        pipeline's device.  Returns views of the outputs for F frames."""
-        frames = match.shape[0]
+        pipeline's device.  An 8-bit `match` may also have its own size [F, C, H, W, 3] (the decoded
+        images): it is then resized to the matching resolution, as the reference's input
+        preparation resizes (python/utils.py:198-201), while it is staged.  Returns views of the
+        outputs for F frames."""
+        frames = match.shape[0] if match.dim() else 0
         if not 1 <= frames <= self.max_frames:
             raise ValueError(f"batch of {frames} frames outside [1, {self.max_frames}]")
         st = self.st
-        for name, t, shape in (("images_to_match", match, (frames, self.C, self.rows, self.cols, 3)),
+        match_shape = (frames, self.C, self.rows, self.cols, 3)
+        if match.dtype == torch.uint8 and match.dim() == 5 and match.shape[4] == 3 and min(match.shape[2:4]) >= 1:
+            match_shape = (frames, self.C, match.shape[2], match.shape[3], 3)
+        for name, t, shape in (("images_to_match", match, match_shape),
                                ("images_to_stitch", stitch, (frames, self.R, st.image_rows, st.image_cols, 3))):
             N.require(t, name, torch.uint8 if t.dtype == torch.uint8 else torch.float32, shape, self.device)
         self._apply_tuning(match, stitch, frames)

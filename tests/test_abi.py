@@ -112,3 +112,34 @@ def test_misaligned_cells_and_entries_rejected_without_a_device(native, ss):
     assert native.ssg_sweep_cost_batch(64, 64, 1, 2, cams, 1, refs, poses, M, A, A, A, cand, 32, F16, A, None) == \
         N.SSG_ERR_INVALID_ARGUMENT
     assert "32-byte aligned" in N.last_error()
+
+
+def test_resized_staging_and_entry_sizes_checked_without_a_device(native, ss):
+    """The one-pass resize + staging refuses misaligned planes, and declines (SSG_ERR_UNSUPPORTED,
+    so that the caller resizes first) sources whose images do not start on 4-byte boundaries or
+    whose tile windows would not fit in shared memory; the sweep's entry size is 16 or 32 bytes,
+    32 whenever float images are given.  All before anything is launched."""
+    N = ss._native
+    A, M = 0x100000, 0x100010
+    refs = N.ints([0])
+    assert native.ssg_stage_images_resized(A, 1216, 1216, 1, 2, 1024, 1024, refs, 1, M, A, A, None) == \
+        N.SSG_ERR_INVALID_ARGUMENT
+    assert "32-byte" in N.last_error()
+    assert native.ssg_stage_images_resized(A, 33, 35, 1, 2, 20, 20, refs, 1, A, A, A, None) == N.SSG_ERR_UNSUPPORTED
+    assert "4-byte" in N.last_error()
+    assert native.ssg_stage_images_resized(A + 2, 64, 64, 1, 2, 20, 20, refs, 1, A, A, A, None) == \
+        N.SSG_ERR_UNSUPPORTED
+    assert native.ssg_stage_images_resized(A, 4096, 4096, 1, 2, 256, 256, refs, 1, A, A, A, None) == \
+        N.SSG_ERR_UNSUPPORTED
+    assert "shared memory" in N.last_error()
+    cams = N.cameras_array([N.ssg_camera(100, 100, 32, 32, -0.2, 0.6)] * 2)
+    poses = N.floats([0.0] * 24)
+    cand = N.floats([1.0 + k for k in range(32)])
+    assert native.ssg_sweep_cost_batch_entries(64, 64, 1, 2, cams, 1, refs, poses, A, 24, None, A, A, cand, 32, 0,
+                                               A, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "entry_bytes" in N.last_error()
+    assert native.ssg_sweep_cost_batch_entries(64, 64, 1, 2, cams, 1, refs, poses, A, 16, A, A, A, cand, 32, 0,
+                                               A, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert native.ssg_sweep_cost_batch_entries(64, 64, 1, 2, cams, 1, refs, poses, M, 32, None, A, A, cand, 32, 0,
+                                               A, None) == N.SSG_ERR_INVALID_ARGUMENT
+    assert "32-byte aligned" in N.last_error()
