@@ -438,8 +438,10 @@ SSG_API int ssg_merge_panorama_batch_approx(const float* d_lut, const float* d_w
  * above, then a soft-argmin inverse distance q = sum_k softmax(-F_k / temperature) / d_k over the
  * filtered costs F, fused with the last filter level.  Backward: the transposes of those linear
  * steps (the filter's weights come from uint8 guides and receive no gradient) and of the sweep.
- * Gradient buffers are float32 planar volumes like the forward's; atomic adds make the sums'
- * order, and so their last bits, run-dependent.
+ * Gradient buffers are float32 planar volumes like the forward's.  Every gradient is
+ * bit-reproducible run to run: the filter's transposed steps gather (each output cell sums what
+ * it receives in a fixed order), the image gradient is summed in 64-bit fixed point, and the
+ * pose gradient by a fixed float64 reduction tree.
  * ------------------------------------------------------------------------------------------- */
 
 /* Last ISB level (level 1 -> 0) fused with the soft-argmin: d_inverse_distance fine pixels. */
@@ -449,20 +451,20 @@ SSG_API int ssg_isb_upsample_softargmin(const uint8_t* d_guide_in, const float* 
                                         float var_inv_i, const float* candidates, float temperature,
                                         float* d_inverse_distance, void* stream);
 
-/* Backward of ssg_isb_upsample_softargmin: writes dL/d(level-0 cost) (own-pixel part) and adds
- * dL/d(filtered level 1) into d_grad_filtered_coarse (zero it first). */
+/* Backward of ssg_isb_upsample_softargmin: writes dL/dF, the gradient with respect to the
+ * filtered level-0 costs (candidate planes of the fine level); ssg_isb_upsample_transpose of
+ * the same level then splits it into the level-0 cost gradient and the filtered level-1 one. */
 SSG_API int ssg_isb_upsample_softargmin_backward(const uint8_t* d_guide_in, const float* d_cost_in, int rows_in,
                                                  int cols_in, const uint8_t* d_guide_fine, const float* d_cost_fine,
                                                  int rows_fine, int cols_fine, int candidate_count, float weight_up,
                                                  float weight_down, float var_inv_i, const float* candidates,
                                                  float temperature, const float* d_grad_inverse_distance,
-                                                 float* d_grad_cost_fine, float* d_grad_filtered_coarse,
-                                                 void* stream);
+                                                 float* d_grad_filtered_fine, void* stream);
 
-/* Transpose of one upsampling step (python/isb_filter.cu:132-329): adds the own-pixel part of
- * dL/d(filtered fine level) to d_grad_cost_fine and its coarse-tap part to
- * d_grad_filtered_coarse.  d_guide_coarse: filtered coarse guide; d_guide_fine: the fine guide
- * before its own upsampling step. */
+/* Transpose of one upsampling step (python/isb_filter.cu:132-329): writes the own-pixel part of
+ * dL/d(filtered fine level) to d_grad_cost_fine and its coarse-tap part to d_grad_filtered_coarse
+ * (every cell of both is written).  d_guide_coarse: filtered coarse guide; d_guide_fine: the fine
+ * guide before its own upsampling step. */
 SSG_API int ssg_isb_upsample_transpose(const uint8_t* d_guide_coarse, int rows_in, int cols_in,
                                        const uint8_t* d_guide_fine, int rows_fine, int cols_fine,
                                        int candidate_count, float weight_up, float weight_down, float var_inv_i,
@@ -470,7 +472,7 @@ SSG_API int ssg_isb_upsample_transpose(const uint8_t* d_guide_coarse, int rows_i
                                        float* d_grad_filtered_coarse, void* stream);
 
 /* Transpose of one downsampling step (python/isb_filter.cu:44-119): adds the coarse gradient,
- * spread over the 3 x 3 taps, into d_grad_cost_fine. */
+ * spread over the 3 x 3 taps, into d_grad_cost_fine (each fine cell gathers its share). */
 SSG_API int ssg_isb_downsample_transpose(const uint8_t* d_guide_in, int rows_in, int cols_in, int rows_out,
                                          int cols_out, int candidate_count, float var_inv_i,
                                          const float* d_grad_cost_coarse, float* d_grad_cost_fine, void* stream);
@@ -478,12 +480,18 @@ SSG_API int ssg_isb_downsample_transpose(const uint8_t* d_guide_in, int rows_in,
 /* Backward of ssg_sweep_cost (python/depth_estimation.py:141-175): adds dL/d(image) into
  * d_grad_images (camera_count device pointers, rows x cols x 3 float32) and the per-camera
  * 6-DoF gradient into d_grad_pose (camera_count x 6 float64: rotation, then translation, of a
- * right perturbation T <- T [Exp(omega), v] evaluated at zero). */
+ * right perturbation T <- T [Exp(omega), v] evaluated at zero).  The image gradient of the call
+ * is summed in 64-bit fixed point: multiples of 2^-e, with 2^e the largest power of two for which
+ * 2 x pixels x candidates x max |d_grad_cost| x 2^e stays below 2^62 (a contribution is rounded by
+ * at most 2^-(e+1)); a non-finite d_grad_cost makes it NaN.  d_scratch: 256-byte aligned,
+ * ssg_sweep_backward_scratch_bytes(cols, rows, camera_count) bytes, not shared by calls in
+ * flight at once. */
+SSG_API size_t ssg_sweep_backward_scratch_bytes(int cols, int rows, int camera_count);
 SSG_API int ssg_sweep_cost_backward(int cols, int rows, int camera_count, const ssg_camera* cameras, int reference,
                                     const float* relative_poses, const float* const* d_images,
                                     float* const* d_grad_images, const int8_t* d_selected, const float* candidates,
                                     int candidate_count, const float* d_grad_cost, double* d_grad_pose,
-                                    void* stream);
+                                    void* d_scratch, void* stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Uneven batches (no counterpart in the reference, which estimates one rig's frame per call of

@@ -133,11 +133,12 @@ SIGNATURES = {
     "ssg_inpaint_holes_batch": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _D, _I, _P]),
     "ssg_inpaint_noalloc": (_I, [_P, _P, _I, _I, _D, _I, _P]),
     "ssg_isb_upsample_softargmin": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P]),
-    "ssg_isb_upsample_softargmin_backward": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P, _P,
+    "ssg_isb_upsample_softargmin_backward": (_I, [_P, _P, _I, _I, _P, _P, _I, _I, _I, _F, _F, _F, _P, _F, _P, _P,
                                                   _P]),
     "ssg_isb_upsample_transpose": (_I, [_P, _I, _I, _P, _I, _I, _I, _F, _F, _F, _P, _P, _P, _P]),
     "ssg_isb_downsample_transpose": (_I, [_P, _I, _I, _I, _I, _I, _F, _P, _P, _P]),
-    "ssg_sweep_cost_backward": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
+    "ssg_sweep_backward_scratch_bytes": (ctypes.c_size_t, [_I, _I, _I]),
+    "ssg_sweep_cost_backward": (_I, [_I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P]),
     "ssg_merge_panorama_batch": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
     "ssg_convert_u8": (_I, [_P, _P, _I64, _P]),
     "ssg_tuning_set": (_I, [_I, _I]),

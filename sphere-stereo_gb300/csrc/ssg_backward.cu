@@ -5,19 +5,26 @@
 // ssg_isb.cu, then per pixel q = sum_k softmax(-F_k / tau) / d_k over the filtered costs F,
 // fused with the last filter level.
 //
-// Backward, with the cost volume recomputed instead of stored:
-//   * seed: the last level recomputes F, runs an online softmax over the candidates (two passes)
-//     and writes dL/dF mapped through the level's linear operator: its own-pixel part to the
-//     level-0 cost gradient, its coarse-tap part to the level-1 gradient (atomic adds);
+// Backward, with the cost volume recomputed instead of stored, and every sum formed in an order
+// that does not depend on thread timing (the gradients are bit-reproducible run to run):
+//   * seed: the last level recomputes F and runs an online softmax over the candidates (two
+//     passes); dL/dF is written per fine pixel;
 //   * the ISB filter is linear in the cost for a fixed guide (its weights come from uint8 guides
-//     and get no gradient), so each up step and each down step is run transposed, from the
-//     coarsest level back to level 0;
+//     and get no gradient), so each up step and each down step is run transposed, from level 0's
+//     dL/dF up to the coarsest level and back down to level 0.  Each transposed step is a
+//     gather: every output cell recomputes the weights with which the forward step read it and
+//     sums its contributions in a fixed order, so that no two threads write one cell;
 //   * the sweep's backward recomputes every sample, maps dL/dcost through the clamp, the L1 and
-//     the bilinear sample to the images (atomic scatter into the source image, direct sum into
-//     the reference image) and through the double-sphere projection to the 6-DoF pose deltas of
-//     the source and reference cameras, reduced per block and added in float64.
+//     the bilinear sample to the images and through the double-sphere projection to the 6-DoF
+//     pose deltas of the source and reference cameras.  A source texel receives contributions
+//     from any sample that lands on it, so the image gradient is accumulated in 64-bit fixed
+//     point (multiples of 2^-e, e from the largest |dL/dcost| and the number of samples):
+//     integer sums do not depend on the order of the atomic adds.  The pose gradient is reduced
+//     per block by a fixed warp-shuffle tree in float64, and the block sums are added in block
+//     order.
 // Pose deltas are right perturbations, T_c <- T_c exp(delta_c), delta = (omega, v): the
 // relative pose reference -> camera becomes exp(-delta_c) rel exp(delta_ref).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -87,13 +94,13 @@ __global__ void __launch_bounds__(kBwdBlock) isb_up_softargmin_kernel(
         if (u.set[f]) q[u.fidx[f]] = sm[f].t / sm[f].s;
 }
 
-// dL/dF of the soft-argmin, pushed through the last level: level-0 part (own pixel) written,
-// level-1 part (coarse taps) added atomically.
+// dL/dF of the soft-argmin for every fine pixel and candidate, written to grad_F (candidate
+// planes of the fine level); ssg_isb_upsample_transpose then takes it through the last level.
 __global__ void __launch_bounds__(kBwdBlock) isb_up_softargmin_backward_kernel(
     const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in, int rows_in, int cols_in,
     const uint8_t* __restrict__ guide_fine, const float* __restrict__ cost_fine, int rows_io, int cols_io,
     float weight_up, float weight_down, float var_inv_i, const __grid_constant__ SoftParams sp,
-    const float* __restrict__ grad_q, float* __restrict__ grad_c0, float* __restrict__ grad_f1)
+    const float* __restrict__ grad_q, float* __restrict__ grad_F)
 {
     const int64_t pin = (int64_t)rows_in * cols_in, pio = (int64_t)rows_io * cols_io;
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -112,58 +119,53 @@ __global__ void __launch_bounds__(kBwdBlock) isb_up_softargmin_backward_kernel(
         for (int f = 0; f < 4; ++f)
             if (u.set[f]) sm[f].push(-c[f] * inv_tau, sp.inv_cand[z]);
     }
-    float qv[4], gq[4], own[4];
+    float qv[4], gq[4];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
         qv[f] = u.set[f] ? sm[f].t / sm[f].s : 0.0f;
         gq[f] = u.set[f] ? grad_q[u.fidx[f]] : 0.0f;
-        own[f] = weight_up * u.inv[f];  // d F / d (level-0 cost) of the own pixel
     }
-    // normalised coarse-tap weights of each fine pixel
-    float w1[9], w2[6], w3[6], w4[4];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) w1[i] = u.w1[i] * u.inv[0];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        w2[i] = u.w2[i] * u.inv[1];
-        w3[i] = u.w3[i] * u.inv[2];
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) w4[i] = u.w4[i] * u.inv[3];
-    const int64_t c2[6] = SSG_TAPS2(u.cidx);
-    const int64_t c3[6] = SSG_TAPS3(u.cidx);
-    const int64_t c4[4] = SSG_TAPS4(u.cidx);
     for (int z = 0; z < sp.ncand; ++z) {
         float c[4];
         fine_costs(u, cost_in + (int64_t)z * pin, cost_fine + (int64_t)z * pio, weight_up, c);
-        float gF[4];
 #pragma unroll
         for (int f = 0; f < 4; ++f) {
-            if (!u.set[f]) {
-                gF[f] = 0.0f;
-                continue;
-            }
+            if (!u.set[f]) continue;
             const float w = expf(-c[f] * inv_tau - sm[f].m) / sm[f].s;
-            gF[f] = gq[f] * (-inv_tau) * w * (sp.inv_cand[z] - qv[f]);
-            grad_c0[(int64_t)z * pio + u.fidx[f]] = own[f] * gF[f];
+            grad_F[(int64_t)z * pio + u.fidx[f]] = gq[f] * (-inv_tau) * w * (sp.inv_cand[z] - qv[f]);
         }
-        float* g1 = grad_f1 + (int64_t)z * pin;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) atomicAdd(g1 + u.cidx[i], w1[i] * gF[0]);
-        if (u.set[1])
-#pragma unroll
-            for (int i = 0; i < 6; ++i) atomicAdd(g1 + c2[i], w2[i] * gF[1]);
-        if (u.set[2])
-#pragma unroll
-            for (int i = 0; i < 6; ++i) atomicAdd(g1 + c3[i], w3[i] * gF[2]);
-        if (u.set[3])
-#pragma unroll
-            for (int i = 0; i < 4; ++i) atomicAdd(g1 + c4[i], w4[i] * gF[3]);
     }
 }
 
 // Transpose of one up step s (fine level s, coarse level s + 1):
-//   f_s = a * c_s + B f_{s+1}   =>   g_c_s += a * g_f_s ,  g_f_{s+1} += B^T g_f_s
+//   f_s = a * c_s + B f_{s+1}   =>   g_c_s = a * g_f_s ,  g_f_{s+1} = B^T g_f_s
+// One thread per coarse cell (X, Y): the own-pixel part of the four fine pixels of (X, Y) is
+// written, and g_f_{s+1}(X, Y) gathers the fine gradients of every fine pixel that read the cell
+// in the forward step -- the fine pixels of the coarse 3 x 3 neighbourhood whose edge-clamped tap
+// lists hold (X, Y), with the weights the forward step gave those taps.  Contributions are summed
+// in a fixed order (neighbour, then fine pixel).
+__device__ __forceinline__ void add_tap_weights(const UpWeights& u, int64_t me, float (&k)[4])
+{
+    const int64_t c2[6] = SSG_TAPS2(u.cidx);
+    const int64_t c3[6] = SSG_TAPS3(u.cidx);
+    const int64_t c4[4] = SSG_TAPS4(u.cidx);
+    k[0] = k[1] = k[2] = k[3] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+        if (u.cidx[i] == me) k[0] += u.w1[i] * u.inv[0];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        if (c2[i] == me) k[1] += u.w2[i] * u.inv[1];
+        if (c3[i] == me) k[2] += u.w3[i] * u.inv[2];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (c4[i] == me) k[3] += u.w4[i] * u.inv[3];
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+        if (!u.set[f]) k[f] = 0.0f;
+}
+
 __global__ void __launch_bounds__(kBwdBlock) isb_up_transpose_kernel(
     const uint8_t* __restrict__ guide_coarse, int rows_in, int cols_in, const uint8_t* __restrict__ guide_fine,
     int rows_io, int cols_io, int ncand, float weight_up, float weight_down, float var_inv_i,
@@ -172,70 +174,81 @@ __global__ void __launch_bounds__(kBwdBlock) isb_up_transpose_kernel(
     const int64_t pin = (int64_t)rows_in * cols_in, pio = (int64_t)rows_io * cols_io;
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= pin) return;
-    UpWeights u;
-    up_weights(guide_coarse, rows_in, cols_in, const_cast<uint8_t*>(guide_fine), rows_io, cols_io, (int)(o % cols_in),
-               (int)(o / cols_in), weight_up, weight_down, var_inv_i, false, u);
-    float own[4], w1[9], w2[6], w3[6], w4[4];
+    const int X = (int)(o % cols_in), Y = (int)(o / cols_in);
+    // per neighbour n = 3 (dy + 1) + (dx + 1): the fine index of its pixel F = 0 (the others
+    // are + cols_io, + 1, + cols_io + 1 when set) and the weights k[n][F] with which they read (X, Y)
+    int base[9];
+    float k[9][4];
+    float own[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int f = 0; f < 4; ++f) own[f] = weight_up * u.inv[f];
+    for (int n = 0; n < 9; ++n) {
+        const int x = X + n % 3 - 1, y = Y + n / 3 - 1;
+        base[n] = 0;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) w1[i] = u.w1[i] * u.inv[0];
+        for (int f = 0; f < 4; ++f) k[n][f] = 0.0f;
+        if (x < 0 || y < 0 || x >= cols_in || y >= rows_in) continue;
+        UpWeights u;
+        up_weights(guide_coarse, rows_in, cols_in, const_cast<uint8_t*>(guide_fine), rows_io, cols_io, x, y,
+                   weight_up, weight_down, var_inv_i, false, u);
+        add_tap_weights(u, o, k[n]);
+        base[n] = (int)u.fidx[0];
+        if (n == 4)
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        w2[i] = u.w2[i] * u.inv[1];
-        w3[i] = u.w3[i] * u.inv[2];
+            for (int f = 0; f < 4; ++f) own[f] = u.set[f] ? weight_up * u.inv[f] : 0.0f;
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) w4[i] = u.w4[i] * u.inv[3];
-    const int64_t c2[6] = SSG_TAPS2(u.cidx);
-    const int64_t c3[6] = SSG_TAPS3(u.cidx);
-    const int64_t c4[4] = SSG_TAPS4(u.cidx);
+    const int x2 = 2 * X, y2 = 2 * Y;
+    const bool set1 = y2 + 1 < rows_io, set2 = x2 + 1 < cols_io;
+    const int64_t fo[4] = {(int64_t)y2 * cols_io + x2, (int64_t)(y2 + 1) * cols_io + x2, (int64_t)y2 * cols_io + x2 + 1,
+                           (int64_t)(y2 + 1) * cols_io + x2 + 1};
+    const bool fset[4] = {true, set1, set2, set1 && set2};
     for (int z = 0; z < ncand; ++z) {
         const float* gf = grad_f_fine + (int64_t)z * pio;
-        float* gc = grad_c_fine + (int64_t)z * pio;
-        float* g1 = grad_f_coarse + (int64_t)z * pin;
-        float g[4];
+        float acc = 0.0f;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {
-            g[f] = u.set[f] ? gf[u.fidx[f]] : 0.0f;
-            if (u.set[f]) gc[u.fidx[f]] += own[f] * g[f];
+        for (int n = 0; n < 9; ++n) {
+            const float* g = gf + base[n];
+            if (k[n][0] != 0.0f) acc += k[n][0] * g[0];
+            if (k[n][1] != 0.0f) acc += k[n][1] * g[cols_io];
+            if (k[n][2] != 0.0f) acc += k[n][2] * g[1];
+            if (k[n][3] != 0.0f) acc += k[n][3] * g[cols_io + 1];
         }
+        grad_f_coarse[(int64_t)z * pin + o] = acc;
+        float* gc = grad_c_fine + (int64_t)z * pio;
 #pragma unroll
-        for (int i = 0; i < 9; ++i) atomicAdd(g1 + u.cidx[i], w1[i] * g[0]);
-        if (u.set[1])
-#pragma unroll
-            for (int i = 0; i < 6; ++i) atomicAdd(g1 + c2[i], w2[i] * g[1]);
-        if (u.set[2])
-#pragma unroll
-            for (int i = 0; i < 6; ++i) atomicAdd(g1 + c3[i], w3[i] * g[2]);
-        if (u.set[3])
-#pragma unroll
-            for (int i = 0; i < 4; ++i) atomicAdd(g1 + c4[i], w4[i] * g[3]);
+        for (int f = 0; f < 4; ++f)
+            if (fset[f]) gc[fo[f]] = own[f] * gf[fo[f]];
     }
 }
 
 // Transpose of one down step s (fine level s - 1, coarse level s):
-//   c_s[o] = sum_t w_t c_{s-1}[idx_t] / wsum   =>   g_c_{s-1}[idx_t] += w_t / wsum * g_c_s[o]
-__global__ void __launch_bounds__(kBwdBlock) isb_down_transpose_kernel(const uint8_t* __restrict__ guide_in,
-                                                                       int rows_in, int cols_in, int rows_out,
-                                                                       int cols_out, int ncand, float var_inv_i,
-                                                                       const float* __restrict__ grad_c_coarse,
-                                                                       float* __restrict__ grad_c_fine)
+//   c_s[o] = sum_t w_t c_{s-1}[idx_t] / wsum   =>   g_c_{s-1}[i] += sum_{o, t: idx_t(o) = i} w_t / wsum * g_c_s[o]
+// One thread per fine cell i = (X, Y): the coarse pixels whose edge-clamped 3 x 3 taps can hold
+// it are those with |X - 2 x| <= 1 and |Y - 2 y| <= 1 (at most four); their normalised weights
+// are recomputed as the forward step forms them, and the cell adds their gradients in a fixed
+// order to what it holds (the up transpose's own-pixel part).
+__device__ __forceinline__ void down_taps(int x, int y, int rows_in, int cols_in, int64_t (&idx)[9])
 {
-    const int64_t pout = (int64_t)rows_out * cols_out, pin = (int64_t)rows_in * cols_in;
-    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= pout) return;
-    const int x = (int)(o % cols_out), y = (int)(o / cols_out);
     const int x2 = 2 * x, y2 = 2 * y;
     const int px = min(x2 + 1, cols_in - 1), py = min(y2 + 1, rows_in - 1);
     const int mx = max(x2 - 1, 0), my = max(y2 - 1, 0);
-    const int64_t idx[9] = {(int64_t)y2 * cols_in + x2,  (int64_t)my * cols_in + mx, (int64_t)y2 * cols_in + mx,
-                            (int64_t)py * cols_in + mx,  (int64_t)py * cols_in + x2, (int64_t)py * cols_in + px,
-                            (int64_t)y2 * cols_in + px,  (int64_t)my * cols_in + px, (int64_t)my * cols_in + x2};
+    idx[0] = (int64_t)y2 * cols_in + x2;
+    idx[1] = (int64_t)my * cols_in + mx;
+    idx[2] = (int64_t)y2 * cols_in + mx;
+    idx[3] = (int64_t)py * cols_in + mx;
+    idx[4] = (int64_t)py * cols_in + x2;
+    idx[5] = (int64_t)py * cols_in + px;
+    idx[6] = (int64_t)y2 * cols_in + px;
+    idx[7] = (int64_t)my * cols_in + px;
+    idx[8] = (int64_t)my * cols_in + x2;
+}
+
+// normalised weights of the 3 x 3 taps of coarse pixel (x, y) (isb_filter.cu:44-119)
+__device__ __forceinline__ void down_weights(const uint8_t* __restrict__ guide_in, const int64_t (&idx)[9],
+                                             float var_inv_i, float (&w)[9])
+{
     float cur[3];
     load_guide(guide_in, idx[0], cur);
     const float base[8] = {0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f, 0.25f, 0.5f};
-    float w[9];
     w[0] = 1.0f;
     float wsum = 1.0f;
 #pragma unroll
@@ -247,13 +260,46 @@ __global__ void __launch_bounds__(kBwdBlock) isb_down_transpose_kernel(const uin
     }
 #pragma unroll
     for (int t = 0; t < 9; ++t) w[t] = w[t] / wsum;
-    (void)pin;
-    for (int z = 0; z < ncand; ++z) {
-        const float g = grad_c_coarse[(int64_t)z * pout + o];
-        if (g == 0.0f) continue;
-        float* gf = grad_c_fine + (int64_t)z * pin;
+}
+
+__global__ void __launch_bounds__(kBwdBlock) isb_down_transpose_kernel(const uint8_t* __restrict__ guide_in,
+                                                                       int rows_in, int cols_in, int rows_out,
+                                                                       int cols_out, int ncand, float var_inv_i,
+                                                                       const float* __restrict__ grad_c_coarse,
+                                                                       float* __restrict__ grad_c_fine)
+{
+    const int64_t pout = (int64_t)rows_out * cols_out, pin = (int64_t)rows_in * cols_in;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pin) return;
+    const int X = (int)(i % cols_in), Y = (int)(i / cols_in);
+    int64_t co[4];
+    float k[4];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) atomicAdd(gf + idx[t], w[t] * g);
+    for (int n = 0; n < 4; ++n) {
+        // odd X: x in {(X - 1) / 2, (X + 1) / 2}; even X: x = X / 2 only (n & 1 = 1 is skipped)
+        const int x = (X >> 1) + (n & 1), y = (Y >> 1) + (n >> 1);
+        co[n] = 0;
+        k[n] = 0.0f;
+        const bool none = ((n & 1) && !(X & 1)) || ((n >> 1) && !(Y & 1));
+        if (none || x >= cols_out || y >= rows_out) continue;
+        int64_t idx[9];
+        down_taps(x, y, rows_in, cols_in, idx);
+        float w[9];
+        down_weights(guide_in, idx, var_inv_i, w);
+        float kk = 0.0f;
+#pragma unroll
+        for (int t = 0; t < 9; ++t)
+            if (idx[t] == i) kk += w[t];
+        co[n] = (int64_t)y * cols_out + x;
+        k[n] = kk;
+    }
+    for (int z = 0; z < ncand; ++z) {
+        const float* gc = grad_c_coarse + (int64_t)z * pout;
+        float acc = 0.0f;
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+            if (k[n] != 0.0f) acc += k[n] * gc[co[n]];
+        grad_c_fine[(int64_t)z * pin + i] += acc;
     }
 }
 
@@ -268,7 +314,6 @@ struct SweepBwdParams {
     TorchCam cams[SSG_MAX_CAMERAS];
     float rt[SSG_MAX_CAMERAS][12];
     const float* images[SSG_MAX_CAMERAS];
-    float* grad_images[SSG_MAX_CAMERAS];
     float cand[SSG_MAX_CANDIDATES];
 };
 
@@ -302,20 +347,53 @@ __device__ __forceinline__ void project_jacobian(const float p[3], const TorchCa
     jv[2] = k.fy * (-y * dn[2] * in2);
 }
 
+// The image gradient's fixed-point scale: 2^e with e = 62 - ceil(log2 count) - ceil(log2 m), m the
+// largest |dL/dcost| (its float bits) and count a bound on the contributions one texel can receive
+// (each at most m x the candidates in magnitude): no sum leaves the int64 range, and a
+// contribution is rounded by at most m 2^-(63 - log2 count).  0 when m is 0, inf or NaN.
+__device__ __forceinline__ float fixed_scale(uint32_t absmax_bits, double count)
+{
+    const float m = __uint_as_float(absmax_bits);
+    if (!(m > 0.0f) || !(m <= 3.0e38f)) return 0.0f;
+    int em, ec;
+    frexpf(m, &em);     // m < 2^em
+    frexp(count, &ec);  // count < 2^ec
+    const int e = max(-120, min(62 - ec - em, 120));
+    return ldexpf(1.0f, e);
+}
+
+__device__ __forceinline__ void fixed_add(long long* acc, float x, float scale)
+{
+    const long long q = __float2ll_rn(x * scale);
+    if (q) atomicAdd(reinterpret_cast<unsigned long long*>(acc), (unsigned long long)q);
+}
+
+// largest |x| over n values, as float bits (monotonic for non-negative floats; NaN above inf)
+__global__ void __launch_bounds__(kBwdBlock) absmax_kernel(const float* __restrict__ x, int64_t n,
+                                                           uint32_t* __restrict__ out)
+{
+    uint32_t m = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, __float_as_uint(x[i]) & 0x7FFFFFFFu);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xFFFFFFFFu, m, off));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_constant__ SweepBwdParams p,
                                                                    const int8_t* __restrict__ selected,
                                                                    const float* __restrict__ grad_cost,
-                                                                   double* __restrict__ grad_pose)
+                                                                   const uint32_t* __restrict__ absmax,
+                                                                   long long* __restrict__ image_acc,
+                                                                   double* __restrict__ pose_partial)
 {
-    // the extrinsic-gradient reduction in float64: a pixel's candidates are summed in float32,
-    // pixels and blocks in float64
-    __shared__ double pose_acc[SSG_MAX_CAMERAS][6];
-    for (int j = threadIdx.x; j < SSG_MAX_CAMERAS * 6; j += blockDim.x) (&pose_acc[0][0])[j] = 0.0;
-    __syncthreads();
     const int64_t P = (int64_t)p.cols * p.rows;
+    const float scale = fixed_scale(*absmax, 2.0 * (double)P * p.ncand);
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int sel = i < P ? selected[i] : -1;
-    if (i < P && sel >= 0 && sel < p.ncam) {
+    const bool active = i < P && sel >= 0 && sel < p.ncam;
+    float gsrc[6] = {0, 0, 0, 0, 0, 0}, gref6[6] = {0, 0, 0, 0, 0, 0};
+    if (active) {
         float pu[3];
         unproject_torch((float)(i % p.cols), (float)(i / p.cols), p.ref, pu);
         const float* refimg = p.images[p.reference] + 3 * i;
@@ -325,9 +403,8 @@ __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_
 #pragma unroll
         for (int j = 0; j < 12; ++j) rt[j] = p.rt[sel][j];
         const float* img = p.images[sel];
-        float* gimg = p.grad_images[sel];
+        long long* gimg = image_acc + (int64_t)sel * P * 3;
         float gref[3] = {0.0f, 0.0f, 0.0f};
-        float gsrc[6] = {0, 0, 0, 0, 0, 0}, gref6[6] = {0, 0, 0, 0, 0, 0};
         for (int k = 0; k < p.ncand; ++k) {
             const float g = grad_cost[(int64_t)k * P + i];
             if (g == 0.0f) continue;
@@ -386,9 +463,9 @@ __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_
 #pragma unroll
             for (int t = 0; t < 4; ++t)
                 if (in[t]) {
-                    float* gv = gimg + 3 * ((int64_t)(int)ys[t] * p.cols + (int)xs[t]);
+                    long long* gv = gimg + 3 * ((int64_t)(int)ys[t] * p.cols + (int)xs[t]);
 #pragma unroll
-                    for (int ch = 0; ch < 3; ++ch) atomicAdd(gv + ch, gs[ch] * w[t]);
+                    for (int ch = 0; ch < 3; ++ch) fixed_add(gv + ch, gs[ch] * w[t], scale);
                 }
             // d ix / d u = d iy / d v = 1 (the normalisation round trip is the identity)
             const float gu = gs[0] * sx[0] + gs[1] * sx[1] + gs[2] * sx[2];
@@ -415,20 +492,71 @@ __global__ void __launch_bounds__(kBwdBlock) sweep_backward_kernel(const __grid_
             gref6[4] += h[1];
             gref6[5] += h[2];
         }
-        float* gr = p.grad_images[p.reference] + 3 * i;
+        long long* gr = image_acc + ((int64_t)p.reference * P + i) * 3;
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) atomicAdd(gr + ch, gref[ch]);
+        for (int ch = 0; ch < 3; ++ch) fixed_add(gr + ch, gref[ch], scale);
+    }
+    // the pose gradient of the block, per camera: a pixel's candidates were summed in float32;
+    // pixels are summed in float64 by a fixed shuffle tree per warp and the warps in order
+    __shared__ double warp_sum[kBwdBlock / 32][6];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = 0; c < p.ncam; ++c) {
+        double v[6];
 #pragma unroll
         for (int j = 0; j < 6; ++j) {
-            atomicAdd(&pose_acc[sel][j], (double)gsrc[j]);
-            atomicAdd(&pose_acc[p.reference][j], (double)gref6[j]);
+            v[j] = 0.0;
+            if (active && sel == c) v[j] += (double)gsrc[j];
+            if (active && c == p.reference) v[j] += (double)gref6[j];
         }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int j = 0; j < 6; ++j) v[j] += __shfl_down_sync(0xFFFFFFFFu, v[j], off);
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < 6; ++j) warp_sum[warp][j] = v[j];
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            double t = 0.0;
+            for (int w = 0; w < kBwdBlock / 32; ++w) t += warp_sum[w][threadIdx.x];
+            pose_partial[((int64_t)blockIdx.x * p.ncam + c) * 6 + threadIdx.x] = t;
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int j = threadIdx.x; j < p.ncam * 6; j += blockDim.x) {
-        const double v = (&pose_acc[0][0])[j];
-        if (v != 0.0) atomicAdd(grad_pose + j, v);
+}
+
+// grad_images[c] += image_acc[c] * 2^-e, every camera (NaN where the incoming gradient was not finite)
+struct GradImages {
+    float* ptr[SSG_MAX_CAMERAS];
+};
+
+__global__ void __launch_bounds__(kBwdBlock) image_grad_convert_kernel(const long long* __restrict__ image_acc,
+                                                                       int64_t per_camera, int cameras,
+                                                                       const uint32_t* __restrict__ absmax,
+                                                                       double count, GradImages out)
+{
+    const float scale = fixed_scale(*absmax, count);
+    const bool finite = __uint_as_float(*absmax) <= 3.0e38f;
+    const float inv = scale > 0.0f ? 1.0f / scale : 0.0f;  // a power of two: exact
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < per_camera * cameras;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(k / per_camera);
+        const int64_t e = k - (int64_t)c * per_camera;
+        const long long q = image_acc[k];
+        if (!finite) out.ptr[c][e] = __int_as_float(0x7FFFFFFF);
+        else if (q) out.ptr[c][e] += __ll2float_rn(q) * inv;
     }
+}
+
+// grad_pose[c][j] += the block sums in block order
+__global__ void pose_grad_sum_kernel(const double* __restrict__ pose_partial, int blocks, int cameras,
+                                     double* __restrict__ grad_pose)
+{
+    const int k = threadIdx.x;
+    if (k >= cameras * 6) return;
+    double t = 0.0;
+    for (int b = 0; b < blocks; ++b) t += pose_partial[(int64_t)b * cameras * 6 + k];
+    grad_pose[k] += t;
 }
 
 static SoftParams soft_params(const float* candidates, int ncand, float tau)
@@ -476,11 +604,11 @@ extern "C" int ssg_isb_upsample_softargmin_backward(const uint8_t* d_guide_in, c
                                                     int rows_fine, int cols_fine, int candidate_count,
                                                     float weight_up, float weight_down, float var_inv_i,
                                                     const float* candidates, float temperature,
-                                                    const float* d_grad_inverse_distance, float* d_grad_cost_fine,
-                                                    float* d_grad_filtered_coarse, void* stream)
+                                                    const float* d_grad_inverse_distance, float* d_grad_filtered_fine,
+                                                    void* stream)
 {
     SSG_REQUIRE(d_guide_in && d_cost_in && d_guide_fine && d_cost_fine && candidates && d_grad_inverse_distance &&
-                    d_grad_cost_fine && d_grad_filtered_coarse,
+                    d_grad_filtered_fine,
                 "null pointer");
     if (int e = check_up_sizes(rows_in, cols_in, rows_fine, cols_fine)) return e;
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
@@ -489,8 +617,8 @@ extern "C" int ssg_isb_upsample_softargmin_backward(const uint8_t* d_guide_in, c
     isb_up_softargmin_backward_kernel<<<grid_1d((int64_t)rows_in * cols_in, kBwdBlock), kBwdBlock, 0,
                                         as_stream(stream)>>>(d_guide_in, d_cost_in, rows_in, cols_in, d_guide_fine,
                                                              d_cost_fine, rows_fine, cols_fine, weight_up, weight_down,
-                                                             var_inv_i, sp, d_grad_inverse_distance, d_grad_cost_fine,
-                                                             d_grad_filtered_coarse);
+                                                             var_inv_i, sp, d_grad_inverse_distance,
+                                                             d_grad_filtered_fine);
     return launch_status("isb_up_softargmin_backward_kernel");
 }
 
@@ -517,22 +645,35 @@ extern "C" int ssg_isb_downsample_transpose(const uint8_t* d_guide_in, int rows_
     SSG_REQUIRE(d_guide_in && d_grad_cost_coarse && d_grad_cost_fine, "null pointer");
     if (int e = check_up_sizes(rows_out, cols_out, rows_in, cols_in)) return e;
     SSG_REQUIRE(candidate_count >= 1, "candidate_count must be positive");
-    isb_down_transpose_kernel<<<grid_1d((int64_t)rows_out * cols_out, kBwdBlock), kBwdBlock, 0, as_stream(stream)>>>(
+    isb_down_transpose_kernel<<<grid_1d((int64_t)rows_in * cols_in, kBwdBlock), kBwdBlock, 0, as_stream(stream)>>>(
         d_guide_in, rows_in, cols_in, rows_out, cols_out, candidate_count, var_inv_i, d_grad_cost_coarse,
         d_grad_cost_fine);
     return launch_status("isb_down_transpose_kernel");
+}
+
+// scratch of ssg_sweep_cost_backward: the largest |dL/dcost| (256 bytes), the fixed-point image
+// sums (camera_count x pixels x 3 int64) and the block sums of the pose gradient
+static int64_t sweep_backward_blocks(int cols, int rows) { return grid_1d((int64_t)cols * rows, kBwdBlock); }
+
+extern "C" size_t ssg_sweep_backward_scratch_bytes(int cols, int rows, int camera_count)
+{
+    if (cols <= 0 || rows <= 0 || camera_count < 1 || camera_count > SSG_MAX_CAMERAS) return 0;
+    const int64_t P = (int64_t)cols * rows;
+    return (size_t)(256 + (int64_t)camera_count * P * 3 * 8 +
+                    sweep_backward_blocks(cols, rows) * camera_count * 6 * 8);
 }
 
 extern "C" int ssg_sweep_cost_backward(int cols, int rows, int camera_count, const ssg_camera* cameras, int reference,
                                        const float* relative_poses, const float* const* d_images,
                                        float* const* d_grad_images, const int8_t* d_selected,
                                        const float* candidates, int candidate_count, const float* d_grad_cost,
-                                       double* d_grad_pose, void* stream)
+                                       double* d_grad_pose, void* d_scratch, void* stream)
 {
     SSG_REQUIRE(cols > 0 && rows > 0, "resolution must be positive");
     SSG_REQUIRE(cameras && relative_poses && d_images && d_grad_images && d_selected && candidates && d_grad_cost &&
-                    d_grad_pose,
+                    d_grad_pose && d_scratch,
                 "null pointer");
+    SSG_REQUIRE(((uintptr_t)d_scratch & 255) == 0, "d_scratch must be 256-byte aligned");
     SSG_REQUIRE(camera_count >= 1 && camera_count <= SSG_MAX_CAMERAS, "camera_count out of range");
     SSG_REQUIRE(reference >= 0 && reference < camera_count, "reference out of range");
     SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
@@ -549,16 +690,33 @@ extern "C" int ssg_sweep_cost_backward(int cols, int rows, int camera_count, con
     p.inv_cols = 1.0f / (float)cols;
     p.inv_rows = 1.0f / (float)rows;
     p.ref = make_torch_cam(cameras[reference]);
+    GradImages out{};
     for (int c = 0; c < camera_count; ++c) {
         SSG_REQUIRE(d_images[c] && d_grad_images[c], "image %d or its gradient is NULL", c);
         p.cams[c] = make_torch_cam(cameras[c]);
         p.images[c] = d_images[c];
-        p.grad_images[c] = d_grad_images[c];
+        out.ptr[c] = d_grad_images[c];
         std::memcpy(p.rt[c], relative_poses + 12 * c, sizeof(float) * 12);
     }
     for (int k = 0; k < candidate_count; ++k) p.cand[k] = candidates[k];
     const int64_t P = (int64_t)cols * rows;
-    sweep_backward_kernel<<<grid_1d(P, kBwdBlock), kBwdBlock, 0, as_stream(stream)>>>(p, d_selected, d_grad_cost,
-                                                                                      d_grad_pose);
+    const int64_t blocks = sweep_backward_blocks(cols, rows);
+    uint8_t* scratch = static_cast<uint8_t*>(d_scratch);
+    uint32_t* absmax = reinterpret_cast<uint32_t*>(scratch);
+    long long* image_acc = reinterpret_cast<long long*>(scratch + 256);
+    double* pose_partial = reinterpret_cast<double*>(scratch + 256 + (int64_t)camera_count * P * 3 * 8);
+    cudaStream_t st = as_stream(stream);
+    const cudaError_t e = cudaMemsetAsync(scratch, 0, 256 + (size_t)camera_count * P * 3 * 8, st);
+    if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    const int64_t volume = P * candidate_count;
+    absmax_kernel<<<(unsigned)std::min<int64_t>(grid_1d(volume, kBwdBlock), 4096), kBwdBlock, 0, st>>>(d_grad_cost,
+                                                                                                       volume, absmax);
+    sweep_backward_kernel<<<(unsigned)blocks, kBwdBlock, 0, st>>>(p, d_selected, d_grad_cost, absmax, image_acc,
+                                                                  pose_partial);
+    const double count = 2.0 * (double)P * candidate_count;  // the sweep kernel's bound
+    image_grad_convert_kernel<<<(unsigned)std::min<int64_t>(grid_1d(P * 3 * camera_count, kBwdBlock), 8192),
+                                kBwdBlock, 0, st>>>(image_acc, P * 3, camera_count, absmax, count, out);
+    pose_grad_sum_kernel<<<1, 32 * ((camera_count * 6 + 31) / 32), 0, st>>>(pose_partial, (int)blocks, camera_count,
+                                                                             d_grad_pose);
     return launch_status("sweep_backward_kernel");
 }

@@ -11,7 +11,9 @@ library).  It is differentiable with respect to the matching images and to per-c
 pose deltas delta_c = (omega_c, v_c), the camera poses being T_c [Exp(omega_c), v_c].  The
 backward pass recomputes the cost volume and the filter pyramid instead of storing them, runs
 the filter transposed (its weights come from uint8 guides and get no gradient), and reduces the
-pose gradient per camera in float64; the pose composition is float64 on the host.
+pose gradient per camera in float64; the pose composition is float64 on the host.  The gradients
+are bit-reproducible run to run: the transposed filter steps gather in a fixed order, the image
+gradient is summed in 64-bit fixed point and the pose gradient by a fixed float64 tree.
 
 Temperature: 2 cost units by default.  Costs are sums of three absolute 8-bit differences; near
 the minimum, neighbouring candidates typically differ by a few units, so tau = 2 keeps the
@@ -98,6 +100,9 @@ class DifferentiableSweep:
         self.gc = [torch.empty(self.N * r * c, **f32) for r, c in self.shapes]
         self.weights = level_weights(self.L, self.sigma_s)
         self.var_inv_i = 1 / (2 * self.sigma_i * self.sigma_i)
+        # the sweep backward's fixed-point image sums and pose block sums
+        scratch = N.library().ssg_sweep_backward_scratch_bytes(self.cols, self.rows, self.C)
+        self._bwd_scratch = torch.empty((scratch + 255) // 256 * 256, dtype=torch.uint8, device=dev)
 
     def set_selection(self, selected):
         """Use another run's camera-selection maps ([references][rows, cols])."""
@@ -161,16 +166,14 @@ class DifferentiableSweep:
             self._pyramid(r, images, rel, stream)
             (rc, cc) = self.shapes[1]
             wu, wd = self.weights[0]
-            for t in self.gf[1:]:
-                t.zero_()
+            # dL/dF of the filtered level 0, then every up step transposed from level 0 upwards:
+            # each writes its level's own-pixel gradient and the next level's filtered gradient
             N.call("ssg_isb_upsample_softargmin_backward", self.g_filt[1].data_ptr(), self.costs[1].data_ptr(), rc, cc,
                    self.g_orig[0].data_ptr(), self.costs[0].data_ptr(), rows, cols, n, wu, wd, self.var_inv_i,
-                   self._cand, self.temperature, grad_q[slot].data_ptr(), self.gc[0].data_ptr(),
-                   self.gf[1].data_ptr(), stream)
-            for s in range(1, self.L - 1):
+                   self._cand, self.temperature, grad_q[slot].data_ptr(), self.gf[0].data_ptr(), stream)
+            for s in range(0, self.L - 1):
                 (rc, cc), (rf, cf) = self.shapes[s + 1], self.shapes[s]
                 wu, wd = self.weights[s]
-                self.gc[s].zero_()
                 N.call("ssg_isb_upsample_transpose", self.g_filt[s + 1].data_ptr(), rc, cc, self.g_orig[s].data_ptr(),
                        rf, cf, n, wu, wd, self.var_inv_i, self.gf[s].data_ptr(), self.gc[s].data_ptr(),
                        self.gf[s + 1].data_ptr(), stream)
@@ -183,7 +186,7 @@ class DifferentiableSweep:
                    N.pointers([images[c].data_ptr() for c in range(self.C)]),
                    N.pointers([grad_images[c].data_ptr() for c in range(self.C)]),
                    self.selected[slot].data_ptr(), self._cand, n, self.gc[0].data_ptr(), grad_local.data_ptr(),
-                   stream)
+                   self._bwd_scratch.data_ptr(), stream)
         # local right perturbations at T [Exp(omega), v]  ->  gradients with respect to (omega, v)
         g = grad_local.cpu()
         out = torch.empty_like(g)

@@ -68,6 +68,24 @@ def test_forward_matches_float64(setting):
     assert err <= 3e-5
 
 
+def test_gradients_are_bit_reproducible(setting):
+    """Two backward passes of the same inputs give the same bits: the transposed filter steps
+    gather in a fixed order, the image gradient is summed in 64-bit fixed point, and the pose
+    gradient by a fixed float64 tree (no float atomic adds)."""
+    sweep, ref, images, gt = setting
+    gt_t = torch.as_tensor(gt)
+    grads = []
+    for _ in range(3):
+        im = torch.as_tensor(images, device=DEV).requires_grad_()
+        de = torch.zeros(4, 6, dtype=torch.float64, device=DEV, requires_grad=True)
+        _loss(sweep(im, de).double().cpu(), gt_t).backward()
+        grads.append((im.grad.cpu().numpy(), de.grad.cpu().numpy()))
+    assert np.abs(grads[0][0]).max() > 0 and np.abs(grads[0][1]).max() > 0
+    for g_im, g_de in grads[1:]:
+        np.testing.assert_array_equal(g_im, grads[0][0])
+        np.testing.assert_array_equal(g_de, grads[0][1])
+
+
 def test_gradients_match_float64_autograd_and_finite_differences(setting):
     sweep, ref, images, gt = setting
     gt_t = torch.as_tensor(gt)
@@ -195,10 +213,10 @@ def _c4_loss64(frames, deltas):
 
 
 def test_c4_gradients_at_full_size(c4):
-    """Gradients of the 8-frame loss with respect to the 6-DoF pose deltas and the images: against
-    central differences of the float64 loss (relative error <= 1e-3 at step 1e-4, with the float64
-    gradient's own error at that step as the control, and at step 1e-7) and against float64
-    autograd (bars below)."""
+    """Gradients of the 8-frame loss with respect to the 6-DoF pose deltas and the images: the same
+    bits from a second backward; against central differences of the float64 loss (relative error
+    <= 1e-3 at step 1e-4, with the float64 gradient's own error at that step as the control, and at
+    step 1e-7) and against float64 autograd (bars below)."""
     sweep, frames = c4
     de = torch.zeros(4, 6, dtype=torch.float64, device=DEV, requires_grad=True)
     ims = [torch.as_tensor(im, device=DEV).requires_grad_() for im, _, _ in frames]
@@ -206,6 +224,12 @@ def test_c4_gradients_at_full_size(c4):
     loss.backward()
     g_de = de.grad.detach().cpu()
     g_im = [x.grad.detach().double() for x in ims]
+    # a second backward of the same inputs gives the same bits
+    de2 = torch.zeros(4, 6, dtype=torch.float64, device=DEV, requires_grad=True)
+    ims2 = [torch.as_tensor(im, device=DEV).requires_grad_() for im, _, _ in frames]
+    (sum(_loss(sweep(x, de2).double(), gt) for x, (_, gt, _) in zip(ims2, frames)) / len(frames)).backward()
+    assert torch.equal(de2.grad.cpu(), g_de)
+    assert all(torch.equal(a.grad, b.grad) for a, b in zip(ims2, ims))
 
     # float64 autograd one frame at a time (each frame's graph holds ~20 GB of intermediates)
     de64 = torch.zeros(4, 6, dtype=torch.float64, device=DEV, requires_grad=True)
