@@ -96,6 +96,13 @@ typedef struct {
                                          block barrier between chunks (same bits; default); 0 =
                                          double-buffered chunk tiles */
 #define SSG_TUNE_UP_WHOLE 12          /* the same for the chunked coarse upsampling steps (default 0) */
+#define SSG_TUNE_ISB_TAIL 13          /* ssg_isb_filter_batch: from the first level of at most this many
+                                         pixels (0, 256, 1024 or 4096; 0 = none), the remaining down and
+                                         up steps run as one launch, one block per instance (same bits;
+                                         default 1024) */
+#define SSG_TUNE_POST_TAIL 14         /* the same for the batched single-candidate filter
+                                         (ssg_isb_apply_batch with one candidate: the distance
+                                         post-filter): 0, 1024, 4096 or 16384 (default 4096) */
 #define SSG_TUNE_TMA_WITHHOLD 7       /* tests of the bounded TMA wait: 1 = the TMA-staged upsampling arms
                                          its tile barriers but issues no copy, so every block's first
                                          wait runs out (after a short limit), it writes nothing and
@@ -359,6 +366,17 @@ SSG_API int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_cost
  * python/depth_estimation.py:179-198): float32 coarse level, fine (level-0) volume stored as
  * `storage`; d_distance / d_index instances x fine pixels; d_distance_copy (or NULL) receives the
  * same distances (the post-filter's input, which it filters in place). */
+/* The cost filter of a batch up to level 1 (python/isb_filter.py:72-134 without the last up
+ * step, which ssg_isb_upsample_select_batch fuses with the selection): level 0 (`storage`) down to
+ * level level_count - 1, then back up to level 1.  d_guides / d_costs: level_count device pointers
+ * to the levels of every instance (the layouts of ssg_isb_downsample_batch; levels from 1 on
+ * float32, 32-byte aligned); weight_up / weight_down: host arrays of the up steps' weights, indexed
+ * by the fine level.  The small levels run as one fused launch (SSG_TUNE_ISB_TAIL): the same
+ * results bit for bit as one ssg_isb_downsample_batch / ssg_isb_upsample_batch call per step. */
+SSG_API int ssg_isb_filter_batch(uint8_t* const* d_guides, void* const* d_costs, int level_count, int rows, int cols,
+                                 int candidate_count, int instances, int storage, const float* weight_up,
+                                 const float* weight_down, float var_inv_i, void* stream);
+
 SSG_API int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in, int cols_in,
                                           uint8_t* d_guide_inout, const void* d_cost_fine, int rows_fine,
                                           int cols_fine, int candidate_count, int instances, int storage,

@@ -7,6 +7,7 @@ NativeLibraryError.  Device pointers are passed as integers (``tensor.data_ptr()
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import threading
 
@@ -36,6 +37,8 @@ TUNE_SWEEP_TILES = 9
 TUNE_HOLE_TAIL = 10
 TUNE_SELECT_WHOLE = 11
 TUNE_UP_WHOLE = 12
+TUNE_ISB_TAIL = 13
+TUNE_POST_TAIL = 14
 STATUS_TMA_TIMEOUT = 1
 STATUS_BARRIER_TIMEOUT = 2
 HOLE_SCRATCH_HEADER = 8
@@ -118,6 +121,7 @@ SIGNATURES = {
     "ssg_stage_images": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ssg_stage_images_u8": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ssg_sweep_cost_batch": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P]),
+    "ssg_isb_filter_batch": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _F, _P]),
     "ssg_stage_images_resized": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _I, _P, _P, _P, _P]),
     "ssg_sweep_cost_batch_entries": (_I, [_I, _I, _I, _I, _P, _I, _P, _P, _P, _I, _P, _P, _P, _P, _I, _I, _P,
                                           _P]),
@@ -263,6 +267,32 @@ def hole_filling_launches(iterations: int) -> int:
     return 1 + iterations
 
 
+def isb_tail_first(rows: int, cols: int, levels: int, max_pixels: int) -> int:
+    """The first level of a pyramid's fused tail (the library's rule): the first level s >= 1 of at
+    most max_pixels pixels with s <= levels - 2, else levels (no tail)."""
+    if max_pixels <= 0:
+        return levels
+    for s in range(1, levels - 1):
+        if math.ceil(rows / 2 ** s) * math.ceil(cols / 2 ** s) <= max_pixels:
+            return s
+    return levels
+
+
+def isb_filter_launches(rows: int, cols: int, levels: int) -> int:
+    """Kernels ssg_isb_filter_batch launches: a down step per level up to the tail's first, the
+    tail, an up step per level below it (SSG_TUNE_ISB_TAIL)."""
+    first = isb_tail_first(rows, cols, levels, library().ssg_tuning_get(TUNE_ISB_TAIL))
+    return 2 * first if first < levels else (levels - 1) + (levels - 2)
+
+
+def isb_apply_launches(rows: int, cols: int, levels: int, candidates: int) -> int:
+    """Kernels ssg_isb_apply_batch launches (the single-candidate filter fuses its small levels,
+    SSG_TUNE_POST_TAIL)."""
+    first = isb_tail_first(rows, cols, levels, library().ssg_tuning_get(TUNE_POST_TAIL)) if candidates == 1 \
+        else levels
+    return 2 * first + 1 if first < levels else 2 * max(0, levels - 1)
+
+
 def kernels_launched(name: str, args) -> int:
     """Number of kernels one call of entry point ``name`` with ``args`` launches."""
     if name in ("ssg_last_error", "ssg_version", "ssg_limits", "ssg_isb_level_count", "ssg_tuning_set",
@@ -270,8 +300,12 @@ def kernels_launched(name: str, args) -> int:
         return 0
     if name == "ssg_eval_panoramas":
         return 3
-    if name in ("ssg_isb_apply", "ssg_isb_apply_batch"):
+    if name == "ssg_isb_apply":
         return 2 * max(0, int(args[2]) - 1)
+    if name == "ssg_isb_apply_batch":
+        return isb_apply_launches(int(args[3]), int(args[4]), int(args[2]), int(args[5]))
+    if name == "ssg_isb_filter_batch":
+        return isb_filter_launches(int(args[3]), int(args[4]), int(args[2]))
     if name == "ssg_reproject_distance":
         return 2 if args[6] else 1
     if name in ("ssg_reproject_distance_batch", "ssg_reproject_distance_batch_approx"):

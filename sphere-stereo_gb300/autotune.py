@@ -30,14 +30,17 @@ KNOBS = {
     "hole_blocks_per_sm": (N.TUNE_HOLE_BLOCKS_PER_SM, ("ssg_inpaint_holes_batch",)),
     "merge_frames": (N.TUNE_MERGE_FRAMES, ("ssg_merge_panorama_batch_approx",)),
     "uneven_span": (N.TUNE_UNEVEN_SPAN, ("ssg_uneven_run",)),
-    "isb_up_blocks": (N.TUNE_ISB_UP_BLOCKS, ("ssg_isb_upsample_batch",)),
+    "isb_up_blocks": (N.TUNE_ISB_UP_BLOCKS, ("ssg_isb_upsample_batch", "ssg_isb_filter_batch")),
     "isb_select_blocks": (N.TUNE_ISB_SELECT_BLOCKS, ("ssg_isb_upsample_select_batch",)),
-    "isb_tile_tma": (N.TUNE_ISB_TILE_TMA, ("ssg_isb_upsample_batch", "ssg_isb_upsample_select_batch")),
+    "isb_tile_tma": (N.TUNE_ISB_TILE_TMA, ("ssg_isb_upsample_batch", "ssg_isb_filter_batch",
+                                           "ssg_isb_upsample_select_batch")),
     "hole_persistent": (N.TUNE_HOLE_PERSISTENT, ("ssg_inpaint_holes_batch",)),
     "sweep_tiles": (N.TUNE_SWEEP_TILES, ("ssg_sweep_cost_batch", "ssg_sweep_cost_batch_entries")),
     "hole_tail": (N.TUNE_HOLE_TAIL, ("ssg_inpaint_holes_batch",)),
     "select_whole": (N.TUNE_SELECT_WHOLE, ("ssg_isb_upsample_select_batch",)),
-    "up_whole": (N.TUNE_UP_WHOLE, ("ssg_isb_upsample_batch",)),
+    "up_whole": (N.TUNE_UP_WHOLE, ("ssg_isb_upsample_batch", "ssg_isb_filter_batch")),
+    "isb_tail": (N.TUNE_ISB_TAIL, ("ssg_isb_filter_batch",)),
+    "post_tail": (N.TUNE_POST_TAIL, ("ssg_isb_apply_batch",)),
 }
 
 

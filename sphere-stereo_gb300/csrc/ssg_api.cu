@@ -70,6 +70,8 @@ constexpr int kUnevenSpans[] = {1, 2, 4};
 constexpr int kIsbUpBlocks[] = {2, 3};
 constexpr int kSweepTiles[] = {0, 16, 32};
 constexpr int kHoleTail[] = {0, 3, 4, 6, 8};
+constexpr int kIsbTail[] = {0, 256, 1024, 4096};
+constexpr int kPostTail[] = {0, 1024, 4096, 16384};
 Knob g_knobs[] = {
     {kSweepVariants, 4, {0}},      // SSG_TUNE_SWEEP_VARIANT
     {kHoleBlocks, 3, {4}},         // SSG_TUNE_HOLE_BLOCKS_PER_SM
@@ -84,6 +86,8 @@ Knob g_knobs[] = {
     {kHoleTail, 5, {8}},           // SSG_TUNE_HOLE_TAIL
     {kOnOff, 2, {1}},              // SSG_TUNE_SELECT_WHOLE
     {kOnOff, 2, {0}},              // SSG_TUNE_UP_WHOLE
+    {kIsbTail, 4, {1024}},         // SSG_TUNE_ISB_TAIL
+    {kPostTail, 4, {4096}},        // SSG_TUNE_POST_TAIL
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

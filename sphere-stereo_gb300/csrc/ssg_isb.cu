@@ -137,11 +137,28 @@ const float* range_table(float var_inv_i, cudaStream_t stream)
 // float32 out.
 // One coarse pixel o of a level: pointers are the instance's own; `lut` is the block's filled
 // range table.
-template <int W, typename Tin, typename GL>
+// W float32 costs through L2 (ld.global.cg): for cells written earlier in the same launch, which
+// the read-only path does not see
+template <int W>
+__device__ __forceinline__ void load_coherent(const float* p, float* v)
+{
+    if constexpr (W == 1) {
+        v[0] = __ldcg(p);
+    } else {
+        static_assert(W == 8, "cells of 1 or 8 candidates");
+        const float4 a = __ldcg(reinterpret_cast<const float4*>(p)), b = __ldcg(reinterpret_cast<const float4*>(p) + 1);
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    }
+}
+
+// kCoherent: the costs are read through L2 (with GL = G4C for the guides), for a launch that runs
+// several levels one after the other
+template <int W, typename Tin, typename GL, bool kCoherent = false>
 __device__ __forceinline__ void isb_down_pixel(const uint8_t* __restrict__ guide_in, const Tin* __restrict__ cost_in,
                                                uint8_t* __restrict__ guide_out, float* __restrict__ cost_out,
                                                const LevelGeom& g, int chunks, int o, const float* lut)
 {
+    static_assert(!kCoherent || std::is_same<Tin, float>::value, "coherent reads are of float32 levels");
     const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
     DownTapsT<int> t;
     const int y = o / g.cols_out;  // 32-bit: a level holds fewer than 2^31 pixels
@@ -154,11 +171,13 @@ __device__ __forceinline__ void isb_down_pixel(const uint8_t* __restrict__ guide
     for (int c = 0; c < chunks; ++c) {
         const Tin* src = cost_in + (int64_t)c * pin * W;
         float acc[W];
-        CellIO<W, Tin>::load(src + (int64_t)t.centre * W, acc);
+        if constexpr (kCoherent) load_coherent<W>(reinterpret_cast<const float*>(src) + (int64_t)t.centre * W, acc);
+        else CellIO<W, Tin>::load(src + (int64_t)t.centre * W, acc);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             float v[W];
-            CellIO<W, Tin>::load(src + (int64_t)t.idx[i] * W, v);
+            if constexpr (kCoherent) load_coherent<W>(reinterpret_cast<const float*>(src) + (int64_t)t.idx[i] * W, v);
+            else CellIO<W, Tin>::load(src + (int64_t)t.idx[i] * W, v);
 #pragma unroll
             for (int j = 0; j < W; ++j) acc[j] = kFast ? fmaf(v[j], t.w[i], acc[j]) : fadd(acc[j], fmul(v[j], t.w[i]));
         }
@@ -742,7 +761,7 @@ static cudaError_t launch_up_whole(dim3 grid, cudaStream_t st, const uint8_t* gi
 // ---------------------------------------------------------------------------------------------
 constexpr int kUp1X = 32, kUp1Y = 8;
 
-template <int F, typename GL, bool kWriteGuide>
+template <int F, typename GL, bool kWriteGuide, bool kCoherent = false>
 __device__ __forceinline__ void up1_fine(const typename GL::Pix (&gd)[9], const float (&cv)[9],
                                          uint8_t* __restrict__ guide_io, float* __restrict__ cost_io,
                                          const LevelGeom& g, int x, int y, float weight_up, float weight_down,
@@ -754,7 +773,7 @@ __device__ __forceinline__ void up1_fine(const typename GL::Pix (&gd)[9], const 
     const typename GL::Pix up = GL::load(guide_io, index);
     float w[UpTaps<F>::n], gsum[3];
     const float inv = fine_weights<F, LutRange, GL>(gd, up, weight_up, weight_down, range, w, gsum);
-    float acc = fmul(weight_up, __ldg(cost_io + index));
+    float acc = fmul(weight_up, kCoherent ? __ldcg(cost_io + index) : __ldg(cost_io + index));
 #pragma unroll
     for (int i = 0; i < UpTaps<F>::n; ++i) acc = fadd(acc, fmul(w[i], cv[UpTaps<F>::tap(i)]));
     cost_io[index] = fmul(acc, inv);
@@ -767,7 +786,7 @@ __device__ __forceinline__ void up1_fine(const typename GL::Pix (&gd)[9], const 
 }
 
 // coarse pixel (x, y) of one instance's level pair; `lut` is the block's filled range table
-template <typename GL, bool kWriteGuide>
+template <typename GL, bool kWriteGuide, bool kCoherent = false>
 __device__ __forceinline__ void isb_up1_pixel(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
                                               uint8_t* __restrict__ guide_io, float* __restrict__ cost_io,
                                               const LevelGeom& g, float weight_up, float weight_down, int x, int y,
@@ -778,12 +797,115 @@ __device__ __forceinline__ void isb_up1_pixel(const uint8_t* __restrict__ guide_
     coarse_neighbourhood<int, GL>(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
     float cv[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) cv[k] = __ldg(cost_in + ci[k]);
+    for (int k = 0; k < 9; ++k) cv[k] = kCoherent ? __ldcg(cost_in + ci[k]) : __ldg(cost_in + ci[k]);
     const LutRange range{lut};
-    up1_fine<0, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
-    up1_fine<1, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
-    up1_fine<2, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
-    up1_fine<3, GL, kWriteGuide>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<0, GL, kWriteGuide, kCoherent>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<1, GL, kWriteGuide, kCoherent>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<2, GL, kWriteGuide, kCoherent>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+    up1_fine<3, GL, kWriteGuide, kCoherent>(gd, cv, guide_io, cost_io, g, x, y, weight_up, weight_down, range);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Pyramid tails.  The small levels of a pyramid hold too little work to fill the GPU, and one
+// launch per step costs more than the step: one launch runs every step from level `first` down
+// to the coarsest level and back, one block per instance, the steps separated by block barriers.
+// Each step calls the per-pixel functions of the per-level kernels (the same arithmetic, so the
+// same bits), reading through L2 what earlier steps of the launch wrote.
+// ---------------------------------------------------------------------------------------------
+
+// chunked upsampling of coarse pixel (x, y): its four fine pixels, every chunk, with the per-
+// element arithmetic of up_part (whole 8-candidate cells instead of halves; the candidates are
+// independent)
+template <int F>
+__device__ __forceinline__ void up8_fine(const float (&tap)[9][8], const FinePixel& px, float weight_up,
+                                         float* __restrict__ fine_chunk)
+{
+    if (!px.active) return;
+    float acc[8];
+    load_coherent<8>(fine_chunk + (int64_t)px.index * 8, acc);
+    filter_part<F, 8, true>(tap, px.w, px.inv, weight_up, acc);
+    stg256(fine_chunk + (int64_t)px.index * 8, acc);
+}
+
+__device__ __forceinline__ void isb_up8_pixel(const uint8_t* __restrict__ guide_in, const float* __restrict__ cost_in,
+                                              uint8_t* __restrict__ guide_io, float* __restrict__ cost_io,
+                                              const LevelGeom& g, int chunks, float weight_up, float weight_down,
+                                              int x, int y, const float* lut)
+{
+    const int64_t pin = (int64_t)g.rows_in * g.cols_in, pio = (int64_t)g.rows_out * g.cols_out;
+    int ci[9];
+    G4C::Pix gd[9];
+    coarse_neighbourhood<int, G4C>(guide_in, g.rows_in, g.cols_in, x, y, ci, gd);
+    const LutRange range{lut};
+    FinePixel px[4];
+    fine_setup<0, true, G4C>(gd, guide_io, g, x, y, true, weight_up, weight_down, range, px[0]);
+    fine_setup<1, true, G4C>(gd, guide_io, g, x, y, true, weight_up, weight_down, range, px[1]);
+    fine_setup<2, true, G4C>(gd, guide_io, g, x, y, true, weight_up, weight_down, range, px[2]);
+    fine_setup<3, true, G4C>(gd, guide_io, g, x, y, true, weight_up, weight_down, range, px[3]);
+    for (int c = 0; c < chunks; ++c) {
+        const float* coarse = cost_in + (int64_t)c * pin * 8;
+        float* fine = cost_io + (int64_t)c * pio * 8;
+        float tap[9][8];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) load_coherent<8>(coarse + (int64_t)ci[t] * 8, tap[t]);
+        up8_fine<0>(tap, px[0], weight_up, fine);
+        up8_fine<1>(tap, px[1], weight_up, fine);
+        up8_fine<2>(tap, px[2], weight_up, fine);
+        up8_fine<3>(tap, px[3], weight_up, fine);
+    }
+}
+
+// Levels of a tail: level s of instance 0 (instance i at + i x its pixels x 4 guide bytes and
+// + i x chunks x its pixels x W floats)
+struct TailParams {
+    int levels, first, chunks;
+    int rows[SSG_MAX_LEVELS], cols[SSG_MAX_LEVELS];
+    uint8_t* guides[SSG_MAX_LEVELS];
+    float* costs[SSG_MAX_LEVELS];
+    float weight_up[SSG_MAX_LEVELS], weight_down[SSG_MAX_LEVELS];
+};
+
+template <int W>
+constexpr int kTailThreads = W == 8 ? 256 : 512;
+
+// blockIdx.x: instance.  Down steps first -> first + 1 ... levels - 2 -> levels - 1, then up steps
+// levels - 1 -> levels - 2 ... first + 1 -> first (W = 1: one value per pixel, isb_up1_pixel; W = 8:
+// the chunked layout, isb_up8_pixel).  The up steps form the filtered fine guides.
+template <int W>
+__global__ void __launch_bounds__(kTailThreads<W>) isb_tail_kernel(const __grid_constant__ TailParams T,
+                                                                   float var_inv_i, const float* __restrict__ table)
+{
+    __shared__ __align__(16) float lut[kRangeLutStride];
+    load_range_lut(lut, table, var_inv_i);
+    __syncthreads();
+    const int64_t inst = blockIdx.x;
+    for (int s = T.first + 1; s < T.levels; ++s) {
+        const LevelGeom g{T.rows[s - 1], T.cols[s - 1], T.rows[s], T.cols[s]};
+        const int64_t pin = (int64_t)g.rows_in * g.cols_in, pout = (int64_t)g.rows_out * g.cols_out;
+        const uint8_t* gi = T.guides[s - 1] + inst * pin * 4;
+        const float* ci = T.costs[s - 1] + inst * T.chunks * pin * W;
+        uint8_t* go = T.guides[s] + inst * pout * 4;
+        float* co = T.costs[s] + inst * T.chunks * pout * W;
+        for (int o = threadIdx.x; o < pout; o += blockDim.x)
+            isb_down_pixel<W, float, G4C, true>(gi, ci, go, co, g, T.chunks, o, lut);
+        __syncthreads();
+    }
+    for (int s = T.levels - 2; s >= T.first; --s) {
+        const LevelGeom g{T.rows[s + 1], T.cols[s + 1], T.rows[s], T.cols[s]};
+        const int64_t pc = (int64_t)g.rows_in * g.cols_in, pf = (int64_t)g.rows_out * g.cols_out;
+        const uint8_t* gi = T.guides[s + 1] + inst * pc * 4;
+        const float* ci = T.costs[s + 1] + inst * T.chunks * pc * W;
+        uint8_t* gio = T.guides[s] + inst * pf * 4;
+        float* cio = T.costs[s] + inst * T.chunks * pf * W;
+        for (int k = threadIdx.x; k < pc; k += blockDim.x) {
+            const int y = k / g.cols_in, x = k - y * g.cols_in;
+            if constexpr (W == 1)
+                isb_up1_pixel<G4C, true, true>(gi, ci, gio, cio, g, T.weight_up[s], T.weight_down[s], x, y, lut);
+            else
+                isb_up8_pixel(gi, ci, gio, cio, g, T.chunks, T.weight_up[s], T.weight_down[s], x, y, lut);
+        }
+        __syncthreads();
+    }
 }
 
 // blockIdx.z: instance of contiguous levels
@@ -1101,6 +1223,39 @@ static int launch_up(const uint8_t* gi, const float* ci, int rc, int cc, uint8_t
     return launch_status(kSelect ? "isb_up_kernel<select>" : "isb_up_kernel");
 }
 
+// The first level of a pyramid's fused tail: the first level s >= 1 of at most `max_pixels`
+// pixels, provided the tail then has a step (s <= levels - 2); otherwise `levels` (no tail).
+static int tail_first(int rows, int cols, int levels, int max_pixels)
+{
+    if (max_pixels <= 0) return levels;
+    for (int s = 1; s + 2 <= levels; ++s)
+        if ((int64_t)level_rows(rows, s) * level_rows(cols, s) <= max_pixels) return s;
+    return levels;
+}
+
+template <int W>
+static int launch_tail(uint8_t* const* guides, float* const* costs, int levels, int first, int rows, int cols,
+                       int chunks, int instances, const float* weight_up, const float* weight_down, float var_inv_i,
+                       cudaStream_t st)
+{
+    TailParams T{};
+    T.levels = levels;
+    T.first = first;
+    T.chunks = chunks;
+    for (int s = 0; s < levels; ++s) {
+        T.rows[s] = level_rows(rows, s);
+        T.cols[s] = level_rows(cols, s);
+        T.guides[s] = guides[s];
+        T.costs[s] = costs[s];
+        if (s + 1 < levels) {
+            T.weight_up[s] = weight_up[s];
+            T.weight_down[s] = weight_down[s];
+        }
+    }
+    isb_tail_kernel<W><<<instances, kTailThreads<W>, 0, st>>>(T, var_inv_i, range_table(var_inv_i, st));
+    return launch_status("isb_tail_kernel");
+}
+
 // the whole filter on planar levels (W = 1, chunks = candidates): python/isb_filter.py:72-136
 template <typename GL>
 static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int level_count, int rows, int cols,
@@ -1108,15 +1263,27 @@ static int apply_planar(uint8_t* const* d_guides, float* const* d_costs, int lev
                         int flags = 0)
 {
     const Levels c = isb_constants(level_count, sigma_i, sigma_s);
-    for (int s = 1; s < level_count; ++s) {
+    for (int s = 1; s < level_count; ++s)
+        if (int e = check_levels(level_rows(rows, s - 1), level_rows(cols, s - 1), level_rows(rows, s),
+                                 level_rows(cols, s)))
+            return e;
+    // the batched single-candidate filter (the distance post-filter) runs its small levels as one
+    // fused tail (SSG_TUNE_POST_TAIL: the largest first level, in pixels; 0 = none)
+    const int first = std::is_same<GL, G4>::value && candidate_count == 1
+                          ? tail_first(rows, cols, level_count, tuning(SSG_TUNE_POST_TAIL))
+                          : level_count;
+    for (int s = 1; s < level_count && s <= first; ++s) {
         const int ri = level_rows(rows, s - 1), ci = level_rows(cols, s - 1), ro = level_rows(rows, s),
                   co = level_rows(cols, s);
-        if (int e = check_levels(ri, ci, ro, co)) return e;
         if (int e = launch_down<1, float, GL>(d_guides[s - 1], d_costs[s - 1], ri, ci, d_guides[s], d_costs[s], ro,
                                               co, candidate_count, instances, c.var_inv_i, st))
             return e;
     }
-    for (int s = level_count - 2; s >= 0; --s) {
+    if (first < level_count)
+        if (int e = launch_tail<1>(d_guides, d_costs, level_count, first, rows, cols, 1, instances, c.weight_up,
+                                   c.weight_down, c.var_inv_i, st))
+            return e;
+    for (int s = (first < level_count ? first : level_count - 1) - 1; s >= 0; --s) {
         const int rc = level_rows(rows, s + 1), cc = level_rows(cols, s + 1), rf = level_rows(rows, s),
                   cf = level_rows(cols, s);
         if (int e = launch_up<1, float, false, GL>(d_guides[s + 1], d_costs[s + 1], rc, cc, d_guides[s], d_costs[s],
@@ -1274,6 +1441,47 @@ extern "C" int ssg_isb_upsample_batch(const uint8_t* d_guide_in, const void* d_c
                                       d_guide_inout, static_cast<float*>(d_cost_inout), rows_inout, cols_inout, chunks,
                                       chunks * 8, instances, weight_up, weight_down, var_inv_i, SelectOut{},
                                       as_stream(stream));
+}
+
+extern "C" int ssg_isb_filter_batch(uint8_t* const* d_guides, void* const* d_costs, int level_count, int rows,
+                                    int cols, int candidate_count, int instances, int storage,
+                                    const float* weight_up, const float* weight_down, float var_inv_i, void* stream)
+{
+    SSG_REQUIRE(d_guides && d_costs && weight_up && weight_down, "null pointer");
+    SSG_REQUIRE(level_count >= 2 && level_count <= SSG_MAX_LEVELS, "level_count %d outside [2, %d]", level_count,
+                SSG_MAX_LEVELS);
+    SSG_REQUIRE(rows > 0 && cols > 0, "sizes must be positive");
+    SSG_REQUIRE(instances >= 1 && instances <= 65535, "instances out of range");
+    SSG_REQUIRE(candidate_count >= 1 && candidate_count <= SSG_MAX_CANDIDATES, "candidate_count out of range");
+    for (int s = 0; s < level_count; ++s) {
+        SSG_REQUIRE(d_guides[s] && d_costs[s], "level %d is NULL", s);
+        if (s > 0)
+            if (int e = check_cells(d_costs[s], SSG_STORAGE_F32, "a float32 level")) return e;
+    }
+    const int chunks = chunks_of(candidate_count);
+    cudaStream_t st = as_stream(stream);
+    // small levels as one fused tail (SSG_TUNE_ISB_TAIL: the largest first level, in pixels)
+    const int first = tail_first(rows, cols, level_count, tuning(SSG_TUNE_ISB_TAIL));
+    for (int s = 1; s < level_count && s <= first; ++s)
+        if (int e = ssg_isb_downsample_batch(d_guides[s - 1], d_costs[s - 1], level_rows(rows, s - 1),
+                                             level_rows(cols, s - 1), d_guides[s], d_costs[s], level_rows(rows, s),
+                                             level_rows(cols, s), candidate_count, instances,
+                                             s == 1 ? storage : SSG_STORAGE_F32, var_inv_i, stream))
+            return e;
+    if (first < level_count) {
+        float* costs[SSG_MAX_LEVELS] = {};
+        for (int s = 1; s < level_count; ++s) costs[s] = static_cast<float*>(d_costs[s]);
+        if (int e = launch_tail<8>(d_guides, costs, level_count, first, rows, cols, chunks, instances, weight_up,
+                                   weight_down, var_inv_i, st))
+            return e;
+    }
+    for (int s = (first < level_count ? first : level_count - 1) - 1; s >= 1; --s)
+        if (int e = ssg_isb_upsample_batch(d_guides[s + 1], d_costs[s + 1], level_rows(rows, s + 1),
+                                           level_rows(cols, s + 1), d_guides[s], d_costs[s], level_rows(rows, s),
+                                           level_rows(cols, s), candidate_count, instances, SSG_STORAGE_F32,
+                                           weight_up[s], weight_down[s], var_inv_i, stream))
+            return e;
+    return SSG_OK;
 }
 
 extern "C" int ssg_isb_upsample_select_batch(const uint8_t* d_guide_in, const void* d_cost_in, int rows_in,

@@ -99,6 +99,15 @@ struct G4 {
     }
 };
 
+// G4 read through L2 (ld.global.cg): for kernels that read guides written earlier in the same
+// launch, where the read-only path is not coherent
+struct G4C : G4 {
+    __device__ static __forceinline__ Pix load(const uint8_t* g, int64_t idx)
+    {
+        return __ldcg(reinterpret_cast<const uint32_t*>(g) + idx);
+    }
+};
+
 struct ExpRange {  // evaluates the weight of a colour distance
     float var_inv_i;
     __device__ __forceinline__ float operator()(int d) const { return range_weight((float)d, var_inv_i); }

@@ -7,8 +7,8 @@ One batch of F frames runs the per-frame steps of RGBD_Estimator.estimate_RGBD_p
     ssg_stage_images[_u8|_resized] inputs -> footprints + guides of the references      1 launch
                                    (_resized: decoded 8-bit images of any size, resized on the way)
     ssg_sweep_cost_batch           sweep + cost, 16-bit chunked volume                  1
-    ssg_isb_downsample_batch       L - 1 levels                                         L - 1
-    ssg_isb_upsample_batch         levels L - 2 .. 1                                    L - 2
+    ssg_isb_filter_batch           L - 1 down and L - 2 up steps, the small levels'     fewer than
+                                   steps fused into one launch                          2 L - 3
     ssg_isb_upsample_select_batch  last level + argmin / sub-candidate step             1
     ssg_isb_apply_batch            distance post-filter, fp32, N = 1                    2L - 2
     ssg_reproject_distance_batch_approx  fill + z-buffer                                2
@@ -184,15 +184,9 @@ class BatchPipeline:
 
         if L >= 2:
             weights = level_weights(L, e.sigma_s)
-            for s in range(1, L):
-                (ri, ci), (ro, co) = self.shapes[s - 1], self.shapes[s]
-                N.call("ssg_isb_downsample_batch", guide(s - 1), cost(s - 1), ri, ci, guide(s), cost(s), ro, co,
-                       self.N, inst, self.storage if s == 1 else F32, var_inv_i, stream)
-            for s in range(L - 2, 0, -1):
-                (rc, cc), (rf, cf) = self.shapes[s + 1], self.shapes[s]
-                wu, wd = weights[s]
-                N.call("ssg_isb_upsample_batch", guide(s + 1), cost(s + 1), rc, cc, guide(s), cost(s), rf, cf,
-                       self.N, inst, F32, wu, wd, var_inv_i, stream)
+            N.call("ssg_isb_filter_batch", N.pointers([guide(s) for s in range(L)]),
+                   N.pointers([cost(s) for s in range(L)]), L, rows, cols, self.N, inst, self.storage,
+                   N.floats([w for w, _ in weights]), N.floats([w for _, w in weights]), var_inv_i, stream)
         # the selection writes the raw distance and, for the post-filter to filter in place, a copy
         dist = self.distance.view(-1)[i0 * P:(i0 + inst) * P]
         raw = self.distance_raw.data_ptr() + 4 * i0 * P
@@ -351,7 +345,8 @@ class BatchPipeline:
     # in tuning order: a register bound before the staging it pairs with (a staging choice is timed
     # at the bound already picked)
     TUNED_KNOBS = ("sweep_variant", "sweep_tiles", "isb_up_blocks", "up_whole", "isb_select_blocks", "select_whole",
-                   "isb_tile_tma", "hole_blocks_per_sm", "hole_persistent", "hole_tail", "merge_frames")
+                   "isb_tile_tma", "isb_tail", "post_tail", "hole_blocks_per_sm", "hole_persistent", "hole_tail",
+                   "merge_frames")
     GROUP_CHOICES = (1, 2, 4)
 
     def _apply_tuning(self, match, stitch, frames) -> None:
@@ -382,8 +377,8 @@ class BatchPipeline:
         conversion per group)."""
         frames = self.max_frames if frames is None else frames
         L = self.L
-        isb = (L - 1) + (L - 2) + 1 if L >= 2 else 1
-        post = 2 * (L - 1) if L >= 2 else 0
+        isb = N.isb_filter_launches(self.rows, self.cols, L) + 1 if L >= 2 else 1
+        post = N.isb_apply_launches(self.rows, self.cols, L, 1) if L >= 2 else 0
         inpaint = N.hole_filling_launches(self.st.inpainting_iterations)
         per_group = 2 + isb + post + (1 if float_stitch else 0) + 2 + inpaint + 1
         return per_group * len(self._groups(frames, self._group_count(frames)))

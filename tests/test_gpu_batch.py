@@ -328,6 +328,63 @@ def test_isb_apply_batch_skip_fine_guide(ss, native):
         run(4)
 
 
+@pytest.mark.parametrize("rows,cols", [(96, 80), (257, 190), (1024, 1024)])
+def test_isb_tails_equal_a_launch_per_step(ss, native, rows, cols):
+    """The small levels of both pyramids fused into one launch (SSG_TUNE_ISB_TAIL for the chunked
+    cost filter, SSG_TUNE_POST_TAIL for the single-candidate post-filter) give every level's costs
+    and guides bit for bit as one launch per step."""
+    N = ss._native
+    tune = __import__("importlib").import_module("sphere-stereo_gb300.autotune")
+    isb_filter = __import__("importlib").import_module("sphere-stereo_gb300.isb_filter")
+    rng = np.random.default_rng(rows + cols)
+    levels = native.ssg_isb_level_count(cols, rows)
+    shapes = [(-(-rows // 2 ** s), -(-cols // 2 ** s)) for s in range(levels)]
+    inst, ncand = 2, 24
+    chunks = (ncand + 7) // 8
+    g0 = rng.integers(0, 256, (inst, rows, cols, 4), dtype=np.uint8)
+    g0[..., 3] = 0
+    c0 = (rng.random((inst, chunks, rows * cols, 8)) * 300).astype(np.float16)
+    d0 = rng.random((inst, rows, cols), dtype=np.float32) * 50
+    weights = isb_filter.level_weights(levels, 25.0)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def cost_filter():
+        guides = [torch.as_tensor(g0.copy(), device=DEV)] + [
+            torch.zeros(inst * r * c * 4, dtype=torch.uint8, device=DEV) for r, c in shapes[1:]]
+        costs = [torch.as_tensor(c0.view(np.int16).copy(), device=DEV)] + [
+            torch.zeros(inst * chunks * r * c * 8, dtype=torch.float32, device=DEV) for r, c in shapes[1:]]
+        N.call("ssg_isb_filter_batch", N.pointers([g.data_ptr() for g in guides]),
+               N.pointers([c.data_ptr() for c in costs]), levels, rows, cols, ncand, inst, 0,
+               N.floats([w for w, _ in weights]), N.floats([w for _, w in weights]), 1 / 200, stream)
+        torch.cuda.synchronize()
+        return [g.cpu().numpy() for g in guides[1:]] + [c.cpu().numpy() for c in costs[1:]]
+
+    def post_filter():
+        guides = [torch.as_tensor(g0.copy(), device=DEV)] + [
+            torch.zeros(inst * r * c * 4, dtype=torch.uint8, device=DEV) for r, c in shapes[1:]]
+        costs = [torch.as_tensor(d0.copy(), device=DEV)] + [
+            torch.zeros(inst * r * c, dtype=torch.float32, device=DEV) for r, c in shapes[1:]]
+        N.call("ssg_isb_apply_batch", N.pointers([g.data_ptr() for g in guides]),
+               N.pointers([c.data_ptr() for c in costs]), levels, rows, cols, 1, inst, 5.0, 12.5, 0, stream)
+        torch.cuda.synchronize()
+        return [g.cpu().numpy() for g in guides] + [c.cpu().numpy() for c in costs]
+
+    for knob, run in (("isb_tail", cost_filter), ("post_tail", post_filter)):
+        saved = tune.get(knob)
+        try:
+            outs = {}
+            for v in tune.choices(knob):
+                tune.set_knob(knob, v)
+                outs[v] = run()
+            for v, out in outs.items():
+                for k, (a, b) in enumerate(zip(out, outs[0])):
+                    np.testing.assert_array_equal(a, b, err_msg=f"{knob} = {v}, array {k}")
+        finally:
+            tune.set_knob(knob, saved)
+    # the tail's launch count: fewer kernels than a launch per step once a tail exists
+    assert N.isb_filter_launches(rows, cols, levels) <= 2 * levels - 3
+
+
 def test_tma_tiles_equal_cp_async_tiles(ss, native, golden_c1):
     """The chunked ISB upsampling stages its coarse tiles by TMA (cp.async.bulk.tensor with an
     mbarrier) or by cp.async: the same bits either way, at every level and in the fused selection,
