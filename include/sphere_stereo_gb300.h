@@ -103,6 +103,10 @@ typedef struct {
 #define SSG_TUNE_POST_TAIL 14         /* the same for the batched single-candidate filter
                                          (ssg_isb_apply_batch with one candidate: the distance
                                          post-filter): 0, 1024, 4096 or 16384 (default 4096) */
+#define SSG_TUNE_STAGE_COLUMNS 15     /* image staging (ssg_stage_images, _u8, _resized): 1 = a warp per
+                                         strip of texel columns walking down its rows, footprints formed
+                                         in registers (default); 0 = blocks of shared-memory texel tiles.
+                                         Same bits */
 #define SSG_TUNE_TMA_WITHHOLD 7       /* tests of the bounded TMA wait: 1 = the TMA-staged upsampling arms
                                          its tile barriers but issues no copy, so every block's first
                                          wait runs out (after a short limit), it writes nothing and
@@ -319,8 +323,9 @@ SSG_API int ssg_stage_images_u8(const uint8_t* d_images, int frames, int cameras
  * images in memory.  The entries are 32 bytes (sweep with ssg_sweep_cost_batch_entries,
  * entry_bytes 32, d_images NULL: resized 8-bit values never need the float path).  d_staged
  * 32-byte aligned.  SSG_ERR_UNSUPPORTED (resize with ssg_resize_linear and stage the result
- * instead) when d_images is not 4-byte aligned, src_cols x src_rows is not a multiple of 4, or a
- * tile's source window exceeds 160 KB of shared memory (reductions beyond about 2.5x). */
+ * instead) when d_images is not 4-byte aligned or src_cols x src_rows is not a multiple of 4, and
+ * with SSG_TUNE_STAGE_COLUMNS = 0 when a tile's source window exceeds 160 KB of shared memory
+ * (reductions beyond about 2.5x). */
 SSG_API int ssg_stage_images_resized(const uint8_t* d_images, int src_cols, int src_rows, int frames, int cameras,
                                      int cols, int rows, const int* reference_cameras, int references,
                                      float* d_staged, uint8_t* d_guides, int32_t* d_plane_flags, void* stream);

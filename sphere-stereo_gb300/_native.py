@@ -39,6 +39,7 @@ TUNE_SELECT_WHOLE = 11
 TUNE_UP_WHOLE = 12
 TUNE_ISB_TAIL = 13
 TUNE_POST_TAIL = 14
+TUNE_STAGE_COLUMNS = 15
 STATUS_TMA_TIMEOUT = 1
 STATUS_BARRIER_TIMEOUT = 2
 HOLE_SCRATCH_HEADER = 8

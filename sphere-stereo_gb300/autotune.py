@@ -41,6 +41,7 @@ KNOBS = {
     "up_whole": (N.TUNE_UP_WHOLE, ("ssg_isb_upsample_batch", "ssg_isb_filter_batch")),
     "isb_tail": (N.TUNE_ISB_TAIL, ("ssg_isb_filter_batch",)),
     "post_tail": (N.TUNE_POST_TAIL, ("ssg_isb_apply_batch",)),
+    "stage_columns": (N.TUNE_STAGE_COLUMNS, ("ssg_stage_images", "ssg_stage_images_u8", "ssg_stage_images_resized")),
 }
 
 

@@ -88,6 +88,7 @@ Knob g_knobs[] = {
     {kOnOff, 2, {0}},              // SSG_TUNE_UP_WHOLE
     {kIsbTail, 4, {1024}},         // SSG_TUNE_ISB_TAIL
     {kPostTail, 4, {4096}},        // SSG_TUNE_POST_TAIL
+    {kOnOff, 2, {1}},              // SSG_TUNE_STAGE_COLUMNS
 };
 constexpr int kKnobCount = sizeof(g_knobs) / sizeof(g_knobs[0]);
 }  // namespace

@@ -305,6 +305,280 @@ __global__ void __launch_bounds__(kBatchBlock) stage_resized_kernel(const __grid
     stage_tile<float>(p, src, inst, i0, j0, staged, guides, plane_flags);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Column-sweep staging: the same entries, guides and plane classes as stage_tile, with no shared
+// tile and no block barrier.  A warp walks down a strip of 32 texel columns, x = ib - 1 + lane,
+// over kColRows + 1 texel rows (the first a halo); at each texel row y it forms its texel's codes,
+// takes its right neighbour's from lane + 1 (one shuffle per plane) and, with the previous row's
+// kept in registers, writes the entry of row y for lanes 0..30 (entry ib + lane).  Strips overlap
+// by one texel column; the guide of pixel (x, y) is written by the lane for which x is not the
+// halo column (lanes 1..31) and for the rows that are not the halo row.
+// ---------------------------------------------------------------------------------------------
+constexpr int kColStrip = 31;  // entry columns per strip (32 lanes: 32 texel columns)
+constexpr int kColRows = 31;   // entry rows per warp (32 texel rows with the halo)
+constexpr int kColWarps = 8;   // warps per block
+
+// the three codes of a texel as words of high and low bytes (byte 3 zero; the codes are 16-bit)
+__device__ __forceinline__ void pack_codes(uint32_t q0, uint32_t q1, uint32_t q2, uint32_t& hi, uint32_t& lo)
+{
+    const uint32_t q01 = __byte_perm(q0, q1, 0x5410);
+    hi = __byte_perm(q01, q2, 0x6531);
+    lo = __byte_perm(q01, q2, 0x6420);
+}
+
+// texels of images at the matching resolution: three consecutive values
+template <typename Tin>
+struct ColumnImage {
+    const Tin* img;
+    int cols;
+    __device__ __forceinline__ void rows(int, int, int) {}
+    __device__ __forceinline__ void get(int x, int y, int, Tin (&v)[3])
+    {
+        const int64_t o = ((int64_t)y * cols + x) * 3;
+        v[0] = __ldg(img + o);
+        v[1] = __ldg(img + o + 1);
+        v[2] = __ldg(img + o + 2);
+    }
+};
+
+// a byte of a word as a float: 2^23 + b assembled in the bits, minus 2^23 (exact)
+__device__ __forceinline__ float byte_float(uint32_t w, int k)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)k)) - 8388608.0f;
+}
+
+// Texels resized from 8-bit source images (ssg_prep.cu's u8 -> float32 linear resize: its taps and
+// its separately rounded products and sums).  Each lane forms its column's taps once; the row taps
+// of the warp's texel rows are formed one per lane and shuffled to the warp row by row (rows()).
+// The last two source rows read (values of the lane's two source texels, three channels each)
+// are kept, so a source row shared by consecutive texel rows is read once.  (Reading the next
+// row's source texels one row ahead was measured slower: 80 registers instead of 64.)
+struct ColumnResized {
+    const uint8_t* img;  // this image's bytes (4-byte aligned, a multiple of 4 bytes long)
+    int src_cols, area2;
+    Tap tx;
+    float a0, a1;
+    Tap ty;                // the current row's taps (rows())
+    int lane_s0, lane_s1;  // the row taps of texel row y0 + lane, y0 the warp's first texel row
+    float lane_f;
+    int ra = -1, rb = -1;
+    float va[6], vb[6];
+    __device__ __forceinline__ void init(const ResizeParams& rp, int x, int y0, int cols, int rows)
+    {
+        tx = column_tap(rp, min(max(x, 0), cols - 1));
+        a0 = __fsub_rn(1.0f, tx.f);
+        a1 = tx.f;
+        const int lane = threadIdx.x & 31;
+        const Tap t = row_tap(rp, min(max(y0 + lane, 0), rows - 1));
+        lane_s0 = t.s0;
+        lane_s1 = t.s1;
+        lane_f = t.f;
+    }
+    // every lane, texel row y0 + k
+    __device__ __forceinline__ void rows(int k, int, int)
+    {
+        ty.s0 = __shfl_sync(0xFFFFFFFFu, lane_s0, k);
+        ty.s1 = __shfl_sync(0xFFFFFFFFu, lane_s1, k);
+        ty.f = __shfl_sync(0xFFFFFFFFu, lane_f, k);
+    }
+    // the lane's two source texels of source row r
+    __device__ __forceinline__ void load_row(int r, float (&v)[6]) const
+    {
+        const uint32_t* words = reinterpret_cast<const uint32_t*>(img);
+        const int64_t b = ((int64_t)r * src_cols + tx.s0) * 3;
+        const int64_t w = b >> 2;
+        const int off = (int)(b & 3);
+        const bool pair = tx.s1 != tx.s0;
+        const int last = off + (pair ? 5 : 2);  // the last byte, counted from word w
+        const uint32_t w0 = __ldg(words + w);
+        const uint32_t w1 = last >= 4 ? __ldg(words + w + 1) : 0u;
+        const uint32_t w2 = last >= 8 ? __ldg(words + w + 2) : 0u;
+        const uint32_t lo = __funnelshift_r(w0, w1, 8 * off), hi = __funnelshift_r(w1, w2, 8 * off);
+        v[0] = byte_float(lo, 0);
+        v[1] = byte_float(lo, 1);
+        v[2] = byte_float(lo, 2);
+        if (pair) {
+            v[3] = byte_float(lo, 3);
+            v[4] = byte_float(hi, 0);
+            v[5] = byte_float(hi, 1);
+        } else {
+            v[3] = v[0];
+            v[4] = v[1];
+            v[5] = v[2];
+        }
+    }
+    __device__ __forceinline__ void get(int, int, int, float (&out)[3])
+    {
+        float top[6], bot[6];
+        // rows only advance: the new top row is one of the kept rows or a new one, the bottom row too
+        if (ty.s0 == rb) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) top[i] = vb[i];
+        } else if (ty.s0 == ra) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) top[i] = va[i];
+        } else {
+            load_row(ty.s0, top);
+        }
+        if (ty.s1 == ty.s0) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) bot[i] = top[i];
+        } else if (ty.s1 == rb) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) bot[i] = vb[i];
+        } else {
+            load_row(ty.s1, bot);
+        }
+        ra = ty.s0;
+        rb = ty.s1;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            va[i] = top[i];
+            vb[i] = bot[i];
+        }
+        if (area2) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                out[c] = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(top[c], top[3 + c]), bot[c]), bot[3 + c]), 0.25f);
+        } else {
+            const float b0 = __fsub_rn(1.0f, ty.f), b1 = ty.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float h0 = __fadd_rn(__fmul_rn(top[c], a0), __fmul_rn(top[3 + c], a1));
+                const float h1 = __fadd_rn(__fmul_rn(bot[c], a0), __fmul_rn(bot[3 + c], a1));
+                out[c] = __fadd_rn(__fmul_rn(h0, b0), __fmul_rn(h1, b1));
+            }
+        }
+    }
+};
+
+// One warp's strip.  Src: ColumnImage<Tin> or ColumnResized (Tin = float), initialised for the
+// lane's column; inst: frame * cameras + camera.
+template <typename Tin, typename Src>
+__device__ __forceinline__ void stage_strip(const StageParams& p, Src& src, int inst, int ib, int jb,
+                                            uint4* __restrict__ staged, uint32_t* __restrict__ guides,
+                                            int* __restrict__ plane_flags)
+{
+    constexpr bool kLowPlane = sizeof(Tin) == 4;
+    const int lane = threadIdx.x & 31;
+    const int pitch = p.cols + 2;
+    const int64_t P = (int64_t)p.cols * p.rows, plane = (int64_t)pitch * (p.rows + 2);
+    const int frame = inst / p.cameras, cam = inst % p.cameras;
+    const int slot = p.ref_slot[cam];
+    uint32_t* guide = slot >= 0 ? guides + ((int64_t)frame * p.references + slot) * P : nullptr;
+    uint4* out = staged + (int64_t)(2 * inst) * plane;
+    const int x = ib - 1 + lane;
+    const bool col_in = x >= 0 && x < p.cols;
+    const int i = ib + lane;  // this lane's entry column
+    const bool writes = lane < kColStrip && i < pitch;
+    int cls = 0;
+    uint32_t up_hi = 0, up_lo = 0, up_hi_r = 0, up_lo_r = 0;  // the previous texel row's words
+    const int y_end = min(jb + kColRows, p.rows + 2);
+    for (int y = jb - 1, k = 0; y < y_end; ++y, ++k) {
+        src.rows(k, y, p.rows);
+        uint32_t hi = 0, lo = 0;
+        if (col_in && y >= 0 && y < p.rows) {
+            Tin r[3];
+            src.get(x, y, k, r);
+            const int k0 = value_class(r[0]), k1 = value_class(r[1]), k2 = value_class(r[2]);
+            cls = max(cls, max(k0, max(k1, k2)));
+            pack_codes(fixed_code(r[0], k0), fixed_code(r[1], k1), fixed_code(r[2], k2), hi, lo);
+            if (guide && lane > 0 && y >= jb) {
+                // utils.py:144-155, the arithmetic of ssg_rgb_to_guide, from the input values
+                const float c0 = texel_value(r[0]), c1 = texel_value(r[1]), c2 = texel_value(r[2]);
+                const float yy = fadd(fadd(fadd(fmul(c0, 0.1826f), 16.0f), fmul(c1, 0.6142f)), fmul(c2, 0.062f));
+                const float cb = fadd(fsub(fsub(128.0f, fmul(c0, 0.1006f)), fmul(c1, 0.3386f)), fmul(c2, 0.4392f));
+                const float cr = fsub(fsub(fadd(fmul(c0, 0.4392f), 128.0f), fmul(c1, 0.3989f)), fmul(c2, 0.0403f));
+                const uint32_t g0 = __float2uint_rz(fminf(fmaxf(yy, 16.0f), 235.0f));
+                const uint32_t g1 = __float2uint_rz(fminf(fmaxf(cb, 16.0f), 240.0f));
+                const uint32_t g2 = __float2uint_rz(fminf(fmaxf(cr, 16.0f), 240.0f));
+                guide[(int64_t)y * p.cols + x] = g0 | (g1 << 8) | (g2 << 16);
+            }
+        }
+        const uint32_t hi_r = __shfl_down_sync(0xFFFFFFFFu, hi, 1);
+        const uint32_t lo_r = kLowPlane ? __shfl_down_sync(0xFFFFFFFFu, lo, 1) : 0u;
+        if (y >= jb && writes) {
+            // entry (i, y): taps (x, y - 1), (x + 1, y - 1), (x, y), (x + 1, y) as bytes 0..3
+            uint32_t word[2][3];
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                const uint32_t sel = (uint32_t)ch | ((uint32_t)(4 + ch) << 4);
+                word[0][ch] = __byte_perm(__byte_perm(up_hi, up_hi_r, sel), __byte_perm(hi, hi_r, sel), 0x5410);
+                if constexpr (kLowPlane)
+                    word[1][ch] = __byte_perm(__byte_perm(up_lo, up_lo_r, sel), __byte_perm(lo, lo_r, sel), 0x5410);
+            }
+            const int64_t at = (int64_t)y * pitch + i;
+            if constexpr (kLowPlane) {
+                const unsigned long long w0 = word[0][0] | (unsigned long long)word[0][1] << 32,
+                                         w1 = word[0][2] | (unsigned long long)word[1][0] << 32,
+                                         w2 = word[1][1] | (unsigned long long)word[1][2] << 32;
+                asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(out + 2 * at), "l"(w0), "l"(w1),
+                             "l"(w2), "l"(0ull)
+                             : "memory");
+            } else {
+                out[at] = make_uint4(word[0][0], word[0][1], word[0][2], 0u);
+            }
+        }
+        up_hi = hi;
+        up_lo = lo;
+        up_hi_r = hi_r;
+        up_lo_r = lo_r;
+    }
+    cls = __reduce_max_sync(0xFFFFFFFFu, cls);
+    if (lane == 0 && cls) atomicMax(plane_flags + inst, cls);
+}
+
+// the strip of warp w of an image: strips of kColStrip entry columns by kColRows entry rows
+__device__ __forceinline__ bool strip_origin(const StageParams& p, int& ib, int& jb)
+{
+    const int strips_x = (p.cols + 2 + kColStrip - 1) / kColStrip;
+    const int strips = strips_x * ((p.rows + 2 + kColRows - 1) / kColRows);
+    const int w = blockIdx.x * kColWarps + (int)(threadIdx.x >> 5);
+    if (w >= strips) return false;
+    ib = (w % strips_x) * kColStrip;
+    jb = (w / strips_x) * kColRows;
+    return true;
+}
+
+template <typename Tin>
+__global__ void __launch_bounds__(kColWarps * 32) stage_columns_kernel(const __grid_constant__ StageParams p,
+                                                                      const Tin* __restrict__ images,
+                                                                      uint4* __restrict__ staged,
+                                                                      uint32_t* __restrict__ guides,
+                                                                      int* __restrict__ plane_flags)
+{
+    int ib, jb;
+    if (!strip_origin(p, ib, jb)) return;  // whole warps
+    const int inst = blockIdx.y;
+    ColumnImage<Tin> src{images + (int64_t)inst * p.cols * p.rows * 3, p.cols};
+    stage_strip<Tin>(p, src, inst, ib, jb, staged, guides, plane_flags);
+}
+
+__global__ void __launch_bounds__(kColWarps * 32) stage_resized_columns_kernel(const __grid_constant__ StageParams p,
+                                                                              const __grid_constant__ ResizeParams rp,
+                                                                              const uint8_t* __restrict__ images,
+                                                                              uint4* __restrict__ staged,
+                                                                              uint32_t* __restrict__ guides,
+                                                                              int* __restrict__ plane_flags)
+{
+    int ib, jb;
+    if (!strip_origin(p, ib, jb)) return;  // whole warps
+    const int inst = blockIdx.y;
+    ColumnResized src;
+    src.img = images + (int64_t)inst * rp.src_cols * rp.src_rows * 3;
+    src.src_cols = rp.src_cols;
+    src.area2 = rp.area2;
+    src.init(rp, ib - 1 + (int)(threadIdx.x & 31), jb - 1, p.cols, p.rows);
+    stage_strip<float>(p, src, inst, ib, jb, staged, guides, plane_flags);
+}
+
+static dim3 column_grid(int cols, int rows, int images)
+{
+    const int64_t strips =
+        (int64_t)((cols + 2 + kColStrip - 1) / kColStrip) * ((rows + 2 + kColRows - 1) / kColRows);
+    return dim3((unsigned)((strips + kColWarps - 1) / kColWarps), (unsigned)images);
+}
+
 // channel c (0..2) of texel k (0: nw, 1: ne, 2: sw, 3: se) of an entry
 __device__ __forceinline__ float entry_texel(const uint4& q, int c, int k)
 {
@@ -833,6 +1107,11 @@ static int stage_images(const Tin* d_images, int frames, int cameras, int cols, 
     const int64_t tiles = (int64_t)((cols + 2 + kStageTileX - 1) / kStageTileX) *
                           ((rows + 2 + kStageTileY - 1) / kStageTileY);
     SSG_REQUIRE(tiles < ((int64_t)1 << 31), "images of %dx%d pixels are too large", cols, rows);
+    if (tuning(SSG_TUNE_STAGE_COLUMNS) == 1) {
+        stage_columns_kernel<Tin><<<column_grid(cols, rows, frames * cameras), kColWarps * 32, 0, as_stream(stream)>>>(
+            p, d_images, reinterpret_cast<uint4*>(d_staged), reinterpret_cast<uint32_t*>(d_guides), d_plane_flags);
+        return launch_status("stage_columns_kernel");
+    }
     dim3 grid((unsigned)tiles, frames * cameras);
     stage_images_kernel<Tin><<<grid, kBatchBlock, 0, as_stream(stream)>>>(
         p, d_images, reinterpret_cast<uint4*>(d_staged), reinterpret_cast<uint32_t*>(d_guides), d_plane_flags);
@@ -910,6 +1189,24 @@ extern "C" int ssg_stage_images_resized(const uint8_t* d_images, int src_cols, i
                     src_cols, src_rows);
     SSG_REQUIRE((int64_t)src_cols * src_rows * 3 < ((int64_t)1 << 40), "source images too large");
     const ResizeParams rp = make_resize_params(src_cols, src_rows, cols, rows, 3);
+    StageParams p{};
+    p.cameras = cameras;
+    p.references = references;
+    p.cols = cols;
+    p.rows = rows;
+    for (int c = 0; c < SSG_MAX_CAMERAS; ++c) p.ref_slot[c] = -1;
+    for (int r = 0; r < references; ++r) {
+        SSG_REQUIRE(reference_cameras[r] >= 0 && reference_cameras[r] < cameras, "reference camera out of range");
+        p.ref_slot[reference_cameras[r]] = r;
+    }
+    if (tuning(SSG_TUNE_STAGE_COLUMNS) == 1) {
+        const cudaError_t e = cudaMemsetAsync(d_plane_flags, 0, sizeof(int32_t) * frames * cameras, as_stream(stream));
+        if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+        stage_resized_columns_kernel<<<column_grid(cols, rows, frames * cameras), kColWarps * 32, 0,
+                                       as_stream(stream)>>>(p, rp, d_images, reinterpret_cast<uint4*>(d_staged),
+                                                            reinterpret_cast<uint32_t*>(d_guides), d_plane_flags);
+        return launch_status("stage_resized_columns_kernel");
+    }
     // the largest source window of any tile: texel columns [i0 - 1, i0 + kStageTileX - 1] and
     // rows [j0 - 1, j0 + kStageTileY - 1] clamped into the image, taps as the kernel forms them
     int win_cols = 0, win_rows = 0;
@@ -941,16 +1238,6 @@ extern "C" int ssg_stage_images_resized(const uint8_t* d_images, int src_cols, i
             if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
             opted[dev].store(smem);
         }
-    }
-    StageParams p{};
-    p.cameras = cameras;
-    p.references = references;
-    p.cols = cols;
-    p.rows = rows;
-    for (int c = 0; c < SSG_MAX_CAMERAS; ++c) p.ref_slot[c] = -1;
-    for (int r = 0; r < references; ++r) {
-        SSG_REQUIRE(reference_cameras[r] >= 0 && reference_cameras[r] < cameras, "reference camera out of range");
-        p.ref_slot[reference_cameras[r]] = r;
     }
     const cudaError_t e = cudaMemsetAsync(d_plane_flags, 0, sizeof(int32_t) * frames * cameras, as_stream(stream));
     if (e != cudaSuccess) return fail(SSG_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));

@@ -129,9 +129,15 @@ def test_resized_staging_and_entry_sizes_checked_without_a_device(native, ss):
     assert "4-byte" in N.last_error()
     assert native.ssg_stage_images_resized(A + 2, 64, 64, 1, 2, 20, 20, refs, 1, A, A, A, None) == \
         N.SSG_ERR_UNSUPPORTED
-    assert native.ssg_stage_images_resized(A, 4096, 4096, 1, 2, 256, 256, refs, 1, A, A, A, None) == \
-        N.SSG_ERR_UNSUPPORTED
-    assert "shared memory" in N.last_error()
+    # the shared-memory tile staging declines windows beyond its limit (the column staging has none)
+    saved = native.ssg_tuning_get(N.TUNE_STAGE_COLUMNS)
+    assert native.ssg_tuning_set(N.TUNE_STAGE_COLUMNS, 0) == 0
+    try:
+        assert native.ssg_stage_images_resized(A, 4096, 4096, 1, 2, 256, 256, refs, 1, A, A, A, None) == \
+            N.SSG_ERR_UNSUPPORTED
+        assert "shared memory" in N.last_error()
+    finally:
+        native.ssg_tuning_set(N.TUNE_STAGE_COLUMNS, saved)
     cams = N.cameras_array([N.ssg_camera(100, 100, 32, 32, -0.2, 0.6)] * 2)
     poses = N.floats([0.0] * 24)
     cand = N.floats([1.0 + k for k in range(32)])

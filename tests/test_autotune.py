@@ -32,6 +32,7 @@ def test_knobs_and_choices(tune):
     assert tune.choices("up_whole") == [0, 1]
     assert tune.choices("isb_tail") == [0, 256, 1024, 4096]
     assert tune.choices("post_tail") == [0, 1024, 4096, 16384]
+    assert tune.choices("stage_columns") == [0, 1]
     tune.set_knob("merge_frames", 8)
     assert tune.get("merge_frames") == 8
     with pytest.raises(ValueError):

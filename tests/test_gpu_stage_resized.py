@@ -14,15 +14,17 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda:0"
 
 
-def _stage_both(N, imgs: np.ndarray, cols: int, rows: int, refs: list[int]):
-    """imgs: uint8 [frames, cameras, H, W, 3].  Returns ((staged, guides, flags) two-pass,
-    (staged, guides, flags) fused) as numpy arrays."""
+def _stage_both(N, imgs: np.ndarray, cols: int, rows: int, refs: list[int], columns: int):
+    """imgs: uint8 [frames, cameras, H, W, 3].  Returns ((staged, guides, flags) two-pass with the
+    shared-memory tile staging, (staged, guides, flags) one-pass with the staging kernel
+    `columns` selects) as numpy arrays."""
     F, C, H, W, _ = imgs.shape
     src = torch.as_tensor(imgs, device=DEV)
     stream = torch.cuda.current_stream().cuda_stream
     plane = (rows + 2) * (cols + 2)
     out = []
     for fused in (False, True):
+        N.call("ssg_tuning_set", N.TUNE_STAGE_COLUMNS, columns if fused else 0)
         staged = torch.full((F * C * 2 * plane * 4,), 7.0, device=DEV)  # a pattern every entry overwrites
         guides = torch.zeros(F * len(refs) * rows * cols * 4, dtype=torch.uint8, device=DEV)
         flags = torch.full((F * C,), -1, dtype=torch.int32, device=DEV)
@@ -47,8 +49,11 @@ CASES = [((1216, 1216), (1024, 1024)), ((200, 120), (100, 60)), ((100, 60), (130
          ((64, 36), (150, 101)), ((1216, 1216), (512, 512)), ((333, 212), (257, 161))]
 
 
+@pytest.mark.parametrize("columns", [1, 0])
 @pytest.mark.parametrize("src,dst", CASES)
-def test_stage_resized_equals_resize_then_stage(ss, native, src, dst):
+def test_stage_resized_equals_resize_then_stage(ss, native, src, dst, columns):
+    """Both staging kernels (SSG_TUNE_STAGE_COLUMNS: warps walking down column strips, or
+    shared-memory texel tiles) against the two passes."""
     N = ss._native
     rng = np.random.default_rng(sum(src) + 7 * sum(dst))
     (W, H), (cols, rows) = src, dst
@@ -56,7 +61,7 @@ def test_stage_resized_equals_resize_then_stage(ss, native, src, dst):
     imgs = rng.integers(0, 256, (frames, cams, H, W, 3), dtype=np.uint8)
     imgs[0, 0, : H // 3] = 255  # saturated and flat regions next to noise
     imgs[-1, -1, :, : W // 4] = 0
-    (s2, g2, f2), (s1, g1, f1) = _stage_both(N, imgs, cols, rows, [0, cams - 1])
+    (s2, g2, f2), (s1, g1, f1) = _stage_both(N, imgs, cols, rows, [0, cams - 1], columns)
     np.testing.assert_array_equal(f1, f2)
     np.testing.assert_array_equal(g1, g2)
     np.testing.assert_array_equal(s1, s2)
@@ -120,3 +125,42 @@ def test_pipeline_decoded_inputs_equal_resized_inputs(ss, native, synthetic, src
         assert (pipe.plane_flags.cpu().numpy() == 1).all()  # resized renders hold fractions: 8.8 entries
     for a, b in zip(outs[0], outs[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "uint8"])
+@pytest.mark.parametrize("cols,rows", [(1024, 1024), (37, 50), (130, 70)])
+def test_column_staging_equals_tile_staging(ss, native, dtype, cols, rows):
+    """ssg_stage_images / ssg_stage_images_u8: the column-strip kernel gives the tile kernel's
+    entries, guides and plane classes bit for bit (integer, fractional and out-of-range values)."""
+    N = ss._native
+    rng = np.random.default_rng(cols * rows)
+    F, C, refs = 2, 3, [0, 2]
+    imgs = rng.integers(0, 256, (F, C, rows, cols, 3)).astype(np.float32)
+    if dtype == "float32":
+        imgs[0, 1] += rng.uniform(-0.49, 0.49, imgs[0, 1].shape).astype(np.float32)
+        imgs[0, 1] = np.clip(imgs[0, 1], 0, 255)
+        imgs[1, 2, rows // 2, cols // 3, 1] = -3.0
+        src = torch.as_tensor(imgs, device=DEV)
+        entry = "ssg_stage_images"
+    else:
+        src = torch.as_tensor(imgs.astype(np.uint8), device=DEV)
+        entry = "ssg_stage_images_u8"
+    plane = (rows + 2) * (cols + 2)
+    stream = torch.cuda.current_stream().cuda_stream
+    out = []
+    try:
+        for columns in (0, 1):
+            N.call("ssg_tuning_set", N.TUNE_STAGE_COLUMNS, columns)
+            staged = torch.full((F * C * 2 * plane * 4,), 7.0, device=DEV)
+            guides = torch.zeros(F * len(refs) * rows * cols * 4, dtype=torch.uint8, device=DEV)
+            flags = torch.full((F * C,), -1, dtype=torch.int32, device=DEV)
+            N.call(entry, src.data_ptr(), F, C, cols, rows, N.ints(refs), len(refs), staged.data_ptr(),
+                   guides.data_ptr(), flags.data_ptr(), stream)
+            torch.cuda.synchronize()
+            out.append((staged.cpu().numpy().view(np.uint32), guides.cpu().numpy(), flags.cpu().numpy()))
+    finally:
+        N.call("ssg_tuning_set", N.TUNE_STAGE_COLUMNS, 1)
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+    if dtype == "float32":
+        assert out[0][2].tolist() == [0, 1, 0, 0, 0, 2]
