@@ -374,12 +374,20 @@ struct ColumnResized {
         lane_s1 = t.s1;
         lane_f = t.f;
     }
-    // every lane, texel row y0 + k
+    // every lane, texel row y0 + k.  Lanes 0 and 31 also ask L2 for the first and the last
+    // source texel of the warp's segment of the bottom source row of texel row k + 3 (about 38
+    // texels, 114 bytes, one or two lines), so that the first read of a source row finds it there
     __device__ __forceinline__ void rows(int k, int, int)
     {
         ty.s0 = __shfl_sync(0xFFFFFFFFu, lane_s0, k);
         ty.s1 = __shfl_sync(0xFFFFFFFFu, lane_s1, k);
         ty.f = __shfl_sync(0xFFFFFFFFu, lane_f, k);
+        const int ahead = __shfl_sync(0xFFFFFFFFu, lane_s1, min(k + 3, 31));
+        const int lane = threadIdx.x & 31;
+        if (lane == 0 || lane == 31) {
+            const uint8_t* p = img + ((int64_t)ahead * src_cols + tx.s0) * 3;  // a byte of the image
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+        }
     }
     // the lane's two source texels of source row r
     __device__ __forceinline__ void load_row(int r, float (&v)[6]) const
