@@ -455,6 +455,22 @@ SSG_API int ssg_merge_panorama_batch_approx(const float* d_lut, const float* d_w
                                             int pano_cols, int pano_rows, int frames, float* d_distance_panorama,
                                             uint8_t* d_rgb_panorama, void* stream);
 
+/* The same with the images given as image_count images per frame (image_rows x image_cols x 3
+ * bytes each, frames contiguous), reference r stitching image image_slots[r] (host array of
+ * reference_count indices): for instance every camera's decoded image of a batch, of which the
+ * references' are the images to stitch when the stitch resolution is the decoded one (the
+ * reference's input preparation then resizes them to their own size, python/utils.py:198-201).
+ * ssg_merge_panorama_batch_approx is this with image_count = reference_count, image_slots = 0, 1,
+ * ... */
+SSG_API int ssg_merge_panorama_batch_approx_images(const float* d_lut, const float* d_weights,
+                                                   const float* d_reprojected, const float* d_distances,
+                                                   const uint8_t* d_images, int image_count, const int* image_slots,
+                                                   int image_rows, int image_cols, const float* translations,
+                                                   const ssg_intrinsics* intrinsics, int reference_count, int cols,
+                                                   int rows, int pano_cols, int pano_rows, int frames,
+                                                   float* d_distance_panorama, uint8_t* d_rgb_panorama,
+                                                   void* stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Differentiable sweep (no counterpart in the reference, whose selection is a hard argmin with
  * a parabolic step, python/depth_estimation.py:179-198).  Forward: the fp32 sweep and ISB filter

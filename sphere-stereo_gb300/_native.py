@@ -156,6 +156,8 @@ SIGNATURES = {
     "ssg_uneven_launches": (_I, [_P]),
     "ssg_uneven_destroy": (None, [_P]),
     "ssg_merge_panorama_batch_approx": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "ssg_merge_panorama_batch_approx_images": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, _I, _P, _P, _I, _I, _I, _I, _I,
+                                                    _I, _P, _P, _P]),
     "ssg_resize_linear": (_I, [_P, _I, _I, _I, _I, _P, _I, _I, _I, _I, _P]),
     "ssg_eval_scratch_bytes": (ctypes.c_size_t, [_I, _I]),
     "ssg_eval_panoramas": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),

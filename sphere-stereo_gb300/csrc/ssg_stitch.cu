@@ -1006,6 +1006,12 @@ struct MergeParams {
     int cols, rows, pano_cols, pano_rows, nref, image_rows, image_cols;
     float ratio_x, ratio_y;
     int word_rows;  // the images start and end on 4-byte boundaries: texel pairs read as words
+    int64_t image_frame;                // bytes of a frame's images
+    // the image of a frame that reference r stitches.  The sample row is formed as in a stack of
+    // the references' images (row + r x image_rows, in float as stitcher.cu forms it), and the
+    // image pointer is moved by (image_slot[r] - r) images, so that the arithmetic does not depend
+    // on where the images lie
+    int image_slot[SSG_MAX_REFERENCES];
     Intr k[SSG_MAX_REFERENCES];
     float t[SSG_MAX_REFERENCES][3];
 };
@@ -1128,7 +1134,7 @@ __global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_consta
     const int64_t frame = blockIdx.y;
     reproj += frame * p.nref * (int64_t)p.cols * p.rows;
     dists += frame * p.nref * (int64_t)p.cols * p.rows;
-    images += frame * p.nref * (int64_t)p.image_cols * p.image_rows * 3;
+    images += frame * p.image_frame;
     dist_pano += frame * Q;
     rgb_pano += frame * Q * 3;
     float inv = 0.0f, rgb[3] = {0.0f, 0.0f, 0.0f};
@@ -1157,7 +1163,8 @@ __global__ void __launch_bounds__(kStitchBlock) merge_kernel(const __grid_consta
         o[1] = fminf(fmaxf(o[1], 0.1f), rowsm);
         o[1] = fadd(o[1], (float)(r * p.image_rows));
         float c[3];
-        interp_rgb(images, o[0], o[1], p.image_cols, c);
+        interp_rgb(images + (int64_t)(p.image_slot[r] - r) * p.image_rows * p.image_cols * 3, o[0], o[1],
+                   p.image_cols, c);
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) rgb[ch] = fadd(rgb[ch], fmul(c[ch], w));
     }
@@ -1186,7 +1193,7 @@ __global__ void __launch_bounds__(kStitchBlock) merge_frames_kernel(const __grid
     const int f0 = blockIdx.y * kMergeFrames;
     const int nf = min(kMergeFrames, frames - f0);
     const int64_t map_frame = (int64_t)p.nref * p.cols * p.rows;
-    const int64_t image_frame = (int64_t)p.nref * p.image_cols * p.image_rows * 3;
+    const int64_t image_frame = p.image_frame;
     reproj += f0 * map_frame;
     dists += f0 * map_frame;
     images += f0 * image_frame;
@@ -1224,7 +1231,9 @@ __global__ void __launch_bounds__(kStitchBlock) merge_frames_kernel(const __grid
                 project_fast(pt, p.k[r], o);
                 o[0] = fminf(fmaxf(fmul(o[0], p.ratio_x), 0.1f), colsm);
                 o[1] = fadd(fminf(fmaxf(fmul(o[1], p.ratio_y), 0.1f), rowsm), (float)(r * p.image_rows));
-                interp_rgb_fast(images + f * image_frame, o[0], o[1], p.image_cols, c, p.word_rows != 0);
+                interp_rgb_fast(images + f * image_frame + (int64_t)(p.image_slot[r] - r) * p.image_rows *
+                                                               p.image_cols * 3,
+                                o[0], o[1], p.image_cols, c, p.word_rows != 0);
 #pragma unroll
                 for (int ch = 0; ch < 3; ++ch) rgb[f][ch] = fmaf(c[ch], w, rgb[f][ch]);
             }
@@ -1580,11 +1589,13 @@ extern "C" int ssg_merge_panorama(const float* d_lut, const float* d_weights, co
 }
 
 template <bool kFast>
+// image_count images of image_rows x image_cols x 3 bytes per frame in d_images; reference r
+// stitches image image_slots[r] (nullptr: image r, image_count = reference_count)
 static int merge_batch(const float* d_lut, const float* d_weights, const float* d_reprojected,
                        const float* d_distances, const uint8_t* d_images, int image_rows, int image_cols,
                        const float* translations, const ssg_intrinsics* intrinsics, int reference_count, int cols,
                        int rows, int pano_cols, int pano_rows, int frames, float* d_distance_panorama,
-                       uint8_t* d_rgb_panorama, void* stream)
+                       uint8_t* d_rgb_panorama, void* stream, int image_count = 0, const int* image_slots = nullptr)
 {
     SSG_REQUIRE(frames >= 1 && frames <= 65535, "frames out of range");
     SSG_REQUIRE(d_lut && d_weights && d_reprojected && d_distances && d_images && translations &&
@@ -1595,7 +1606,16 @@ static int merge_batch(const float* d_lut, const float* d_weights, const float* 
     SSG_REQUIRE(reference_count >= 1 && reference_count <= SSG_MAX_REFERENCES, "reference_count %d outside [1, %d]",
                 reference_count, SSG_MAX_REFERENCES);
     if (int e = check_intrinsics(intrinsics, reference_count)) return e;
+    if (!image_slots) image_count = reference_count;
+    SSG_REQUIRE(image_count >= 1 && image_count <= SSG_MAX_CAMERAS, "image_count %d outside [1, %d]", image_count,
+                SSG_MAX_CAMERAS);
     MergeParams p{};
+    for (int r = 0; r < reference_count; ++r) {
+        p.image_slot[r] = image_slots ? image_slots[r] : r;
+        SSG_REQUIRE(p.image_slot[r] >= 0 && p.image_slot[r] < image_count, "image slot %d of reference %d outside [0, %d)",
+                    p.image_slot[r], r, image_count);
+    }
+    p.image_frame = (int64_t)image_count * image_rows * image_cols * 3;
     p.cols = cols;
     p.rows = rows;
     p.pano_cols = pano_cols;
@@ -1611,8 +1631,9 @@ static int merge_batch(const float* d_lut, const float* d_weights, const float* 
     }
     const int64_t Q = (int64_t)pano_cols * pano_rows;
     dim3 grid(grid_1d(Q, kStitchBlock), frames);
-    const int64_t image_bytes = (int64_t)frames * reference_count * image_rows * image_cols * 3;
-    p.word_rows = ((uintptr_t)d_images & 3) == 0 && (image_bytes & 3) == 0;
+    // every image starts and ends on a 4-byte boundary when the buffer does and an image's bytes are
+    // a multiple of 4
+    p.word_rows = ((uintptr_t)d_images & 3) == 0 && (((int64_t)image_rows * image_cols * 3) & 3) == 0;
     if constexpr (kFast) {
         const int group = tuning(SSG_TUNE_MERGE_FRAMES);
         const dim3 fgrid(grid_1d(Q, kStitchBlock), (frames + group - 1) / group);
@@ -1644,6 +1665,21 @@ extern "C" int ssg_merge_panorama_batch(const float* d_lut, const float* d_weigh
     return merge_batch<false>(d_lut, d_weights, d_reprojected, d_distances, d_images, image_rows, image_cols,
                               translations, intrinsics, reference_count, cols, rows, pano_cols, pano_rows, frames,
                               d_distance_panorama, d_rgb_panorama, stream);
+}
+
+extern "C" int ssg_merge_panorama_batch_approx_images(const float* d_lut, const float* d_weights,
+                                                      const float* d_reprojected, const float* d_distances,
+                                                      const uint8_t* d_images, int image_count,
+                                                      const int* image_slots, int image_rows, int image_cols,
+                                                      const float* translations, const ssg_intrinsics* intrinsics,
+                                                      int reference_count, int cols, int rows, int pano_cols,
+                                                      int pano_rows, int frames, float* d_distance_panorama,
+                                                      uint8_t* d_rgb_panorama, void* stream)
+{
+    SSG_REQUIRE(image_slots, "null image_slots");
+    return merge_batch<true>(d_lut, d_weights, d_reprojected, d_distances, d_images, image_rows, image_cols,
+                             translations, intrinsics, reference_count, cols, rows, pano_cols, pano_rows, frames,
+                             d_distance_panorama, d_rgb_panorama, stream, image_count, image_slots);
 }
 
 extern "C" int ssg_merge_panorama_batch_approx(const float* d_lut, const float* d_weights,

@@ -326,15 +326,17 @@ class RGBD_Estimator:
             st.images_to_stitch_list[slot].copy_(image)  # float -> uint8 truncation (depth_estimation.py:239-240)
         return st.stitch(st.images_to_stitch_list, st.distances_list)
 
-    def estimate_RGBD_panoramas(self, images_to_match, images_to_stitch):
+    def estimate_RGBD_panoramas(self, images_to_match, images_to_stitch=None):
         """Batched ``estimate_RGBD_panorama`` (no counterpart in the reference, which takes one
         frame per call) on the 16-bit pipeline.
 
         Args:
             images_to_match: [frames, cameras, matching_rows, matching_cols, 3] float32 in [0, 255],
-                or uint8 (the 8-bit images the float inputs are made from)
+                or uint8 (the 8-bit images the float inputs are made from); uint8 images of another
+                size (the decoded images) are resized to the matching resolution as they are staged
             images_to_stitch: [frames, references, rgb_stitching_rows, rgb_stitching_cols, 3]
-                float32 in [0, 255], or uint8
+                float32 in [0, 255], or uint8; None when images_to_match are the decoded uint8
+                images at the stitch resolution (their references' images are stitched)
         Returns:
             rgb: [frames, rows, cols, 3] uint8, distance: [frames, rows, cols] float32 (views of
             the pipeline's buffers, overwritten by the next call)

@@ -219,10 +219,13 @@ class BatchPipeline:
             N.call("ssg_isb_apply_batch", N.pointers(df_guides), N.pointers(df_costs), L, rows, cols, 1, inst,
                    float(e.sigma_i) / 2, float(e.sigma_s) / 2, N.ISB_SKIP_FINE_GUIDE, stream)
         # stitch (python/stitcher.py:166-220)
-        s_img = stitch[f0:f0 + frames]
-        if stitch.dtype == torch.uint8:
-            images_u8 = s_img
+        if stitch is None:
+            # the references' own decoded images in the images to match (at the stitch resolution)
+            images_u8 = None
+        elif stitch.dtype == torch.uint8:
+            images_u8 = stitch[f0:f0 + frames]
         else:
+            s_img = stitch[f0:f0 + frames]
             images_u8 = self.images_u8[f0:f0 + frames]
             # float -> uint8 truncation (depth_estimation.py:239)
             N.call("ssg_convert_u8", s_img.data_ptr(), images_u8.data_ptr(),
@@ -233,10 +236,17 @@ class BatchPipeline:
         holes = self.holes.data_ptr() + 4 * (3 * i0 * P + N.HOLE_SCRATCH_HEADER * group)
         N.call("ssg_inpaint_holes_batch", reprojected, self.tables.data_ptr(), self.stamps.data_ptr() + i0 * P, holes,
                cols, rows, inst, R, st.max_dist, st.inpainting_iterations, stream)
-        N.call("ssg_merge_panorama_batch_approx", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
-               reprojected, dist.data_ptr(), images_u8.data_ptr(), st.image_rows, st.image_cols, st._trans, st._intr,
-               R, cols, rows, st.pano_cols, st.pano_rows, frames, self.pano_distance[f0].data_ptr(),
-               self.rgb[f0].data_ptr(), stream)
+        if images_u8 is None:
+            N.call("ssg_merge_panorama_batch_approx_images", st.blending_sampling.data_ptr(),
+                   st.blending_weights.data_ptr(), reprojected, dist.data_ptr(),
+                   self._match_images[f0:f0 + frames].data_ptr(), self.C, self._refs, st.image_rows, st.image_cols,
+                   st._trans, st._intr, R, cols, rows, st.pano_cols, st.pano_rows, frames,
+                   self.pano_distance[f0].data_ptr(), self.rgb[f0].data_ptr(), stream)
+        else:
+            N.call("ssg_merge_panorama_batch_approx", st.blending_sampling.data_ptr(), st.blending_weights.data_ptr(),
+                   reprojected, dist.data_ptr(), images_u8.data_ptr(), st.image_rows, st.image_cols, st._trans,
+                   st._intr, R, cols, rows, st.pano_cols, st.pano_rows, frames, self.pano_distance[f0].data_ptr(),
+                   self.rgb[f0].data_ptr(), stream)
 
     def _stream(self, handle: int) -> torch.cuda.Stream:
         if not handle:
@@ -280,13 +290,15 @@ class BatchPipeline:
         done.record(side)
         main.wait_event(done)
 
-    def run(self, match: torch.Tensor, stitch: torch.Tensor):
+    def run(self, match: torch.Tensor, stitch: torch.Tensor | None):
         """match: [F, C, rows, cols, 3], stitch: [F, R, image_rows, image_cols, 3], each float32 or
         uint8 (8-bit images: a quarter of the upload, no conversion pass), contiguous on the
         pipeline's device.  An 8-bit `match` may also have its own size [F, C, H, W, 3] (the decoded
         images): it is then resized to the matching resolution, as the reference's input
-        preparation resizes (python/utils.py:198-201), while it is staged.  Returns views of the
-        outputs for F frames."""
+        preparation resizes (python/utils.py:198-201), while it is staged.  `stitch` may be None when
+        `match` holds the decoded 8-bit images at the stitch resolution: the references' images in
+        it are stitched in place (the reference's images to stitch are those decoded images, resized
+        to their own size).  Returns views of the outputs for F frames."""
         frames = match.shape[0] if match.dim() else 0
         if not 1 <= frames <= self.max_frames:
             raise ValueError(f"batch of {frames} frames outside [1, {self.max_frames}]")
@@ -294,9 +306,16 @@ class BatchPipeline:
         match_shape = (frames, self.C, self.rows, self.cols, 3)
         if match.dtype == torch.uint8 and match.dim() == 5 and match.shape[4] == 3 and min(match.shape[2:4]) >= 1:
             match_shape = (frames, self.C, match.shape[2], match.shape[3], 3)
-        for name, t, shape in (("images_to_match", match, match_shape),
-                               ("images_to_stitch", stitch, (frames, self.R, st.image_rows, st.image_cols, 3))):
+        checks = [("images_to_match", match, match_shape)]
+        if stitch is None:
+            if match.dtype != torch.uint8 or tuple(match.shape[2:4]) != (st.image_rows, st.image_cols):
+                raise ValueError("images_to_stitch may only be omitted when images_to_match are the decoded uint8 "
+                                 f"images at the stitch resolution {st.image_cols}x{st.image_rows}")
+        else:
+            checks.append(("images_to_stitch", stitch, (frames, self.R, st.image_rows, st.image_cols, 3)))
+        for name, t, shape in checks:
             N.require(t, name, torch.uint8 if t.dtype == torch.uint8 else torch.float32, shape, self.device)
+        self._match_images = match
         self._apply_tuning(match, stitch, frames)
         tma = N.library().ssg_tuning_get(N.TUNE_ISB_TILE_TMA) == 1
         self._run(match, stitch, frames)
@@ -322,7 +341,8 @@ class BatchPipeline:
         if not self.cuda_graphs:
             self._launch(match, stitch, frames, N.stream_of(match))
         else:
-            key = (match.data_ptr(), match.dtype, stitch.data_ptr(), stitch.dtype, frames, self._group_count(frames))
+            key = (match.data_ptr(), match.dtype, stitch.data_ptr() if stitch is not None else 0,
+                   stitch.dtype if stitch is not None else None, frames, self._group_count(frames))
             graph = self._graphs.get(key)
             if graph is None:
                 # one eager run (first-use set-up such as shared-memory opt-in happens outside capture)

@@ -164,3 +164,26 @@ def test_column_staging_equals_tile_staging(ss, native, dtype, cols, rows):
         np.testing.assert_array_equal(a, b)
     if dtype == "float32":
         assert out[0][2].tolist() == [0, 1, 0, 0, 0, 2]
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_stitch_from_the_decoded_batch(ss, native, synthetic, graphs):
+    """estimate_RGBD_panoramas(decoded) without images to stitch stitches the references' decoded
+    images in place: the same panoramas bit for bit as passing those images explicitly."""
+    width, refs, src_width = 256, [1, 3], 304
+    calibs, vp, masks, frame = _rig(ss, synthetic, width, refs=refs, src=(src_width, src_width))
+    decoded = torch.as_tensor(np.stack(frame.images_to_match), device=DEV)[None].repeat(2, 1, 1, 1, 1).contiguous()
+    decoded[1] = decoded[1].flip(1)
+    est = ss.RGBD_Estimator(calibs, 0.55, 100.0, 32, refs, vp, masks, (width, width), (src_width, src_width),
+                            (2 * width, width), 10.0, 6.25, DEV, cost_storage="fp16", max_batch=2, cuda_graphs=graphs)
+    rgb, dist = (t.clone() for t in est.estimate_RGBD_panoramas(decoded, decoded[:, refs].contiguous()))
+    for _ in range(2):  # the second run replays the captured graph
+        rgb2, dist2 = est.estimate_RGBD_panoramas(decoded)
+    torch.cuda.synchronize()
+    assert torch.equal(rgb2, rgb) and torch.equal(dist2, dist)
+    # only decoded uint8 images at the stitch resolution can stand in for the images to stitch
+    with pytest.raises(ValueError):
+        est.estimate_RGBD_panoramas(decoded.float())
+    small = ss.utils.resize_linear(decoded.view(-1, src_width, src_width, 3), (width, width), torch.uint8)
+    with pytest.raises(ValueError):
+        est.estimate_RGBD_panoramas(small.view(2, 4, width, width, 3).contiguous())
