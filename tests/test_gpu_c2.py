@@ -174,3 +174,19 @@ def test_c3_shape_against_oracle(ss, oracle_mod, c2):
     assert same >= 0.999
     assert mae_f <= 1e-4 and mae_p <= 1e-4
     assert p >= 50
+
+
+def test_c2_decoded_inputs_equal_the_resized_path(ss, c2):
+    """The end-to-end path of the benchmark: the decoded 1216^2 uint8 renders of every camera,
+    resized while they are staged, the references' renders stitched in place (no images to
+    stitch).  Its outputs equal those of the resized float32 images above bit for bit, so the
+    acceptance bars against the reference hold for it too."""
+    est, cfg = _estimator(ss, c2, "fp16")
+    rgb_f, dist_f = (t.clone() for t in est.estimate_RGBD_panoramas(c2["match"][None].contiguous(),
+                                                                     c2["stitch"][None].contiguous()))
+    index_f = est.batch_index_maps[0].clone()
+    decoded = torch.as_tensor(c2["renders"], device=DEV)[None].contiguous()
+    rgb_d, dist_d = est.estimate_RGBD_panoramas(decoded)
+    torch.cuda.synchronize()
+    assert torch.equal(est.batch_index_maps[0], index_f)
+    assert torch.equal(rgb_d, rgb_f) and torch.equal(dist_d, dist_f)
