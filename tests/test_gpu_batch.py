@@ -468,3 +468,50 @@ def test_merge_word_and_byte_texel_reads_agree(ss, native, golden_c1):
         outs.append((rgb, dist))
     torch.testing.assert_close(outs[0][0], outs[1][0], rtol=0, atol=0)
     torch.testing.assert_close(outs[0][1], outs[1][1], rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("decoded", [False, True])
+def test_launch_count_matches_the_captured_graph(ss, native, golden_c1, decoded):
+    """The kernel launches the benchmark reports (BatchPipeline.launches_per_batch) are the kernel
+    nodes of the batch's captured CUDA graph, counted through the driver API."""
+    import ctypes
+
+    if not hasattr(torch.cuda.CUDAGraph, "raw_cuda_graph"):
+        pytest.skip("this torch does not expose the captured graph")
+    g = golden_c1
+    est, cfg = _estimator(ss, g, "fp16", max_batch=2, graphs=False)
+    pipe = est.pipeline()
+    if decoded:
+        cols, rows = cfg["matching_resolution"]
+        match = torch.as_tensor(g["images_to_match"], device=DEV).to(torch.uint8)[None].repeat(2, 1, 1, 1, 1)
+        stitch = torch.as_tensor(g["images_to_stitch"], device=DEV).to(torch.uint8)[None].repeat(2, 1, 1, 1, 1)
+    else:
+        match, stitch = _batch(g, 2)
+    match, stitch = match.contiguous(), stitch.contiguous()
+    est.estimate_RGBD_panoramas(match, stitch)  # first-use set-up outside the capture
+    torch.cuda.synchronize()
+    try:
+        graph = torch.cuda.CUDAGraph(keep_graph=True)
+    except TypeError:
+        graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(DEV)
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            pipe._launch(match, stitch, 2, side.cuda_stream)
+    torch.cuda.current_stream().wait_stream(side)
+    try:
+        raw = graph.raw_cuda_graph()
+    except RuntimeError as err:
+        pytest.skip(f"the captured graph is not kept by this torch: {err}")
+    cuda = ctypes.CDLL("libcuda.so.1")
+    n = ctypes.c_size_t(0)
+    assert cuda.cuGraphGetNodes(ctypes.c_void_p(raw), None, ctypes.byref(n)) == 0
+    nodes = (ctypes.c_void_p * n.value)()
+    assert cuda.cuGraphGetNodes(ctypes.c_void_p(raw), nodes, ctypes.byref(n)) == 0
+    kernels = 0
+    for node in nodes:
+        kind = ctypes.c_int(-1)
+        assert cuda.cuGraphNodeGetType(ctypes.c_void_p(node), ctypes.byref(kind)) == 0
+        kernels += kind.value == 0  # CU_GRAPH_NODE_TYPE_KERNEL
+    assert kernels == pipe.launches_per_batch(2, float_stitch=stitch.dtype != torch.uint8)
