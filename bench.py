@@ -269,7 +269,7 @@ def frame_bytes(cols: int, rows: int, cameras: int, references: int, candidates:
     return b_in + references * per_ref + b_stitch
 
 
-def _estimator(ss, calibration, device, storage, batch, graphs, tuner=None):
+def _estimator(ss, calibration, device, storage, batch, graphs, tuner=None, output_slots=1):
     import torch
 
     W = WORKLOAD
@@ -281,7 +281,8 @@ def _estimator(ss, calibration, device, storage, batch, graphs, tuner=None):
     masks = [torch.ones(1, mh, mw, device=device) for _ in calibs]
     return ss.RGBD_Estimator(calibs, W["min_dist"], W["max_dist"], W["candidates"], W["refs"], vp, masks,
                              W["matching"], W["stitch"], W["panorama"], W["sigma_i"], W["sigma_s"], device,
-                             cost_storage=storage, max_batch=batch, cuda_graphs=graphs, tuner=tuner)
+                             cost_storage=storage, max_batch=batch, cuda_graphs=graphs, tuner=tuner,
+                             output_slots=output_slots)
 
 
 def run_ours(args, rank, world, device, rendered):
@@ -296,7 +297,7 @@ def run_ours(args, rank, world, device, rendered):
     for kv in args.knob:
         name, value = kv.split("=")
         autotune.set_knob(name, int(value))
-    est = _estimator(ss, calibration, device, args.storage, B, True, tuner)
+    est = _estimator(ss, calibration, device, args.storage, B, True, tuner, output_slots=2)
     pipe = est.pipeline()
     if args.overlap_groups is not None:
         pipe.overlap_groups = args.overlap_groups
@@ -334,10 +335,10 @@ def run_ours(args, rank, world, device, rendered):
     # end to end through the public API: pinned host inputs in, panoramas back to pinned host
     # memory, every step.  The next batch's upload runs on an upload stream and the previous
     # batch's download on a download stream, both overlapping the current batch's work: the
-    # outputs (which alias the pipeline's buffers) are first copied to one of two device slots.
+    # estimator writes its panoramas to two buffers in turn (output_slots=2), so a batch's are
+    # downloaded while the next batch computes into the other buffer.
     pinned = [(torch.as_tensor(m).pin_memory(), torch.as_tensor(st).pin_memory()) for m, st in host_batches]
     staging = [(torch.empty_like(dev_batches[0][0]), torch.empty_like(dev_batches[0][1])) for _ in range(2)]
-    out_dev = [(torch.empty_like(pipe.rgb), torch.empty_like(pipe.pano_distance)) for _ in range(2)]
     out_host = [(torch.empty(pipe.rgb.shape, dtype=torch.uint8).pin_memory(),
                  torch.empty(pipe.pano_distance.shape).pin_memory()) for _ in range(2)]
     h2d = sum(t.numel() * t.element_size() for t in pinned[0])
@@ -366,16 +367,15 @@ def run_ours(args, rank, world, device, rendered):
                 upload(i + 1)
             slot = i % 2
             compute.wait_event(uploaded[slot])
+            # the outputs this batch overwrites were those of batch i - 2: downloaded by now
+            compute.wait_event(downloaded[slot])
             rgb, dist = est.estimate_RGBD_panoramas(*staging[slot])
             consumed[slot].record(compute)
-            compute.wait_event(downloaded[slot])
-            out_dev[slot][0].copy_(rgb, non_blocking=True)
-            out_dev[slot][1].copy_(dist, non_blocking=True)
             produced[slot].record(compute)
             with torch.cuda.stream(down_stream):
                 down_stream.wait_event(produced[slot])
-                out_host[slot][0].copy_(out_dev[slot][0], non_blocking=True)
-                out_host[slot][1].copy_(out_dev[slot][1], non_blocking=True)
+                out_host[slot][0].copy_(rgb, non_blocking=True)
+                out_host[slot][1].copy_(dist, non_blocking=True)
                 downloaded[slot].record(down_stream)
         for ev in downloaded:
             compute.wait_event(ev)  # the timed region ends with every output on the host
@@ -464,16 +464,14 @@ def run_ours(args, rank, world, device, rendered):
                     upload_u8(i + 1)
                 slot = i % 2
                 compute.wait_event(uploaded[slot])
+                compute.wait_event(downloaded[slot])  # the outputs of batch i - 2 are on the host
                 rgb, dist = est.estimate_RGBD_panoramas(slots_u8[slot])
                 consumed[slot].record(compute)
-                compute.wait_event(downloaded[slot])
-                out_dev[slot][0].copy_(rgb, non_blocking=True)
-                out_dev[slot][1].copy_(dist, non_blocking=True)
                 produced[slot].record(compute)
                 with torch.cuda.stream(down_stream):
                     down_stream.wait_event(produced[slot])
-                    out_host[slot][0].copy_(out_dev[slot][0], non_blocking=True)
-                    out_host[slot][1].copy_(out_dev[slot][1], non_blocking=True)
+                    out_host[slot][0].copy_(rgb, non_blocking=True)
+                    out_host[slot][1].copy_(dist, non_blocking=True)
                     downloaded[slot].record(down_stream)
             for ev in downloaded:
                 compute.wait_event(ev)

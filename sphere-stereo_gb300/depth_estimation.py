@@ -37,7 +37,7 @@ def distance_candidates(min_dist, max_dist, candidate_count) -> torch.Tensor:
 class RGBD_Estimator:
     def __init__(self, calibrations, min_dist, max_dist, candidate_count, references_indices, reprojection_viewpoint,
                  masks, matching_resolution, rgb_to_stitch_resolution, panorama_resolution, sigma_i, sigma_s, device,
-                 *, cost_storage="fp32", max_batch=1, cuda_graphs=True, tuner=None):
+                 *, cost_storage="fp32", max_batch=1, cuda_graphs=True, tuner=None, output_slots=1):
         """Prepare RGB-D estimation: camera selection for adaptive matching, filters, stitcher.
 
         Args:
@@ -57,6 +57,10 @@ class RGBD_Estimator:
                 arithmetic bit for bit against the oracle; "fp16" / "unorm16" store the cost
                 volume with 16 bits per candidate (fp32 arithmetic) and run frames in batches
             max_batch (keyword only): largest batch of ``estimate_RGBD_panoramas``
+            output_slots (keyword only): ``estimate_RGBD_panoramas`` writes its panoramas to this
+                many buffers in turn, so a batch's outputs stay valid while the next
+                output_slots - 1 batches run (for a caller that downloads one batch while the
+                next computes); 1 = every call overwrites the last, as in the reference
             cuda_graphs (keyword only): replay each batch from a captured CUDA graph
             tuner (keyword only): an autotune.Tuner that picks the batched kernels' launch
                 shapes on first use (None: the library's defaults)
@@ -117,6 +121,7 @@ class RGBD_Estimator:
         self.max_batch = int(max_batch)
         self.cuda_graphs = bool(cuda_graphs)
         self.tuner = tuner
+        self.output_slots = int(output_slots)
         self._pipeline = None
 
     @property
@@ -175,7 +180,8 @@ class RGBD_Estimator:
             from .pipeline import BatchPipeline
 
             storage = "fp16" if self.cost_storage == "fp32" else self.cost_storage
-            self._pipeline = BatchPipeline(self, self.max_batch, storage, self.cuda_graphs, self.tuner)
+            self._pipeline = BatchPipeline(self, self.max_batch, storage, self.cuda_graphs, self.tuner,
+                                           output_slots=self.output_slots)
         return self._pipeline
 
     # --------------------------------------------------------------------------------------

@@ -37,17 +37,21 @@ class BatchPipeline:
     MAX_GROUPS = 8
 
     def __init__(self, estimator, max_frames: int, storage: str = "fp16", cuda_graphs: bool = True,
-                 tuner=None, overlap_groups: int | None = None):
+                 tuner=None, overlap_groups: int | None = None, output_slots: int = 1):
         """overlap_groups: the batch's frames are split into this many groups; the distance
         post-filter and the stitch of a group run on a second stream while the next group's sweep
         and cost filter run (1 = one group, no overlap; None = the tuner's pick, or 1 without a
-        tuner)."""
+        tuner).  output_slots: the panoramas of consecutive runs go to this many buffers in turn,
+        so the outputs of a run stay valid for the next output_slots - 1 runs (1: each run
+        overwrites the last, as the reference's outputs alias its stitcher buffers)."""
         if storage not in STORAGE:
             raise ValueError(f"storage must be one of {sorted(STORAGE)}")
         if max_frames < 1:
             raise ValueError("max_frames must be positive")
         if overlap_groups is not None and not 1 <= overlap_groups <= self.MAX_GROUPS:
             raise ValueError(f"overlap_groups must be in [1, {self.MAX_GROUPS}]")
+        if not 1 <= output_slots <= 4:
+            raise ValueError("output_slots must be in [1, 4]")
         self.overlap_groups = overlap_groups
         e = estimator
         self.e = e
@@ -92,8 +96,11 @@ class BatchPipeline:
         self.holes = torch.empty(3 * F * R * P + N.HOLE_SCRATCH_HEADER * self.MAX_GROUPS, dtype=torch.int32,
                                  device=dev)
         self.images_u8 = torch.empty(F, R, st.image_rows, st.image_cols, 3, **u8)
-        self.rgb = torch.empty(F, st.pano_rows, st.pano_cols, 3, **u8)
-        self.pano_distance = torch.empty(F, st.pano_rows, st.pano_cols, **f32)
+        # the panoramas: output_slots buffers used in turn; rgb / pano_distance are the current one
+        self._out_slots = [(torch.empty(F, st.pano_rows, st.pano_cols, 3, **u8),
+                            torch.empty(F, st.pano_rows, st.pano_cols, **f32)) for _ in range(output_slots)]
+        self._next_slot = self._slot = 0
+        self.rgb, self.pano_distance = self._out_slots[0]
         self.tables = torch.stack(st.inpainting_weights_list).contiguous()
         self.selected = torch.stack(e._selected).contiguous()
         self._refs = N.ints(e.references_indices)
@@ -316,6 +323,9 @@ class BatchPipeline:
         for name, t, shape in checks:
             N.require(t, name, torch.uint8 if t.dtype == torch.uint8 else torch.float32, shape, self.device)
         self._match_images = match
+        self._slot = self._next_slot
+        self.rgb, self.pano_distance = self._out_slots[self._slot]
+        self._next_slot = (self._slot + 1) % len(self._out_slots)
         self._apply_tuning(match, stitch, frames)
         tma = N.library().ssg_tuning_get(N.TUNE_ISB_TILE_TMA) == 1
         self._run(match, stitch, frames)
@@ -343,24 +353,32 @@ class BatchPipeline:
         else:
             key = (match.data_ptr(), match.dtype, stitch.data_ptr() if stitch is not None else 0,
                    stitch.dtype if stitch is not None else None, frames, self._group_count(frames))
-            graph = self._graphs.get(key)
-            if graph is None:
+            graphs = self._graphs.get(key)
+            if graphs is None:
                 # one eager run (first-use set-up such as shared-memory opt-in happens outside capture)
                 self._launch(match, stitch, frames, N.stream_of(match))
                 # objects that are already garbage (an earlier graph, say) are freed now: a graph
                 # destroyed while this capture runs would invalidate it
                 gc.collect()
-                graph = torch.cuda.CUDAGraph()
-                side = torch.cuda.Stream(self.device)
-                side.wait_stream(torch.cuda.current_stream(self.device))
-                with torch.cuda.stream(side):
-                    with torch.cuda.graph(graph, stream=side):
-                        self._launch(match, stitch, frames, side.cuda_stream)
-                torch.cuda.current_stream(self.device).wait_stream(side)
+                # one graph per output slot, all captured now: later runs of these inputs replay,
+                # whichever slot their turn falls on
+                current = (self.rgb, self.pano_distance)
+                graphs = []
+                for out in self._out_slots:
+                    self.rgb, self.pano_distance = out
+                    graph = torch.cuda.CUDAGraph()
+                    side = torch.cuda.Stream(self.device)
+                    side.wait_stream(torch.cuda.current_stream(self.device))
+                    with torch.cuda.stream(side):
+                        with torch.cuda.graph(graph, stream=side):
+                            self._launch(match, stitch, frames, side.cuda_stream)
+                    torch.cuda.current_stream(self.device).wait_stream(side)
+                    graphs.append(graph)
+                self.rgb, self.pano_distance = current
                 if len(self._graphs) >= 8:
                     self._graphs.pop(next(iter(self._graphs)))
-                self._graphs[key] = graph
-            graph.replay()
+                self._graphs[key] = graphs
+            graphs[self._slot].replay()
 
     # in tuning order: a register bound before the staging it pairs with (a staging choice is timed
     # at the bound already picked)

@@ -515,3 +515,32 @@ def test_launch_count_matches_the_captured_graph(ss, native, golden_c1, decoded)
         assert cuda.cuGraphNodeGetType(ctypes.c_void_p(node), ctypes.byref(kind)) == 0
         kernels += kind.value == 0  # CU_GRAPH_NODE_TYPE_KERNEL
     assert kernels == pipe.launches_per_batch(2, float_stitch=stitch.dtype != torch.uint8)
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_output_slots_alternate_and_keep_the_previous_batch(ss, native, golden_c1, graphs):
+    """output_slots=2: consecutive batches write their panoramas to two buffers in turn, so a
+    batch's outputs stay valid while the next one runs; the values are those of one slot."""
+    g = golden_c1
+    one, _ = _estimator(ss, g, "fp16", max_batch=2, graphs=graphs)
+    two, _ = _estimator(ss, g, "fp16", max_batch=2, graphs=graphs)
+    two.output_slots = 2
+    match, stitch = _batch(g, 2)
+    flipped = (match.flip(2).contiguous(), stitch.flip(2).contiguous())
+    want_a = [t.clone() for t in one.estimate_RGBD_panoramas(match, stitch)]
+    want_b = [t.clone() for t in one.estimate_RGBD_panoramas(*flipped)]
+    a = two.estimate_RGBD_panoramas(match, stitch)
+    b = two.estimate_RGBD_panoramas(*flipped)
+    torch.cuda.synchronize()
+    assert a[0].data_ptr() != b[0].data_ptr()
+    for got, want in zip(list(a) + list(b), want_a + want_b):  # a's outputs survive batch b
+        torch.testing.assert_close(got, want, rtol=0, atol=0)
+    c = two.estimate_RGBD_panoramas(*flipped)  # the third batch reuses a's buffers
+    torch.cuda.synchronize()
+    assert c[0].data_ptr() == a[0].data_ptr()
+    for got, want in zip(c, want_b):
+        torch.testing.assert_close(got, want, rtol=0, atol=0)
+    with pytest.raises(ValueError):
+        bad, _ = _estimator(ss, g, "fp16", max_batch=1, graphs=False)
+        bad.output_slots = 5
+        bad.estimate_RGBD_panoramas(match[:1].contiguous(), stitch[:1].contiguous())
