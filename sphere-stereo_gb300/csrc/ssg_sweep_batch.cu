@@ -706,19 +706,29 @@ __device__ __forceinline__ void sample_pair_codes(const uint4* __restrict__ entr
                                                   float2 iy, uint32_t (&s)[2][3])
 {
     static_assert(!kFixed || kStride == 2, "fixed-point codes are staged in 32-byte entries");
-    float2 x0, y0, wa, wb, wc, wd;
-    bilinear_pair(cols, rows, ix, iy, x0, y0, wa, wb, wc, wd);
+    // bilinear_pair's clamp, floors and weights, the floors formed on the FMA pipe: the clamped
+    // coordinate plus 2^23 + 1, rounded down, is exactly floor + 1 + 2^23 (the sum lies in
+    // [2^23, 2^24), where floats are the integers), so its bits hold floor + 1 and subtracting
+    // 2^23 + 1 gives the floor itself
+    const float colsf = (float)cols, rowsf = (float)rows;
+    ix = make_float2(fminf(fmaxf(ix.x, -1.0f), colsf), fminf(fmaxf(ix.y, -1.0f), colsf));
+    iy = make_float2(fminf(fmaxf(iy.x, -1.0f), rowsf), fminf(fmaxf(iy.y, -1.0f), rowsf));
+    const float2 tx = add2_rd(ix, splat(8388609.0f)), ty = add2_rd(iy, splat(8388609.0f));
+    const float2 x0 = add2(tx, splat(-8388609.0f)), y0 = add2(ty, splat(-8388609.0f));
+    const float2 fx = add2(ix, make_float2(-x0.x, -x0.y)), fy = add2(iy, make_float2(-y0.x, -y0.y));
+    const float2 gx = add2(splat(1.0f), make_float2(-fx.x, -fx.y)), gy = add2(splat(1.0f), make_float2(-fy.x, -fy.y));
+    const float2 wa = mul2(gx, gy), wb = mul2(fx, gy), wc = mul2(gx, fy), wd = mul2(fx, fy);
     const float2 scale = splat(65535.0f), magic = splat(12582912.0f);
     const float2 qa = fma2(wa, scale, magic), qb = fma2(wb, scale, magic), qc = fma2(wc, scale, magic),
                  qd = fma2(wd, scale, magic);
-    // entry index (y0 + 1) * pitch + x0 + 1, exact in float (below 2^24 entries a plane)
-    const float pitchf = (float)(cols + 2);
-    const float2 e = fma2(add2(y0, splat(1.0f)), splat(pitchf), add2(x0, splat(1.0f)));
+    // entry index (y0 + 1) * pitch + x0 + 1 from the bits of tx, ty (0x4B000000 + floor + 1 each),
+    // in wrapping 32-bit arithmetic: the offsets cancel and the index fits
+    const uint32_t pitch = (uint32_t)cols + 2u, bias = 0x4B000000u * (pitch + 1u);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const uint32_t top = __byte_perm(__float_as_uint(h ? qa.y : qa.x), __float_as_uint(h ? qb.y : qb.x), 0x5410);
         const uint32_t bot = __byte_perm(__float_as_uint(h ? qc.y : qc.x), __float_as_uint(h ? qd.y : qd.x), 0x5410);
-        const uint32_t idx = __float2uint_rz(h ? e.y : e.x);  // e >= 0: an unsigned offset
+        const uint32_t idx = __float_as_uint(h ? ty.y : ty.x) * pitch + __float_as_uint(h ? tx.y : tx.x) - bias;
         uint4 q, r;
         if constexpr (kFixed) load_entry32(entries + kStride * idx, q, r);  // both halves of the entry
         else q = __ldg(entries + kStride * idx);
