@@ -393,11 +393,32 @@ __device__ __forceinline__ float fine_weights_padded(const typename GL::Pix (&gd
 }
 
 // filtered costs of fine pixel F from the staged taps: the arithmetic and order of up_costs, or
-// (kFast, the chunked 16-bit path) the same sum with fused multiply-adds
-template <int F, int E, bool kFast>
+// (kFast, the chunked 16-bit path) the same sum with fused multiply-adds; kPacked: two candidates
+// at a time (the same bits; taken by the steps that store their cells, the selecting step keeps
+// the scalar form, which leaves its three-block build fewer spilled registers)
+template <int F, int E, bool kFast, bool kPacked = true>
 __device__ __forceinline__ void filter_part(const float (&tap)[9][E], const float (&w)[9], float inv, float weight_up,
                                             float acc[E])
 {
+    if constexpr (kFast && kPacked && E % 2 == 0) {
+        // two candidates per packed f32x2 operation: each lane rounds as the scalar form does
+        float2 pair[E / 2];
+#pragma unroll
+        for (int j = 0; j < E / 2; ++j) pair[j] = mul2(splat(weight_up), make_float2(acc[2 * j], acc[2 * j + 1]));
+#pragma unroll
+        for (int i = 0; i < UpTaps<F>::n; ++i) {
+            const float* t = tap[UpTaps<F>::tap(i)];
+#pragma unroll
+            for (int j = 0; j < E / 2; ++j) pair[j] = fma2(splat(w[i]), make_float2(t[2 * j], t[2 * j + 1]), pair[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < E / 2; ++j) {
+            pair[j] = mul2(pair[j], splat(inv));
+            acc[2 * j] = pair[j].x;
+            acc[2 * j + 1] = pair[j].y;
+        }
+        return;
+    }
 #pragma unroll
     for (int e = 0; e < E; ++e) acc[e] = fmul(weight_up, acc[e]);
 #pragma unroll
@@ -456,7 +477,7 @@ __device__ __forceinline__ void up_part(const float (&tap)[9][UpTile<W>::E], con
     constexpr int E = UpTile<W>::E;
     float acc[E];
     raw.part(part, acc);
-    filter_part<F, E, W == 8>(tap, px.w, px.inv, weight_up, acc);
+    filter_part<F, E, W == 8, !kSelect>(tap, px.w, px.inv, weight_up, acc);
     if constexpr (kSelect) {
         if (full) {
 #pragma unroll
